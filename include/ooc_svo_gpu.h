@@ -1,0 +1,134 @@
+/*
+ * ooc_svo_gpu.h -- C ABI of the GB300 partition -> voxelize -> SVO-build path.
+ *
+ * Library: ooc_svo_builder_gb300/libooc_svo_gpu.so (CUDA sm_103a).
+ *
+ * The reference (ooc_svo_builder v1.6.4) has no plugin or FFI layer; its
+ * boundary is the svo_builder / svo_builder_binary command line and the
+ * .tri/.tridata -> .octree/.octreenodes/.octreedata file formats.  The calls
+ * below replace the reference's internal C++ seams that main.cpp drives:
+ *
+ *   ooc_estimate_partitions   estimate_partitions      partitioner.cpp:12-28
+ *   ooc_build / ooc_build_device
+ *                             partition                partitioner.cpp:101-149
+ *                             + voxelize_schwarz_method voxelizer.cpp:139-307
+ *                             + std::sort + colour modes main.cpp:354-385
+ *                             + OctreeBuilder::addVoxel / finalizeTree
+ *                                                      OctreeBuilder.cpp:34-167
+ *                             (the whole loop of main.cpp:294-392)
+ *
+ * Output bytes are those of the reference's files: the node file is n_nodes
+ * records of 24 bytes {u64 data, u64 children_base, i8 children_offset[8]}
+ * (octree_io.h:62-66), the data file n_data records of 32 bytes
+ * {u64 morton, f32 color[3], f32 normal[3]} (octree_io.h:49-53).
+ *
+ * Conventions: every call returns OOC_OK (0) or an OOC_ERR_* code and never
+ * throws; ooc_last_error() describes the last failure of a context.  One host
+ * thread per context; any number of contexts.  All device memory and streams
+ * belong to the library.
+ */
+#ifndef OOC_SVO_GPU_H_
+#define OOC_SVO_GPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OOC_OK 0
+#define OOC_ERR_INVALID 1  /* bad argument (gridsize not a power of two, ...)    */
+#define OOC_ERR_OOM 2      /* device or pinned-host allocation failed            */
+#define OOC_ERR_DEVICE 3   /* a CUDA call or kernel failed                       */
+#define OOC_ERR_IO 4       /* file could not be read or written                  */
+#define OOC_ERR_SINK 5     /* the caller's sink returned non-zero                */
+
+/* Colour modes of svo_builder's -c flag (main.cpp:23, 154-179). */
+#define OOC_COLOR_MODEL 0
+#define OOC_COLOR_FIXED 1
+#define OOC_COLOR_LINEAR 2
+#define OOC_COLOR_NORMAL 3
+
+/* Which file a sink call carries. */
+#define OOC_STREAM_NODES 0
+#define OOC_STREAM_DATA 1
+
+typedef struct ooc_ctx ooc_ctx;
+
+/* Build parameters: the flags of main.cpp:100-196 plus the .tri header. */
+typedef struct {
+  uint64_t gridsize;        /* -s: power of two, 1 .. 65536                   */
+  uint64_t memory_limit_mb; /* -l: sets the partition count like the reference */
+  int32_t geometry_only;    /* 1: svo_builder_binary (9 floats / triangle);
+                               0: svo_builder with payload (21 floats)         */
+  int32_t color_mode;       /* OOC_COLOR_*; ignored when geometry_only == 1    */
+  int32_t generate_levels;  /* -levels                                         */
+  int32_t reserved;         /* must be 0                                       */
+  float bbox_min[3];        /* .tri header bbox (only max.x - min.x is used,   */
+  float bbox_max[3];        /*  as in main.cpp:311)                            */
+} ooc_build_params;
+
+typedef struct {
+  uint64_t n_nodes;      /* octree header n_nodes                         */
+  uint64_t n_data;       /* octree header n_data                          */
+  uint64_t n_filled;     /* "Total amount of voxels" (main.cpp:391)       */
+  uint64_t n_partitions; /* estimate_partitions result                    */
+  uint64_t n_stripes;    /* device work units the grid was processed in   */
+  uint64_t n_items;      /* (triangle, partition) pairs after binning     */
+} ooc_build_info;
+
+/* Receives the node file (kind OOC_STREAM_NODES) and the data file
+ * (OOC_STREAM_DATA) in file order, in pieces.  `bytes` is valid only during
+ * the call.  Return 0 to continue, non-zero to abort with OOC_ERR_SINK. */
+typedef int (*ooc_sink_fn)(void* user, int32_t kind, const void* bytes, uint64_t nbytes);
+
+/* Create a context on CUDA device `device`. */
+int ooc_ctx_create(int32_t device, ooc_ctx** out);
+void ooc_ctx_destroy(ooc_ctx* ctx);
+/* Text of the last error of `ctx` (never NULL; "" after success). */
+const char* ooc_last_error(const ooc_ctx* ctx);
+
+/* estimate_partitions (partitioner.cpp:12-28): 1 if gridsize^3 bytes fit in
+ * memory_limit_mb, otherwise the smallest 8^k that brings a partition under
+ * the limit, dividing the megabyte count by 8 with integer division. */
+uint64_t ooc_estimate_partitions(uint64_t gridsize, uint64_t memory_limit_mb);
+
+/* Whole path from host triangles (n_tris records of 9 or 21 FP32 values,
+ * pinned or pageable) to the octree, streamed to `sink` in file order.
+ * Replaces main.cpp:294-392. */
+int ooc_build(ooc_ctx* ctx, const ooc_build_params* params, const float* tris_host, uint64_t n_tris,
+              ooc_sink_fn sink, void* user, ooc_build_info* info);
+
+/* Same path from triangles already in device memory; the octree stays in
+ * device memory (see ooc_result_device).  `stream` is a cudaStream_t (NULL:
+ * the context's own stream); all work is ordered on it and the call returns
+ * after the stream has drained. */
+int ooc_build_device(ooc_ctx* ctx, const ooc_build_params* params, const float* tris_device, uint64_t n_tris,
+                     void* stream, ooc_build_info* info);
+
+/* Device pointers to the node and data files produced by the last
+ * ooc_build_device call of `ctx`; valid until the next build on `ctx`. */
+int ooc_result_device(ooc_ctx* ctx, const void** nodes_device, const void** data_device);
+
+/* Device time in milliseconds of each phase of the last build of `ctx`
+ * (CUDA events on the build stream): [0] partition binning, [1] voxelization
+ * (both passes), [2] occupancy pyramid + scans, [3] octree layout and record
+ * emission, [4] host<->device copies, [5] whole build.  `n` entries are
+ * written (at most 6).  Phase timing is recorded only after
+ * ooc_set_phase_timing(ctx, 1). */
+int ooc_set_phase_timing(ooc_ctx* ctx, int32_t enable);
+int ooc_phase_times(const ooc_ctx* ctx, float* ms, int32_t n);
+
+/* Launch count of this library's kernels in the last build of `ctx`. */
+uint64_t ooc_kernel_launches(const ooc_ctx* ctx);
+
+/* File front end used by the svo_builder CLIs: reads <base>.tri/.tridata and
+ * writes <base><gridsize>_<npartitions>.octree/.octreenodes/.octreedata
+ * (main.cpp:296-398).  `out_base` receives the output base name (may be NULL). */
+int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_build_params* params, char* out_base,
+                    uint64_t out_base_len, ooc_build_info* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OOC_SVO_GPU_H_ */

@@ -1,0 +1,214 @@
+"""GB300-native partition -> voxelize -> SVO-build path of ooc_svo_builder.
+
+Python binding of ``libooc_svo_gpu.so`` (C ABI in ``include/ooc_svo_gpu.h``).
+The library is required: importing the binding raises if it has not been built
+(``python -c "import __graft_entry__ as g; g.build()"``).  There is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import octree as _octree
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libooc_svo_gpu.so")
+
+OOC_OK = 0
+ERRORS = {1: "OOC_ERR_INVALID", 2: "OOC_ERR_OOM", 3: "OOC_ERR_DEVICE", 4: "OOC_ERR_IO", 5: "OOC_ERR_SINK"}
+COLOR_MODES = {"model": 0, "fixed": 1, "linear": 2, "normal": 3}
+PHASES = ("partition", "voxelize", "pyramid", "octree", "copies", "build")
+
+# Every symbol declared in include/ooc_svo_gpu.h.
+EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_partitions", "ooc_build",
+           "ooc_build_device", "ooc_result_device", "ooc_set_phase_timing", "ooc_phase_times",
+           "ooc_kernel_launches", "ooc_build_files")
+
+
+class BuildParams(ctypes.Structure):
+    _fields_ = [("gridsize", ctypes.c_uint64), ("memory_limit_mb", ctypes.c_uint64),
+                ("geometry_only", ctypes.c_int32), ("color_mode", ctypes.c_int32),
+                ("generate_levels", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("bbox_min", ctypes.c_float * 3), ("bbox_max", ctypes.c_float * 3)]
+
+
+class BuildInfo(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_uint64), ("n_data", ctypes.c_uint64), ("n_filled", ctypes.c_uint64),
+                ("n_partitions", ctypes.c_uint64), ("n_stripes", ctypes.c_uint64), ("n_items", ctypes.c_uint64)]
+
+
+SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_uint64)
+
+
+class OocError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s: %s" % (ERRORS.get(code, str(code)), msg))
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load libooc_svo_gpu.so and declare its signatures; raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("libooc_svo_gpu.so not built at %s; run __graft_entry__.build()" % path)
+    lib = ctypes.CDLL(path)
+    P = ctypes.POINTER
+    lib.ooc_ctx_create.argtypes = [ctypes.c_int32, P(ctypes.c_void_p)]
+    lib.ooc_ctx_create.restype = ctypes.c_int
+    lib.ooc_ctx_destroy.argtypes = [ctypes.c_void_p]
+    lib.ooc_ctx_destroy.restype = None
+    lib.ooc_last_error.argtypes = [ctypes.c_void_p]
+    lib.ooc_last_error.restype = ctypes.c_char_p
+    lib.ooc_estimate_partitions.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+    lib.ooc_estimate_partitions.restype = ctypes.c_uint64
+    lib.ooc_build.argtypes = [ctypes.c_void_p, P(BuildParams), ctypes.c_void_p, ctypes.c_uint64, SINK,
+                              ctypes.c_void_p, P(BuildInfo)]
+    lib.ooc_build.restype = ctypes.c_int
+    lib.ooc_build_device.argtypes = [ctypes.c_void_p, P(BuildParams), ctypes.c_void_p, ctypes.c_uint64,
+                                     ctypes.c_void_p, P(BuildInfo)]
+    lib.ooc_build_device.restype = ctypes.c_int
+    lib.ooc_result_device.argtypes = [ctypes.c_void_p, P(ctypes.c_void_p), P(ctypes.c_void_p)]
+    lib.ooc_result_device.restype = ctypes.c_int
+    lib.ooc_set_phase_timing.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    lib.ooc_set_phase_timing.restype = ctypes.c_int
+    lib.ooc_phase_times.argtypes = [ctypes.c_void_p, P(ctypes.c_float), ctypes.c_int32]
+    lib.ooc_phase_times.restype = ctypes.c_int
+    lib.ooc_kernel_launches.argtypes = [ctypes.c_void_p]
+    lib.ooc_kernel_launches.restype = ctypes.c_uint64
+    lib.ooc_build_files.argtypes = [ctypes.c_void_p, ctypes.c_char_p, P(BuildParams), ctypes.c_char_p,
+                                    ctypes.c_uint64, P(BuildInfo)]
+    lib.ooc_build_files.restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def estimate_partitions(gridsize: int, memory_limit_mb: int) -> int:
+    """estimate_partitions (partitioner.cpp:12-28), through the library."""
+    return int(load_library().ooc_estimate_partitions(gridsize, memory_limit_mb))
+
+
+def make_params(gridsize: int, memory_limit_mb: int = 2048, geometry_only: bool = True, color: str = "model",
+                levels: bool = False, bbox_min=(0.0, 0.0, 0.0), bbox_max=(1.0, 1.0, 1.0)) -> BuildParams:
+    p = BuildParams()
+    p.gridsize = gridsize
+    p.memory_limit_mb = memory_limit_mb
+    p.geometry_only = 1 if geometry_only else 0
+    p.color_mode = COLOR_MODES[color] if isinstance(color, str) else int(color)
+    p.generate_levels = 1 if levels else 0
+    p.reserved = 0
+    for a in range(3):
+        p.bbox_min[a] = float(bbox_min[a])
+        p.bbox_max[a] = float(bbox_max[a])
+    return p
+
+
+@dataclass
+class BuildResult:
+    tree: _octree.Octree
+    info: dict
+
+
+def _info_dict(info: BuildInfo) -> dict:
+    return {k: int(getattr(info, k)) for k, _ in BuildInfo._fields_}
+
+
+class Builder:
+    """One library context on one CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.ooc_ctx_create(device, ctypes.byref(h))
+        if rc != OOC_OK:
+            raise OocError(rc, "ooc_ctx_create(%d) failed" % device)
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.ooc_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != OOC_OK:
+            raise OocError(rc, self.lib.ooc_last_error(self.h).decode(errors="replace"))
+
+    def set_phase_timing(self, on: bool = True):
+        self._check(self.lib.ooc_set_phase_timing(self.h, 1 if on else 0))
+
+    def phase_times(self) -> dict:
+        arr = (ctypes.c_float * 6)()
+        self._check(self.lib.ooc_phase_times(self.h, arr, 6))
+        return {k: float(arr[i]) for i, k in enumerate(PHASES)}
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.ooc_kernel_launches(self.h))
+
+    def build(self, tris: np.ndarray, params: BuildParams, sink=None) -> BuildResult:
+        """Host triangles in, octree bytes out (through the sink into host memory)."""
+        tris = np.ascontiguousarray(tris, dtype=np.float32)
+        width = 9 if params.geometry_only else 21
+        if tris.ndim != 2 or tris.shape[1] != width:
+            raise ValueError("triangles must be [T, %d] float32 for this mode" % width)
+        parts = {0: [], 1: []}
+
+        if sink is None:
+            def _collect(user, kind, ptr, n):
+                parts[kind].append(ctypes.string_at(ptr, n))
+                return 0
+            cb = SINK(_collect)
+        else:
+            cb = SINK(sink)
+        info = BuildInfo()
+        rc = self.lib.ooc_build(self.h, ctypes.byref(params), tris.ctypes.data_as(ctypes.c_void_p),
+                                tris.shape[0], cb, None, ctypes.byref(info))
+        self._check(rc)
+        tree = _octree.from_bytes(int(params.gridsize), b"".join(parts[0]), b"".join(parts[1]))
+        return BuildResult(tree, _info_dict(info))
+
+    def build_ptr(self, tris_ptr: int, n_tris: int, params: BuildParams, sink) -> dict:
+        """Host triangles given by address (e.g. pinned memory); `sink` is a SINK instance."""
+        info = BuildInfo()
+        self._check(self.lib.ooc_build(self.h, ctypes.byref(params), ctypes.c_void_p(tris_ptr), n_tris, sink,
+                                       None, ctypes.byref(info)))
+        return _info_dict(info)
+
+    def build_device(self, tris_dev_ptr: int, n_tris: int, params: BuildParams, stream: int = 0) -> dict:
+        """Triangles already in device memory; the octree stays on the device."""
+        info = BuildInfo()
+        self._check(self.lib.ooc_build_device(self.h, ctypes.byref(params), ctypes.c_void_p(tris_dev_ptr), n_tris,
+                                              ctypes.c_void_p(stream or None), ctypes.byref(info)))
+        return _info_dict(info)
+
+    def result_device(self):
+        n = ctypes.c_void_p()
+        d = ctypes.c_void_p()
+        self._check(self.lib.ooc_result_device(self.h, ctypes.byref(n), ctypes.byref(d)))
+        return int(n.value or 0), int(d.value or 0)
+
+    def build_files(self, tri_path: str, params: BuildParams):
+        out = ctypes.create_string_buffer(4096)
+        info = BuildInfo()
+        self._check(self.lib.ooc_build_files(self.h, tri_path.encode(), ctypes.byref(params), out, 4096,
+                                             ctypes.byref(info)))
+        return out.value.decode(), _info_dict(info)

@@ -1,0 +1,109 @@
+// Internal interfaces between the orchestration (ooc_api.cu) and the kernels
+// (ooc_kernels.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ooc {
+
+// Maximum stripe: 8^10 = 2^30 voxels, a 1024^3 Morton-aligned cube whose
+// occupancy bitfield (128 MiB) is about the size of the GB300's 129 MB L2, so
+// the voxelization atomics mostly stay on chip.
+constexpr int kMaxStripeDepth = 10;
+constexpr int kMaxLevels = kMaxStripeDepth + 1;
+
+// One level of the per-stripe occupancy pyramid.  Level l has 8^l bits; its
+// words are padded to whole 256-bit blocks (8 words) and each block has a
+// popcount entry in the concatenated scan array.
+struct Level {
+  uint64_t off_w;    // first word of this level in the bits buffer
+  uint64_t off_b;    // first block entry of this level in the scan buffer
+  uint64_t nwords;   // padded word count (multiple of 8)
+  uint64_t nblocks;  // nwords / 8
+  uint64_t koff;     // first node of this level in the per-node arrays
+  uint64_t n;        // set bits (nodes) at this level, filled after the scan
+};
+
+struct Pyramid {
+  int depth;  // Ds: levels 0..Ds, level Ds = voxels of the stripe
+  Level lv[kMaxLevels];
+  uint32_t* bits;  // all levels' words
+  uint32_t* scan;  // exclusive prefix popcount per 256-bit block, all levels (+1 total)
+};
+
+// Inputs of the voxelization kernels for one stripe.
+struct VoxJob {
+  const float* tris;
+  int stride;               // 9 (binary) or 21 (payload)
+  const uint32_t* item_tri; // triangle of each item (NULL: item i is triangle ibeg + i)
+  uint64_t ibeg;
+  uint64_t n_items;
+  int pa[3], pb[3];         // partition box in grid coordinates (inclusive)
+  int sa[3], sb[3];         // stripe box in grid coordinates (inclusive)
+  float u, unit_div;
+  uint32_t small_vol;       // items with at most this many candidates run one per thread
+  uint32_t* leafbits;       // level-Ds words
+  // pass B (payload winners)
+  const uint32_t* leafscan; // scan entries of level Ds (exclusive, minus its base)
+  uint32_t leafscan_base;
+  uint32_t* winners;        // per leaf: min triangle index
+  uint64_t* task_off;       // per item: exclusive prefix of warp tasks (n_items + 1)
+  unsigned long long* task_counter;
+};
+
+struct EmitJob {
+  int binary;
+  int levels;
+  int color_mode;
+  uint64_t gridsize;
+  uint64_t stripe_base;     // global Morton code of the stripe's first voxel
+  int origin[3];            // stripe origin in grid coordinates
+  const float* tris;
+  int stride;
+  float unit_div;
+  const uint32_t* keys;     // per node: local key (Morton prefix within its level)
+  uint32_t* size;           // per node: nodes in its subtree
+  uint32_t* dsize;          // per node: data records in its subtree
+  uint64_t* start;          // per node: global index of the first node written inside its subtree
+  uint64_t* dstart;         // per node: global index of its subtree's first data record
+  float* cache;             // per node: 6 floats (colour, normal) used by -levels and leaves
+  const uint32_t* winners;
+  uint64_t* node_win;       // node window (3 u64 per record)
+  uint64_t node_win_base;   // global node index of node_win[0]
+  unsigned char* data_win;  // data window (32 bytes per record)
+  uint64_t data_win_base;
+  uint64_t node_win_len;    // records the node window holds
+  uint64_t data_win_len;    // records the data window holds
+  uint64_t n_tris;          // triangles in `tris`
+  uint32_t* flag;           // set non-zero by a kernel that finds an index out of range
+};
+
+// ---- launches (ooc_kernels.cu); all asynchronous on `st` ----
+extern unsigned long long g_launches;  // kernel launches since the last reset (host counter)
+
+void scan_u32_exclusive(uint32_t* data, uint64_t n, uint32_t* partials, cudaStream_t st);
+void scan_u64_exclusive(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st);
+uint64_t scan_partials_needed(uint64_t n);
+
+void launch_part_count(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
+                       int pa_bits, uint64_t n_parts, uint32_t* hist, cudaStream_t st);
+void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
+                      int pa_bits, uint64_t n_parts, uint32_t* cursor, uint32_t* items, cudaStream_t st);
+
+void launch_vox_small(const VoxJob& j, int pass, cudaStream_t st);
+void launch_vox_large(const VoxJob& j, int pass, cudaStream_t st, int num_sms);
+
+void launch_pyramid(const Pyramid& p, int level, cudaStream_t st);
+void launch_compact(const Pyramid& p, int level, uint32_t* keys, cudaStream_t st);
+void launch_leaf_payload(const Pyramid& p, const EmitJob& e, int color_mode, cudaStream_t st);
+void launch_bottom_up(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st);
+void launch_set_root(const EmitJob& e, uint64_t node_base, uint64_t data_base, cudaStream_t st);
+void launch_top_down(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st);
+// Writes the stripe root's child mask and cache to out[0..6] and its own data
+// record (with -levels, or the payload of a one-voxel stripe).
+void launch_root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base, uint32_t* out, cudaStream_t st);
+// src holds n entries of (index, `words` u64 values); dst[index*words + q] = value q.
+void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st);
+
+}  // namespace ooc

@@ -1,0 +1,746 @@
+// CUDA kernels of the partition -> voxelize -> SVO-build path (sm_103a).
+//
+// Compiled with -fmad=false; FP32 arithmetic additionally goes through the
+// __f*_rn intrinsics so that each operation rounds once, as in the
+// reference's x86-64 build.
+#include <cuda_runtime.h>
+
+#include "ooc_device.cuh"
+#include "ooc_internal.h"
+
+namespace ooc {
+
+unsigned long long g_launches = 0;
+
+namespace {
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int SCAN_THREADS = 1024;
+
+inline unsigned grid_for(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// ===========================================================================
+// Exclusive scan (three phases: per-CTA reduce, scan of CTA sums, down-sweep)
+// ===========================================================================
+template <typename T>
+__device__ __forceinline__ T warp_inclusive(T v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T y = __shfl_up_sync(FULL, v, o);
+    if (lane >= o) v += y;
+  }
+  return v;
+}
+
+// Exclusive scan of one value per thread across the CTA; `total` gets the CTA sum.
+template <typename T>
+__device__ __forceinline__ T block_exclusive(T v, T& total) {
+  __shared__ T warp_sums[33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const T inc = warp_inclusive(v);
+  if (lane == 31) warp_sums[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    const T w = lane < nw ? warp_sums[lane] : T(0);
+    const T wi = warp_inclusive(w);
+    if (lane < nw) warp_sums[lane] = wi - w;
+    if (lane == 31) warp_sums[32] = wi;
+  }
+  __syncthreads();
+  const T r = inc - v + warp_sums[warp];
+  total = warp_sums[32];
+  __syncthreads();
+  return r;
+}
+
+template <typename T>
+__global__ void k_scan_reduce(const T* __restrict__ in, uint64_t n, T* __restrict__ partials) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  T v = i < n ? in[i] : T(0);
+  T total;
+  block_exclusive(v, total);
+  if (threadIdx.x == 0) partials[blockIdx.x] = total;
+}
+
+template <typename T>
+__global__ void k_scan_partials(T* partials, uint64_t np) {
+  T carry = 0;
+  for (uint64_t base = 0; base < np; base += blockDim.x) {
+    const uint64_t i = base + threadIdx.x;
+    const T v = i < np ? partials[i] : T(0);
+    T total;
+    const T ex = block_exclusive(v, total);
+    if (i < np) partials[i] = ex + carry;
+    carry += total;
+  }
+}
+
+template <typename T>
+__global__ void k_scan_down(T* data, uint64_t n, const T* __restrict__ partials) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const T v = i < n ? data[i] : T(0);
+  T total;
+  const T ex = block_exclusive(v, total);
+  if (i < n) data[i] = ex + partials[blockIdx.x];
+}
+
+template <typename T>
+void scan_exclusive(T* data, uint64_t n, T* partials, cudaStream_t st) {
+  if (n == 0) return;
+  const unsigned nb = grid_for(n, SCAN_THREADS);
+  k_scan_reduce<T><<<nb, SCAN_THREADS, 0, st>>>(data, n, partials);
+  k_scan_partials<T><<<1, SCAN_THREADS, 0, st>>>(partials, nb);
+  k_scan_down<T><<<nb, SCAN_THREADS, 0, st>>>(data, n, partials);
+  g_launches += 3;
+}
+
+// ===========================================================================
+// Partition binning (partitioner.cpp:101-149 with BBoxBuffer.h:70-84)
+// ===========================================================================
+struct WorldBox {
+  float lo[3], hi[3];
+};
+
+__device__ __forceinline__ WorldBox tri_world_box(const float* __restrict__ tris, uint64_t t, int stride) {
+  const TriVerts tv = load_verts(tris, t, stride);
+  WorldBox b;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    b.lo[a] = smin(tv.v[0][a], smin(tv.v[1][a], tv.v[2][a]));
+    b.hi[a] = smax(tv.v[0][a], smax(tv.v[1][a], tv.v[2][a]));
+  }
+  return b;
+}
+
+// Per axis, the partitions j whose world slab [lo_j, hi_j] passes the
+// reference's inclusive test form one contiguous run [j0, j1].
+__device__ __forceinline__ bool axis_run(float lo, float hi, const float* __restrict__ alo,
+                                         const float* __restrict__ ahi, int PA, int& j0, int& j1) {
+  j0 = -1;
+  j1 = -2;
+  for (int j = 0; j < PA; j++) {
+    const bool ok = !(hi < alo[j]) && !(lo > ahi[j]);
+    if (ok) {
+      if (j0 < 0) j0 = j;
+      j1 = j;
+    }
+  }
+  return j0 >= 0;
+}
+
+__global__ void k_part_count(const float* __restrict__ tris, int stride, uint64_t n_tris,
+                             const float* __restrict__ axis_lo, const float* __restrict__ axis_hi, int pa_bits,
+                             uint32_t n_parts, uint32_t* __restrict__ hist, int use_smem) {
+  extern __shared__ uint32_t sh[];
+  if (use_smem) {
+    for (uint32_t i = threadIdx.x; i < n_parts; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+  }
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n_tris) {
+    const int PA = 1 << pa_bits;
+    const WorldBox b = tri_world_box(tris, t, stride);
+    int x0, x1, y0, y1, z0, z1;
+    if (axis_run(b.lo[0], b.hi[0], axis_lo, axis_hi, PA, x0, x1) &&
+        axis_run(b.lo[1], b.hi[1], axis_lo + PA, axis_hi + PA, PA, y0, y1) &&
+        axis_run(b.lo[2], b.hi[2], axis_lo + 2 * PA, axis_hi + 2 * PA, PA, z0, z1)) {
+      for (int jx = x0; jx <= x1; jx++)
+        for (int jy = y0; jy <= y1; jy++)
+          for (int jz = z0; jz <= z1; jz++) {
+            const uint32_t p = morton_local(jx, jy, jz);
+            if (use_smem) atomicAdd(&sh[p], 1u);
+            else atomicAdd(&hist[p], 1u);
+          }
+    }
+  }
+  if (use_smem) {
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n_parts; i += blockDim.x)
+      if (sh[i]) atomicAdd(&hist[i], sh[i]);
+  }
+}
+
+__global__ void k_part_emit(const float* __restrict__ tris, int stride, uint64_t n_tris,
+                            const float* __restrict__ axis_lo, const float* __restrict__ axis_hi, int pa_bits,
+                            uint32_t n_parts, uint32_t* __restrict__ cursor, uint32_t* __restrict__ items,
+                            int use_smem) {
+  extern __shared__ uint32_t sh[];  // [n_parts] counts, [n_parts] bases
+  uint32_t* cnt = sh;
+  uint32_t* base = sh + n_parts;
+  if (use_smem) {
+    for (uint32_t i = threadIdx.x; i < n_parts; i += blockDim.x) cnt[i] = 0;
+    __syncthreads();
+  }
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int PA = 1 << pa_bits;
+  int x0 = 0, x1 = -1, y0 = 0, y1 = -1, z0 = 0, z1 = -1;
+  bool hit = false;
+  if (t < n_tris) {
+    const WorldBox b = tri_world_box(tris, t, stride);
+    hit = axis_run(b.lo[0], b.hi[0], axis_lo, axis_hi, PA, x0, x1) &&
+          axis_run(b.lo[1], b.hi[1], axis_lo + PA, axis_hi + PA, PA, y0, y1) &&
+          axis_run(b.lo[2], b.hi[2], axis_lo + 2 * PA, axis_hi + 2 * PA, PA, z0, z1);
+  }
+  if (!use_smem) {
+    if (hit)
+      for (int jx = x0; jx <= x1; jx++)
+        for (int jy = y0; jy <= y1; jy++)
+          for (int jz = z0; jz <= z1; jz++) {
+            const uint32_t p = morton_local(jx, jy, jz);
+            items[atomicAdd(&cursor[p], 1u)] = (uint32_t)t;
+          }
+    return;
+  }
+  if (hit)
+    for (int jx = x0; jx <= x1; jx++)
+      for (int jy = y0; jy <= y1; jy++)
+        for (int jz = z0; jz <= z1; jz++) atomicAdd(&cnt[morton_local(jx, jy, jz)], 1u);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < n_parts; i += blockDim.x) {
+    base[i] = cnt[i] ? atomicAdd(&cursor[i], cnt[i]) : 0u;
+    cnt[i] = 0;
+  }
+  __syncthreads();
+  if (hit)
+    for (int jx = x0; jx <= x1; jx++)
+      for (int jy = y0; jy <= y1; jy++)
+        for (int jz = z0; jz <= z1; jz++) {
+          const uint32_t p = morton_local(jx, jy, jz);
+          items[base[p] + atomicAdd(&cnt[p], 1u)] = (uint32_t)t;
+        }
+}
+
+// ===========================================================================
+// Voxelization (voxelizer.cpp:168-306)
+//
+// Pass 0 sets the Morton-ordered occupancy bits of the stripe; pass 1 (payload
+// mode) revisits only set voxels and keeps the smallest passing triangle
+// index per voxel, which is the reference's first-writer-wins rule
+// (voxelizer.cpp:263, 293-299).
+// ===========================================================================
+__device__ __forceinline__ bool item_box(const VoxJob& j, const TriVerts& tv, int lo[3], int hi[3]) {
+  int gmin[3], gmax[3];
+  grid_box(tv, j.unit_div, gmin, gmax);
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    // clamp to the partition (voxelizer.cpp:199-204), then keep the part in this stripe
+    lo[a] = clampi(gmin[a], j.pa[a], j.pb[a]);
+    hi[a] = clampi(gmax[a], j.pa[a], j.pb[a]);
+    lo[a] = lo[a] < j.sa[a] ? j.sa[a] : lo[a];
+    hi[a] = hi[a] > j.sb[a] ? j.sb[a] : hi[a];
+  }
+  return lo[0] <= hi[0] && lo[1] <= hi[1] && lo[2] <= hi[2];
+}
+
+// Rank of bit `b` among the set bits of the leaf level.
+__device__ __forceinline__ uint32_t leaf_rank(const VoxJob& j, uint32_t b) {
+  const uint32_t w = b >> 5, blk = w >> 3;
+  uint32_t r = j.leafscan[blk] - j.leafscan_base;
+  for (uint32_t q = blk * 8; q < w; q++) r += __popc(j.leafbits[q]);
+  return r + __popc(j.leafbits[w] & ((1u << (b & 31)) - 1u));
+}
+
+template <int PASS>
+__device__ __forceinline__ void vox_column(const VoxJob& j, const TriSetup& s, uint32_t tri, int x, int y, int z0,
+                                           int z1) {
+  const float px = __fmul_rn((float)x, j.u);
+  const float py = __fmul_rn((float)y, j.u);
+  if (!pass_xy(s, px, py)) return;
+  const float nxy = plane_xy(s, px, py);
+  const uint32_t mxy = spread3_10((uint32_t)(x - j.sa[0])) | (spread3_10((uint32_t)(y - j.sa[1])) << 1);
+  uint32_t cur_w = 0xffffffffu, acc = 0;
+  for (int z = z0; z <= z1; z++) {
+    const uint32_t m = mxy | (spread3_10((uint32_t)(z - j.sa[2])) << 2);
+    if (PASS == 0) {
+      if (pass_z(s, nxy, px, py, __fmul_rn((float)z, j.u))) {
+        const uint32_t w = m >> 5;
+        if (w != cur_w) {
+          if (acc) atomicOr(&j.leafbits[cur_w], acc);
+          cur_w = w;
+          acc = 0;
+        }
+        acc |= 1u << (m & 31);
+      }
+    } else {
+      const uint32_t word = j.leafbits[m >> 5];
+      if ((word >> (m & 31)) & 1u) {
+        if (pass_z(s, nxy, px, py, __fmul_rn((float)z, j.u))) atomicMin(&j.winners[leaf_rank(j, m)], tri);
+      }
+    }
+  }
+  if (PASS == 0 && acc) atomicOr(&j.leafbits[cur_w], acc);
+}
+
+__device__ __forceinline__ uint64_t item_triangle(const VoxJob& j, uint64_t i) {
+  return j.item_tri ? (uint64_t)j.item_tri[j.ibeg + i] : j.ibeg + i;
+}
+
+// One thread per item; items with at most small_vol candidates are finished
+// here, larger ones get a warp-task count (32 columns per task) in pass 0.
+template <int PASS>
+__global__ void k_vox_small(VoxJob j) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= j.n_items) return;
+  const uint64_t t = item_triangle(j, i);
+  const TriVerts tv = load_verts(j.tris, t, j.stride);
+  int lo[3], hi[3];
+  uint64_t cost = 0;
+  if (item_box(j, tv, lo, hi)) {
+    const uint64_t bx = (uint64_t)(hi[0] - lo[0] + 1), by = (uint64_t)(hi[1] - lo[1] + 1),
+                   bz = (uint64_t)(hi[2] - lo[2] + 1);
+    if (bx * by * bz <= j.small_vol) {
+      TriSetup s;
+      tri_setup(tv, j.u, s);
+      for (int x = lo[0]; x <= hi[0]; x++)
+        for (int y = lo[1]; y <= hi[1]; y++) vox_column<PASS>(j, s, (uint32_t)t, x, y, lo[2], hi[2]);
+    } else {
+      cost = (bx * by + 31) / 32;
+    }
+  }
+  if (PASS == 0) j.task_off[i] = cost;
+}
+
+// Persistent warps pull 32-column tasks of large items from a global counter.
+template <int PASS>
+__global__ void __launch_bounds__(256) k_vox_large(VoxJob j) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t total = j.task_off[j.n_items];
+  for (;;) {
+    unsigned long long task = 0;
+    if (lane == 0) task = atomicAdd(j.task_counter, 1ull);
+    task = __shfl_sync(FULL, task, 0);
+    if (task >= total) break;
+    uint64_t lo_i = 0, hi_i = j.n_items;  // task_off[lo_i] <= task < task_off[hi_i]
+    while (hi_i - lo_i > 1) {
+      const uint64_t mid = (lo_i + hi_i) >> 1;
+      if (j.task_off[mid] <= task) lo_i = mid;
+      else hi_i = mid;
+    }
+    const uint64_t t = item_triangle(j, lo_i);
+    const TriVerts tv = load_verts(j.tris, t, j.stride);
+    int lo[3], hi[3];
+    if (!item_box(j, tv, lo, hi)) continue;  // cannot happen: the task count came from the same box
+    const uint64_t bx = (uint64_t)(hi[0] - lo[0] + 1), by = (uint64_t)(hi[1] - lo[1] + 1);
+    const uint64_t c = (task - j.task_off[lo_i]) * 32 + lane;
+    if (c < bx * by) {
+      TriSetup s;
+      tri_setup(tv, j.u, s);
+      const int x = lo[0] + (int)(c % bx);
+      const int y = lo[1] + (int)(c / bx);
+      vox_column<PASS>(j, s, (uint32_t)t, x, y, lo[2], hi[2]);
+    }
+  }
+}
+
+// ===========================================================================
+// Occupancy pyramid: level l-1 bit i = (byte i of level l != 0); the byte is
+// node i's 8-bit child mask.  Also the popcount of every 256-bit block.
+// ===========================================================================
+__device__ __forceinline__ uint32_t nonzero_bytes(uint32_t w) {
+  const uint32_t t = (((w & 0x7f7f7f7fu) + 0x7f7f7f7fu) | w) & 0x80808080u;
+  return ((t >> 7) & 1u) | ((t >> 14) & 2u) | ((t >> 21) & 4u) | ((t >> 28) & 8u);
+}
+
+__global__ void k_pyramid(uint32_t* __restrict__ bits, uint64_t off_w, uint64_t nblocks, int has_parent,
+                          uint64_t off_wp, uint32_t* __restrict__ counts) {
+  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nblocks) return;
+  const uint4* p = reinterpret_cast<const uint4*>(bits + off_w + 8 * b);
+  const uint4 q0 = p[0], q1 = p[1];
+  const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+  uint32_t c = 0, pw = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    c += __popc(w[k]);
+    pw |= nonzero_bytes(w[k]) << (4 * k);
+  }
+  counts[b] = c;
+  if (has_parent) bits[off_wp + b] = pw;
+}
+
+// Global node index of bit `b` of a level: the concatenated scan already
+// counts every node of the shallower levels.
+__device__ __forceinline__ uint64_t node_index(const uint32_t* __restrict__ bits, const uint32_t* __restrict__ scan,
+                                               const Level& L, uint64_t b) {
+  const uint64_t w = b >> 5, blk = w >> 3;
+  uint32_t r = scan[L.off_b + blk];
+  for (uint64_t q = blk * 8; q < w; q++) r += __popc(bits[L.off_w + q]);
+  return (uint64_t)r + __popc(bits[L.off_w + w] & ((1u << (b & 31)) - 1u));
+}
+
+__device__ __forceinline__ uint32_t child_mask(const uint32_t* __restrict__ bits, const Level& C, uint32_t k) {
+  return (bits[C.off_w + (k >> 2)] >> ((k & 3) * 8)) & 0xffu;
+}
+
+__global__ void k_compact(const uint32_t* __restrict__ bits, const uint32_t* __restrict__ scan, Level L,
+                          uint32_t* __restrict__ keys) {
+  const uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= L.nwords) return;
+  uint32_t word = bits[L.off_w + w];
+  if (!word) return;
+  uint64_t r = node_index(bits, scan, L, w << 5);
+  while (word) {
+    const int b = __ffs(word) - 1;
+    keys[r++] = (uint32_t)((w << 5) | (uint64_t)b);
+    word &= word - 1;
+  }
+}
+
+// ===========================================================================
+// Leaf payload (voxelizer.cpp:295-299, BarycentricCoords.h, main.cpp:373-382)
+// ===========================================================================
+__device__ void payload_color(const TriVerts& tv, const float n[3], int x, int y, int z, float unit_div,
+                              const float* __restrict__ tr, float col[3]) {
+  const float qx = __fdiv_rn((float)x, unit_div);
+  const float qy = __fdiv_rn((float)y, unit_div);
+  const float qz = __fdiv_rn((float)z, unit_div);
+  const float coeffD = -dot3(tv.v[0][0], tv.v[0][1], tv.v[0][2], n[0], n[1], n[2]);
+  const float nn = __fadd_rn(__fadd_rn(__fmul_rn(n[0], n[0]), __fmul_rn(n[1], n[1])), __fmul_rn(n[2], n[2]));
+  const float k = __fdiv_rn(__fadd_rn(dot3(qx, qy, qz, n[0], n[1], n[2]), coeffD), nn);
+  const float ptx = __fsub_rn(qx, __fmul_rn(k, n[0]));
+  const float pty = __fsub_rn(qy, __fmul_rn(k, n[1]));
+  const float ptz = __fsub_rn(qz, __fmul_rn(k, n[2]));
+  // inverse(mat3(v0, v1, v2)) by adjugate over determinant
+  const float a = tv.v[0][0], b = tv.v[1][0], c = tv.v[2][0];
+  const float d = tv.v[0][1], e = tv.v[1][1], f = tv.v[2][1];
+  const float g = tv.v[0][2], h = tv.v[1][2], i = tv.v[2][2];
+  const float C00 = __fsub_rn(__fmul_rn(e, i), __fmul_rn(f, h));
+  const float C01 = __fsub_rn(__fmul_rn(f, g), __fmul_rn(d, i));
+  const float C02 = __fsub_rn(__fmul_rn(d, h), __fmul_rn(e, g));
+  const float det = __fadd_rn(__fadd_rn(__fmul_rn(a, C00), __fmul_rn(b, C01)), __fmul_rn(c, C02));
+  const float r = __fdiv_rn(1.0f, det);
+  const float C10 = __fsub_rn(__fmul_rn(c, h), __fmul_rn(b, i));
+  const float C11 = __fsub_rn(__fmul_rn(a, i), __fmul_rn(c, g));
+  const float C12 = __fsub_rn(__fmul_rn(b, g), __fmul_rn(a, h));
+  const float C20 = __fsub_rn(__fmul_rn(b, f), __fmul_rn(c, e));
+  const float C21 = __fsub_rn(__fmul_rn(c, d), __fmul_rn(a, f));
+  const float C22 = __fsub_rn(__fmul_rn(a, e), __fmul_rn(b, d));
+  const float i00 = __fmul_rn(C00, r), i10 = __fmul_rn(C01, r), i20 = __fmul_rn(C02, r);
+  const float i01 = __fmul_rn(C10, r), i11 = __fmul_rn(C11, r), i21 = __fmul_rn(C12, r);
+  const float i02 = __fmul_rn(C20, r), i12 = __fmul_rn(C21, r), i22 = __fmul_rn(C22, r);
+  const float bx = __fadd_rn(__fadd_rn(__fmul_rn(i00, ptx), __fmul_rn(i01, pty)), __fmul_rn(i02, ptz));
+  const float by = __fadd_rn(__fadd_rn(__fmul_rn(i10, ptx), __fmul_rn(i11, pty)), __fmul_rn(i12, ptz));
+  const float bz = __fadd_rn(__fadd_rn(__fmul_rn(i20, ptx), __fmul_rn(i21, pty)), __fmul_rn(i22, ptz));
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    const float c0 = __ldg(tr + 12 + q), c1 = __ldg(tr + 15 + q), c2 = __ldg(tr + 18 + q);
+    col[q] = __fadd_rn(__fadd_rn(__fmul_rn(bx, c0), __fmul_rn(by, c1)), __fmul_rn(bz, c2));
+  }
+}
+
+__global__ void k_leaf_payload(Pyramid p, EmitJob e) {
+  const Level& L = p.lv[p.depth];
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.n) return;
+  const uint32_t key = e.keys[L.koff + i];
+  uint32_t lx, ly, lz;
+  morton_local_decode(key, lx, ly, lz);
+  const int x = e.origin[0] + (int)lx, y = e.origin[1] + (int)ly, z = e.origin[2] + (int)lz;
+  const uint64_t t = e.winners[i];
+  if (t >= e.n_tris) {  // every set voxel has a passing triangle; anything else is a bug
+    atomicOr(e.flag, 4u);
+    return;
+  }
+  const float* tr = e.tris + t * 21;
+  float* out = e.cache + (L.koff + i) * 6;
+  const float nx = __ldg(tr + 9), ny = __ldg(tr + 10), nz = __ldg(tr + 11);
+  float col[3];
+  if (e.color_mode == 1) {  // COLOR_FIXED
+    col[0] = col[1] = col[2] = 1.0f;
+  } else if (e.color_mode == 2) {  // COLOR_LINEAR: mortonToRGB (svo_builder_util.h:14-18)
+    const float fn = (float)e.gridsize;
+    col[0] = __fdiv_rn((float)z, fn);
+    col[1] = __fdiv_rn((float)y, fn);
+    col[2] = __fdiv_rn((float)x, fn);
+  } else if (e.color_mode == 3) {  // COLOR_NORMAL
+    float a = nx, b = ny, c = nz;
+    normalize3(a, b, c);
+    col[0] = __fdiv_rn(__fadd_rn(a, 1.0f), 2.0f);
+    col[1] = __fdiv_rn(__fadd_rn(b, 1.0f), 2.0f);
+    col[2] = __fdiv_rn(__fadd_rn(c, 1.0f), 2.0f);
+  } else {  // COLOR_FROM_MODEL
+    const TriVerts tv = load_verts(e.tris, t, 21);
+    float n[3];
+    tri_normal(tv, n);
+    payload_color(tv, n, x, y, z, e.unit_div, tr, col);
+  }
+  out[0] = col[0];
+  out[1] = col[1];
+  out[2] = col[2];
+  out[3] = nx;
+  out[4] = ny;
+  out[5] = nz;
+}
+
+// ===========================================================================
+// Octree layout.  Subtree sizes bottom-up, then top-down the index of the
+// first node / data record written inside every subtree; the reference writes
+// a node's 8-child group when the Morton cursor leaves the node's region, so
+// the node file is the post-order of groups (OctreeBuilder.cpp:58-128).
+// ===========================================================================
+__device__ __forceinline__ void average_children(const EmitJob& e, uint32_t mask, uint64_t c0, bool child_leaf,
+                                                 float out[6]) {
+  // OctreeBuilder.cpp:81-99: sum over the 8 slots in child order (null slots
+  // add zero), divide by the non-null count, normalise the normal.
+  float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  float notnull = 0.0f;
+  uint64_t c = c0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    if ((mask >> k) & 1u) {
+      notnull = __fadd_rn(notnull, 1.0f);
+      if (child_leaf && e.binary) {
+#pragma unroll
+        for (int q = 0; q < 6; q++) acc[q] = __fadd_rn(acc[q], 0.0f);
+      } else {
+        const float* cc = e.cache + c * 6;
+#pragma unroll
+        for (int q = 0; q < 6; q++) acc[q] = __fadd_rn(acc[q], cc[q]);
+      }
+      c++;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 6; q++) acc[q] = __fadd_rn(acc[q], 0.0f);
+    }
+  }
+  out[0] = __fdiv_rn(acc[0], notnull);
+  out[1] = __fdiv_rn(acc[1], notnull);
+  out[2] = __fdiv_rn(acc[2], notnull);
+  float tx = __fdiv_rn(acc[3], notnull), ty = __fdiv_rn(acc[4], notnull), tz = __fdiv_rn(acc[5], notnull);
+  normalize3(tx, ty, tz);
+  out[3] = tx;
+  out[4] = ty;
+  out[5] = tz;
+}
+
+__global__ void k_bottom_up(Pyramid p, EmitJob e, int l) {
+  const Level& L = p.lv[l];
+  const Level& C = p.lv[l + 1];
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.n) return;
+  const uint64_t gi = L.koff + i;
+  const uint32_t k = e.keys[gi];
+  const uint32_t mask = child_mask(p.bits, C, k);
+  const int nch = __popc(mask);
+  const uint64_t c0 = node_index(p.bits, p.scan, C, (uint64_t)k << 3);
+  const bool child_leaf = (l + 1 == p.depth);
+  uint32_t sz, dsz;
+  if (child_leaf) {
+    sz = 1u + (uint32_t)nch;
+    dsz = (uint32_t)e.levels + (e.binary ? 0u : (uint32_t)nch);
+  } else {
+    sz = 1u;
+    dsz = (uint32_t)e.levels;
+    for (int q = 0; q < nch; q++) {
+      sz += e.size[c0 + q];
+      dsz += e.dsize[c0 + q];
+    }
+  }
+  e.size[gi] = sz;
+  e.dsize[gi] = dsz;
+  if (e.levels) average_children(e, mask, c0, child_leaf, e.cache + gi * 6);
+}
+
+__global__ void k_set_root(EmitJob e, uint64_t node_base, uint64_t data_base) {
+  e.start[0] = node_base;
+  e.dstart[0] = data_base;
+}
+
+__device__ __forceinline__ void store_data_record(const EmitJob& e, uint64_t idx, uint64_t morton, const float* v) {
+  if (idx < e.data_win_base || idx - e.data_win_base >= e.data_win_len) {
+    atomicOr(e.flag, 2u);
+    return;
+  }
+  uint4* dst = reinterpret_cast<uint4*>(e.data_win + (idx - e.data_win_base) * 32);
+  dst[0] = make_uint4((uint32_t)morton, (uint32_t)(morton >> 32), __float_as_uint(v[0]), __float_as_uint(v[1]));
+  dst[1] = make_uint4(__float_as_uint(v[2]), __float_as_uint(v[3]), __float_as_uint(v[4]), __float_as_uint(v[5]));
+}
+
+__device__ __forceinline__ uint64_t child_offsets(uint32_t mask) {
+  uint64_t off = 0;
+  uint32_t r = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const uint64_t byte = ((mask >> k) & 1u) ? (uint64_t)(r++) : 0xffull;
+    off |= byte << (8 * k);
+  }
+  return off;
+}
+
+__global__ void k_top_down(Pyramid p, EmitJob e, int l) {
+  const Level& L = p.lv[l];
+  const Level& P = p.lv[l - 1];
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.n) return;
+  const uint64_t gi = L.koff + i;
+  const uint32_t k = e.keys[gi];
+  const uint32_t pk = k >> 3;
+  const uint64_t pidx = node_index(p.bits, p.scan, P, pk);
+  const uint64_t c0 = node_index(p.bits, p.scan, L, (uint64_t)pk << 3);
+  const bool leaf = (l == p.depth);
+  const uint64_t pstart = e.start[pidx];
+  uint64_t st = pstart, dst = e.dstart[pidx];
+  for (uint64_t q = c0; q < gi; q++) {
+    if (!leaf) {
+      st += (uint64_t)e.size[q] - 1;
+      dst += e.dsize[q];
+    } else if (!e.binary) {
+      dst += 1;
+    }
+  }
+  const uint32_t pmask = child_mask(p.bits, L, pk);
+  const uint64_t pcb = pstart + (uint64_t)e.size[pidx] - 1 - (uint64_t)__popc(pmask);
+  const uint64_t pos = pcb + (gi - c0);
+  uint64_t r0, r1, r2;
+  if (!leaf) {
+    e.start[gi] = st;
+    e.dstart[gi] = dst;
+    const uint32_t mask = child_mask(p.bits, p.lv[l + 1], k);
+    const uint64_t sz = e.size[gi], dsz = e.dsize[gi];
+    r1 = st + sz - 1 - (uint64_t)__popc(mask);
+    r0 = e.levels ? dst + dsz - 1 : 0;
+    r2 = child_offsets(mask);
+    if (e.levels) store_data_record(e, dst + dsz - 1, 0, e.cache + gi * 6);
+  } else {
+    r0 = e.binary ? 1 : dst;
+    r1 = 0;
+    r2 = ~0ull;
+    if (!e.binary) store_data_record(e, dst, e.stripe_base + k, e.cache + gi * 6);
+  }
+  if (pos < e.node_win_base || pos - e.node_win_base >= e.node_win_len) {
+    atomicOr(e.flag, 1u);
+    return;
+  }
+  uint64_t* rec = e.node_win + (pos - e.node_win_base) * 3;
+  rec[0] = r0;
+  rec[1] = r1;
+  rec[2] = r2;
+}
+
+// Stripe root: child mask and payload for the host, and (with -levels, or a
+// one-voxel stripe in payload mode) the root's own data record.
+__global__ void k_root_info(Pyramid p, EmitJob e, uint64_t data_base, uint32_t* out) {
+  float c[6];
+  for (int q = 0; q < 6; q++) c[q] = e.cache ? e.cache[q] : 0.0f;
+  out[0] = p.depth >= 1 ? child_mask(p.bits, p.lv[1], 0) : 0u;
+  for (int q = 0; q < 6; q++) out[1 + q] = __float_as_uint(c[q]);
+  if (p.depth >= 1) {
+    if (e.levels) store_data_record(e, data_base + e.dsize[0] - 1, 0, c);
+  } else if (!e.binary) {
+    store_data_record(e, data_base, e.stripe_base, c);
+  }
+}
+
+__global__ void k_scatter_records(const uint64_t* __restrict__ src, uint64_t n, int words, uint64_t* __restrict__ dst) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t* s = src + i * (1 + words);
+  uint64_t* d = dst + s[0] * words;
+  for (int q = 0; q < words; q++) d[q] = s[1 + q];
+}
+
+}  // namespace
+
+// ===========================================================================
+// Launch wrappers
+// ===========================================================================
+uint64_t scan_partials_needed(uint64_t n) { return (n + SCAN_THREADS - 1) / SCAN_THREADS + 1; }
+
+void scan_u32_exclusive(uint32_t* data, uint64_t n, uint32_t* partials, cudaStream_t st) {
+  scan_exclusive<uint32_t>(data, n, partials, st);
+}
+void scan_u64_exclusive(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st) {
+  scan_exclusive<unsigned long long>(reinterpret_cast<unsigned long long*>(data), n,
+                                     reinterpret_cast<unsigned long long*>(partials), st);
+}
+
+void launch_part_count(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
+                       int pa_bits, uint64_t n_parts, uint32_t* hist, cudaStream_t st) {
+  if (n_tris == 0) return;
+  const int use_smem = n_parts <= 4096;
+  const size_t smem = use_smem ? n_parts * sizeof(uint32_t) : 0;
+  k_part_count<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
+                                                          (uint32_t)n_parts, hist, use_smem);
+  g_launches++;
+}
+
+void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
+                      int pa_bits, uint64_t n_parts, uint32_t* cursor, uint32_t* items, cudaStream_t st) {
+  if (n_tris == 0) return;
+  const int use_smem = n_parts <= 4096;
+  const size_t smem = use_smem ? 2 * n_parts * sizeof(uint32_t) : 0;
+  k_part_emit<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
+                                                         (uint32_t)n_parts, cursor, items, use_smem);
+  g_launches++;
+}
+
+void launch_vox_small(const VoxJob& j, int pass, cudaStream_t st) {
+  if (j.n_items == 0) return;
+  if (pass == 0) k_vox_small<0><<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
+  else k_vox_small<1><<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
+  g_launches++;
+}
+
+void launch_vox_large(const VoxJob& j, int pass, cudaStream_t st, int num_sms) {
+  if (j.n_items == 0) return;
+  cudaMemsetAsync(j.task_counter, 0, sizeof(unsigned long long), st);
+  const unsigned grid = (unsigned)num_sms * 8;
+  if (pass == 0) k_vox_large<0><<<grid, 256, 0, st>>>(j);
+  else k_vox_large<1><<<grid, 256, 0, st>>>(j);
+  g_launches++;
+}
+
+void launch_pyramid(const Pyramid& p, int level, cudaStream_t st) {
+  const Level& L = p.lv[level];
+  const int has_parent = level > 0;
+  const uint64_t off_wp = has_parent ? p.lv[level - 1].off_w : 0;
+  k_pyramid<<<grid_for(L.nblocks, 256), 256, 0, st>>>(p.bits, L.off_w, L.nblocks, has_parent, off_wp,
+                                                       p.scan + L.off_b);
+  g_launches++;
+}
+
+void launch_compact(const Pyramid& p, int level, uint32_t* keys, cudaStream_t st) {
+  const Level& L = p.lv[level];
+  if (L.n == 0) return;
+  k_compact<<<grid_for(L.nwords, 256), 256, 0, st>>>(p.bits, p.scan, L, keys);
+  g_launches++;
+}
+
+void launch_leaf_payload(const Pyramid& p, const EmitJob& e, int, cudaStream_t st) {
+  const uint64_t n = p.lv[p.depth].n;
+  if (n == 0) return;
+  k_leaf_payload<<<grid_for(n, 256), 256, 0, st>>>(p, e);
+  g_launches++;
+}
+
+void launch_bottom_up(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st) {
+  const uint64_t n = p.lv[level].n;
+  if (n == 0) return;
+  k_bottom_up<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
+  g_launches++;
+}
+
+void launch_set_root(const EmitJob& e, uint64_t node_base, uint64_t data_base, cudaStream_t st) {
+  k_set_root<<<1, 1, 0, st>>>(e, node_base, data_base);
+  g_launches++;
+}
+
+void launch_top_down(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st) {
+  const uint64_t n = p.lv[level].n;
+  if (n == 0) return;
+  k_top_down<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
+  g_launches++;
+}
+
+void launch_root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base, uint32_t* out, cudaStream_t st) {
+  k_root_info<<<1, 1, 0, st>>>(p, e, data_base, out);
+  g_launches++;
+}
+
+void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st) {
+  if (n == 0) return;
+  k_scatter_records<<<grid_for(n, 128), 128, 0, st>>>(src, n, words, dst);
+  g_launches++;
+}
+
+}  // namespace ooc

@@ -1,0 +1,229 @@
+// svo_builder / svo_builder_binary: drop-in command lines for the reference's
+// executables (src/svo_builder/main.cpp), running the path on the GPU through
+// libooc_svo_gpu.so.  Built twice; -DOOC_CLI_BINARY gives svo_builder_binary.
+//
+// Flags, messages, output file names and exit codes follow main.cpp:100-398:
+// every error prints a message and exits with status 0, as the reference does.
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <string>
+
+#include "ooc_svo_gpu.h"
+
+namespace {
+
+const char* kVersion = "1.6.4";
+
+std::string filename;
+uint64_t gridsize = 1024;      // main.cpp:30
+uint64_t memory_limit = 2048;  // main.cpp:31
+int color = OOC_COLOR_MODEL;
+bool generate_levels = false;
+bool verbose = false;
+
+void print_info() {
+  std::cout << "--------------------------------------------------------------------" << std::endl;
+#ifdef OOC_CLI_BINARY
+  std::cout << "Out-Of-Core SVO Builder " << kVersion << " - Geometry only version (GB300)" << std::endl;
+#else
+  std::cout << "Out-Of-Core SVO Builder " << kVersion << " (GB300)" << std::endl;
+#endif
+  std::cout << "--------------------------------------------------------------------" << std::endl << std::endl;
+}
+
+void print_help() {
+  std::cout << "Example: svo_builder -f /home/user/bunny.tri" << std::endl << std::endl;
+  std::cout << "All available program options:" << std::endl << std::endl;
+  std::cout << "-f <filename.tri>     Path to a .tri input file." << std::endl;
+  std::cout << "-s <gridsize>         Voxel gridsize, should be a power of 2. Default 1024." << std::endl;
+  std::cout << "-l <memory_limit>     Memory limit for process, in Mb. Default 2048." << std::endl;
+  std::cout << "-levels               Generate intermediary voxel levels by averaging voxel data" << std::endl;
+  std::cout << "-c <option>           Coloring of voxels (Options: model (default), fixed, linear, normal)" << std::endl;
+  std::cout << "-d <percentage>       Accepted for compatibility; does not change the output" << std::endl;
+  std::cout << "-v                    Be very verbose." << std::endl;
+  std::cout << "-h                    Print help and exit." << std::endl;
+}
+
+void print_invalid() {
+  std::cout << "Not enough or invalid arguments, please try again." << std::endl;
+  std::cout << "At the bare minimum, I need a path to a .TRI file" << std::endl << std::endl;
+  print_help();
+}
+
+bool is_pow2(unsigned int x) { return x != 0 && !(x & (x - 1)); }
+
+// parseProgramParameters (main.cpp:100-196)
+void parse(int argc, char** argv) {
+  std::cout << "Reading program parameters ..." << std::endl;
+  if (argc < 3) {
+    print_invalid();
+    std::exit(0);
+  }
+  for (int i = 1; i < argc; i++) {
+    const std::string a = argv[i];
+    const bool has_next = i + 1 < argc;
+    if (a == "-f" && has_next) {
+      filename = argv[i + 1];
+      if (filename.find(".tri") == std::string::npos) {
+        std::cout << "Data filename does not end in .tri - I only support that file format" << std::endl;
+        print_invalid();
+        std::exit(0);
+      }
+      i++;
+    } else if (a == "-s" && has_next) {
+      gridsize = (uint64_t)std::atoi(argv[i + 1]);
+      if (!is_pow2((unsigned int)gridsize)) {
+        std::cout << "Requested gridsize is not a power of 2" << std::endl;
+        print_invalid();
+        std::exit(0);
+      }
+      i++;
+    } else if (a == "-l" && has_next) {
+      const long v = std::atoi(argv[i + 1]);
+      if (v <= 1) {
+        std::cout << "Requested memory limit is nonsensical. Use a value >= 1" << std::endl;
+        print_invalid();
+        std::exit(0);
+      }
+      memory_limit = (uint64_t)v;
+      i++;
+    } else if (a == "-d" && has_next) {
+      const int percent = std::atoi(argv[i + 1]);
+      if (percent / 100.0f < 0) {
+        std::cout << "Requested data memory limit is nonsensical. Use a value > 0" << std::endl;
+        print_invalid();
+        std::exit(0);
+      }
+      i++;
+    } else if (a == "-v") {
+      verbose = true;
+    } else if (a == "-levels") {
+      generate_levels = true;
+    } else if (a == "-c" && has_next) {
+      const std::string c = argv[i + 1];
+#ifdef OOC_CLI_BINARY
+      (void)c;
+      std::cout << "You asked to generate colors, but we're only doing binary voxelisation." << std::endl;
+#else
+      if (c == "model") color = OOC_COLOR_MODEL;
+      else if (c == "linear") color = OOC_COLOR_LINEAR;
+      else if (c == "normal") color = OOC_COLOR_NORMAL;
+      else if (c == "fixed") color = OOC_COLOR_FIXED;
+      else std::cout << "Unrecognized color switch: " << c << ", so reverting to colors from model." << std::endl;
+#endif
+      i++;
+    } else if (a == "-h") {
+      print_help();
+      std::exit(0);
+    } else {
+      print_invalid();
+      std::exit(0);
+    }
+  }
+  if (verbose) {
+    std::cout << "  filename: " << filename << std::endl;
+    std::cout << "  gridsize: " << gridsize << std::endl;
+    std::cout << "  memory limit: " << memory_limit << std::endl;
+    std::cout << "  generate levels: " << generate_levels << std::endl;
+  }
+}
+
+// readTriHeader's checks (main.cpp:244-267)
+void check_tri(const std::string& fn) {
+  std::cout << "Parsing tri header " << fn << " ..." << std::endl;
+  std::ifstream f(fn.c_str());
+  if (!f) {
+    std::cout << "  Error: file " << fn << " does not exist." << std::endl;
+    std::exit(0);
+  }
+  std::string tok;
+  int geo = 0;
+  bool seen_end = false;
+  while (f >> tok) {
+    if (tok == "geo_only") f >> geo;
+    if (tok == "END") {
+      seen_end = true;
+      break;
+    }
+  }
+  const std::string base = fn.substr(0, fn.find_last_of("."));
+  std::ifstream d((base + ".tridata").c_str());
+  if (!seen_end || !d) {
+    std::cout << "Not all required .tri or .tridata files exist. Please regenerate using tri_convert." << std::endl;
+    std::exit(0);
+  }
+#ifdef OOC_CLI_BINARY
+  if (!geo) {
+    std::cout << "You're using a .tri file which contains more than just geometry with a geometry-only SVO Builder! "
+                 "Regenerate that .tri file using tri_convert_binary."
+              << std::endl;
+    std::exit(0);
+  }
+#else
+  if (geo) {
+    std::cout << "You're using a .tri file which contains only geometry with the regular SVO Builder! Regenerate "
+                 "that .tri file using tri_convert."
+              << std::endl;
+    std::exit(0);
+  }
+#endif
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  const auto t0 = std::chrono::steady_clock::now();
+  print_info();
+  parse(argc, argv);
+  check_tri(filename);
+  const uint64_t P = ooc_estimate_partitions(gridsize, memory_limit);
+  std::cout << "Partitioning data into " << P << " partitions ... ";
+  std::cout.flush();
+
+  ooc_ctx* ctx = nullptr;
+  if (ooc_ctx_create(0, &ctx) != OOC_OK) {
+    std::cout << std::endl << "No CUDA device available." << std::endl;
+    return 0;
+  }
+  ooc_set_phase_timing(ctx, 1);
+  ooc_build_params prm = {};
+  prm.gridsize = gridsize;
+  prm.memory_limit_mb = memory_limit;
+#ifdef OOC_CLI_BINARY
+  prm.geometry_only = 1;
+#else
+  prm.geometry_only = 0;
+#endif
+  prm.color_mode = color;
+  prm.generate_levels = generate_levels ? 1 : 0;
+  ooc_build_info info = {};
+  char out_base[4096];
+  const int rc = ooc_build_files(ctx, filename.c_str(), &prm, out_base, sizeof(out_base), &info);
+  std::cout << "done." << std::endl;
+  if (rc != OOC_OK) {
+    std::cout << "Build failed (" << rc << "): " << ooc_last_error(ctx) << std::endl;
+    ooc_ctx_destroy(ctx);
+    return 0;
+  }
+  std::cout << "Voxelized and built " << info.n_stripes << " stripe(s) on the GPU" << std::endl;
+  std::cout << "done" << std::endl;
+  std::cout << "Total amount of voxels: " << info.n_filled << std::endl;
+  float ms[6] = {0, 0, 0, 0, 0, 0};
+  ooc_phase_times(ctx, ms, 6);
+  ooc_ctx_destroy(ctx);
+  const double main_ms =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  std::cout << "Total MAIN time      : " << main_ms << " ms." << std::endl;
+  std::cout << "GPU PHASES (device time)" << std::endl;
+  std::cout << "  partitioning        : " << ms[0] << " ms." << std::endl;
+  std::cout << "  voxelizing          : " << ms[1] << " ms." << std::endl;
+  std::cout << "  occupancy pyramid   : " << ms[2] << " ms." << std::endl;
+  std::cout << "  octree layout       : " << ms[3] << " ms." << std::endl;
+  std::cout << "  host<->device copies: " << ms[4] << " ms." << std::endl;
+  std::cout << "  whole build         : " << ms[5] << " ms." << std::endl;
+  std::cout << "Output: " << out_base << ".octree" << std::endl;
+  return 0;
+}

@@ -1,0 +1,122 @@
+"""GPU path against the CPU oracle on the same seeded inputs (through the C ABI).
+
+Bar: node files byte-identical; data files identical field by field with FP32
+compared by bit pattern, except that NaN equals NaN (NaN bits differ between
+x86-64, AArch64 and the GPU even for the reference itself).
+"""
+import numpy as np
+import pytest
+
+import pyoracle
+from ooc_svo_builder_gb300 import make_params, octree, tri
+
+pytestmark = pytest.mark.gpu
+
+
+def run_both(builder, tris, N, limit=2048, color="model", levels=False, bbox_max=(1.0, 1.0, 1.0)):
+    binary = tris.shape[1] == 9
+    prm = make_params(N, limit, geometry_only=binary, color=color, levels=levels, bbox_max=bbox_max)
+    got = builder.build(tris, prm)
+    nodes, data, info = pyoracle.build(tris, N, limit, color=color, levels=levels, bbox_max=bbox_max)
+    want = octree.Octree(N, nodes, data)
+    return got, want, info
+
+
+def assert_same(got, want, info):
+    d = octree.diff(got.tree, want)
+    assert not d, "\n".join(d)
+    assert got.info["n_filled"] == info["n_filled"]
+    assert got.info["n_partitions"] == info["n_partitions"]
+    assert got.info["n_nodes"] == want.nodes.shape[0]
+    assert got.info["n_data"] == want.data.shape[0]
+
+
+@pytest.mark.parametrize("N", [1, 2, 8, 64, 256])
+def test_icosphere_binary(builder, N):
+    t = tri.icosphere_tris(4)
+    assert_same(*run_both(builder, t, N))
+
+
+@pytest.mark.parametrize("N,limit", [(256, 2), (512, 2), (128, 2048)])
+def test_partitions_binary(builder, N, limit):
+    t = tri.random_tris(3000, 11, False, lo=-0.05, hi=1.05, max_edge=0.15)
+    got, want, info = run_both(builder, t, N, limit)
+    assert_same(got, want, info)
+
+
+@pytest.mark.parametrize("color", ["model", "fixed", "linear", "normal"])
+@pytest.mark.parametrize("levels", [False, True])
+def test_payload_modes(builder, color, levels):
+    t = tri.icosphere_tris(3, payload=True)
+    assert_same(*run_both(builder, t, 64, color=color, levels=levels))
+
+
+def test_binary_levels(builder):
+    t = tri.icosphere_tris(3)
+    assert_same(*run_both(builder, t, 64, levels=True))
+
+
+@pytest.mark.parametrize("levels", [False, True])
+def test_payload_partitions(builder, levels):
+    t = tri.random_tris(2000, 5, True, lo=-0.1, hi=1.1, max_edge=0.1)
+    assert_same(*run_both(builder, t, 256, limit=2, levels=levels))
+
+
+def test_large_triangles(builder):
+    # bounding boxes up to the whole grid: the warp-task path
+    t = tri.random_tris(40, 3, True, lo=0.0, hi=1.0, max_edge=1.5)
+    assert_same(*run_both(builder, t, 128))
+
+
+def test_overlapping_first_writer(builder):
+    # many coincident triangles with different colours: the payload must come
+    # from the first one in stream order (voxelizer.cpp:263)
+    base = tri.random_tris(50, 9, True, max_edge=0.2)
+    rng = np.random.default_rng(4)
+    reps = np.repeat(base, 4, axis=0)
+    reps[:, 12:21] = rng.random((reps.shape[0], 9), dtype=np.float32)
+    assert_same(*run_both(builder, reps, 64, levels=True))
+
+
+def test_degenerate_triangles(builder):
+    rng = np.random.default_rng(8)
+    a = rng.random((100, 3), dtype=np.float32)
+    b = rng.random((100, 3), dtype=np.float32)
+    pts = np.stack([a, a, b], 1).reshape(100, 9)             # two equal vertices
+    mid = ((a + b) * np.float32(0.5)).astype(np.float32)
+    line = np.stack([a, mid, b], 1).reshape(100, 9)          # collinear
+    same = np.stack([a, a, a], 1).reshape(100, 9)            # a point
+    t = np.concatenate([pts, line, same], 0).astype(np.float32)
+    assert_same(*run_both(builder, t, 64))
+    col = rng.random((300, 12), dtype=np.float32)
+    tp = np.concatenate([t, col[:, :3], col[:, 3:]], 1).astype(np.float32)
+    assert_same(*run_both(builder, tp, 32, levels=True))
+
+
+def test_grid_aligned_vertices(builder):
+    # vertices exactly on voxel faces: truncation puts max in the next cell
+    g = np.arange(0, 17, dtype=np.float32) / np.float32(16)
+    rng = np.random.default_rng(12)
+    idx = rng.integers(0, 17, size=(500, 9))
+    t = g[idx].astype(np.float32)
+    assert_same(*run_both(builder, t, 16))
+    assert_same(*run_both(builder, t, 64, limit=2048))
+
+
+def test_empty_mesh(builder):
+    t = np.zeros((0, 9), np.float32)
+    assert_same(*run_both(builder, t, 32))
+    tp = np.zeros((0, 21), np.float32)
+    assert_same(*run_both(builder, tp, 32, levels=True))
+
+
+def test_outside_grid(builder):
+    # triangles partly or fully outside [0, 1]^3 are clamped to the partition
+    t = tri.random_tris(1000, 21, True, lo=-0.4, hi=1.4, max_edge=0.3)
+    assert_same(*run_both(builder, t, 64))
+    assert_same(*run_both(builder, tri.to_binary(t), 256, limit=2))
+
+
+def test_non_unit_bbox(builder):
+    t = tri.random_tris(800, 31, False, lo=0.0, hi=3.0, max_edge=0.5)
+    assert_same(*run_both(builder, t, 128, bbox_max=(3.0, 3.0, 3.0)))
