@@ -1,0 +1,81 @@
+"""Pin the CPU oracle: against the golden fixtures made by the reference itself, and
+(where the reference sources are present) against the reference build on fresh seeds."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import golden_cases
+import pyoracle
+from ooc_svo_builder_gb300 import octree, tri
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("name", golden_cases.names())
+def test_oracle_matches_golden(name):
+    tris, meta, want = golden_cases.load(name)
+    nodes, data, info = pyoracle.build(tris, meta["s"], meta.get("l", 2048), color=meta.get("c", "model"),
+                                       levels=meta.get("levels", False))
+    got = octree.Octree(meta["s"], nodes, data)
+    d = octree.diff(got, want)
+    assert not d, "\n".join(d)
+    assert info["n_partitions"] == meta["n_partitions"]
+    assert info["n_filled"] == meta["n_filled"]
+    assert octree.header_text(meta["s"], nodes.shape[0], data.shape[0]) == meta["header"]
+
+
+def test_golden_set_is_present():
+    assert len(golden_cases.names()) >= 15
+
+
+def _reference_available(binary):
+    return os.path.exists(pyoracle.ref_binary(binary))
+
+
+def _run_ref(tmp_path, tris, N, limit, extra=()):
+    base = str(tmp_path / "m")
+    tri.write_tri(base, tris)
+    exe = pyoracle.ref_binary(tris.shape[1] == 9)
+    out = subprocess.run([exe, "-f", base + ".tri", "-s", str(N), "-l", str(limit), *extra], cwd=str(tmp_path),
+                         stdout=subprocess.PIPE, text=True, check=True).stdout
+    P = int([ln for ln in out.splitlines() if ln.startswith("Partitioning data into")][0].split()[3])
+    return octree.read_octree(base + "%d_%d" % (N, P))
+
+
+@pytest.mark.parametrize("seed,N,limit,payload,extra", [
+    (201, 128, 2048, False, ()), (202, 256, 2, False, ()), (203, 64, 2048, True, ()),
+    (204, 64, 2048, True, ("-levels",)), (205, 128, 2, True, ("-c", "linear")),
+    (206, 64, 2048, True, ("-c", "normal", "-levels")), (207, 512, 2, False, ("-levels",)),
+])
+def test_oracle_matches_reference_build(tmp_path, seed, N, limit, payload, extra):
+    if not _reference_available(not payload):
+        pytest.skip("reference build not present (make -C oracle ref needs the reference sources)")
+    tris = tri.random_tris(1500, seed, payload, lo=-0.1, hi=1.1, max_edge=0.2)
+    want = _run_ref(tmp_path, tris, N, limit, extra)
+    color = extra[extra.index("-c") + 1] if "-c" in extra else "model"
+    nodes, data, _ = pyoracle.build(tris, N, limit, color=color, levels="-levels" in extra)
+    d = octree.diff(octree.Octree(N, nodes, data), want)
+    assert not d, "\n".join(d)
+
+
+def test_reference_optimisation_levels_agree(tmp_path):
+    """The reference has undefined behaviour in its uint_fast32_t& casts; -O0 and the
+    recipe's -O3 -fno-strict-aliasing must give the same octree."""
+    src = "/root/reference/src/svo_builder"
+    if not (os.path.isdir(src) and _reference_available(True)):
+        pytest.skip("reference sources not present")
+    exe = str(tmp_path / "ref_O0")
+    inc = ["-I", os.path.join(ROOT, "oracle", "glm_shim"), "-I", "/root/reference/src/libs/libtri/include",
+           "-I", "/root/reference/src/libs/libmorton/include"]
+    srcs = [os.path.join(src, f) for f in ("main.cpp", "OctreeBuilder.cpp", "partitioner.cpp", "voxelizer.cpp")]
+    subprocess.run(["g++", "-std=c++11", "-O0", "-ffp-contract=off", "-w", "-DBINARY_VOXELIZATION", *inc, *srcs,
+                    "-o", exe], check=True)
+    tris = tri.random_tris(800, 301, False, lo=-0.1, hi=1.1, max_edge=0.2)
+    a = _run_ref(tmp_path, tris, 256, 2)
+    base = str(tmp_path / "m")
+    subprocess.run([exe, "-f", base + ".tri", "-s", "256", "-l", "2"], cwd=str(tmp_path), stdout=subprocess.PIPE,
+                   check=True)
+    b = octree.read_octree(base + "256_8")
+    assert not octree.diff(a, b)
