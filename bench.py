@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Benchmark of the GPU partition -> voxelize -> SVO-build path.
+
+Workload (default): configuration 2 -- payload-mode ``svo_builder -s 1024 -l 2048
+-c model`` (one partition) on a seeded 1024x1024-vertex value-noise heightfield,
+2,093,058 FP32 triangles (176 MB of .tridata, larger than the 129 MB L2).
+A step is one complete build: voxelization, payload, octree layout and records.
+
+* ``value``: Mtri/s with the triangles resident in HBM (``ooc_build_device``),
+  CUDA events on the build stream around exactly ``--steps`` builds.
+* ``e2e``: the same metric through ``ooc_build`` (the C ABI call the CLI uses):
+  host->device copy of the pinned triangles and device->host copy of the node
+  and data files inside the timed region, wall clock.
+* ``roofline``: the dominant kernel, timed live with CUDA events in the timed
+  region; algorithmic bytes per launch from the workload.
+* ``cpu_baseline``: the CPU oracle (a plain-C restatement of the reference,
+  single-threaded like the reference) on the same mesh.
+
+``--impl reference`` times the reference's CPU path (the oracle port; the
+reference sources are not available on the GPU host) on the same workload.
+Multi-GPU (torchrun): independent replicas, one mesh per rank, max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from ooc_svo_builder_gb300 import tri  # noqa: E402
+
+HEIGHTFIELD_N = 1024
+WORKLOADS = {
+    "heightfield1024": dict(gridsize=1024, limit=2048, payload=True, color="model",
+                            desc="configuration 2: payload svo_builder -s 1024 -l 2048 -c model on a 1024x1024-vertex "
+                                 "value-noise heightfield (2,093,058 triangles, one partition)"),
+    "icosphere256": dict(gridsize=256, limit=2048, payload=False, color="model",
+                         desc="configuration 1: svo_builder_binary -s 256 -l 2048 on a subdivision-5 icosphere "
+                              "(20,480 triangles)"),
+}
+
+
+def make_mesh(name: str) -> np.ndarray:
+    if name == "heightfield1024":
+        return tri.heightfield_tris(HEIGHTFIELD_N, seed=2, payload=True)
+    if name == "icosphere256":
+        return tri.icosphere_tris(5, radius=0.4, jitter=0.002, seed=1)
+    raise SystemExit("unknown workload " + name)
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_port_time(tris, w, budget_s: float, max_runs: int, min_runs: int = 1):
+    """Time the oracle port on the whole mesh; returns (seconds per build, runs)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    times = []
+    t_start = time.perf_counter()
+    while len(times) < max_runs and (len(times) < min_runs or time.perf_counter() - t_start < budget_s):
+        t0 = time.perf_counter()
+        pyoracle.build(tris, w["gridsize"], w["limit"], color=w["color"])
+        times.append(time.perf_counter() - t0)
+    return statistics.mean(times), len(times)
+
+
+def algorithmic_bytes(kernel: str, n_tris: int, info: dict, S: int, payload: bool) -> float:
+    """Minimum DRAM bytes one launch of `kernel` must move for this workload."""
+    tri_bytes = 84 if payload else 36
+    leaf_words = S // 32
+    if kernel in ("vox_small_occupancy", "vox_small_winner", "vox_large_occupancy", "vox_large_winner"):
+        # vertices of every triangle (36 B) + the task count per item (8 B)
+        return n_tris * (36 + 8)
+    if kernel == "pyramid":  # leaf level dominates: read bits, write parent bits + block counts
+        return leaf_words * 4 * (1 + 1 / 8 + 1 / 8)
+    if kernel == "compact":
+        return leaf_words * 4 + info["n_nodes"] * 4
+    if kernel == "leaf_payload":
+        return info["n_filled"] * (4 + 4 + tri_bytes + 24)
+    if kernel in ("top_down", "bottom_up"):
+        return info["n_nodes"] * (4 + 4 + 4 + 8 + 8 + 24) + info["n_data"] * 32
+    return 0.0
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import ooc_svo_builder_gb300 as ooc
+
+    w = WORKLOADS[args.workload]
+    torch.cuda.set_device(local)
+    tris = make_mesh(args.workload)
+    T = tris.shape[0]
+    prm = ooc.make_params(w["gridsize"], w["limit"], geometry_only=not w["payload"], color=w["color"])
+    d_tris = torch.from_numpy(tris).to(f"cuda:{local}")
+    h_tris = torch.from_numpy(tris).pin_memory()
+    stream = torch.cuda.Stream(device=local)
+    b = ooc.Builder(local)
+
+    # warm-up (also sizes every device buffer)
+    for _ in range(args.warmup):
+        info = b.build_device(d_tris.data_ptr(), T, prm, stream.cuda_stream)
+    torch.cuda.synchronize()
+    # one profiling build: phases and every kernel (outside the timed region)
+    b.set_phase_timing(True)
+    b.set_kernel_timing("*")
+    info = b.build_device(d_tris.data_ptr(), T, prm, stream.cuda_stream)
+    phases = b.phase_times()
+    kt = b.kernel_times()
+    b.set_phase_timing(False)
+    dominant = max(kt.items(), key=lambda kv: kv[1][0])[0] if kt else None
+    b.set_kernel_timing(dominant)
+
+    # ---- timed region: device-resident input ----
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    launches = 0
+    dom_ms, dom_n = 0.0, 0
+    ev0.record(stream)
+    for _ in range(args.steps):
+        info = b.build_device(d_tris.data_ptr(), T, prm, stream.cuda_stream)
+        launches += b.kernel_launches()
+        ms, n = b.kernel_times().get(dominant, (0.0, 0))
+        dom_ms += ms
+        dom_n += n
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = sampler.stop()
+    ms_total = max_over_ranks(ev0.elapsed_time(ev1), world)
+    b.set_kernel_timing(None)
+    ms_step = ms_total / args.steps
+    value = world * T / (ms_step / 1e3) / 1e6
+    nodes_per_s = world * info["n_nodes"] / (ms_step / 1e3)
+
+    # ---- end to end through the C ABI: pinned host triangles in, host octree out ----
+    got = {"n": 0}
+
+    def sink(user, kind, ptr, n):
+        got["n"] += n
+        return 0
+
+    cb = ooc.SINK(sink)
+    for _ in range(max(1, args.warmup)):
+        b.build_ptr(h_tris.data_ptr(), T, prm, cb)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_info = b.build_ptr(h_tris.data_ptr(), T, prm, cb)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    barrier(world)
+    e2e_value = world * T / (e2e_s / args.steps) / 1e6
+    stripes = e2e_info["n_stripes"]
+    h2d = T * tris.shape[1] * 4
+    # the stripe spans are copied back; header records and the stripe roots are written on the host
+    payload = w["payload"]
+    d2h = (e2e_info["n_nodes"] - stripes) * 24 + (e2e_info["n_data"] - (1 if payload else 2)) * 32 + stripes * 36
+
+    # ---- roofline of the dominant kernel ----
+    peaks = measured_peaks()
+    S = min(w["gridsize"] ** 3, 1 << 30)
+    alg = algorithmic_bytes(dominant, T, info, S, payload) if dominant else 0.0
+    per_launch_ms = dom_ms / dom_n if dom_n else float("nan")
+    launches_per_build = kt.get(dominant, (0, 1))[1] if dominant else 1
+    alg_per_launch = alg / max(1, launches_per_build)
+    achieved = alg_per_launch / (per_launch_ms / 1e3) / 1e9 if dom_n else None
+    roofline = {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": args.traffic,
+                "peak_source": peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
+                "per_launch_ms": per_launch_ms, "algorithmic_bytes_per_launch": alg_per_launch}
+
+    line = {
+        "metric": "Mtri/s", "value": value, "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w["desc"], "name": args.workload, "gridsize": w["gridsize"],
+                   "memory_limit_mb": w["limit"], "n_triangles": T, "mode": "payload" if payload else "binary",
+                   "partitions": info["n_partitions"], "stripes": info["n_stripes"],
+                   "l2": "inputs larger than L2 (%.0f MB of triangles per step; L2 129 MB)" % (h2d / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "svo_nodes_per_s": nodes_per_s, "n_nodes": info["n_nodes"], "n_data": info["n_data"],
+        "n_filled": info["n_filled"],
+        "e2e": {"value": e2e_value, "unit": "Mtri/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_s / args.steps * 1e3},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "phases_ms": phases,
+        "kernels_ms": {k: v[0] for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])},
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sec, runs = cpu_port_time(tris, w, budget_s=10.0, max_runs=8)
+        line["cpu_baseline"] = {"value": T / sec / 1e6, "unit": "Mtri/s", "cores": 1, "kind": "port",
+                                "sample": "whole %s mesh (%d triangles), %d build(s), mean; single thread like the "
+                                          "reference" % (args.workload, T, runs)}
+    b.close()
+    return line
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    w = WORKLOADS[args.workload]
+    tris = make_mesh(args.workload)
+    T = tris.shape[0]
+    # warm-up builds, then the timed steps; one step = one whole build of the mesh
+    cpu_port_time(tris, w, budget_s=0.0, max_runs=args.warmup, min_runs=args.warmup)
+    sec, runs = cpu_port_time(tris, w, budget_s=0.0, max_runs=args.steps, min_runs=args.steps)
+    value = T / sec / 1e6
+    return {
+        "metric": "Mtri/s", "value": value, "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": w["desc"], "name": args.workload, "gridsize": w["gridsize"],
+                   "memory_limit_mb": w["limit"], "n_triangles": T},
+        "cpu_baseline": {"value": value, "unit": "Mtri/s", "cores": 1, "kind": "port",
+                         "sample": "whole mesh per step, %d steps" % runs},
+        "e2e": {"value": value, "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="heightfield1024", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per launch of the dominant kernel from an ncu capture")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        line = run_reference(args, world, rank)
+    else:
+        line = run_ours(args, world, rank, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -109,6 +109,9 @@ int ooc_build_device(ooc_ctx* ctx, const ooc_build_params* params, const float* 
 /* Device pointers to the node and data files produced by the last
  * ooc_build_device call of `ctx`; valid until the next build on `ctx`. */
 int ooc_result_device(ooc_ctx* ctx, const void** nodes_device, const void** data_device);
+/* Copy the last ooc_build_device result to host memory: n_nodes * 24 bytes to
+ * `nodes_host` and n_data * 32 bytes to `data_host` (either may be NULL). */
+int ooc_result_copy(ooc_ctx* ctx, void* nodes_host, void* data_host);
 
 /* Device time in milliseconds of each phase of the last build of `ctx`
  * (CUDA events on the build stream): [0] partition binning, [1] voxelization
@@ -121,6 +124,15 @@ int ooc_phase_times(const ooc_ctx* ctx, float* ms, int32_t n);
 
 /* Launch count of this library's kernels in the last build of `ctx`. */
 uint64_t ooc_kernel_launches(const ooc_ctx* ctx);
+
+/* Per-kernel CUDA-event timing of later builds on `ctx`: `kernel` names one
+ * kernel (e.g. "vox_small_occupancy"), "*" selects all, NULL or "" turns it
+ * off.  Each timed launch is bracketed by two events on the build stream. */
+int ooc_set_kernel_timing(ooc_ctx* ctx, const char* kernel);
+/* Entry `index` (0-based) of the last build's per-kernel timing: kernel name
+ * (valid until the next build), summed device milliseconds, launch count.
+ * Returns OOC_ERR_INVALID past the last entry. */
+int ooc_kernel_time(const ooc_ctx* ctx, int32_t index, const char** name, float* total_ms, uint64_t* launches);
 
 /* File front end used by the svo_builder CLIs: reads <base>.tri/.tridata and
  * writes <base><gridsize>_<npartitions>.octree/.octreenodes/.octreedata

@@ -25,8 +25,8 @@ PHASES = ("partition", "voxelize", "pyramid", "octree", "copies", "build")
 
 # Every symbol declared in include/ooc_svo_gpu.h.
 EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_partitions", "ooc_build",
-           "ooc_build_device", "ooc_result_device", "ooc_set_phase_timing", "ooc_phase_times",
-           "ooc_kernel_launches", "ooc_build_files")
+           "ooc_build_device", "ooc_result_device", "ooc_result_copy", "ooc_set_phase_timing", "ooc_phase_times",
+           "ooc_kernel_launches", "ooc_build_files", "ooc_set_kernel_timing", "ooc_kernel_time")
 
 
 class BuildParams(ctypes.Structure):
@@ -78,6 +78,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_build_device.restype = ctypes.c_int
     lib.ooc_result_device.argtypes = [ctypes.c_void_p, P(ctypes.c_void_p), P(ctypes.c_void_p)]
     lib.ooc_result_device.restype = ctypes.c_int
+    lib.ooc_result_copy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.ooc_result_copy.restype = ctypes.c_int
     lib.ooc_set_phase_timing.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     lib.ooc_set_phase_timing.restype = ctypes.c_int
     lib.ooc_phase_times.argtypes = [ctypes.c_void_p, P(ctypes.c_float), ctypes.c_int32]
@@ -87,6 +89,11 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_build_files.argtypes = [ctypes.c_void_p, ctypes.c_char_p, P(BuildParams), ctypes.c_char_p,
                                     ctypes.c_uint64, P(BuildInfo)]
     lib.ooc_build_files.restype = ctypes.c_int
+    lib.ooc_set_kernel_timing.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    lib.ooc_set_kernel_timing.restype = ctypes.c_int
+    lib.ooc_kernel_time.argtypes = [ctypes.c_void_p, ctypes.c_int32, P(ctypes.c_char_p), P(ctypes.c_float),
+                                    P(ctypes.c_uint64)]
+    lib.ooc_kernel_time.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -164,6 +171,24 @@ class Builder:
     def kernel_launches(self) -> int:
         return int(self.lib.ooc_kernel_launches(self.h))
 
+    def set_kernel_timing(self, kernel):
+        """Time `kernel` ("*" = all, None = off) with CUDA events in later builds."""
+        self._check(self.lib.ooc_set_kernel_timing(self.h, kernel.encode() if kernel else None))
+
+    def kernel_times(self) -> dict:
+        """{kernel: (total device ms, launches)} of the last build."""
+        out = {}
+        i = 0
+        while True:
+            name = ctypes.c_char_p()
+            ms = ctypes.c_float()
+            n = ctypes.c_uint64()
+            if self.lib.ooc_kernel_time(self.h, i, ctypes.byref(name), ctypes.byref(ms), ctypes.byref(n)) != 0:
+                break
+            out[name.value.decode()] = (float(ms.value), int(n.value))
+            i += 1
+        return out
+
     def build(self, tris: np.ndarray, params: BuildParams, sink=None) -> BuildResult:
         """Host triangles in, octree bytes out (through the sink into host memory)."""
         tris = np.ascontiguousarray(tris, dtype=np.float32)
@@ -205,6 +230,14 @@ class Builder:
         d = ctypes.c_void_p()
         self._check(self.lib.ooc_result_device(self.h, ctypes.byref(n), ctypes.byref(d)))
         return int(n.value or 0), int(d.value or 0)
+
+    def result_tree(self, gridsize: int, n_nodes: int, n_data: int) -> _octree.Octree:
+        """Copy the last build_device result to host memory."""
+        nodes = np.empty(n_nodes, dtype=_octree.NODE_DTYPE)
+        data = np.empty(n_data, dtype=_octree.DATA_DTYPE)
+        self._check(self.lib.ooc_result_copy(self.h, nodes.ctypes.data_as(ctypes.c_void_p),
+                                             data.ctypes.data_as(ctypes.c_void_p)))
+        return _octree.Octree(gridsize, nodes, data)
 
     def build_files(self, tri_path: str, params: BuildParams):
         out = ctypes.create_string_buffer(4096)

@@ -118,6 +118,13 @@ struct ooc_ctx {
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   std::vector<std::array<size_t, 3>> marks;  // phase, start event, end event
+  // per-kernel timing: "" off, "*" every kernel, otherwise one kernel name
+  std::string kfilter;
+  std::vector<std::pair<const char*, std::array<size_t, 2>>> kmarks;
+  size_t kopen = 0;
+  std::vector<std::string> knames;
+  std::vector<float> kms;
+  std::vector<uint64_t> kcount;
 };
 
 namespace {
@@ -609,20 +616,60 @@ void build_core(ooc_ctx* c, const ooc_build_params* prm, const float* d_tris, ui
 
 void finish_timing(ooc_ctx* c) {
   for (float& v : c->phase_ms) v = 0.0f;
-  if (!c->timing) return;
-  for (const auto& m : c->marks) {
-    float ms = 0.0f;
-    if (cudaEventElapsedTime(&ms, c->ev_pool[m[1]], c->ev_pool[m[2]]) == cudaSuccess) c->phase_ms[m[0]] += ms;
+  if (c->timing) {
+    for (const auto& m : c->marks) {
+      float ms = 0.0f;
+      if (cudaEventElapsedTime(&ms, c->ev_pool[m[1]], c->ev_pool[m[2]]) == cudaSuccess) c->phase_ms[m[0]] += ms;
+    }
   }
+  c->knames.clear();
+  c->kms.clear();
+  c->kcount.clear();
+  for (const auto& m : c->kmarks) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, c->ev_pool[m.second[0]], c->ev_pool[m.second[1]]) != cudaSuccess) continue;
+    size_t i = 0;
+    while (i < c->knames.size() && c->knames[i] != m.first) i++;
+    if (i == c->knames.size()) {
+      c->knames.push_back(m.first);
+      c->kms.push_back(0.0f);
+      c->kcount.push_back(0);
+    }
+    c->kms[i] += ms;
+    c->kcount[i] += 1;
+  }
+}
+
+void kernel_begin(void* user, const char* name, cudaStream_t st) {
+  ooc_ctx* c = static_cast<ooc_ctx*>(user);
+  if (c->kfilter != "*" && c->kfilter != name) return;
+  c->kopen = c->ev_used;
+  cudaEventRecord(next_event(c), st);
+}
+
+void kernel_end(void* user, const char* name, cudaStream_t st) {
+  ooc_ctx* c = static_cast<ooc_ctx*>(user);
+  if (c->kfilter != "*" && c->kfilter != name) return;
+  const size_t e = c->ev_used;
+  cudaEventRecord(next_event(c), st);
+  c->kmarks.push_back({name, {c->kopen, e}});
 }
 
 void begin_build(ooc_ctx* c) {
   ck(cudaSetDevice(c->device), "cudaSetDevice");
   c->err.clear();
   c->marks.clear();
+  c->kmarks.clear();
   c->ev_used = 0;
   c->res_valid = false;
   g_launches = 0;
+  if (c->kfilter.empty()) {
+    g_hooks = KernelHooks();
+  } else {
+    g_hooks.user = c;
+    g_hooks.begin = kernel_begin;
+    g_hooks.end = kernel_end;
+  }
 }
 
 template <typename F>
@@ -760,6 +807,17 @@ int ooc_result_device(ooc_ctx* c, const void** nodes_device, const void** data_d
   return OOC_OK;
 }
 
+int ooc_result_copy(ooc_ctx* c, void* nodes_host, void* data_host) {
+  return guarded(c, [&] {
+    if (!c->res_valid) fail(OOC_ERR_INVALID, "no device result: run ooc_build_device first");
+    ck(cudaSetDevice(c->device), "cudaSetDevice");
+    if (nodes_host && c->res_nodes)
+      ck(cudaMemcpy(nodes_host, c->d_nodes.p, c->res_nodes * 24, cudaMemcpyDeviceToHost), "D2H nodes");
+    if (data_host && c->res_data)
+      ck(cudaMemcpy(data_host, c->d_data.p, c->res_data * 32, cudaMemcpyDeviceToHost), "D2H data");
+  });
+}
+
 int ooc_set_phase_timing(ooc_ctx* c, int32_t enable) {
   if (!c) return OOC_ERR_INVALID;
   c->timing = enable != 0;
@@ -773,5 +831,19 @@ int ooc_phase_times(const ooc_ctx* c, float* ms, int32_t n) {
 }
 
 uint64_t ooc_kernel_launches(const ooc_ctx* c) { return c ? c->launches : 0; }
+
+int ooc_set_kernel_timing(ooc_ctx* c, const char* kernel) {
+  if (!c) return OOC_ERR_INVALID;
+  c->kfilter = kernel ? kernel : "";
+  return OOC_OK;
+}
+
+int ooc_kernel_time(const ooc_ctx* c, int32_t index, const char** name, float* total_ms, uint64_t* launches) {
+  if (!c || index < 0 || (size_t)index >= c->knames.size()) return OOC_ERR_INVALID;
+  if (name) *name = c->knames[index].c_str();
+  if (total_ms) *total_ms = c->kms[index];
+  if (launches) *launches = c->kcount[index];
+  return OOC_OK;
+}
 
 }  // extern "C"

@@ -82,6 +82,14 @@ struct EmitJob {
 // ---- launches (ooc_kernels.cu); all asynchronous on `st` ----
 extern unsigned long long g_launches;  // kernel launches since the last reset (host counter)
 
+// Optional callbacks around every kernel launch (per-kernel CUDA-event timing).
+struct KernelHooks {
+  void* user = nullptr;
+  void (*begin)(void* user, const char* kernel, cudaStream_t st) = nullptr;
+  void (*end)(void* user, const char* kernel, cudaStream_t st) = nullptr;
+};
+extern KernelHooks g_hooks;
+
 void scan_u32_exclusive(uint32_t* data, uint64_t n, uint32_t* partials, cudaStream_t st);
 void scan_u64_exclusive(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st);
 uint64_t scan_partials_needed(uint64_t n);

@@ -11,9 +11,23 @@
 namespace ooc {
 
 unsigned long long g_launches = 0;
+KernelHooks g_hooks;
 
 namespace {
 constexpr unsigned FULL = 0xffffffffu;
+
+// Counts one launch and brackets it with the timing hooks when they are set.
+struct KScope {
+  const char* name;
+  cudaStream_t st;
+  KScope(const char* n, cudaStream_t s) : name(n), st(s) {
+    g_launches++;
+    if (g_hooks.begin) g_hooks.begin(g_hooks.user, name, st);
+  }
+  ~KScope() {
+    if (g_hooks.end) g_hooks.end(g_hooks.user, name, st);
+  }
+};
 constexpr int SCAN_THREADS = 1024;
 
 inline unsigned grid_for(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
@@ -88,10 +102,18 @@ template <typename T>
 void scan_exclusive(T* data, uint64_t n, T* partials, cudaStream_t st) {
   if (n == 0) return;
   const unsigned nb = grid_for(n, SCAN_THREADS);
-  k_scan_reduce<T><<<nb, SCAN_THREADS, 0, st>>>(data, n, partials);
-  k_scan_partials<T><<<1, SCAN_THREADS, 0, st>>>(partials, nb);
-  k_scan_down<T><<<nb, SCAN_THREADS, 0, st>>>(data, n, partials);
-  g_launches += 3;
+  {
+    KScope k("scan_reduce", st);
+    k_scan_reduce<T><<<nb, SCAN_THREADS, 0, st>>>(data, n, partials);
+  }
+  {
+    KScope k("scan_partials", st);
+    k_scan_partials<T><<<1, SCAN_THREADS, 0, st>>>(partials, nb);
+  }
+  {
+    KScope k("scan_down", st);
+    k_scan_down<T><<<nb, SCAN_THREADS, 0, st>>>(data, n, partials);
+  }
 }
 
 // ===========================================================================
@@ -659,9 +681,11 @@ void launch_part_count(const float* tris, int stride, uint64_t n_tris, const flo
   if (n_tris == 0) return;
   const int use_smem = n_parts <= 4096;
   const size_t smem = use_smem ? n_parts * sizeof(uint32_t) : 0;
-  k_part_count<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
+  {
+    KScope k("part_count", st);
+    k_part_count<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
                                                           (uint32_t)n_parts, hist, use_smem);
-  g_launches++;
+  }
 }
 
 void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
@@ -669,78 +693,96 @@ void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const floa
   if (n_tris == 0) return;
   const int use_smem = n_parts <= 4096;
   const size_t smem = use_smem ? 2 * n_parts * sizeof(uint32_t) : 0;
-  k_part_emit<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
+  {
+    KScope k("part_emit", st);
+    k_part_emit<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
                                                          (uint32_t)n_parts, cursor, items, use_smem);
-  g_launches++;
+  }
 }
 
 void launch_vox_small(const VoxJob& j, int pass, cudaStream_t st) {
   if (j.n_items == 0) return;
+  KScope k(pass == 0 ? "vox_small_occupancy" : "vox_small_winner", st);
   if (pass == 0) k_vox_small<0><<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
   else k_vox_small<1><<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
-  g_launches++;
 }
 
 void launch_vox_large(const VoxJob& j, int pass, cudaStream_t st, int num_sms) {
   if (j.n_items == 0) return;
   cudaMemsetAsync(j.task_counter, 0, sizeof(unsigned long long), st);
   const unsigned grid = (unsigned)num_sms * 8;
+  KScope k(pass == 0 ? "vox_large_occupancy" : "vox_large_winner", st);
   if (pass == 0) k_vox_large<0><<<grid, 256, 0, st>>>(j);
   else k_vox_large<1><<<grid, 256, 0, st>>>(j);
-  g_launches++;
 }
 
 void launch_pyramid(const Pyramid& p, int level, cudaStream_t st) {
   const Level& L = p.lv[level];
   const int has_parent = level > 0;
   const uint64_t off_wp = has_parent ? p.lv[level - 1].off_w : 0;
-  k_pyramid<<<grid_for(L.nblocks, 256), 256, 0, st>>>(p.bits, L.off_w, L.nblocks, has_parent, off_wp,
+  {
+    KScope k("pyramid", st);
+    k_pyramid<<<grid_for(L.nblocks, 256), 256, 0, st>>>(p.bits, L.off_w, L.nblocks, has_parent, off_wp,
                                                        p.scan + L.off_b);
-  g_launches++;
+  }
 }
 
 void launch_compact(const Pyramid& p, int level, uint32_t* keys, cudaStream_t st) {
   const Level& L = p.lv[level];
   if (L.n == 0) return;
-  k_compact<<<grid_for(L.nwords, 256), 256, 0, st>>>(p.bits, p.scan, L, keys);
-  g_launches++;
+  {
+    KScope k("compact", st);
+    k_compact<<<grid_for(L.nwords, 256), 256, 0, st>>>(p.bits, p.scan, L, keys);
+  }
 }
 
 void launch_leaf_payload(const Pyramid& p, const EmitJob& e, int, cudaStream_t st) {
   const uint64_t n = p.lv[p.depth].n;
   if (n == 0) return;
-  k_leaf_payload<<<grid_for(n, 256), 256, 0, st>>>(p, e);
-  g_launches++;
+  {
+    KScope k("leaf_payload", st);
+    k_leaf_payload<<<grid_for(n, 256), 256, 0, st>>>(p, e);
+  }
 }
 
 void launch_bottom_up(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st) {
   const uint64_t n = p.lv[level].n;
   if (n == 0) return;
-  k_bottom_up<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
-  g_launches++;
+  {
+    KScope k("bottom_up", st);
+    k_bottom_up<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
+  }
 }
 
 void launch_set_root(const EmitJob& e, uint64_t node_base, uint64_t data_base, cudaStream_t st) {
-  k_set_root<<<1, 1, 0, st>>>(e, node_base, data_base);
-  g_launches++;
+  {
+    KScope k("set_root", st);
+    k_set_root<<<1, 1, 0, st>>>(e, node_base, data_base);
+  }
 }
 
 void launch_top_down(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st) {
   const uint64_t n = p.lv[level].n;
   if (n == 0) return;
-  k_top_down<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
-  g_launches++;
+  {
+    KScope k("top_down", st);
+    k_top_down<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
+  }
 }
 
 void launch_root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base, uint32_t* out, cudaStream_t st) {
-  k_root_info<<<1, 1, 0, st>>>(p, e, data_base, out);
-  g_launches++;
+  {
+    KScope k("root_info", st);
+    k_root_info<<<1, 1, 0, st>>>(p, e, data_base, out);
+  }
 }
 
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st) {
   if (n == 0) return;
-  k_scatter_records<<<grid_for(n, 128), 128, 0, st>>>(src, n, words, dst);
-  g_launches++;
+  {
+    KScope k("scatter_records", st);
+    k_scatter_records<<<grid_for(n, 128), 128, 0, st>>>(src, n, words, dst);
+  }
 }
 
 }  // namespace ooc

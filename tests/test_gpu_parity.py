@@ -120,3 +120,21 @@ def test_outside_grid(builder):
 def test_non_unit_bbox(builder):
     t = tri.random_tris(800, 31, False, lo=0.0, hi=3.0, max_edge=0.5)
     assert_same(*run_both(builder, t, 128, bbox_max=(3.0, 3.0, 3.0)))
+
+
+@pytest.mark.parametrize("payload,N,limit,levels", [(False, 128, 2048, False), (True, 64, 2048, True),
+                                                    (False, 256, 2, True), (True, 256, 2, False)])
+def test_device_resident_build(builder, payload, N, limit, levels):
+    """ooc_build_device keeps the octree on the GPU; copied back it equals the host-API result."""
+    torch = pytest.importorskip("torch")
+    t = tri.random_tris(1500, 77, payload, lo=-0.05, hi=1.05, max_edge=0.15)
+    prm = make_params(N, limit, geometry_only=not payload, levels=levels)
+    d = torch.from_numpy(t).cuda()
+    for _ in range(2):  # the second call reuses every buffer
+        info = builder.build_device(d.data_ptr(), t.shape[0], prm)
+        dev = builder.result_tree(N, info["n_nodes"], info["n_data"])
+        host = builder.build(t, prm)
+        diffs = octree.diff(dev, host.tree)
+        assert not diffs, "\n".join(diffs)
+    nodes, data, _ = pyoracle.build(t, N, limit, levels=levels)
+    assert not octree.diff(dev, octree.Octree(N, nodes, data))
