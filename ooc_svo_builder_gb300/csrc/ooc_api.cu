@@ -111,7 +111,8 @@ struct ooc_ctx {
   float phase_ms[kPhases] = {0, 0, 0, 0, 0, 0};
   unsigned long long launches = 0;
   DevBuf d_tris, d_items, d_hist, d_axis, d_bits, d_scan, d_scanpart, d_keys, d_size, d_dsize, d_start, d_dstart,
-      d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo;
+      d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo, d_itemmask,
+      d_firstchild;
   PinBuf h_nodes, h_data, h_misc, h_recs;
   uint64_t res_nodes = 0, res_data = 0;
   bool res_valid = false;
@@ -329,11 +330,14 @@ struct StripeOut {
 };
 
 StripeOut run_stripe(ooc_ctx* c, cudaStream_t st, const Plan& pl, const ooc_build_params* prm, const float* d_tris,
-                     uint64_t n_tris_total, const uint32_t* items, uint64_t ibeg, uint64_t n_items, uint64_t part, uint64_t stripe,
-                     uint64_t node_base, uint64_t data_base, bool device_mode) {
+                     uint64_t n_tris_total, const uint32_t* items, uint64_t ibeg, uint64_t n_items, uint64_t part,
+                     uint64_t stripe, uint64_t node_base, uint64_t data_base, bool device_mode) {
   StripeOut res;
   const int Ds = pl.Ds;
   const int stride = pl.binary ? 9 : 21;
+  // Levels with at most this many 256-bit blocks (pyramid) or nodes (layout)
+  // run together in one CTA instead of one launch each.
+  constexpr uint64_t kSmallBlocks = 2048, kSmallNodes = 8192;
   // ---- pyramid layout ----
   Pyramid pyr;
   std::memset(&pyr, 0, sizeof(pyr));
@@ -379,25 +383,28 @@ StripeOut run_stripe(ooc_ctx* c, cudaStream_t st, const Plan& pl, const ooc_buil
   j.leafbits = pyr.bits + pyr.lv[Ds].off_w;
   j.task_off = ensure<uint64_t>(c->d_taskoff, (n_items + 1) * 8);
   j.task_counter = ensure<unsigned long long>(c->d_counter, 16);
+  j.item_mask = pl.binary ? nullptr : ensure<uint64_t>(c->d_itemmask, n_items * 8);
   uint64_t* taskpart = ensure<uint64_t>(c->d_taskpart, scan_partials_needed(n_items + 1) * 8);
 
   {
     PhaseScope ph(c, PH_VOX, st);
     ck(cudaMemsetAsync(pyr.bits, 0, words * 4, st), "memset bits");
-    ck(cudaMemsetAsync(pyr.scan + blocks, 0, 4, st), "memset scan");
     ck(cudaMemsetAsync(j.task_off + n_items, 0, 8, st), "memset task_off");
     launch_vox_small(j, 0, st);
     scan_u64_exclusive(j.task_off, n_items + 1, taskpart, st);
     launch_vox_large(j, 0, st, c->num_sms);
   }
   uint32_t* lvl = ensure_pinned<uint32_t>(c->h_misc, 64 * 4);
+  uint32_t* d_root = ensure<uint32_t>(c->d_rootinfo, 64 * 4);
   {
     PhaseScope ph(c, PH_PYR, st);
-    for (int l = Ds; l >= 0; l--) launch_pyramid(pyr, l, st);
+    ck(cudaMemsetAsync(pyr.scan + blocks, 0, 4, st), "memset scan");
+    int l = Ds;
+    for (; l >= 0 && pyr.lv[l].nblocks > kSmallBlocks; l--) launch_pyramid(pyr, l, st);
+    if (l >= 0) launch_pyramid_top(pyr, l, st);
     scan_u32_exclusive(pyr.scan, blocks + 1, scanpart, st);
-    for (int l = 0; l <= Ds; l++)
-      ck(cudaMemcpyAsync(lvl + l, pyr.scan + pyr.lv[l].off_b, 4, cudaMemcpyDeviceToHost, st), "level base");
-    ck(cudaMemcpyAsync(lvl + Ds + 1, pyr.scan + blocks, 4, cudaMemcpyDeviceToHost, st), "level total");
+    launch_level_bases(pyr, blocks, d_root + 16, st);
+    ck(cudaMemcpyAsync(lvl, d_root + 16, (Ds + 2) * 4, cudaMemcpyDeviceToHost, st), "level bases");
   }
   ck(cudaStreamSynchronize(st), "stripe level counts");
   for (int l = 0; l <= Ds; l++) {
@@ -410,7 +417,6 @@ StripeOut run_stripe(ooc_ctx* c, cudaStream_t st, const Plan& pl, const ooc_buil
   res.empty = false;
   res.filled = n_leaf;
 
-  const bool need_cache = !pl.binary || pl.levels;
   EmitJob e;
   std::memset(&e, 0, sizeof(e));
   e.binary = pl.binary;
@@ -426,9 +432,11 @@ StripeOut run_stripe(ooc_ctx* c, cudaStream_t st, const Plan& pl, const ooc_buil
   e.keys = keys;
   e.size = ensure<uint32_t>(c->d_size, total * 4);
   e.dsize = ensure<uint32_t>(c->d_dsize, total * 4);
+  e.first_child = ensure<uint32_t>(c->d_firstchild, total * 4);
   e.start = ensure<uint64_t>(c->d_start, total * 8);
   e.dstart = ensure<uint64_t>(c->d_dstart, total * 8);
-  e.cache = need_cache ? ensure<float>(c->d_cache, total * 24) : nullptr;
+  e.cache = pl.levels ? ensure<float>(c->d_cache, total * 24) : nullptr;
+  e.leaf_inline = (!pl.binary && !pl.levels) ? 1 : 0;
 
   const uint64_t node_span = total - 1;
   const uint64_t data_span = (pl.binary ? 0 : n_leaf) + (pl.levels ? total - n_leaf : 0);
@@ -450,13 +458,12 @@ StripeOut run_stripe(ooc_ctx* c, cudaStream_t st, const Plan& pl, const ooc_buil
     e.data_win_len = data_span;
   }
   e.n_tris = n_tris_total;
-  uint32_t* d_root = ensure<uint32_t>(c->d_rootinfo, 64);
   e.flag = d_root + 8;
   ck(cudaMemsetAsync(e.flag, 0, 4, st), "memset flag");
 
   {
     PhaseScope ph(c, PH_PYR, st);
-    for (int l = 0; l <= Ds; l++) launch_compact(pyr, l, keys, st);
+    launch_compact(pyr, words, keys, st);
   }
   if (!pl.binary) {
     PhaseScope ph(c, PH_VOX, st);
@@ -468,14 +475,20 @@ StripeOut run_stripe(ooc_ctx* c, cudaStream_t st, const Plan& pl, const ooc_buil
     launch_vox_small(j, 1, st);
     launch_vox_large(j, 1, st, c->num_sms);
     e.winners = winners;
-    launch_leaf_payload(pyr, e, prm->color_mode, st);
+    if (pl.levels) launch_leaf_payload(pyr, e, st);
   }
   uint32_t* h_root = lvl + 32;
   {
     PhaseScope ph(c, PH_TREE, st);
-    for (int l = Ds - 1; l >= 0; l--) launch_bottom_up(pyr, e, l, st);
-    launch_set_root(e, node_base, data_base, st);
-    for (int l = 1; l <= Ds; l++) launch_top_down(pyr, e, l, st);
+    // levels 0 .. l_small hold at most kSmallNodes nodes each (counts grow with depth)
+    int l_small = 0;
+    while (l_small + 1 <= Ds - 1 && pyr.lv[l_small + 1].n <= kSmallNodes) l_small++;
+    if (Ds >= 1) {
+      for (int l = Ds - 1; l > l_small; l--) launch_bottom_up(pyr, e, l, st);
+      launch_bottom_up_top(pyr, e, l_small, st);
+      launch_top_down_top(pyr, e, l_small, node_base, data_base, st);
+      for (int l = l_small + 1; l <= Ds - 1; l++) launch_top_down(pyr, e, l, st);
+    }
     launch_root_info(pyr, e, data_base, d_root, st);
     ck(cudaMemcpyAsync(h_root, d_root, 9 * 4, cudaMemcpyDeviceToHost, st), "root info");
   }
@@ -724,7 +737,7 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   DevBuf* bufs[] = {&c->d_tris, &c->d_items, &c->d_hist, &c->d_axis, &c->d_bits, &c->d_scan, &c->d_scanpart,
                     &c->d_keys, &c->d_size, &c->d_dsize, &c->d_start, &c->d_dstart, &c->d_cache, &c->d_winners,
                     &c->d_taskoff, &c->d_taskpart, &c->d_counter, &c->d_nodes, &c->d_data, &c->d_recs,
-                    &c->d_rootinfo};
+                    &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   PinBuf* pins[] = {&c->h_nodes, &c->h_data, &c->h_misc, &c->h_recs};

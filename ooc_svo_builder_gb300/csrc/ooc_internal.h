@@ -50,6 +50,7 @@ struct VoxJob {
   uint32_t* winners;        // per leaf: min triangle index
   uint64_t* task_off;       // per item: exclusive prefix of warp tasks (n_items + 1)
   unsigned long long* task_counter;
+  uint64_t* item_mask;      // per small item: which of its candidates passed (pass 0 -> pass 1); may be NULL
 };
 
 struct EmitJob {
@@ -67,7 +68,9 @@ struct EmitJob {
   uint32_t* dsize;          // per node: data records in its subtree
   uint64_t* start;          // per node: global index of the first node written inside its subtree
   uint64_t* dstart;         // per node: global index of its subtree's first data record
-  float* cache;             // per node: 6 floats (colour, normal) used by -levels and leaves
+  float* cache;             // per node: 6 floats (colour, normal); only with -levels
+  uint32_t* first_child;    // per internal node: global index of its first child
+  int leaf_inline;          // payload leaves computed while their records are written (no -levels)
   const uint32_t* winners;
   uint64_t* node_win;       // node window (3 u64 per record)
   uint64_t node_win_base;   // global node index of node_win[0]
@@ -103,11 +106,16 @@ void launch_vox_small(const VoxJob& j, int pass, cudaStream_t st);
 void launch_vox_large(const VoxJob& j, int pass, cudaStream_t st, int num_sms);
 
 void launch_pyramid(const Pyramid& p, int level, cudaStream_t st);
-void launch_compact(const Pyramid& p, int level, uint32_t* keys, cudaStream_t st);
-void launch_leaf_payload(const Pyramid& p, const EmitJob& e, int color_mode, cudaStream_t st);
+void launch_pyramid_top(const Pyramid& p, int l_hi, cudaStream_t st);  // levels l_hi..0 in one CTA
+void launch_compact(const Pyramid& p, uint64_t total_words, uint32_t* keys, cudaStream_t st);
+void launch_level_bases(const Pyramid& p, uint64_t total_blocks, uint32_t* out, cudaStream_t st);
+void launch_leaf_payload(const Pyramid& p, const EmitJob& e, cudaStream_t st);
 void launch_bottom_up(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st);
-void launch_set_root(const EmitJob& e, uint64_t node_base, uint64_t data_base, cudaStream_t st);
+void launch_bottom_up_top(const Pyramid& p, const EmitJob& e, int l_hi, cudaStream_t st);
+// Parents of level `level` write their children's records.
 void launch_top_down(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st);
+void launch_top_down_top(const Pyramid& p, const EmitJob& e, int l_lo, uint64_t node_base, uint64_t data_base,
+                         cudaStream_t st);
 // Writes the stripe root's child mask and cache to out[0..6] and its own data
 // record (with -levels, or the payload of a one-voxel stripe).
 void launch_root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base, uint32_t* out, cudaStream_t st);

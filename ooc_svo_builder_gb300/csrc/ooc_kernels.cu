@@ -232,13 +232,15 @@ __global__ void k_part_emit(const float* __restrict__ tris, int stride, uint64_t
         }
 }
 
+
 // ===========================================================================
 // Voxelization (voxelizer.cpp:168-306)
 //
 // Pass 0 sets the Morton-ordered occupancy bits of the stripe; pass 1 (payload
-// mode) revisits only set voxels and keeps the smallest passing triangle
-// index per voxel, which is the reference's first-writer-wins rule
-// (voxelizer.cpp:263, 293-299).
+// mode) keeps, per set voxel, the smallest passing triangle index, which is
+// the reference's first-writer-wins rule (voxelizer.cpp:263, 293-299).  For a
+// small item pass 0 also stores which of its (at most 64) candidates passed,
+// so pass 1 only ranks those voxels instead of testing again.
 // ===========================================================================
 __device__ __forceinline__ bool item_box(const VoxJob& j, const TriVerts& tv, int lo[3], int hi[3]) {
   int gmin[3], gmax[3];
@@ -262,15 +264,22 @@ __device__ __forceinline__ uint32_t leaf_rank(const VoxJob& j, uint32_t b) {
   return r + __popc(j.leafbits[w] & ((1u << (b & 31)) - 1u));
 }
 
+__device__ __forceinline__ uint32_t local_morton(const VoxJob& j, int x, int y, int z) {
+  return morton_local((uint32_t)(x - j.sa[0]), (uint32_t)(y - j.sa[1]), (uint32_t)(z - j.sa[2]));
+}
+
+// One z column of pass 0 (set bits) or pass 1 (winners, re-testing set voxels).
+// Returns the column's pass bits (bit z - z0) for columns of at most 64 voxels.
 template <int PASS>
-__device__ __forceinline__ void vox_column(const VoxJob& j, const TriSetup& s, uint32_t tri, int x, int y, int z0,
-                                           int z1) {
+__device__ __forceinline__ uint64_t vox_column(const VoxJob& j, const TriSetup& s, uint32_t tri, int x, int y, int z0,
+                                               int z1) {
   const float px = __fmul_rn((float)x, j.u);
   const float py = __fmul_rn((float)y, j.u);
-  if (!pass_xy(s, px, py)) return;
+  if (!pass_xy(s, px, py)) return 0;
   const float nxy = plane_xy(s, px, py);
   const uint32_t mxy = spread3_10((uint32_t)(x - j.sa[0])) | (spread3_10((uint32_t)(y - j.sa[1])) << 1);
   uint32_t cur_w = 0xffffffffu, acc = 0;
+  uint64_t col = 0;
   for (int z = z0; z <= z1; z++) {
     const uint32_t m = mxy | (spread3_10((uint32_t)(z - j.sa[2])) << 2);
     if (PASS == 0) {
@@ -282,6 +291,7 @@ __device__ __forceinline__ void vox_column(const VoxJob& j, const TriSetup& s, u
           acc = 0;
         }
         acc |= 1u << (m & 31);
+        if (z - z0 < 64) col |= 1ull << (z - z0);
       }
     } else {
       const uint32_t word = j.leafbits[m >> 5];
@@ -291,35 +301,62 @@ __device__ __forceinline__ void vox_column(const VoxJob& j, const TriSetup& s, u
     }
   }
   if (PASS == 0 && acc) atomicOr(&j.leafbits[cur_w], acc);
+  return col;
 }
 
 __device__ __forceinline__ uint64_t item_triangle(const VoxJob& j, uint64_t i) {
   return j.item_tri ? (uint64_t)j.item_tri[j.ibeg + i] : j.ibeg + i;
 }
 
-// One thread per item; items with at most small_vol candidates are finished
-// here, larger ones get a warp-task count (32 columns per task) in pass 0.
-template <int PASS>
-__global__ void k_vox_small(VoxJob j) {
+// Pass 0, one thread per item: items with at most small_vol (<= 64) candidates
+// are voxelized here and leave their pass mask; larger ones get a warp-task
+// count (32 columns per task).
+__global__ void k_vox_small_occ(VoxJob j) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= j.n_items) return;
   const uint64_t t = item_triangle(j, i);
   const TriVerts tv = load_verts(j.tris, t, j.stride);
   int lo[3], hi[3];
-  uint64_t cost = 0;
+  uint64_t cost = 0, mask = 0;
   if (item_box(j, tv, lo, hi)) {
     const uint64_t bx = (uint64_t)(hi[0] - lo[0] + 1), by = (uint64_t)(hi[1] - lo[1] + 1),
                    bz = (uint64_t)(hi[2] - lo[2] + 1);
     if (bx * by * bz <= j.small_vol) {
       TriSetup s;
       tri_setup(tv, j.u, s);
+      uint32_t shift = 0;
       for (int x = lo[0]; x <= hi[0]; x++)
-        for (int y = lo[1]; y <= hi[1]; y++) vox_column<PASS>(j, s, (uint32_t)t, x, y, lo[2], hi[2]);
+        for (int y = lo[1]; y <= hi[1]; y++) {
+          mask |= vox_column<0>(j, s, (uint32_t)t, x, y, lo[2], hi[2]) << shift;
+          shift += (uint32_t)bz;
+        }
     } else {
       cost = (bx * by + 31) / 32;
     }
   }
-  if (PASS == 0) j.task_off[i] = cost;
+  j.task_off[i] = cost;
+  if (j.item_mask) j.item_mask[i] = mask;
+}
+
+// Pass 1 for small items: rank the voxels their pass mask names.
+__global__ void k_vox_small_win(VoxJob j) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= j.n_items) return;
+  uint64_t mask = j.item_mask[i];
+  if (!mask) return;
+  const uint64_t t = item_triangle(j, i);
+  const TriVerts tv = load_verts(j.tris, t, j.stride);
+  int lo[3], hi[3];
+  if (!item_box(j, tv, lo, hi)) return;
+  const uint32_t bz = (uint32_t)(hi[2] - lo[2] + 1), by = (uint32_t)(hi[1] - lo[1] + 1);
+  while (mask) {
+    const uint32_t q = (uint32_t)(__ffsll((long long)mask) - 1);
+    mask &= mask - 1;
+    const uint32_t col = q / bz, z = q - col * bz;
+    const uint32_t x = col / by, y = col - x * by;
+    const uint32_t m = local_morton(j, lo[0] + (int)x, lo[1] + (int)y, lo[2] + (int)z);
+    atomicMin(&j.winners[leaf_rank(j, m)], (uint32_t)t);
+  }
 }
 
 // Persistent warps pull 32-column tasks of large items from a global counter.
@@ -363,12 +400,10 @@ __device__ __forceinline__ uint32_t nonzero_bytes(uint32_t w) {
   return ((t >> 7) & 1u) | ((t >> 14) & 2u) | ((t >> 21) & 4u) | ((t >> 28) & 8u);
 }
 
-__global__ void k_pyramid(uint32_t* __restrict__ bits, uint64_t off_w, uint64_t nblocks, int has_parent,
-                          uint64_t off_wp, uint32_t* __restrict__ counts) {
-  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nblocks) return;
-  const uint4* p = reinterpret_cast<const uint4*>(bits + off_w + 8 * b);
-  const uint4 q0 = p[0], q1 = p[1];
+__device__ __forceinline__ void pyramid_block(const Pyramid& p, int l, uint64_t b) {
+  const Level& L = p.lv[l];
+  const uint4* q = reinterpret_cast<const uint4*>(p.bits + L.off_w + 8 * b);
+  const uint4 q0 = q[0], q1 = q[1];
   const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
   uint32_t c = 0, pw = 0;
 #pragma unroll
@@ -376,8 +411,21 @@ __global__ void k_pyramid(uint32_t* __restrict__ bits, uint64_t off_w, uint64_t 
     c += __popc(w[k]);
     pw |= nonzero_bytes(w[k]) << (4 * k);
   }
-  counts[b] = c;
-  if (has_parent) bits[off_wp + b] = pw;
+  p.scan[L.off_b + b] = c;
+  if (l > 0) p.bits[p.lv[l - 1].off_w + b] = pw;
+}
+
+__global__ void k_pyramid(Pyramid p, int l) {
+  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < p.lv[l].nblocks) pyramid_block(p, l, b);
+}
+
+// Levels l_hi .. 0 in one CTA (they are small); the barrier orders the levels.
+__global__ void k_pyramid_top(Pyramid p, int l_hi) {
+  for (int l = l_hi; l >= 0; l--) {
+    for (uint64_t b = threadIdx.x; b < p.lv[l].nblocks; b += blockDim.x) pyramid_block(p, l, b);
+    __syncthreads();
+  }
 }
 
 // Global node index of bit `b` of a level: the concatenated scan already
@@ -394,16 +442,31 @@ __device__ __forceinline__ uint32_t child_mask(const uint32_t* __restrict__ bits
   return (bits[C.off_w + (k >> 2)] >> ((k & 3) * 8)) & 0xffu;
 }
 
-__global__ void k_compact(const uint32_t* __restrict__ bits, const uint32_t* __restrict__ scan, Level L,
-                          uint32_t* __restrict__ keys) {
+// Keys of all levels in one launch: one lane per word, the in-block prefix
+// from a warp scan of popcounts (blocks are 8 aligned words, never split
+// between levels).
+__global__ void k_compact(Pyramid p, uint64_t total_words, uint32_t* __restrict__ keys) {
   const uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= L.nwords) return;
-  uint32_t word = bits[L.off_w + w];
+  const int lane = threadIdx.x & 31;
+  uint32_t word = w < total_words ? p.bits[w] : 0u;
+  const uint32_t c = __popc(word);
+  uint32_t inc = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(FULL, inc, o);
+    if (lane >= o) inc += y;
+  }
+  const int first = lane & ~7;
+  const uint32_t before_block = __shfl_sync(FULL, inc, (first + 31) & 31);  // inclusive sum at lane first-1
   if (!word) return;
-  uint64_t r = node_index(bits, scan, L, w << 5);
+  const uint32_t ex = inc - c - (first > 0 ? before_block : 0u);
+  int l = 0;
+  while (l < p.depth && p.lv[l + 1].off_w <= w) l++;
+  const uint64_t wl = w - p.lv[l].off_w;
+  uint64_t r = (uint64_t)p.scan[w >> 3] + ex;
   while (word) {
     const int b = __ffs(word) - 1;
-    keys[r++] = (uint32_t)((w << 5) | (uint64_t)b);
+    keys[r++] = (uint32_t)((wl << 5) | (uint64_t)b);
     word &= word - 1;
   }
 }
@@ -450,48 +513,55 @@ __device__ void payload_color(const TriVerts& tv, const float n[3], int x, int y
   }
 }
 
-__global__ void k_leaf_payload(Pyramid p, EmitJob e) {
-  const Level& L = p.lv[p.depth];
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= L.n) return;
-  const uint32_t key = e.keys[L.koff + i];
+// Colour and normal of leaf `li` (its index within the leaf level), local key `key`.
+// Returns false (and flags) if the leaf has no winning triangle.
+__device__ bool leaf_value(const EmitJob& e, uint64_t li, uint32_t key, float out[6]) {
   uint32_t lx, ly, lz;
   morton_local_decode(key, lx, ly, lz);
   const int x = e.origin[0] + (int)lx, y = e.origin[1] + (int)ly, z = e.origin[2] + (int)lz;
-  const uint64_t t = e.winners[i];
+  const uint64_t t = e.winners[li];
   if (t >= e.n_tris) {  // every set voxel has a passing triangle; anything else is a bug
     atomicOr(e.flag, 4u);
-    return;
+    return false;
   }
   const float* tr = e.tris + t * 21;
-  float* out = e.cache + (L.koff + i) * 6;
   const float nx = __ldg(tr + 9), ny = __ldg(tr + 10), nz = __ldg(tr + 11);
-  float col[3];
   if (e.color_mode == 1) {  // COLOR_FIXED
-    col[0] = col[1] = col[2] = 1.0f;
+    out[0] = out[1] = out[2] = 1.0f;
   } else if (e.color_mode == 2) {  // COLOR_LINEAR: mortonToRGB (svo_builder_util.h:14-18)
     const float fn = (float)e.gridsize;
-    col[0] = __fdiv_rn((float)z, fn);
-    col[1] = __fdiv_rn((float)y, fn);
-    col[2] = __fdiv_rn((float)x, fn);
+    out[0] = __fdiv_rn((float)z, fn);
+    out[1] = __fdiv_rn((float)y, fn);
+    out[2] = __fdiv_rn((float)x, fn);
   } else if (e.color_mode == 3) {  // COLOR_NORMAL
     float a = nx, b = ny, c = nz;
     normalize3(a, b, c);
-    col[0] = __fdiv_rn(__fadd_rn(a, 1.0f), 2.0f);
-    col[1] = __fdiv_rn(__fadd_rn(b, 1.0f), 2.0f);
-    col[2] = __fdiv_rn(__fadd_rn(c, 1.0f), 2.0f);
+    out[0] = __fdiv_rn(__fadd_rn(a, 1.0f), 2.0f);
+    out[1] = __fdiv_rn(__fadd_rn(b, 1.0f), 2.0f);
+    out[2] = __fdiv_rn(__fadd_rn(c, 1.0f), 2.0f);
   } else {  // COLOR_FROM_MODEL
     const TriVerts tv = load_verts(e.tris, t, 21);
     float n[3];
     tri_normal(tv, n);
-    payload_color(tv, n, x, y, z, e.unit_div, tr, col);
+    payload_color(tv, n, x, y, z, e.unit_div, tr, out);
   }
-  out[0] = col[0];
-  out[1] = col[1];
-  out[2] = col[2];
   out[3] = nx;
   out[4] = ny;
   out[5] = nz;
+  return true;
+}
+
+// Leaf payloads into the per-node cache (needed before the -levels averages).
+__global__ void k_leaf_payload(Pyramid p, EmitJob e) {
+  const Level& L = p.lv[p.depth];
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.n) return;
+  float v[6];
+  if (leaf_value(e, i, e.keys[L.koff + i], v)) {
+    float* out = e.cache + (L.koff + i) * 6;
+#pragma unroll
+    for (int q = 0; q < 6; q++) out[q] = v[q];
+  }
 }
 
 // ===========================================================================
@@ -535,11 +605,10 @@ __device__ __forceinline__ void average_children(const EmitJob& e, uint32_t mask
   out[5] = tz;
 }
 
-__global__ void k_bottom_up(Pyramid p, EmitJob e, int l) {
+// Subtree node / data counts, first-child index and (-levels) averages of node i of level l.
+__device__ __forceinline__ void bottom_up_node(const Pyramid& p, const EmitJob& e, int l, uint64_t i) {
   const Level& L = p.lv[l];
   const Level& C = p.lv[l + 1];
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= L.n) return;
   const uint64_t gi = L.koff + i;
   const uint32_t k = e.keys[gi];
   const uint32_t mask = child_mask(p.bits, C, k);
@@ -560,12 +629,21 @@ __global__ void k_bottom_up(Pyramid p, EmitJob e, int l) {
   }
   e.size[gi] = sz;
   e.dsize[gi] = dsz;
+  e.first_child[gi] = (uint32_t)c0;
   if (e.levels) average_children(e, mask, c0, child_leaf, e.cache + gi * 6);
 }
 
-__global__ void k_set_root(EmitJob e, uint64_t node_base, uint64_t data_base) {
-  e.start[0] = node_base;
-  e.dstart[0] = data_base;
+__global__ void k_bottom_up(Pyramid p, EmitJob e, int l) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < p.lv[l].n) bottom_up_node(p, e, l, i);
+}
+
+// Levels l_hi .. 0 in one CTA.
+__global__ void k_bottom_up_top(Pyramid p, EmitJob e, int l_hi) {
+  for (int l = l_hi; l >= 0; l--) {
+    for (uint64_t i = threadIdx.x; i < p.lv[l].n; i += blockDim.x) bottom_up_node(p, e, l, i);
+    __syncthreads();
+  }
 }
 
 __device__ __forceinline__ void store_data_record(const EmitJob& e, uint64_t idx, uint64_t morton, const float* v) {
@@ -576,6 +654,18 @@ __device__ __forceinline__ void store_data_record(const EmitJob& e, uint64_t idx
   uint4* dst = reinterpret_cast<uint4*>(e.data_win + (idx - e.data_win_base) * 32);
   dst[0] = make_uint4((uint32_t)morton, (uint32_t)(morton >> 32), __float_as_uint(v[0]), __float_as_uint(v[1]));
   dst[1] = make_uint4(__float_as_uint(v[2]), __float_as_uint(v[3]), __float_as_uint(v[4]), __float_as_uint(v[5]));
+}
+
+__device__ __forceinline__ void store_node_record(const EmitJob& e, uint64_t pos, uint64_t r0, uint64_t r1,
+                                                  uint64_t r2) {
+  if (pos < e.node_win_base || pos - e.node_win_base >= e.node_win_len) {
+    atomicOr(e.flag, 1u);
+    return;
+  }
+  uint64_t* rec = e.node_win + (pos - e.node_win_base) * 3;
+  rec[0] = r0;
+  rec[1] = r1;
+  rec[2] = r2;
 }
 
 __device__ __forceinline__ uint64_t child_offsets(uint32_t mask) {
@@ -589,61 +679,84 @@ __device__ __forceinline__ uint64_t child_offsets(uint32_t mask) {
   return off;
 }
 
-__global__ void k_top_down(Pyramid p, EmitJob e, int l) {
+// Node i of level l (internal) writes its children's records: they form one
+// contiguous group at its children_base, in child order (groupNodes,
+// OctreeBuilder.cpp:58-79), and each child's subtree starts where the
+// previous sibling's subtree ended.
+__device__ __forceinline__ void top_down_node(const Pyramid& p, const EmitJob& e, int l, uint64_t i) {
   const Level& L = p.lv[l];
-  const Level& P = p.lv[l - 1];
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= L.n) return;
   const uint64_t gi = L.koff + i;
   const uint32_t k = e.keys[gi];
-  const uint32_t pk = k >> 3;
-  const uint64_t pidx = node_index(p.bits, p.scan, P, pk);
-  const uint64_t c0 = node_index(p.bits, p.scan, L, (uint64_t)pk << 3);
-  const bool leaf = (l == p.depth);
-  const uint64_t pstart = e.start[pidx];
-  uint64_t st = pstart, dst = e.dstart[pidx];
-  for (uint64_t q = c0; q < gi; q++) {
-    if (!leaf) {
-      st += (uint64_t)e.size[q] - 1;
-      dst += e.dsize[q];
-    } else if (!e.binary) {
-      dst += 1;
+  const uint32_t mask = child_mask(p.bits, p.lv[l + 1], k);
+  const int nch = __popc(mask);
+  const uint64_t st = e.start[gi];
+  uint64_t run_d = e.dstart[gi];
+  uint64_t run_s = st;
+  const uint64_t cb = st + (uint64_t)e.size[gi] - 1 - (uint64_t)nch;
+  const uint64_t c0 = e.first_child[gi];
+  const bool child_leaf = (l + 1 == p.depth);
+  for (int j = 0; j < nch; j++) {
+    const uint64_t c = c0 + (uint64_t)j;
+    const uint32_t kc = e.keys[c];
+    if (!child_leaf) {
+      const uint32_t mc = child_mask(p.bits, p.lv[l + 2], kc);
+      const uint64_t szc = e.size[c], dszc = e.dsize[c];
+      e.start[c] = run_s;
+      e.dstart[c] = run_d;
+      const uint64_t di = run_d + dszc - 1;
+      store_node_record(e, cb + j, e.levels ? di : 0, run_s + szc - 1 - (uint64_t)__popc(mc), child_offsets(mc));
+      if (e.levels) store_data_record(e, di, 0, e.cache + c * 6);
+      run_s += szc - 1;
+      run_d += dszc;
+    } else if (e.binary) {
+      store_node_record(e, cb + j, 1, 0, ~0ull);
+    } else {
+      store_node_record(e, cb + j, run_d, 0, ~0ull);
+      float v[6];
+      if (e.leaf_inline) {
+        if (!leaf_value(e, c - p.lv[p.depth].koff, kc, v)) return;
+      } else {
+#pragma unroll
+        for (int q = 0; q < 6; q++) v[q] = e.cache[c * 6 + q];
+      }
+      store_data_record(e, run_d, e.stripe_base + kc, v);
+      run_d += 1;
     }
   }
-  const uint32_t pmask = child_mask(p.bits, L, pk);
-  const uint64_t pcb = pstart + (uint64_t)e.size[pidx] - 1 - (uint64_t)__popc(pmask);
-  const uint64_t pos = pcb + (gi - c0);
-  uint64_t r0, r1, r2;
-  if (!leaf) {
-    e.start[gi] = st;
-    e.dstart[gi] = dst;
-    const uint32_t mask = child_mask(p.bits, p.lv[l + 1], k);
-    const uint64_t sz = e.size[gi], dsz = e.dsize[gi];
-    r1 = st + sz - 1 - (uint64_t)__popc(mask);
-    r0 = e.levels ? dst + dsz - 1 : 0;
-    r2 = child_offsets(mask);
-    if (e.levels) store_data_record(e, dst + dsz - 1, 0, e.cache + gi * 6);
-  } else {
-    r0 = e.binary ? 1 : dst;
-    r1 = 0;
-    r2 = ~0ull;
-    if (!e.binary) store_data_record(e, dst, e.stripe_base + k, e.cache + gi * 6);
+}
+
+__global__ void k_top_down(Pyramid p, EmitJob e, int l) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < p.lv[l].n) top_down_node(p, e, l, i);
+}
+
+// Parents of levels 0 .. l_lo in one CTA; the stripe root starts at the bases.
+__global__ void k_top_down_top(Pyramid p, EmitJob e, int l_lo, uint64_t node_base, uint64_t data_base) {
+  if (threadIdx.x == 0) {
+    e.start[0] = node_base;
+    e.dstart[0] = data_base;
   }
-  if (pos < e.node_win_base || pos - e.node_win_base >= e.node_win_len) {
-    atomicOr(e.flag, 1u);
-    return;
+  __syncthreads();
+  for (int l = 0; l <= l_lo; l++) {
+    for (uint64_t i = threadIdx.x; i < p.lv[l].n; i += blockDim.x) top_down_node(p, e, l, i);
+    __syncthreads();
   }
-  uint64_t* rec = e.node_win + (pos - e.node_win_base) * 3;
-  rec[0] = r0;
-  rec[1] = r1;
-  rec[2] = r2;
 }
 
 // Stripe root: child mask and payload for the host, and (with -levels, or a
 // one-voxel stripe in payload mode) the root's own data record.
 __global__ void k_root_info(Pyramid p, EmitJob e, uint64_t data_base, uint32_t* out) {
-  float c[6];
-  for (int q = 0; q < 6; q++) c[q] = e.cache ? e.cache[q] : 0.0f;
+  float c[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  if (p.depth >= 1) {
+    if (e.levels)
+      for (int q = 0; q < 6; q++) c[q] = e.cache[q];
+  } else if (!e.binary) {
+    if (e.cache) {
+      for (int q = 0; q < 6; q++) c[q] = e.cache[q];
+    } else {
+      leaf_value(e, 0, 0, c);
+    }
+  }
   out[0] = p.depth >= 1 ? child_mask(p.bits, p.lv[1], 0) : 0u;
   for (int q = 0; q < 6; q++) out[1 + q] = __float_as_uint(c[q]);
   if (p.depth >= 1) {
@@ -651,6 +764,13 @@ __global__ void k_root_info(Pyramid p, EmitJob e, uint64_t data_base, uint32_t* 
   } else if (!e.binary) {
     store_data_record(e, data_base, e.stripe_base, c);
   }
+}
+
+// Per-level node counts from the scan: out[l] = first node of level l, out[depth+1] = total.
+__global__ void k_level_bases(Pyramid p, uint64_t total_blocks, uint32_t* out) {
+  const int l = threadIdx.x;
+  if (l <= p.depth) out[l] = p.scan[p.lv[l].off_b];
+  if (l == p.depth + 1) out[l] = p.scan[total_blocks];
 }
 
 __global__ void k_scatter_records(const uint64_t* __restrict__ src, uint64_t n, int words, uint64_t* __restrict__ dst) {
@@ -681,11 +801,9 @@ void launch_part_count(const float* tris, int stride, uint64_t n_tris, const flo
   if (n_tris == 0) return;
   const int use_smem = n_parts <= 4096;
   const size_t smem = use_smem ? n_parts * sizeof(uint32_t) : 0;
-  {
-    KScope k("part_count", st);
-    k_part_count<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
+  KScope k("part_count", st);
+  k_part_count<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
                                                           (uint32_t)n_parts, hist, use_smem);
-  }
 }
 
 void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
@@ -693,18 +811,20 @@ void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const floa
   if (n_tris == 0) return;
   const int use_smem = n_parts <= 4096;
   const size_t smem = use_smem ? 2 * n_parts * sizeof(uint32_t) : 0;
-  {
-    KScope k("part_emit", st);
-    k_part_emit<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
+  KScope k("part_emit", st);
+  k_part_emit<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
                                                          (uint32_t)n_parts, cursor, items, use_smem);
-  }
 }
 
 void launch_vox_small(const VoxJob& j, int pass, cudaStream_t st) {
   if (j.n_items == 0) return;
-  KScope k(pass == 0 ? "vox_small_occupancy" : "vox_small_winner", st);
-  if (pass == 0) k_vox_small<0><<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
-  else k_vox_small<1><<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
+  if (pass == 0) {
+    KScope k("vox_small_occupancy", st);
+    k_vox_small_occ<<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
+  } else {
+    KScope k("vox_small_winner", st);
+    k_vox_small_win<<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
+  }
 }
 
 void launch_vox_large(const VoxJob& j, int pass, cudaStream_t st, int num_sms) {
@@ -717,72 +837,66 @@ void launch_vox_large(const VoxJob& j, int pass, cudaStream_t st, int num_sms) {
 }
 
 void launch_pyramid(const Pyramid& p, int level, cudaStream_t st) {
-  const Level& L = p.lv[level];
-  const int has_parent = level > 0;
-  const uint64_t off_wp = has_parent ? p.lv[level - 1].off_w : 0;
-  {
-    KScope k("pyramid", st);
-    k_pyramid<<<grid_for(L.nblocks, 256), 256, 0, st>>>(p.bits, L.off_w, L.nblocks, has_parent, off_wp,
-                                                       p.scan + L.off_b);
-  }
+  KScope k(level == p.depth ? "pyramid_leaf" : "pyramid", st);
+  k_pyramid<<<grid_for(p.lv[level].nblocks, 256), 256, 0, st>>>(p, level);
 }
 
-void launch_compact(const Pyramid& p, int level, uint32_t* keys, cudaStream_t st) {
-  const Level& L = p.lv[level];
-  if (L.n == 0) return;
-  {
-    KScope k("compact", st);
-    k_compact<<<grid_for(L.nwords, 256), 256, 0, st>>>(p.bits, p.scan, L, keys);
-  }
+void launch_pyramid_top(const Pyramid& p, int l_hi, cudaStream_t st) {
+  KScope k("pyramid_top", st);
+  k_pyramid_top<<<1, 1024, 0, st>>>(p, l_hi);
 }
 
-void launch_leaf_payload(const Pyramid& p, const EmitJob& e, int, cudaStream_t st) {
+void launch_compact(const Pyramid& p, uint64_t total_words, uint32_t* keys, cudaStream_t st) {
+  KScope k("compact", st);
+  k_compact<<<grid_for(total_words, 256), 256, 0, st>>>(p, total_words, keys);
+}
+
+void launch_level_bases(const Pyramid& p, uint64_t total_blocks, uint32_t* out, cudaStream_t st) {
+  KScope k("level_bases", st);
+  k_level_bases<<<1, 32, 0, st>>>(p, total_blocks, out);
+}
+
+void launch_leaf_payload(const Pyramid& p, const EmitJob& e, cudaStream_t st) {
   const uint64_t n = p.lv[p.depth].n;
   if (n == 0) return;
-  {
-    KScope k("leaf_payload", st);
-    k_leaf_payload<<<grid_for(n, 256), 256, 0, st>>>(p, e);
-  }
+  KScope k("leaf_payload", st);
+  k_leaf_payload<<<grid_for(n, 256), 256, 0, st>>>(p, e);
 }
 
 void launch_bottom_up(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st) {
   const uint64_t n = p.lv[level].n;
   if (n == 0) return;
-  {
-    KScope k("bottom_up", st);
-    k_bottom_up<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
-  }
+  KScope k(level == p.depth - 1 ? "bottom_up_leaf_parents" : "bottom_up", st);
+  k_bottom_up<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
 }
 
-void launch_set_root(const EmitJob& e, uint64_t node_base, uint64_t data_base, cudaStream_t st) {
-  {
-    KScope k("set_root", st);
-    k_set_root<<<1, 1, 0, st>>>(e, node_base, data_base);
-  }
+void launch_bottom_up_top(const Pyramid& p, const EmitJob& e, int l_hi, cudaStream_t st) {
+  KScope k("bottom_up_top", st);
+  k_bottom_up_top<<<1, 1024, 0, st>>>(p, e, l_hi);
 }
 
 void launch_top_down(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st) {
   const uint64_t n = p.lv[level].n;
   if (n == 0) return;
-  {
-    KScope k("top_down", st);
-    k_top_down<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
-  }
+  KScope k(level == p.depth - 1 ? "top_down_leaf_parents" : "top_down", st);
+  k_top_down<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
+}
+
+void launch_top_down_top(const Pyramid& p, const EmitJob& e, int l_lo, uint64_t node_base, uint64_t data_base,
+                         cudaStream_t st) {
+  KScope k("top_down_top", st);
+  k_top_down_top<<<1, 1024, 0, st>>>(p, e, l_lo, node_base, data_base);
 }
 
 void launch_root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base, uint32_t* out, cudaStream_t st) {
-  {
-    KScope k("root_info", st);
-    k_root_info<<<1, 1, 0, st>>>(p, e, data_base, out);
-  }
+  KScope k("root_info", st);
+  k_root_info<<<1, 1, 0, st>>>(p, e, data_base, out);
 }
 
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st) {
   if (n == 0) return;
-  {
-    KScope k("scatter_records", st);
-    k_scatter_records<<<grid_for(n, 128), 128, 0, st>>>(src, n, words, dst);
-  }
+  KScope k("scatter_records", st);
+  k_scatter_records<<<grid_for(n, 128), 128, 0, st>>>(src, n, words, dst);
 }
 
 }  // namespace ooc
