@@ -337,7 +337,7 @@ StripeOut run_stripe(ooc_ctx* c, cudaStream_t st, const Plan& pl, const ooc_buil
   const int stride = pl.binary ? 9 : 21;
   // Levels with at most this many 256-bit blocks (pyramid) or nodes (layout)
   // run together in one CTA instead of one launch each.
-  constexpr uint64_t kSmallBlocks = 2048, kSmallNodes = 8192;
+  constexpr uint64_t kSmallBlocks = 512, kSmallNodes = 256;
   // ---- pyramid layout ----
   Pyramid pyr;
   std::memset(&pyr, 0, sizeof(pyr));
@@ -463,7 +463,7 @@ StripeOut run_stripe(ooc_ctx* c, cudaStream_t st, const Plan& pl, const ooc_buil
 
   {
     PhaseScope ph(c, PH_PYR, st);
-    launch_compact(pyr, words, keys, st);
+    launch_compact(pyr, blocks, keys, st);
   }
   if (!pl.binary) {
     PhaseScope ph(c, PH_VOX, st);
@@ -486,8 +486,11 @@ StripeOut run_stripe(ooc_ctx* c, cudaStream_t st, const Plan& pl, const ooc_buil
     if (Ds >= 1) {
       for (int l = Ds - 1; l > l_small; l--) launch_bottom_up(pyr, e, l, st);
       launch_bottom_up_top(pyr, e, l_small, st);
-      launch_top_down_top(pyr, e, l_small, node_base, data_base, st);
-      for (int l = l_small + 1; l <= Ds - 1; l++) launch_top_down(pyr, e, l, st);
+      // parents of internal children: levels 0 .. Ds-2; the leaves get one thread each
+      const int top_last = std::min(l_small, Ds - 2);
+      launch_top_down_top(pyr, e, top_last, node_base, data_base, st);
+      for (int l = top_last + 1; l <= Ds - 2; l++) launch_top_down(pyr, e, l, st);
+      launch_top_down_leaves(pyr, e, st);
     }
     launch_root_info(pyr, e, data_base, d_root, st);
     ck(cudaMemcpyAsync(h_root, d_root, 9 * 4, cudaMemcpyDeviceToHost, st), "root info");

@@ -28,7 +28,7 @@ struct KScope {
     if (g_hooks.end) g_hooks.end(g_hooks.user, name, st);
   }
 };
-constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_THREADS = 256;
 
 inline unsigned grid_for(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
@@ -67,17 +67,26 @@ __device__ __forceinline__ T block_exclusive(T v, T& total) {
   return r;
 }
 
+constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
 template <typename T>
-__global__ void k_scan_reduce(const T* __restrict__ in, uint64_t n, T* __restrict__ partials) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  T v = i < n ? in[i] : T(0);
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const T* __restrict__ in, uint64_t n,
+                                                              T* __restrict__ partials) {
+  const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+  T v = 0;
+#pragma unroll
+  for (int q = 0; q < SCAN_ITEMS; q++) {
+    const uint64_t i = base + (uint64_t)q * SCAN_THREADS + threadIdx.x;
+    if (i < n) v += in[i];
+  }
   T total;
   block_exclusive(v, total);
   if (threadIdx.x == 0) partials[blockIdx.x] = total;
 }
 
 template <typename T>
-__global__ void k_scan_partials(T* partials, uint64_t np) {
+__global__ void __launch_bounds__(1024) k_scan_partials(T* partials, uint64_t np) {
   T carry = 0;
   for (uint64_t base = 0; base < np; base += blockDim.x) {
     const uint64_t i = base + threadIdx.x;
@@ -89,26 +98,54 @@ __global__ void k_scan_partials(T* partials, uint64_t np) {
   }
 }
 
+// Each thread scans SCAN_ITEMS consecutive elements staged through shared memory.
 template <typename T>
-__global__ void k_scan_down(T* data, uint64_t n, const T* __restrict__ partials) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const T v = i < n ? data[i] : T(0);
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(T* data, uint64_t n, const T* __restrict__ partials) {
+  __shared__ T tile[SCAN_TILE + SCAN_TILE / 32];
+  const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+#pragma unroll
+  for (int q = 0; q < SCAN_ITEMS; q++) {
+    const uint32_t li = q * SCAN_THREADS + threadIdx.x;
+    const uint64_t i = base + li;
+    tile[li + li / 32] = i < n ? data[i] : T(0);
+  }
+  __syncthreads();
+  T v[SCAN_ITEMS];
+  T sum = 0;
+#pragma unroll
+  for (int q = 0; q < SCAN_ITEMS; q++) {
+    const uint32_t li = threadIdx.x * SCAN_ITEMS + q;
+    v[q] = tile[li + li / 32];
+    sum += v[q];
+  }
   T total;
-  const T ex = block_exclusive(v, total);
-  if (i < n) data[i] = ex + partials[blockIdx.x];
+  T run = block_exclusive(sum, total) + partials[blockIdx.x];
+#pragma unroll
+  for (int q = 0; q < SCAN_ITEMS; q++) {
+    const uint32_t li = threadIdx.x * SCAN_ITEMS + q;
+    tile[li + li / 32] = run;
+    run += v[q];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < SCAN_ITEMS; q++) {
+    const uint32_t li = q * SCAN_THREADS + threadIdx.x;
+    const uint64_t i = base + li;
+    if (i < n) data[i] = tile[li + li / 32];
+  }
 }
 
 template <typename T>
 void scan_exclusive(T* data, uint64_t n, T* partials, cudaStream_t st) {
   if (n == 0) return;
-  const unsigned nb = grid_for(n, SCAN_THREADS);
+  const unsigned nb = (unsigned)((n + SCAN_TILE - 1) / SCAN_TILE);
   {
     KScope k("scan_reduce", st);
     k_scan_reduce<T><<<nb, SCAN_THREADS, 0, st>>>(data, n, partials);
   }
   {
     KScope k("scan_partials", st);
-    k_scan_partials<T><<<1, SCAN_THREADS, 0, st>>>(partials, nb);
+    k_scan_partials<T><<<1, 1024, 0, st>>>(partials, nb);
   }
   {
     KScope k("scan_down", st);
@@ -442,32 +479,27 @@ __device__ __forceinline__ uint32_t child_mask(const uint32_t* __restrict__ bits
   return (bits[C.off_w + (k >> 2)] >> ((k & 3) * 8)) & 0xffu;
 }
 
-// Keys of all levels in one launch: one lane per word, the in-block prefix
-// from a warp scan of popcounts (blocks are 8 aligned words, never split
-// between levels).
-__global__ void k_compact(Pyramid p, uint64_t total_words, uint32_t* __restrict__ keys) {
-  const uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
-  uint32_t word = w < total_words ? p.bits[w] : 0u;
-  const uint32_t c = __popc(word);
-  uint32_t inc = c;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(FULL, inc, o);
-    if (lane >= o) inc += y;
-  }
-  const int first = lane & ~7;
-  const uint32_t before_block = __shfl_sync(FULL, inc, (first + 31) & 31);  // inclusive sum at lane first-1
-  if (!word) return;
-  const uint32_t ex = inc - c - (first > 0 ? before_block : 0u);
+// Keys of all levels in one launch, one thread per 256-bit block (blocks are
+// 8 aligned words and never straddle two levels).
+__global__ void k_compact(Pyramid p, uint64_t total_blocks, uint32_t* __restrict__ keys) {
+  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= total_blocks) return;
+  const uint4* q = reinterpret_cast<const uint4*>(p.bits + 8 * b);
+  const uint4 q0 = q[0], q1 = q[1];
+  if (!(q0.x | q0.y | q0.z | q0.w | q1.x | q1.y | q1.z | q1.w)) return;
+  const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
   int l = 0;
-  while (l < p.depth && p.lv[l + 1].off_w <= w) l++;
-  const uint64_t wl = w - p.lv[l].off_w;
-  uint64_t r = (uint64_t)p.scan[w >> 3] + ex;
-  while (word) {
-    const int b = __ffs(word) - 1;
-    keys[r++] = (uint32_t)((wl << 5) | (uint64_t)b);
-    word &= word - 1;
+  while (l < p.depth && p.lv[l + 1].off_b <= b) l++;
+  const uint64_t wl0 = (b - p.lv[l].off_b) * 8;
+  uint64_t r = p.scan[b];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    uint32_t word = w[k];
+    while (word) {
+      const int bit = __ffs(word) - 1;
+      keys[r++] = (uint32_t)(((wl0 + k) << 5) | (uint64_t)bit);
+      word &= word - 1;
+    }
   }
 }
 
@@ -725,6 +757,36 @@ __device__ __forceinline__ void top_down_node(const Pyramid& p, const EmitJob& e
   }
 }
 
+// Leaf records, one thread per leaf: the parent (level depth-1) already knows
+// where its child group and data run start.
+__global__ void k_top_down_leaves(Pyramid p, EmitJob e) {
+  const Level& L = p.lv[p.depth];
+  const Level& P = p.lv[p.depth - 1];
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.n) return;
+  const uint64_t gi = L.koff + i;
+  const uint32_t k = e.keys[gi];
+  const uint32_t pk = k >> 3;
+  const uint64_t pidx = node_index(p.bits, p.scan, P, pk);
+  const uint64_t rank = gi - e.first_child[pidx];
+  const uint32_t pmask = child_mask(p.bits, L, pk);
+  const uint64_t pcb = e.start[pidx] + (uint64_t)e.size[pidx] - 1 - (uint64_t)__popc(pmask);
+  if (e.binary) {
+    store_node_record(e, pcb + rank, 1, 0, ~0ull);
+    return;
+  }
+  const uint64_t di = e.dstart[pidx] + rank;
+  store_node_record(e, pcb + rank, di, 0, ~0ull);
+  float v[6];
+  if (e.leaf_inline) {
+    if (!leaf_value(e, i, k, v)) return;
+  } else {
+#pragma unroll
+    for (int q = 0; q < 6; q++) v[q] = e.cache[gi * 6 + q];
+  }
+  store_data_record(e, di, e.stripe_base + k, v);
+}
+
 __global__ void k_top_down(Pyramid p, EmitJob e, int l) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < p.lv[l].n) top_down_node(p, e, l, i);
@@ -786,7 +848,7 @@ __global__ void k_scatter_records(const uint64_t* __restrict__ src, uint64_t n, 
 // ===========================================================================
 // Launch wrappers
 // ===========================================================================
-uint64_t scan_partials_needed(uint64_t n) { return (n + SCAN_THREADS - 1) / SCAN_THREADS + 1; }
+uint64_t scan_partials_needed(uint64_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
 
 void scan_u32_exclusive(uint32_t* data, uint64_t n, uint32_t* partials, cudaStream_t st) {
   scan_exclusive<uint32_t>(data, n, partials, st);
@@ -846,9 +908,9 @@ void launch_pyramid_top(const Pyramid& p, int l_hi, cudaStream_t st) {
   k_pyramid_top<<<1, 1024, 0, st>>>(p, l_hi);
 }
 
-void launch_compact(const Pyramid& p, uint64_t total_words, uint32_t* keys, cudaStream_t st) {
+void launch_compact(const Pyramid& p, uint64_t total_blocks, uint32_t* keys, cudaStream_t st) {
   KScope k("compact", st);
-  k_compact<<<grid_for(total_words, 256), 256, 0, st>>>(p, total_words, keys);
+  k_compact<<<grid_for(total_blocks, 256), 256, 0, st>>>(p, total_blocks, keys);
 }
 
 void launch_level_bases(const Pyramid& p, uint64_t total_blocks, uint32_t* out, cudaStream_t st) {
@@ -878,8 +940,15 @@ void launch_bottom_up_top(const Pyramid& p, const EmitJob& e, int l_hi, cudaStre
 void launch_top_down(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st) {
   const uint64_t n = p.lv[level].n;
   if (n == 0) return;
-  KScope k(level == p.depth - 1 ? "top_down_leaf_parents" : "top_down", st);
+  KScope k("top_down", st);
   k_top_down<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
+}
+
+void launch_top_down_leaves(const Pyramid& p, const EmitJob& e, cudaStream_t st) {
+  const uint64_t n = p.lv[p.depth].n;
+  if (n == 0 || p.depth < 1) return;
+  KScope k("top_down_leaves", st);
+  k_top_down_leaves<<<grid_for(n, 256), 256, 0, st>>>(p, e);
 }
 
 void launch_top_down_top(const Pyramid& p, const EmitJob& e, int l_lo, uint64_t node_base, uint64_t data_base,
