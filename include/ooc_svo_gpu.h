@@ -42,6 +42,7 @@ extern "C" {
 #define OOC_ERR_DEVICE 3   /* a CUDA call or kernel failed                       */
 #define OOC_ERR_IO 4       /* file could not be read or written                  */
 #define OOC_ERR_SINK 5     /* the caller's sink returned non-zero                */
+#define OOC_ERR_LIMIT 6    /* input beyond the fixed limits of ooc_voxelize_occupancy_noalloc */
 
 /* Colour modes of svo_builder's -c flag (main.cpp:23, 154-179). */
 #define OOC_COLOR_MODEL 0
@@ -133,6 +134,38 @@ int ooc_set_kernel_timing(ooc_ctx* ctx, const char* kernel);
  * (valid until the next build), summed device milliseconds, launch count.
  * Returns OOC_ERR_INVALID past the last entry. */
 int ooc_kernel_time(const ooc_ctx* ctx, int32_t index, const char** name, float* total_ms, uint64_t* launches);
+
+/* Occupancy pass without any allocation -- no counterpart in the reference.
+ *
+ * For callers that must not allocate GPU memory where they voxelize: code
+ * running while its stream is captured into a CUDA graph, plugins whose host
+ * engine owns and pre-reserves all device memory, and latency-critical loops
+ * in which a cudaMalloc would synchronise the device.  The caller passes the
+ * triangles (device memory, 9 or 21 FP32 values each as geometry_only says)
+ * and the output; the only scratch is a fixed array compiled into the library
+ * (about 8.4 MB held on every GPU that loads it, until the process exits).
+ * Nothing is allocated: no cudaMalloc, no cudaFree, no allocating library call.
+ *
+ * Output: the grid's occupancy bitfield in Morton order, bit (m % 32) of word
+ * m / 32 set when the voxel with Morton code m is set, exactly the voxels of
+ * the reference's voxelize_schwarz_method (voxelizer.cpp:139-307) for a
+ * single partition.  `occupancy_words` must be at least gridsize^3 / 32 (at
+ * least 1); the words are cleared first.  Work is queued on `stream` (a
+ * cudaStream_t on the current device; NULL = default stream) and the call
+ * returns without waiting for it.
+ *
+ * Limits: n_tris <= OOC_NOALLOC_MAX_TRIANGLES, gridsize <= OOC_NOALLOC_MAX_GRIDSIZE
+ * and memory_limit_mb large enough for one partition; beyond them the call
+ * returns OOC_ERR_LIMIT before touching the GPU.
+ * The first call on each device looks up the scratch array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls on a device share the one scratch
+ * array, which keeps the last call's contents: calls that may overlap on the
+ * GPU (different streams without ordering between them) race. */
+#define OOC_NOALLOC_MAX_TRIANGLES 1048576
+#define OOC_NOALLOC_MAX_GRIDSIZE 1024
+int ooc_voxelize_occupancy_noalloc(const ooc_build_params* params, const float* tris_device, uint64_t n_tris,
+                                   uint32_t* occupancy_device, uint64_t occupancy_words, void* stream);
 
 /* File front end used by the svo_builder CLIs: reads <base>.tri/.tridata and
  * writes <base><gridsize>_<npartitions>.octree/.octreenodes/.octreedata

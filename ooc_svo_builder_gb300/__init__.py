@@ -19,14 +19,18 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libooc_svo_gpu.so")
 
 OOC_OK = 0
-ERRORS = {1: "OOC_ERR_INVALID", 2: "OOC_ERR_OOM", 3: "OOC_ERR_DEVICE", 4: "OOC_ERR_IO", 5: "OOC_ERR_SINK"}
+ERRORS = {1: "OOC_ERR_INVALID", 2: "OOC_ERR_OOM", 3: "OOC_ERR_DEVICE", 4: "OOC_ERR_IO", 5: "OOC_ERR_SINK",
+          6: "OOC_ERR_LIMIT"}
+NOALLOC_MAX_TRIANGLES = 1048576
+NOALLOC_MAX_GRIDSIZE = 1024
 COLOR_MODES = {"model": 0, "fixed": 1, "linear": 2, "normal": 3}
 PHASES = ("partition", "voxelize", "pyramid", "octree", "copies", "build")
 
 # Every symbol declared in include/ooc_svo_gpu.h.
 EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_partitions", "ooc_build",
            "ooc_build_device", "ooc_result_device", "ooc_result_copy", "ooc_set_phase_timing", "ooc_phase_times",
-           "ooc_kernel_launches", "ooc_build_files", "ooc_set_kernel_timing", "ooc_kernel_time")
+           "ooc_kernel_launches", "ooc_build_files", "ooc_set_kernel_timing", "ooc_kernel_time",
+           "ooc_voxelize_occupancy_noalloc")
 
 
 class BuildParams(ctypes.Structure):
@@ -94,6 +98,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_kernel_time.argtypes = [ctypes.c_void_p, ctypes.c_int32, P(ctypes.c_char_p), P(ctypes.c_float),
                                     P(ctypes.c_uint64)]
     lib.ooc_kernel_time.restype = ctypes.c_int
+    lib.ooc_voxelize_occupancy_noalloc.argtypes = [P(BuildParams), ctypes.c_void_p, ctypes.c_uint64,
+                                                   ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
+    lib.ooc_voxelize_occupancy_noalloc.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -116,6 +123,22 @@ def make_params(gridsize: int, memory_limit_mb: int = 2048, geometry_only: bool 
         p.bbox_min[a] = float(bbox_min[a])
         p.bbox_max[a] = float(bbox_max[a])
     return p
+
+
+def voxelize_occupancy_noalloc(params: BuildParams, tris_device_ptr: int, n_tris: int, occupancy_device_ptr: int,
+                               occupancy_words: int, stream: int = 0) -> int:
+    """Occupancy bitfield of a single-partition grid without any GPU allocation.
+
+    For callers that may not allocate device memory where they voxelize (stream
+    capture, engines that pre-reserve all memory, latency-critical loops).  The
+    scratch is a fixed array inside the library; at most NOALLOC_MAX_TRIANGLES
+    triangles and gridsize NOALLOC_MAX_GRIDSIZE.  Calls on one device share that
+    scratch, so calls that may overlap on the GPU race.  Returns the OOC_* code;
+    the work is queued on `stream` and not waited for.
+    """
+    return int(load_library().ooc_voxelize_occupancy_noalloc(
+        ctypes.byref(params), ctypes.c_void_p(tris_device_ptr), n_tris, ctypes.c_void_p(occupancy_device_ptr),
+        occupancy_words, ctypes.c_void_p(stream or None)))
 
 
 @dataclass

@@ -24,7 +24,7 @@ BIN = os.path.join(PKG, "bin")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-Xptxas", "-v"]
-CUDA_SOURCES = ["ooc_kernels.cu", "ooc_api.cu"]
+CUDA_SOURCES = ["ooc_kernels.cu", "ooc_api.cu", "ooc_noalloc.cu"]
 CXX_SOURCES = ["ooc_files.cpp"]
 
 
