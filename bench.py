@@ -238,6 +238,10 @@ def run_ours(args, world, rank, local):
     cb = ooc.SINK(sink)
     for _ in range(max(1, args.warmup)):
         b.build_ptr(h_tris.data_ptr(), T, prm, cb)
+    b.set_phase_timing(True)
+    b.build_ptr(h_tris.data_ptr(), T, prm, cb)
+    e2e_phases = b.phase_times()
+    b.set_phase_timing(False)
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -282,6 +286,7 @@ def run_ours(args, world, rank, local):
         "gpu_launches": launches,
         "roofline": roofline,
         "phases_ms": phases,
+        "e2e_phases_ms": e2e_phases,
         "kernels_ms": {k: v[0] for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])},
         "clocks": clocks,
     }

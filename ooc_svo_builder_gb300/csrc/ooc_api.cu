@@ -112,7 +112,7 @@ struct ooc_ctx {
   unsigned long long launches = 0;
   DevBuf d_tris, d_items, d_hist, d_axis, d_bits, d_scan, d_scanpart, d_keys, d_size, d_dsize, d_start, d_dstart,
       d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo, d_itemmask,
-      d_firstchild;
+      d_firstchild, d_itembox;
   PinBuf h_nodes, h_data, h_misc, h_recs;
   uint64_t res_nodes = 0, res_data = 0;
   bool res_valid = false;
@@ -384,6 +384,7 @@ StripeOut run_stripe(ooc_ctx* c, cudaStream_t st, const Plan& pl, const ooc_buil
   j.task_off = ensure<uint64_t>(c->d_taskoff, (n_items + 1) * 8);
   j.task_counter = ensure<unsigned long long>(c->d_counter, 16);
   j.item_mask = pl.binary ? nullptr : ensure<uint64_t>(c->d_itemmask, n_items * 8);
+  j.item_box = pl.binary ? nullptr : ensure<uint64_t>(c->d_itembox, n_items * 8);
   uint64_t* taskpart = ensure<uint64_t>(c->d_taskpart, scan_partials_needed(n_items + 1) * 8);
 
   {
@@ -740,7 +741,7 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   DevBuf* bufs[] = {&c->d_tris, &c->d_items, &c->d_hist, &c->d_axis, &c->d_bits, &c->d_scan, &c->d_scanpart,
                     &c->d_keys, &c->d_size, &c->d_dsize, &c->d_start, &c->d_dstart, &c->d_cache, &c->d_winners,
                     &c->d_taskoff, &c->d_taskpart, &c->d_counter, &c->d_nodes, &c->d_data, &c->d_recs,
-                    &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild};
+                    &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   PinBuf* pins[] = {&c->h_nodes, &c->h_data, &c->h_misc, &c->h_recs};

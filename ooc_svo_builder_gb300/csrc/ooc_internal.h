@@ -51,6 +51,7 @@ struct VoxJob {
   uint64_t* task_off;       // per item: exclusive prefix of warp tasks (n_items + 1)
   unsigned long long* task_counter;
   uint64_t* item_mask;      // per small item: which of its candidates passed (pass 0 -> pass 1); may be NULL
+  uint64_t* item_box;       // per small item with a non-zero mask: its packed stripe-local box
 };
 
 struct EmitJob {

@@ -293,16 +293,23 @@ __device__ __forceinline__ bool item_box(const VoxJob& j, const TriVerts& tv, in
   return lo[0] <= hi[0] && lo[1] <= hi[1] && lo[2] <= hi[2];
 }
 
-// Rank of bit `b` among the set bits of the leaf level.
-__device__ __forceinline__ uint32_t leaf_rank(const VoxJob& j, uint32_t b) {
-  const uint32_t w = b >> 5, blk = w >> 3;
-  uint32_t r = j.leafscan[blk] - j.leafscan_base;
-  for (uint32_t q = blk * 8; q < w; q++) r += __popc(j.leafbits[q]);
-  return r + __popc(j.leafbits[w] & ((1u << (b & 31)) - 1u));
+// Set bits before bit `b` inside its 256-bit block (`blk` points at the block's 8 words).
+__device__ __forceinline__ uint32_t in_block_rank(const uint32_t* __restrict__ blk, uint64_t b) {
+  const uint4* q = reinterpret_cast<const uint4*>(blk);
+  const uint4 q0 = q[0], q1 = q[1];
+  const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+  const uint32_t wi = (uint32_t)(b >> 5) & 7u;
+  const uint32_t lowmask = (1u << (b & 31)) - 1u;
+  uint32_t r = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 8; k++) r += __popc(k < wi ? w[k] : (k == wi ? (w[k] & lowmask) : 0u));
+  return r;
 }
 
-__device__ __forceinline__ uint32_t local_morton(const VoxJob& j, int x, int y, int z) {
-  return morton_local((uint32_t)(x - j.sa[0]), (uint32_t)(y - j.sa[1]), (uint32_t)(z - j.sa[2]));
+// Rank of bit `b` among the set bits of the leaf level.
+__device__ __forceinline__ uint32_t leaf_rank(const VoxJob& j, uint32_t b) {
+  const uint32_t blk = b >> 8;
+  return j.leafscan[blk] - j.leafscan_base + in_block_rank(j.leafbits + (uint64_t)blk * 8, b);
 }
 
 // One z column of pass 0 (set bits) or pass 1 (winners, re-testing set voxels).
@@ -315,10 +322,12 @@ __device__ __forceinline__ uint64_t vox_column(const VoxJob& j, const TriSetup& 
   if (!pass_xy(s, px, py)) return 0;
   const float nxy = plane_xy(s, px, py);
   const uint32_t mxy = spread3_10((uint32_t)(x - j.sa[0])) | (spread3_10((uint32_t)(y - j.sa[1])) << 1);
+  constexpr uint32_t ZBITS = 0x24924924u;  // Morton bit positions of z (2, 5, ..., 29)
+  uint32_t mz = spread3_10((uint32_t)(z0 - j.sa[2])) << 2;
   uint32_t cur_w = 0xffffffffu, acc = 0;
   uint64_t col = 0;
-  for (int z = z0; z <= z1; z++) {
-    const uint32_t m = mxy | (spread3_10((uint32_t)(z - j.sa[2])) << 2);
+  for (int z = z0; z <= z1; z++, mz = ((mz | ~ZBITS) + 4u) & ZBITS) {
+    const uint32_t m = mxy | mz;
     if (PASS == 0) {
       if (pass_z(s, nxy, px, py, __fmul_rn((float)z, j.u))) {
         const uint32_t w = m >> 5;
@@ -367,6 +376,11 @@ __global__ void k_vox_small_occ(VoxJob j) {
           mask |= vox_column<0>(j, s, (uint32_t)t, x, y, lo[2], hi[2]) << shift;
           shift += (uint32_t)bz;
         }
+      if (j.item_mask && mask) {
+        // stripe-local box origin (10 bits per axis) and extents - 1 (6 bits each)
+        j.item_box[i] = (uint64_t)(lo[0] - j.sa[0]) | ((uint64_t)(lo[1] - j.sa[1]) << 10) |
+                        ((uint64_t)(lo[2] - j.sa[2]) << 20) | ((bx - 1) << 30) | ((by - 1) << 36) | ((bz - 1) << 42);
+      }
     } else {
       cost = (bx * by + 31) / 32;
     }
@@ -381,18 +395,17 @@ __global__ void k_vox_small_win(VoxJob j) {
   if (i >= j.n_items) return;
   uint64_t mask = j.item_mask[i];
   if (!mask) return;
-  const uint64_t t = item_triangle(j, i);
-  const TriVerts tv = load_verts(j.tris, t, j.stride);
-  int lo[3], hi[3];
-  if (!item_box(j, tv, lo, hi)) return;
-  const uint32_t bz = (uint32_t)(hi[2] - lo[2] + 1), by = (uint32_t)(hi[1] - lo[1] + 1);
+  const uint32_t t = (uint32_t)item_triangle(j, i);
+  const uint64_t box = j.item_box[i];
+  const uint32_t lx = (uint32_t)box & 1023u, ly = (uint32_t)(box >> 10) & 1023u, lz = (uint32_t)(box >> 20) & 1023u;
+  const uint32_t by = (uint32_t)(box >> 36 & 63u) + 1u, bz = (uint32_t)(box >> 42 & 63u) + 1u;
   while (mask) {
     const uint32_t q = (uint32_t)(__ffsll((long long)mask) - 1);
     mask &= mask - 1;
     const uint32_t col = q / bz, z = q - col * bz;
     const uint32_t x = col / by, y = col - x * by;
-    const uint32_t m = local_morton(j, lo[0] + (int)x, lo[1] + (int)y, lo[2] + (int)z);
-    atomicMin(&j.winners[leaf_rank(j, m)], (uint32_t)t);
+    const uint32_t m = morton_local(lx + x, ly + y, lz + z);
+    atomicMin(&j.winners[leaf_rank(j, m)], t);
   }
 }
 
@@ -469,10 +482,8 @@ __global__ void k_pyramid_top(Pyramid p, int l_hi) {
 // counts every node of the shallower levels.
 __device__ __forceinline__ uint64_t node_index(const uint32_t* __restrict__ bits, const uint32_t* __restrict__ scan,
                                                const Level& L, uint64_t b) {
-  const uint64_t w = b >> 5, blk = w >> 3;
-  uint32_t r = scan[L.off_b + blk];
-  for (uint64_t q = blk * 8; q < w; q++) r += __popc(bits[L.off_w + q]);
-  return (uint64_t)r + __popc(bits[L.off_w + w] & ((1u << (b & 31)) - 1u));
+  const uint64_t blk = b >> 8;
+  return (uint64_t)scan[L.off_b + blk] + in_block_rank(bits + L.off_w + blk * 8, b);
 }
 
 __device__ __forceinline__ uint32_t child_mask(const uint32_t* __restrict__ bits, const Level& C, uint32_t k) {
