@@ -45,6 +45,10 @@ WORKLOADS = {
     "icosphere256": dict(gridsize=256, limit=2048, payload=False, color="model",
                          desc="configuration 1: svo_builder_binary -s 256 -l 2048 on a subdivision-5 icosphere "
                               "(20,480 triangles)"),
+    "soup4096": dict(gridsize=4096, limit=2048, payload=False, color="model",
+                     desc="configuration 3: svo_builder_binary -s 4096 -l 2048 (64 partitions) on a 20M-triangle "
+                          "soup: half small triangles on 200 spheres, half log-normal edges (median 4 voxels, "
+                          "sigma 1.0, clipped at 512)"),
 }
 
 
@@ -53,6 +57,8 @@ def make_mesh(name: str) -> np.ndarray:
         return tri.heightfield_tris(HEIGHTFIELD_N, seed=2, payload=True)
     if name == "icosphere256":
         return tri.icosphere_tris(5, radius=0.4, jitter=0.002, seed=1)
+    if name == "soup4096":
+        return tri.soup_tris(20_000_000, 4096, seed=3, sigma=1.0)
     raise SystemExit("unknown workload " + name)
 
 

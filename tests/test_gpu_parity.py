@@ -138,3 +138,12 @@ def test_device_resident_build(builder, payload, N, limit, levels):
         assert not diffs, "\n".join(diffs)
     nodes, data, _ = pyoracle.build(t, N, limit, levels=levels)
     assert not octree.diff(dev, octree.Octree(N, nodes, data))
+
+
+def test_soup_64_partitions(builder):
+    """Configuration 3 scaled down: skewed log-normal soup plus sphere-surface triangles,
+    gridsize 1024 with -l 16 (64 partitions of 256^3)."""
+    t = tri.soup_tris(400_000, 1024, seed=33, sigma=1.0, n_spheres=50)
+    got, want, info = run_both(builder, t, 1024, limit=16)
+    assert info["n_partitions"] == 64
+    assert_same(got, want, info)
