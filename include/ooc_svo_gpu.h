@@ -100,6 +100,26 @@ uint64_t ooc_estimate_partitions(uint64_t gridsize, uint64_t memory_limit_mb);
 int ooc_build(ooc_ctx* ctx, const ooc_build_params* params, const float* tris_host, uint64_t n_tris,
               ooc_sink_fn sink, void* user, ooc_build_info* info);
 
+/* One mesh of a batch: host triangles (pinned or pageable) and its flags. */
+typedef struct {
+  const float* tris;
+  uint64_t n_tris;
+  ooc_build_params params;
+} ooc_mesh;
+
+/* Like ooc_sink_fn, with the index of the mesh whose file the bytes belong to.
+ * Each mesh's files arrive in file order; meshes may interleave. */
+typedef int (*ooc_batch_sink_fn)(void* user, uint64_t mesh, int32_t kind, const void* bytes, uint64_t nbytes);
+
+/* Many meshes with their own gridsize, mode and flags in one call: every stripe
+ * of every mesh goes through one launch sequence (split into sub-batches only
+ * when the occupancy pyramids exceed the context's memory budget).  Each
+ * mesh's output is byte-identical to ooc_build on that mesh.  `infos` (may be
+ * NULL) receives one ooc_build_info per mesh.  No counterpart in the
+ * reference, which builds one mesh per process. */
+int ooc_build_batch(ooc_ctx* ctx, const ooc_mesh* meshes, uint64_t n_meshes, ooc_batch_sink_fn sink, void* user,
+                    ooc_build_info* infos);
+
 /* Same path from triangles already in device memory; the octree stays in
  * device memory (see ooc_result_device).  `stream` is a cudaStream_t (NULL:
  * the context's own stream); all work is ordered on it and the call returns

@@ -30,7 +30,7 @@ PHASES = ("partition", "voxelize", "pyramid", "octree", "copies", "build")
 EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_partitions", "ooc_build",
            "ooc_build_device", "ooc_result_device", "ooc_result_copy", "ooc_set_phase_timing", "ooc_phase_times",
            "ooc_kernel_launches", "ooc_build_files", "ooc_set_kernel_timing", "ooc_kernel_time",
-           "ooc_voxelize_occupancy_noalloc")
+           "ooc_voxelize_occupancy_noalloc", "ooc_build_batch")
 
 
 class BuildParams(ctypes.Structure):
@@ -46,6 +46,12 @@ class BuildInfo(ctypes.Structure):
 
 
 SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_uint64)
+BATCH_SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p,
+                              ctypes.c_uint64)
+
+
+class Mesh(ctypes.Structure):
+    _fields_ = [("tris", ctypes.c_void_p), ("n_tris", ctypes.c_uint64), ("params", BuildParams)]
 
 
 class OocError(RuntimeError):
@@ -98,6 +104,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_kernel_time.argtypes = [ctypes.c_void_p, ctypes.c_int32, P(ctypes.c_char_p), P(ctypes.c_float),
                                     P(ctypes.c_uint64)]
     lib.ooc_kernel_time.restype = ctypes.c_int
+    lib.ooc_build_batch.argtypes = [ctypes.c_void_p, P(Mesh), ctypes.c_uint64, BATCH_SINK, ctypes.c_void_p,
+                                    P(BuildInfo)]
+    lib.ooc_build_batch.restype = ctypes.c_int
     lib.ooc_voxelize_occupancy_noalloc.argtypes = [P(BuildParams), ctypes.c_void_p, ctypes.c_uint64,
                                                    ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
     lib.ooc_voxelize_occupancy_noalloc.restype = ctypes.c_int
@@ -233,6 +242,38 @@ class Builder:
         self._check(rc)
         tree = _octree.from_bytes(int(params.gridsize), b"".join(parts[0]), b"".join(parts[1]))
         return BuildResult(tree, _info_dict(info))
+
+    def build_batch(self, meshes, params_list) -> list:
+        """Many meshes in one call; returns one BuildResult per mesh (host octree bytes)."""
+        if len(meshes) != len(params_list):
+            raise ValueError("one BuildParams per mesh")
+        arrs = []
+        arr = (Mesh * max(1, len(meshes)))()
+        for i, (t, p) in enumerate(zip(meshes, params_list)):
+            t = np.ascontiguousarray(t, dtype=np.float32)
+            width = 9 if p.geometry_only else 21
+            if t.ndim != 2 or t.shape[1] != width:
+                raise ValueError("mesh %d: triangles must be [T, %d] float32" % (i, width))
+            arrs.append(t)
+            arr[i].tris = t.ctypes.data
+            arr[i].n_tris = t.shape[0]
+            arr[i].params = p
+        parts = [{0: [], 1: []} for _ in meshes]
+
+        def _collect(user, mesh, kind, ptr, n):
+            parts[mesh][kind].append(ctypes.string_at(ptr, n))
+            return 0
+
+        cb = BATCH_SINK(_collect)
+        infos = (BuildInfo * max(1, len(meshes)))()
+        self._check(self.lib.ooc_build_batch(self.h, arr, len(meshes), cb, None, infos))
+        return [BuildResult(_octree.from_bytes(int(params_list[i].gridsize), b"".join(parts[i][0]),
+                                               b"".join(parts[i][1])), _info_dict(infos[i]))
+                for i in range(len(meshes))]
+
+    def build_batch_ptrs(self, mesh_array, n_meshes: int, sink, infos) -> None:
+        """Low-level batch call: a ctypes Mesh array, a BATCH_SINK and a BuildInfo array."""
+        self._check(self.lib.ooc_build_batch(self.h, mesh_array, n_meshes, sink, None, infos))
 
     def build_ptr(self, tris_ptr: int, n_tris: int, params: BuildParams, sink) -> dict:
         """Host triangles given by address (e.g. pinned memory); `sink` is a SINK instance."""

@@ -113,7 +113,10 @@ struct ooc_ctx {
   DevBuf d_tris, d_items, d_hist, d_axis, d_bits, d_scan, d_scanpart, d_keys, d_size, d_dsize, d_start, d_dstart,
       d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo, d_itemmask,
       d_firstchild, d_itembox;
-  PinBuf h_nodes, h_data, h_misc, h_recs;
+  PinBuf h_nodes, h_data, h_misc, h_recs, h_tables1, h_tables2;
+  DevBuf d_tables1, d_tables2;
+  std::vector<DevBuf> d_mesh_items;
+  uint64_t batch_budget_bytes = 4ull << 30;  // occupancy pyramids of one sub-batch
   uint64_t res_nodes = 0, res_data = 0;
   bool res_valid = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -172,30 +175,41 @@ struct TNode {
   bool is_null() const { return off == ~0ull && data == 0; }  // Node::isNull (Node.h:45-47)
 };
 
+// Where a mesh's records go: device files (records written on the host are
+// collected and scattered at the end), a host sink in file order, or nowhere
+// (the dry run that only computes positions).
 struct Emitter {
   bool device = false;
+  bool dry = false;
   // device mode: (index, words...) records scattered into the device files at the end
   std::vector<uint64_t> node_recs, data_recs;
   // host mode
-  ooc_sink_fn sink = nullptr;
+  ooc_batch_sink_fn sink = nullptr;
   void* user = nullptr;
+  uint64_t mesh = 0;
 
+  void span(int32_t kind, const void* bytes, uint64_t n) {
+    if (dry || device) return;
+    if (sink(user, mesh, kind, bytes, n) != 0) fail(OOC_ERR_SINK, "sink returned an error");
+  }
   void node(uint64_t pos, const TNode& n) {
+    if (dry) return;
     if (device) {
       node_recs.insert(node_recs.end(), {pos, n.data, n.cb, n.off});
     } else {
       uint64_t rec[3] = {n.data, n.cb, n.off};
-      if (sink(user, OOC_STREAM_NODES, rec, 24) != 0) fail(OOC_ERR_SINK, "node sink returned an error");
+      if (sink(user, mesh, OOC_STREAM_NODES, rec, 24) != 0) fail(OOC_ERR_SINK, "sink returned an error");
     }
   }
   void data(uint64_t pos, uint64_t morton, const float* v) {
+    if (dry) return;
     uint64_t w[4];
     w[0] = morton;
     std::memcpy(&w[1], v, 24);
     if (device) {
       data_recs.insert(data_recs.end(), {pos, w[0], w[1], w[2], w[3]});
     } else {
-      if (sink(user, OOC_STREAM_DATA, w, 32) != 0) fail(OOC_ERR_SINK, "data sink returned an error");
+      if (sink(user, mesh, OOC_STREAM_DATA, w, 32) != 0) fail(OOC_ERR_SINK, "sink returned an error");
     }
   }
 };
@@ -323,312 +337,547 @@ Plan make_plan(const ooc_build_params* p) {
   return pl;
 }
 
-struct StripeOut {
-  bool empty = true;
-  TNode root;
-  uint64_t node_span = 0, data_span = 0, filled = 0;
+// ---------------------------------------------------------------------------
+// The batch engine.  A batch is a list of meshes; every mesh is split into
+// stripes, and the stripes of all meshes run through one launch sequence (a
+// sub-batch when their occupancy pyramids exceed the memory budget).  Each
+// sub-batch synchronises with the host twice: after the level counts (to size
+// the per-node arrays and place every stripe's records in its file), and at
+// the end (root records for the host-side grouping).
+// ---------------------------------------------------------------------------
+struct MeshWork {
+  const ooc_build_params* prm = nullptr;
+  Plan pl;
+  const float* d_tris = nullptr;
+  uint64_t n_tris = 0;
+  std::vector<uint32_t> part_off;  // P > 1: items of partition p are part_off[p] .. part_off[p+1)
+  const uint32_t* items = nullptr;
+  Emitter* out = nullptr;
+  TopBuilder top;
+  uint64_t next_stripe = 0;  // stripes before this one have been pushed into `top`
+  uint64_t filled = 0;
+  uint64_t n_items = 0;
+  MeshWork(const Plan& p, Emitter* o) : pl(p), out(o), top(p.Ls, p.levels != 0, o) {}
 };
 
-StripeOut run_stripe(ooc_ctx* c, cudaStream_t st, const Plan& pl, const ooc_build_params* prm, const float* d_tris,
-                     uint64_t n_tris_total, const uint32_t* items, uint64_t ibeg, uint64_t n_items, uint64_t part,
-                     uint64_t stripe, uint64_t node_base, uint64_t data_base, bool device_mode) {
-  StripeOut res;
-  const int Ds = pl.Ds;
-  const int stride = pl.binary ? 9 : 21;
-  // Levels with at most this many 256-bit blocks (pyramid) or nodes (layout)
-  // run together in one CTA instead of one launch each.
-  constexpr uint64_t kSmallBlocks = 512, kSmallNodes = 256;
-  // ---- pyramid layout ----
-  Pyramid pyr;
-  std::memset(&pyr, 0, sizeof(pyr));
-  pyr.depth = Ds;
-  uint64_t words = 0, blocks = 0;
+struct StripeRef {
+  uint32_t mesh;
+  uint64_t stripe, part, ibeg, n_items;
+};
+
+struct Placed {  // a stripe after the level counts
+  bool empty = true;
+  uint64_t total = 0, n_leaf = 0, node_span = 0, data_span = 0, node_base = 0, data_base = 0;
+  uint64_t out_node_off = 0, out_data_off = 0;  // host mode: offsets in the batch output buffers
+};
+
+int pyramid_levels(int Ds, Level* lv, uint64_t& words, uint64_t& blocks) {
   for (int l = 0; l <= Ds; l++) {
     const uint64_t nbits = 1ull << (3 * l);
     uint64_t nw = (nbits + 31) / 32;
     nw = (nw + 7) / 8 * 8;
-    pyr.lv[l].off_w = words;
-    pyr.lv[l].off_b = blocks;
-    pyr.lv[l].nwords = nw;
-    pyr.lv[l].nblocks = nw / 8;
+    lv[l].off_w = words;
+    lv[l].off_b = blocks;
+    lv[l].nwords = nw;
+    lv[l].nblocks = nw / 8;
     words += nw;
     blocks += nw / 8;
   }
-  pyr.bits = ensure<uint32_t>(c->d_bits, words * 4);
-  pyr.scan = ensure<uint32_t>(c->d_scan, (blocks + 1) * 4);
+  return Ds;
+}
+
+void add_chunks(std::vector<Chunk>& v, uint32_t stripe, uint32_t level, uint64_t first, uint64_t count) {
+  for (uint64_t k = 0; k < count; k += kChunk) {
+    Chunk c;
+    c.stripe = stripe;
+    c.level = level;
+    c.first = first + k;
+    c.count = (uint32_t)std::min<uint64_t>(kChunk, count - k);
+    c.pad = 0;
+    v.push_back(c);
+  }
+}
+
+// Upload host vectors into one device buffer through pinned staging; returns device pointers.
+struct Uploader {
+  std::vector<std::pair<const void*, size_t>> parts;
+  size_t add(const void* p, size_t bytes) {
+    size_t off = 0;
+    for (auto& q : parts) off += (q.second + 255) / 256 * 256;
+    parts.push_back({p, bytes});
+    return off;
+  }
+  unsigned char* run(ooc_ctx* c, DevBuf& dev, PinBuf& pin, cudaStream_t st) {
+    size_t total = 0;
+    for (auto& q : parts) total += (q.second + 255) / 256 * 256;
+    unsigned char* h = ensure_pinned<unsigned char>(pin, total);
+    unsigned char* d = ensure<unsigned char>(dev, total);
+    size_t off = 0;
+    for (auto& q : parts) {
+      if (q.second) std::memcpy(h + off, q.first, q.second);
+      off += (q.second + 255) / 256 * 256;
+    }
+    ck(cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, st), "upload tables");
+    (void)c;
+    return d;
+  }
+};
+
+void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, const std::vector<StripeRef>& sb,
+                   bool device_mode) {
+  const uint32_t n = (uint32_t)sb.size();
+  // ---- geometry of every stripe ----
+  std::vector<Pyramid> pyr(n);
+  std::vector<VoxJob> vj(n);
+  std::vector<uint64_t> item_beg(n + 1, 0);
+  uint64_t words = 0, blocks = 0, items = 0;
+  int max_depth = 0;
+  for (uint32_t s = 0; s < n; s++) {
+    const StripeRef& r = sb[s];
+    const MeshWork& m = meshes[r.mesh];
+    std::memset(&pyr[s], 0, sizeof(Pyramid));
+    pyr[s].depth = m.pl.Ds;
+    pyramid_levels(m.pl.Ds, pyr[s].lv, words, blocks);
+    max_depth = std::max(max_depth, m.pl.Ds);
+    item_beg[s] = items;
+    items += r.n_items;
+  }
+  item_beg[n] = items;
+  uint32_t* bits = ensure<uint32_t>(c->d_bits, words * 4);
+  uint32_t* scan = ensure<uint32_t>(c->d_scan, (blocks + 1) * 4);
   uint32_t* scanpart = ensure<uint32_t>(c->d_scanpart, scan_partials_needed(blocks + 1) * 4);
+  uint64_t* task_off = ensure<uint64_t>(c->d_taskoff, (items + 1) * 8);
+  uint64_t* taskpart = ensure<uint64_t>(c->d_taskpart, scan_partials_needed(items + 1) * 8);
+  uint64_t* item_mask = ensure<uint64_t>(c->d_itemmask, items * 8);
+  uint64_t* item_box = ensure<uint64_t>(c->d_itembox, items * 8);
+  unsigned long long* counter = ensure<unsigned long long>(c->d_counter, 16);
+  uint32_t* d_root = ensure<uint32_t>(c->d_rootinfo, ((uint64_t)n * 16 + 64) * 4);
+  uint32_t* flag = d_root + (uint64_t)n * 16;
 
-  uint32_t pa[3], pb[3], sa[3];
-  morton_global_decode(part * pl.M, pa[0], pa[1], pa[2]);
-  morton_global_decode(stripe * pl.S, sa[0], sa[1], sa[2]);
-  const uint32_t pside = 1u << pl.Dm, sside = 1u << Ds;
-
-  VoxJob j;
-  std::memset(&j, 0, sizeof(j));
-  j.tris = d_tris;
-  j.stride = stride;
-  j.item_tri = items;
-  j.ibeg = ibeg;
-  j.n_items = n_items;
-  for (int a = 0; a < 3; a++) {
-    pb[a] = pa[a] + pside - 1;
-    j.pa[a] = (int)pa[a];
-    j.pb[a] = (int)pb[a];
-    j.sa[a] = (int)sa[a];
-    j.sb[a] = (int)(sa[a] + sside - 1);
+  std::vector<Chunk> ch_items, ch_pay_items, ch_compact;
+  std::vector<std::vector<Chunk>> ch_pyr(max_depth + 1);
+  constexpr int kTopPyramidLevel = 5;  // levels 0..5 have at most 512 blocks: one CTA per stripe
+  for (uint32_t s = 0; s < n; s++) {
+    const StripeRef& r = sb[s];
+    const MeshWork& m = meshes[r.mesh];
+    Pyramid& P = pyr[s];
+    P.bits = bits;
+    P.scan = scan;
+    VoxJob& j = vj[s];
+    std::memset(&j, 0, sizeof(j));
+    uint32_t pa[3], sa[3];
+    morton_global_decode(r.part * m.pl.M, pa[0], pa[1], pa[2]);
+    morton_global_decode(r.stripe * m.pl.S, sa[0], sa[1], sa[2]);
+    const uint32_t pside = 1u << m.pl.Dm, sside = 1u << m.pl.Ds;
+    j.tris = m.d_tris;
+    j.stride = m.pl.binary ? 9 : 21;
+    j.item_tri = m.items;
+    j.ibeg = r.ibeg;
+    j.n_items = r.n_items;
+    for (int a = 0; a < 3; a++) {
+      j.pa[a] = (int)pa[a];
+      j.pb[a] = (int)(pa[a] + pside - 1);
+      j.sa[a] = (int)sa[a];
+      j.sb[a] = (int)(sa[a] + sside - 1);
+    }
+    j.u = m.pl.u;
+    j.unit_div = m.pl.unit_div;
+    j.small_vol = 64;
+    j.leafbits = bits + P.lv[P.depth].off_w;
+    j.task_off = task_off + item_beg[s];
+    j.task_counter = counter;
+    j.item_mask = m.pl.binary ? nullptr : item_mask + item_beg[s];
+    j.item_box = m.pl.binary ? nullptr : item_box + item_beg[s];
+    add_chunks(ch_items, s, 0, 0, r.n_items);
+    if (!m.pl.binary) add_chunks(ch_pay_items, s, 0, 0, r.n_items);
+    for (int l = P.depth; l > kTopPyramidLevel; l--) add_chunks(ch_pyr[P.depth - l], s, (uint32_t)l, 0, P.lv[l].nblocks);
+    add_chunks(ch_compact, s, 0, P.lv[0].off_b, P.lv[P.depth].off_b + P.lv[P.depth].nblocks - P.lv[0].off_b);
   }
-  j.u = pl.u;
-  j.unit_div = pl.unit_div;
-  j.small_vol = 64;
-  j.leafbits = pyr.bits + pyr.lv[Ds].off_w;
-  j.task_off = ensure<uint64_t>(c->d_taskoff, (n_items + 1) * 8);
-  j.task_counter = ensure<unsigned long long>(c->d_counter, 16);
-  j.item_mask = pl.binary ? nullptr : ensure<uint64_t>(c->d_itemmask, n_items * 8);
-  j.item_box = pl.binary ? nullptr : ensure<uint64_t>(c->d_itembox, n_items * 8);
-  uint64_t* taskpart = ensure<uint64_t>(c->d_taskpart, scan_partials_needed(n_items + 1) * 8);
 
+  Uploader up1;
+  const size_t o_vj = up1.add(vj.data(), n * sizeof(VoxJob));
+  const size_t o_pyr = up1.add(pyr.data(), n * sizeof(Pyramid));
+  const size_t o_beg = up1.add(item_beg.data(), (n + 1) * 8);
+  const size_t o_chi = up1.add(ch_items.data(), ch_items.size() * sizeof(Chunk));
+  std::vector<size_t> o_chp(ch_pyr.size());
+  for (size_t r = 0; r < ch_pyr.size(); r++) o_chp[r] = up1.add(ch_pyr[r].data(), ch_pyr[r].size() * sizeof(Chunk));
+  unsigned char* t1 = up1.run(c, c->d_tables1, c->h_tables1, st);
+  const VoxJob* d_vj = reinterpret_cast<const VoxJob*>(t1 + o_vj);
+  const Pyramid* d_pyr = reinterpret_cast<const Pyramid*>(t1 + o_pyr);
+  const uint64_t* d_beg = reinterpret_cast<const uint64_t*>(t1 + o_beg);
+
+  uint32_t* lvl = ensure_pinned<uint32_t>(c->h_misc, ((uint64_t)n * 16 + 64) * 4);  // level bases, then root info
   {
     PhaseScope ph(c, PH_VOX, st);
-    ck(cudaMemsetAsync(pyr.bits, 0, words * 4, st), "memset bits");
-    ck(cudaMemsetAsync(j.task_off + n_items, 0, 8, st), "memset task_off");
-    launch_vox_small(j, 0, st);
-    scan_u64_exclusive(j.task_off, n_items + 1, taskpart, st);
-    launch_vox_large(j, 0, st, c->num_sms);
+    ck(cudaMemsetAsync(bits, 0, words * 4, st), "memset bits");
+    ck(cudaMemsetAsync(task_off + items, 0, 8, st), "memset task_off");
+    ck(cudaMemsetAsync(flag, 0, 4, st), "memset flag");
+    launch_b_vox_small(d_vj, reinterpret_cast<const Chunk*>(t1 + o_chi), ch_items.size(), 0, st);
+    scan_u64_exclusive(task_off, items + 1, taskpart, st);
+    launch_b_vox_large(d_vj, d_beg, n, task_off, items, counter, 0, st, c->num_sms);
   }
-  uint32_t* lvl = ensure_pinned<uint32_t>(c->h_misc, 64 * 4);
-  uint32_t* d_root = ensure<uint32_t>(c->d_rootinfo, 64 * 4);
   {
     PhaseScope ph(c, PH_PYR, st);
-    ck(cudaMemsetAsync(pyr.scan + blocks, 0, 4, st), "memset scan");
-    int l = Ds;
-    for (; l >= 0 && pyr.lv[l].nblocks > kSmallBlocks; l--) launch_pyramid(pyr, l, st);
-    if (l >= 0) launch_pyramid_top(pyr, l, st);
-    scan_u32_exclusive(pyr.scan, blocks + 1, scanpart, st);
-    launch_level_bases(pyr, blocks, d_root + 16, st);
-    ck(cudaMemcpyAsync(lvl, d_root + 16, (Ds + 2) * 4, cudaMemcpyDeviceToHost, st), "level bases");
+    ck(cudaMemsetAsync(scan + blocks, 0, 4, st), "memset scan");
+    for (size_t r = 0; r < ch_pyr.size(); r++)
+      launch_b_pyramid(d_pyr, reinterpret_cast<const Chunk*>(t1 + o_chp[r]), ch_pyr[r].size(), st);
+    launch_b_pyramid_top(d_pyr, n, kTopPyramidLevel, st);
+    scan_u32_exclusive(scan, blocks + 1, scanpart, st);
+    launch_b_level_bases(d_pyr, n, d_root, st);
+    ck(cudaMemcpyAsync(lvl, d_root, (uint64_t)n * (kMaxLevels + 1) * 4, cudaMemcpyDeviceToHost, st), "levels");
   }
-  ck(cudaStreamSynchronize(st), "stripe level counts");
-  for (int l = 0; l <= Ds; l++) {
-    pyr.lv[l].koff = lvl[l];
-    pyr.lv[l].n = (uint64_t)lvl[l + 1] - lvl[l];
+  ck(cudaStreamSynchronize(st), "level counts");
+
+  // ---- counts, placement in the files ----
+  std::vector<Placed> pl(n);
+  uint64_t total_nodes = 0, summed = 0;
+  for (uint32_t s = 0; s < n; s++) {
+    Pyramid& P = pyr[s];
+    const uint32_t* o = lvl + (uint64_t)s * (kMaxLevels + 1);
+    for (int l = 0; l <= P.depth; l++) {
+      P.lv[l].koff = o[l];
+      P.lv[l].n = (uint64_t)o[l + 1] - o[l];
+    }
+    const MeshWork& m = meshes[sb[s].mesh];
+    Placed& q = pl[s];
+    q.total = (uint64_t)o[P.depth + 1] - o[0];
+    q.n_leaf = P.lv[P.depth].n;
+    q.empty = q.n_leaf == 0;
+    if (!q.empty) {
+      q.node_span = q.total - 1;
+      q.data_span = (m.pl.binary ? 0 : q.n_leaf) + (m.pl.levels ? q.total - q.n_leaf : 0);
+    }
+    total_nodes = std::max<uint64_t>(total_nodes, o[P.depth + 1]);
+    summed += q.total;
   }
-  const uint64_t total = lvl[Ds + 1];
-  const uint64_t n_leaf = pyr.lv[Ds].n;
-  if (n_leaf == 0) return res;
-  res.empty = false;
-  res.filled = n_leaf;
-
-  EmitJob e;
-  std::memset(&e, 0, sizeof(e));
-  e.binary = pl.binary;
-  e.levels = pl.levels;
-  e.color_mode = prm->color_mode;
-  e.gridsize = pl.N;
-  e.stripe_base = stripe * pl.S;
-  for (int a = 0; a < 3; a++) e.origin[a] = (int)sa[a];
-  e.tris = d_tris;
-  e.stride = stride;
-  e.unit_div = pl.unit_div;
-  uint32_t* keys = ensure<uint32_t>(c->d_keys, total * 4);
-  e.keys = keys;
-  e.size = ensure<uint32_t>(c->d_size, total * 4);
-  e.dsize = ensure<uint32_t>(c->d_dsize, total * 4);
-  e.first_child = ensure<uint32_t>(c->d_firstchild, total * 4);
-  e.start = ensure<uint64_t>(c->d_start, total * 8);
-  e.dstart = ensure<uint64_t>(c->d_dstart, total * 8);
-  e.cache = pl.levels ? ensure<float>(c->d_cache, total * 24) : nullptr;
-  e.leaf_inline = (!pl.binary && !pl.levels) ? 1 : 0;
-
-  const uint64_t node_span = total - 1;
-  const uint64_t data_span = (pl.binary ? 0 : n_leaf) + (pl.levels ? total - n_leaf : 0);
-  res.node_span = node_span;
-  res.data_span = data_span;
+  // node indices are 32-bit within a sub-batch (the block scan is u32)
+  if (summed != total_nodes) fail(OOC_ERR_LIMIT, "more than 2^32 nodes in one sub-batch; lower the batch budget");
+  // dry run of the host-side grouping: where every stripe's records start
+  {
+    Emitter dry;
+    dry.dry = true;
+    std::vector<TopBuilder> tops;
+    std::vector<uint64_t> cursor(meshes.size());
+    std::vector<int> have(meshes.size(), -1);
+    for (uint32_t s = 0; s < n; s++) {
+      const uint32_t mi = sb[s].mesh;
+      if (have[mi] < 0) {
+        have[mi] = (int)tops.size();
+        tops.push_back(meshes[mi].top);
+        tops.back().out = &dry;
+        cursor[mi] = meshes[mi].next_stripe;
+      }
+      TopBuilder& tb = tops[have[mi]];
+      for (; cursor[mi] < sb[s].stripe; cursor[mi]++) tb.push(tb.top, TNode());
+      pl[s].node_base = tb.node_pos;
+      pl[s].data_base = tb.data_pos;
+      if (pl[s].empty) {
+        tb.push(tb.top, TNode());
+      } else {
+        tb.node_pos += pl[s].node_span;
+        tb.data_pos += pl[s].data_span;
+        TNode ph;
+        ph.off = 0;  // any non-null node
+        tb.push(tb.top, ph);
+      }
+      cursor[mi]++;
+    }
+  }
+  // ---- per-node arrays and output windows ----
+  bool any_levels = false, any_payload = false;
+  for (auto& m : meshes) {
+    any_levels = any_levels || m.pl.levels;
+    any_payload = any_payload || !m.pl.binary;
+  }
+  uint32_t* keys = ensure<uint32_t>(c->d_keys, total_nodes * 4);
+  uint32_t* size = ensure<uint32_t>(c->d_size, total_nodes * 4);
+  uint32_t* dsize = ensure<uint32_t>(c->d_dsize, total_nodes * 4);
+  uint32_t* first_child = ensure<uint32_t>(c->d_firstchild, total_nodes * 4);
+  uint64_t* start = ensure<uint64_t>(c->d_start, total_nodes * 8);
+  uint64_t* dstart = ensure<uint64_t>(c->d_dstart, total_nodes * 8);
+  float* cache = any_levels ? ensure<float>(c->d_cache, total_nodes * 24) : nullptr;
+  uint32_t* winners = any_payload ? ensure<uint32_t>(c->d_winners, total_nodes * 4) : nullptr;
+  uint64_t out_nodes = 0, out_data = 0;
   if (device_mode) {
-    e.node_win = ensure_keep<uint64_t>(c->d_nodes, (node_base + node_span) * 24, node_base * 24, st);
-    e.data_win = ensure_keep<unsigned char>(c->d_data, (data_base + data_span) * 32, data_base * 32, st);
-    e.node_win_base = 0;
-    e.data_win_base = 0;
-    e.node_win_len = node_base + node_span;
-    e.data_win_len = data_base + data_span;
+    uint64_t need_n = 0, need_d = 0;
+    for (uint32_t s = 0; s < n; s++) {
+      need_n = std::max(need_n, pl[s].node_base + pl[s].node_span);
+      need_d = std::max(need_d, pl[s].data_base + pl[s].data_span);
+    }
+    ensure_keep<uint64_t>(c->d_nodes, need_n * 24, need_n * 24, st);
+    ensure_keep<unsigned char>(c->d_data, need_d * 32, need_d * 32, st);
   } else {
-    e.node_win = ensure<uint64_t>(c->d_nodes, node_span * 24);
-    e.data_win = ensure<unsigned char>(c->d_data, data_span * 32);
-    e.node_win_base = node_base;
-    e.data_win_base = data_base;
-    e.node_win_len = node_span;
-    e.data_win_len = data_span;
+    for (uint32_t s = 0; s < n; s++) {
+      pl[s].out_node_off = out_nodes;
+      pl[s].out_data_off = out_data;
+      out_nodes += pl[s].node_span;
+      out_data += pl[s].data_span;
+    }
+    ensure<uint64_t>(c->d_nodes, out_nodes * 24);
+    ensure<unsigned char>(c->d_data, out_data * 32);
   }
-  e.n_tris = n_tris_total;
-  e.flag = d_root + 8;
-  ck(cudaMemsetAsync(e.flag, 0, 4, st), "memset flag");
+  std::vector<EmitJob> ej(n);
+  std::vector<Chunk> ch_leaves, ch_leafpay;
+  std::vector<std::vector<Chunk>> ch_bu(max_depth + 1), ch_td(max_depth + 1);
+  for (uint32_t s = 0; s < n; s++) {
+    const MeshWork& m = meshes[sb[s].mesh];
+    const Pyramid& P = pyr[s];
+    const Placed& q = pl[s];
+    EmitJob& e = ej[s];
+    std::memset(&e, 0, sizeof(e));
+    e.binary = m.pl.binary;
+    e.levels = m.pl.levels;
+    e.color_mode = m.prm->color_mode;
+    e.gridsize = m.pl.N;
+    e.stripe_base = sb[s].stripe * m.pl.S;
+    for (int a = 0; a < 3; a++) e.origin[a] = vj[s].sa[a];
+    e.tris = m.d_tris;
+    e.stride = vj[s].stride;
+    e.unit_div = m.pl.unit_div;
+    e.keys = keys;
+    e.size = size;
+    e.dsize = dsize;
+    e.first_child = first_child;
+    e.start = start;
+    e.dstart = dstart;
+    e.cache = m.pl.levels ? cache : nullptr;
+    e.leaf_inline = (!m.pl.binary && !m.pl.levels) ? 1 : 0;
+    e.n_tris = m.n_tris;
+    e.flag = flag;
+    e.node_base = q.node_base;
+    e.data_base = q.data_base;
+    if (device_mode) {
+      e.node_win = static_cast<uint64_t*>(c->d_nodes.p);
+      e.data_win = static_cast<unsigned char*>(c->d_data.p);
+      e.node_win_base = 0;
+      e.data_win_base = 0;
+      e.node_win_len = q.node_base + q.node_span;
+      e.data_win_len = q.data_base + q.data_span;
+    } else {
+      e.node_win = static_cast<uint64_t*>(c->d_nodes.p) + q.out_node_off * 3;
+      e.data_win = static_cast<unsigned char*>(c->d_data.p) + q.out_data_off * 32;
+      e.node_win_base = q.node_base;
+      e.data_win_base = q.data_base;
+      e.node_win_len = q.node_span;
+      e.data_win_len = q.data_span;
+    }
+    if (!m.pl.binary) {
+      e.winners = winners + P.lv[P.depth].koff;
+      vj[s].winners = winners + P.lv[P.depth].koff;
+      vj[s].leafscan = scan + P.lv[P.depth].off_b;
+      vj[s].leafscan_base = (uint32_t)P.lv[P.depth].koff;
+    }
+    if (q.empty) continue;
+    int ls = 0;
+    while (ls + 1 <= P.depth - 1 && P.lv[ls + 1].n <= 256) ls++;
+    e.l_small = ls;
+    if (P.depth >= 1) add_chunks(ch_leaves, s, (uint32_t)P.depth, 0, q.n_leaf);  // a depth-0 root is the leaf
+    if (m.pl.levels && !m.pl.binary) add_chunks(ch_leafpay, s, (uint32_t)P.depth, 0, q.n_leaf);
+    for (int l = P.depth - 1; l > ls; l--) add_chunks(ch_bu[P.depth - l], s, (uint32_t)l, 0, P.lv[l].n);
+    for (int l = std::min(ls, P.depth - 2) + 1; l <= P.depth - 2; l++) add_chunks(ch_td[l], s, (uint32_t)l, 0, P.lv[l].n);
+  }
+  Uploader up2;
+  const size_t o_vj2 = up2.add(vj.data(), n * sizeof(VoxJob));
+  const size_t o_pyr2 = up2.add(pyr.data(), n * sizeof(Pyramid));
+  const size_t o_ej = up2.add(ej.data(), n * sizeof(EmitJob));
+  const size_t o_cc = up2.add(ch_compact.data(), ch_compact.size() * sizeof(Chunk));
+  const size_t o_cpi = up2.add(ch_pay_items.data(), ch_pay_items.size() * sizeof(Chunk));
+  const size_t o_cl = up2.add(ch_leaves.data(), ch_leaves.size() * sizeof(Chunk));
+  const size_t o_clp = up2.add(ch_leafpay.data(), ch_leafpay.size() * sizeof(Chunk));
+  std::vector<size_t> o_bu(ch_bu.size()), o_td(ch_td.size());
+  for (size_t r = 0; r < ch_bu.size(); r++) o_bu[r] = up2.add(ch_bu[r].data(), ch_bu[r].size() * sizeof(Chunk));
+  for (size_t r = 0; r < ch_td.size(); r++) o_td[r] = up2.add(ch_td[r].data(), ch_td[r].size() * sizeof(Chunk));
+  unsigned char* t2 = up2.run(c, c->d_tables2, c->h_tables2, st);
+  const VoxJob* d_vj2 = reinterpret_cast<const VoxJob*>(t2 + o_vj2);
+  const Pyramid* d_pyr2 = reinterpret_cast<const Pyramid*>(t2 + o_pyr2);
+  const EmitJob* d_ej = reinterpret_cast<const EmitJob*>(t2 + o_ej);
 
   {
     PhaseScope ph(c, PH_PYR, st);
-    launch_compact(pyr, blocks, keys, st);
+    launch_b_compact(d_pyr2, reinterpret_cast<const Chunk*>(t2 + o_cc), ch_compact.size(), keys, st);
   }
-  if (!pl.binary) {
+  if (any_payload) {
     PhaseScope ph(c, PH_VOX, st);
-    uint32_t* winners = ensure<uint32_t>(c->d_winners, n_leaf * 4);
-    ck(cudaMemsetAsync(winners, 0xff, n_leaf * 4, st), "memset winners");
-    j.winners = winners;
-    j.leafscan = pyr.scan + pyr.lv[Ds].off_b;
-    j.leafscan_base = (uint32_t)pyr.lv[Ds].koff;
-    launch_vox_small(j, 1, st);
-    launch_vox_large(j, 1, st, c->num_sms);
-    e.winners = winners;
-    if (pl.levels) launch_leaf_payload(pyr, e, st);
+    ck(cudaMemsetAsync(winners, 0xff, total_nodes * 4, st), "memset winners");
+    launch_b_vox_small(d_vj2, reinterpret_cast<const Chunk*>(t2 + o_cpi), ch_pay_items.size(), 1, st);
+    launch_b_vox_large(d_vj2, d_beg, n, task_off, items, counter, 1, st, c->num_sms);
+    launch_b_leaf_payload(d_pyr2, d_ej, reinterpret_cast<const Chunk*>(t2 + o_clp), ch_leafpay.size(), st);
   }
-  uint32_t* h_root = lvl + 32;
   {
     PhaseScope ph(c, PH_TREE, st);
-    // levels 0 .. l_small hold at most kSmallNodes nodes each (counts grow with depth)
-    int l_small = 0;
-    while (l_small + 1 <= Ds - 1 && pyr.lv[l_small + 1].n <= kSmallNodes) l_small++;
-    if (Ds >= 1) {
-      for (int l = Ds - 1; l > l_small; l--) launch_bottom_up(pyr, e, l, st);
-      launch_bottom_up_top(pyr, e, l_small, st);
-      // parents of internal children: levels 0 .. Ds-2; the leaves get one thread each
-      const int top_last = std::min(l_small, Ds - 2);
-      launch_top_down_top(pyr, e, top_last, node_base, data_base, st);
-      for (int l = top_last + 1; l <= Ds - 2; l++) launch_top_down(pyr, e, l, st);
-      launch_top_down_leaves(pyr, e, st);
-    }
-    launch_root_info(pyr, e, data_base, d_root, st);
-    ck(cudaMemcpyAsync(h_root, d_root, 9 * 4, cudaMemcpyDeviceToHost, st), "root info");
+    for (size_t r = 1; r < ch_bu.size(); r++)
+      launch_b_bottom_up(d_pyr2, d_ej, reinterpret_cast<const Chunk*>(t2 + o_bu[r]), ch_bu[r].size(), st);
+    launch_b_bottom_up_top(d_pyr2, d_ej, n, st);
+    launch_b_top_down_top(d_pyr2, d_ej, n, st);
+    for (size_t l = 0; l < ch_td.size(); l++)
+      launch_b_top_down(d_pyr2, d_ej, reinterpret_cast<const Chunk*>(t2 + o_td[l]), ch_td[l].size(), st);
+    launch_b_top_down_leaves(d_pyr2, d_ej, reinterpret_cast<const Chunk*>(t2 + o_cl), ch_leaves.size(), st);
+    launch_b_root_info(d_pyr2, d_ej, n, d_root, st);
+    ck(cudaMemcpyAsync(lvl, d_root, ((uint64_t)n * 16 + 1) * 4, cudaMemcpyDeviceToHost, st), "root info");
   }
   if (!device_mode) {
     PhaseScope ph(c, PH_COPY, st);
-    void* hn = ensure_pinned<void>(c->h_nodes, node_span * 24);
-    void* hd = ensure_pinned<void>(c->h_data, data_span * 32);
-    if (node_span) ck(cudaMemcpyAsync(hn, e.node_win, node_span * 24, cudaMemcpyDeviceToHost, st), "D2H nodes");
-    if (data_span) ck(cudaMemcpyAsync(hd, e.data_win, data_span * 32, cudaMemcpyDeviceToHost, st), "D2H data");
+    void* hn = ensure_pinned<void>(c->h_nodes, out_nodes * 24);
+    void* hd = ensure_pinned<void>(c->h_data, out_data * 32);
+    if (out_nodes) ck(cudaMemcpyAsync(hn, c->d_nodes.p, out_nodes * 24, cudaMemcpyDeviceToHost, st), "D2H nodes");
+    if (out_data) ck(cudaMemcpyAsync(hd, c->d_data.p, out_data * 32, cudaMemcpyDeviceToHost, st), "D2H data");
   }
-  ck(cudaStreamSynchronize(st), "stripe");
-  ck(cudaGetLastError(), "stripe kernels");
-  if (h_root[8] != 0) fail(OOC_ERR_DEVICE, "internal layout check failed (flag " + std::to_string(h_root[8]) + ")");
+  ck(cudaStreamSynchronize(st), "sub-batch");
+  ck(cudaGetLastError(), "sub-batch kernels");
+  if (lvl[(uint64_t)n * 16] != 0)
+    fail(OOC_ERR_DEVICE, "internal layout check failed (flag " + std::to_string(lvl[(uint64_t)n * 16]) + ")");
 
-  TNode& r = res.root;
-  const uint32_t mask = h_root[0];
-  float cache[6];
-  std::memcpy(cache, h_root + 1, sizeof(cache));
-  if (Ds >= 1) {
-    r.data = pl.levels ? data_base + data_span - 1 : 0;
-    r.cb = node_base + total - 1 - (uint64_t)__builtin_popcount(mask);
-    r.off = offsets_from_mask(mask);
-    if (pl.levels) std::memcpy(r.cache, cache, sizeof(cache));
-  } else {
-    r.data = pl.binary ? 1 : data_base;
-    r.cb = 0;
-    r.off = ~0ull;
-    if (!pl.binary) std::memcpy(r.cache, cache, sizeof(cache));
+  // ---- hand the stripes to their meshes, in file order ----
+  for (uint32_t s = 0; s < n; s++) {
+    MeshWork& m = meshes[sb[s].mesh];
+    for (; m.next_stripe < sb[s].stripe; m.next_stripe++) m.top.push(m.top.top, TNode());
+    m.next_stripe++;
+    const Placed& q = pl[s];
+    if (q.node_base != m.top.node_pos || q.data_base != m.top.data_pos)
+      fail(OOC_ERR_DEVICE, "internal placement mismatch");
+    if (q.empty) {
+      m.top.push(m.top.top, TNode());
+      continue;
+    }
+    m.filled += q.n_leaf;
+    if (!device_mode) {
+      const char* hn = static_cast<const char*>(c->h_nodes.p) + q.out_node_off * 24;
+      const char* hd = static_cast<const char*>(c->h_data.p) + q.out_data_off * 32;
+      if (q.node_span) m.out->span(OOC_STREAM_NODES, hn, q.node_span * 24);
+      if (q.data_span) m.out->span(OOC_STREAM_DATA, hd, q.data_span * 32);
+    }
+    m.top.node_pos += q.node_span;
+    m.top.data_pos += q.data_span;
+    const uint32_t* h_root = lvl + (uint64_t)s * 16;
+    TNode r;
+    const uint32_t mask = h_root[0];
+    float cf[6];
+    std::memcpy(cf, h_root + 1, sizeof(cf));
+    if (pyr[s].depth >= 1) {
+      r.data = m.pl.levels ? q.data_base + q.data_span - 1 : 0;
+      r.cb = q.node_base + q.total - 1 - (uint64_t)__builtin_popcount(mask);
+      r.off = offsets_from_mask(mask);
+      if (m.pl.levels) std::memcpy(r.cache, cf, sizeof(cf));
+    } else {
+      r.data = m.pl.binary ? 1 : q.data_base;
+      r.cb = 0;
+      r.off = ~0ull;
+      if (!m.pl.binary) std::memcpy(r.cache, cf, sizeof(cf));
+    }
+    m.top.push(m.top.top, r);
   }
-  return res;
 }
 
-void build_core(ooc_ctx* c, const ooc_build_params* prm, const float* d_tris, uint64_t n_tris, cudaStream_t st,
-                Emitter& out, ooc_build_info* info) {
-  const Plan pl = make_plan(prm);
+// Binning of a P > 1 mesh into per-partition item lists (K1).
+void bin_mesh(ooc_ctx* c, cudaStream_t st, MeshWork& m, DevBuf& items_buf) {
+  const Plan& pl = m.pl;
   const int stride = pl.binary ? 9 : 21;
-
-  // ---- partition binning (P > 1) ----
-  std::vector<uint32_t> part_off;
-  uint32_t* items = nullptr;
-  uint64_t n_items = n_tris;
-  if (pl.P > 1) {
-    PhaseScope ph(c, PH_BIN, st);
-    const int PA = 1 << pl.kP;
-    const uint64_t side = pl.N / PA;
-    std::vector<float> axis(6 * PA);
-    for (int a = 0; a < 3; a++)
-      for (int jj = 0; jj < PA; jj++) {
-        // createBuffers world box (partitioner.cpp:56-61)
-        axis[a * PA + jj] = (float)(uint32_t)(jj * side) * pl.u;
-        axis[3 * PA + a * PA + jj] = (float)(uint32_t)((jj + 1) * side) * pl.u;
-      }
-    float* d_axis = ensure<float>(c->d_axis, axis.size() * 4);
-    ck(cudaMemcpyAsync(d_axis, axis.data(), axis.size() * 4, cudaMemcpyHostToDevice, st), "axis boxes");
-    uint32_t* hist = ensure<uint32_t>(c->d_hist, pl.P * 4);
-    ck(cudaMemsetAsync(hist, 0, pl.P * 4, st), "memset hist");
-    launch_part_count(d_tris, stride, n_tris, d_axis, d_axis + 3 * PA, pl.kP, pl.P, hist, st);
-    std::vector<uint32_t> h(pl.P);
-    ck(cudaMemcpyAsync(h.data(), hist, pl.P * 4, cudaMemcpyDeviceToHost, st), "hist");
-    ck(cudaStreamSynchronize(st), "binning");
-    part_off.assign(pl.P + 1, 0);
-    uint64_t acc = 0;
-    for (uint64_t i = 0; i < pl.P; i++) {
-      part_off[i] = (uint32_t)acc;
-      acc += h[i];
-      if (acc >= (1ull << 32)) fail(OOC_ERR_INVALID, "more than 2^32 (triangle, partition) pairs");
+  PhaseScope ph(c, PH_BIN, st);
+  const int PA = 1 << pl.kP;
+  const uint64_t side = pl.N / PA;
+  std::vector<float> axis(6 * PA);
+  for (int a = 0; a < 3; a++)
+    for (int jj = 0; jj < PA; jj++) {
+      // createBuffers world box (partitioner.cpp:56-61)
+      axis[a * PA + jj] = (float)(uint32_t)(jj * side) * pl.u;
+      axis[3 * PA + a * PA + jj] = (float)(uint32_t)((jj + 1) * side) * pl.u;
     }
-    part_off[pl.P] = (uint32_t)acc;
-    n_items = acc;
-    items = ensure<uint32_t>(c->d_items, n_items * 4);
-    ck(cudaMemcpyAsync(hist, part_off.data(), pl.P * 4, cudaMemcpyHostToDevice, st), "cursors");
-    launch_part_emit(d_tris, stride, n_tris, d_axis, d_axis + 3 * PA, pl.kP, pl.P, hist, items, st);
+  float* d_axis = ensure<float>(c->d_axis, axis.size() * 4);
+  ck(cudaMemcpyAsync(d_axis, axis.data(), axis.size() * 4, cudaMemcpyHostToDevice, st), "axis boxes");
+  uint32_t* hist = ensure<uint32_t>(c->d_hist, pl.P * 4);
+  ck(cudaMemsetAsync(hist, 0, pl.P * 4, st), "memset hist");
+  launch_part_count(m.d_tris, stride, m.n_tris, d_axis, d_axis + 3 * PA, pl.kP, pl.P, hist, st);
+  std::vector<uint32_t> h(pl.P);
+  ck(cudaMemcpyAsync(h.data(), hist, pl.P * 4, cudaMemcpyDeviceToHost, st), "hist");
+  ck(cudaStreamSynchronize(st), "binning");
+  m.part_off.assign(pl.P + 1, 0);
+  uint64_t acc = 0;
+  for (uint64_t i = 0; i < pl.P; i++) {
+    m.part_off[i] = (uint32_t)acc;
+    acc += h[i];
+    if (acc >= (1ull << 32)) fail(OOC_ERR_INVALID, "more than 2^32 (triangle, partition) pairs");
   }
+  m.part_off[pl.P] = (uint32_t)acc;
+  m.n_items = acc;
+  uint32_t* items = ensure<uint32_t>(items_buf, acc * 4);
+  ck(cudaMemcpyAsync(hist, m.part_off.data(), pl.P * 4, cudaMemcpyHostToDevice, st), "cursors");
+  ck(cudaStreamSynchronize(st), "cursors");  // part_off is reused on the host
+  launch_part_emit(m.d_tris, stride, m.n_tris, d_axis, d_axis + 3 * PA, pl.kP, pl.P, hist, items, st);
+  m.items = items;
+}
 
-  TopBuilder top(pl.Ls, pl.levels != 0, &out);
-  // data file header records (OctreeBuilder.cpp:22-28)
-  {
+// Whole path for a list of meshes (triangles already on the device).
+void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bool device_mode) {
+  if (c->d_mesh_items.size() < meshes.size()) c->d_mesh_items.resize(meshes.size());
+  for (size_t i = 0; i < meshes.size(); i++) {
+    MeshWork& m = meshes[i];
+    if (m.pl.P > 1) bin_mesh(c, st, m, c->d_mesh_items[i]);
+    else m.n_items = m.n_tris;
+    // data file header records (OctreeBuilder.cpp:22-28)
     float zero[6] = {0, 0, 0, 0, 0, 0};
-    out.data(top.data_pos++, 0, zero);
-    if (pl.binary) {
+    m.out->data(m.top.data_pos++, 0, zero);
+    if (m.pl.binary) {
       float white[6] = {1, 1, 1, 0, 0, 0};
-      out.data(top.data_pos++, 0, white);
+      m.out->data(m.top.data_pos++, 0, white);
     }
   }
-  uint64_t filled = 0;
-  for (uint64_t s = 0; s < pl.n_stripes; s++) {
-    const uint64_t part = s / pl.stripes_per_part;
-    const uint64_t ibeg = pl.P > 1 ? part_off[part] : 0;
-    const uint64_t cnt = pl.P > 1 ? (uint64_t)part_off[part + 1] - part_off[part] : n_tris;
-    if (cnt == 0) {  // main.cpp:330: partitions without triangles are skipped
-      top.push(pl.Ls, TNode());
-      continue;
+  // stripes with items, in mesh order and Morton order, split by the pyramid budget
+  std::vector<StripeRef> sb;
+  uint64_t budget_words = 0;
+  const uint64_t budget = c->batch_budget_bytes / 4;
+  for (uint32_t mi = 0; mi < meshes.size(); mi++) {
+    MeshWork& m = meshes[mi];
+    for (uint64_t s = 0; s < m.pl.n_stripes; s++) {
+      const uint64_t part = s / m.pl.stripes_per_part;
+      const uint64_t ibeg = m.pl.P > 1 ? m.part_off[part] : 0;
+      const uint64_t cnt = m.pl.P > 1 ? (uint64_t)m.part_off[part + 1] - m.part_off[part] : m.n_tris;
+      if (cnt == 0) continue;  // main.cpp:330: partitions without triangles are skipped
+      Level tmp[kMaxLevels];
+      uint64_t w = 0, b = 0;
+      pyramid_levels(m.pl.Ds, tmp, w, b);
+      if (!sb.empty() && budget_words + w > budget) {
+        run_sub_batch(c, st, meshes, sb, device_mode);
+        sb.clear();
+        budget_words = 0;
+      }
+      sb.push_back(StripeRef{mi, s, part, ibeg, cnt});
+      budget_words += w;
     }
-    StripeOut so = run_stripe(c, st, pl, prm, d_tris, n_tris, items, ibeg, cnt, part, s, top.node_pos, top.data_pos, out.device);
-    if (so.empty) {
-      top.push(pl.Ls, TNode());
-      continue;
-    }
-    filled += so.filled;
-    if (!out.device) {
-      if (so.node_span && out.sink(out.user, OOC_STREAM_NODES, c->h_nodes.p, so.node_span * 24) != 0)
-        fail(OOC_ERR_SINK, "node sink returned an error");
-      if (so.data_span && out.sink(out.user, OOC_STREAM_DATA, c->h_data.p, so.data_span * 32) != 0)
-        fail(OOC_ERR_SINK, "data sink returned an error");
-    }
-    top.node_pos += so.node_span;
-    top.data_pos += so.data_span;
-    top.push(pl.Ls, so.root);
   }
-  // finalizeTree: the root is written last (OctreeBuilder.cpp:34-55)
-  out.node(top.node_pos++, top.buf[0][0]);
+  if (!sb.empty()) run_sub_batch(c, st, meshes, sb, device_mode);
+  for (MeshWork& m : meshes) {
+    for (; m.next_stripe < m.pl.n_stripes; m.next_stripe++) m.top.push(m.top.top, TNode());
+    // finalizeTree: the root is written last (OctreeBuilder.cpp:34-55)
+    m.out->node(m.top.node_pos++, m.top.buf[0][0]);
+  }
+}
 
-  if (info) {
-    info->n_nodes = top.node_pos;
-    info->n_data = top.data_pos;
-    info->n_filled = filled;
-    info->n_partitions = pl.P;
-    info->n_stripes = pl.n_stripes;
-    info->n_items = n_items;
-  }
-  if (out.device) {
-    uint64_t* nodes = ensure_keep<uint64_t>(c->d_nodes, top.node_pos * 24, (top.node_pos - 1) * 24, st);
-    unsigned char* data = ensure_keep<unsigned char>(c->d_data, top.data_pos * 32, top.data_pos * 32, st);
-    const uint64_t nr = out.node_recs.size() / 4, dr = out.data_recs.size() / 5;
-    const size_t bytes = (out.node_recs.size() + out.data_recs.size()) * 8;
-    uint64_t* h = ensure_pinned<uint64_t>(c->h_recs, bytes);
-    std::memcpy(h, out.node_recs.data(), out.node_recs.size() * 8);
-    std::memcpy(h + out.node_recs.size(), out.data_recs.data(), out.data_recs.size() * 8);
-    uint64_t* d = ensure<uint64_t>(c->d_recs, bytes);
-    ck(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st), "records");
-    launch_scatter_records(d, nr, 3, nodes, st);
-    launch_scatter_records(d + out.node_recs.size(), dr, 4, reinterpret_cast<uint64_t*>(data), st);
-    c->res_nodes = top.node_pos;
-    c->res_data = top.data_pos;
-    c->res_valid = true;
-  }
+void fill_info(const MeshWork& m, ooc_build_info* info) {
+  if (!info) return;
+  info->n_nodes = m.top.node_pos;
+  info->n_data = m.top.data_pos;
+  info->n_filled = m.filled;
+  info->n_partitions = m.pl.P;
+  info->n_stripes = m.pl.n_stripes;
+  info->n_items = m.n_items;
+}
+
+// Device mode: scatter the host-written records (top levels, header records) into the device files.
+void finish_device_output(ooc_ctx* c, cudaStream_t st, MeshWork& m, Emitter& out) {
+  uint64_t* nodes = ensure_keep<uint64_t>(c->d_nodes, m.top.node_pos * 24, m.top.node_pos * 24, st);
+  unsigned char* data = ensure_keep<unsigned char>(c->d_data, m.top.data_pos * 32, m.top.data_pos * 32, st);
+  const uint64_t nr = out.node_recs.size() / 4, dr = out.data_recs.size() / 5;
+  const size_t bytes = (out.node_recs.size() + out.data_recs.size()) * 8;
+  uint64_t* h = ensure_pinned<uint64_t>(c->h_recs, bytes);
+  std::memcpy(h, out.node_recs.data(), out.node_recs.size() * 8);
+  std::memcpy(h + out.node_recs.size(), out.data_recs.data(), out.data_recs.size() * 8);
+  uint64_t* d = ensure<uint64_t>(c->d_recs, bytes);
+  ck(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st), "records");
+  launch_scatter_records(d, nr, 3, nodes, st);
+  launch_scatter_records(d + out.node_recs.size(), dr, 4, reinterpret_cast<uint64_t*>(data), st);
+  c->res_nodes = m.top.node_pos;
+  c->res_data = m.top.data_pos;
+  c->res_valid = true;
 }
 
 void finish_timing(ooc_ctx* c) {
@@ -744,9 +993,13 @@ void ooc_ctx_destroy(ooc_ctx* c) {
                     &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
-  PinBuf* pins[] = {&c->h_nodes, &c->h_data, &c->h_misc, &c->h_recs};
+  PinBuf* pins[] = {&c->h_nodes, &c->h_data, &c->h_misc, &c->h_recs, &c->h_tables1, &c->h_tables2};
   for (PinBuf* b : pins)
     if (b->p) cudaFreeHost(b->p);
+  if (c->d_tables1.p) cudaFree(c->d_tables1.p);
+  if (c->d_tables2.p) cudaFree(c->d_tables2.p);
+  for (DevBuf& b : c->d_mesh_items)
+    if (b.p) cudaFree(b.p);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
@@ -766,30 +1019,78 @@ uint64_t ooc_estimate_partitions(uint64_t gridsize, uint64_t memory_limit_mb) {
   return n;
 }
 
+namespace {
+struct SingleSink {
+  ooc_sink_fn sink;
+  void* user;
+};
+int single_sink(void* user, uint64_t, int32_t kind, const void* bytes, uint64_t n) {
+  SingleSink* s = static_cast<SingleSink*>(user);
+  return s->sink(s->user, kind, bytes, n);
+}
+}  // namespace
+
 int ooc_build(ooc_ctx* c, const ooc_build_params* prm, const float* tris_host, uint64_t n_tris, ooc_sink_fn sink,
               void* user, ooc_build_info* info) {
+  if (!sink) {
+    if (c) c->err = "sink is NULL";
+    return OOC_ERR_INVALID;
+  }
+  ooc_mesh m;
+  std::memset(&m, 0, sizeof(m));
+  if (prm) m.params = *prm;
+  m.tris = tris_host;
+  m.n_tris = n_tris;
+  SingleSink ss{sink, user};
+  if (!prm) {
+    if (c) c->err = "params is NULL";
+    return OOC_ERR_INVALID;
+  }
+  return ooc_build_batch(c, &m, 1, single_sink, &ss, info);
+}
+
+int ooc_build_batch(ooc_ctx* c, const ooc_mesh* meshes_in, uint64_t n_meshes, ooc_batch_sink_fn sink, void* user,
+                    ooc_build_info* infos) {
   return guarded(c, [&] {
     begin_build(c);
-    check_params(prm, n_tris);
     if (!sink) fail(OOC_ERR_INVALID, "sink is NULL");
-    if (n_tris && !tris_host) fail(OOC_ERR_INVALID, "triangles are NULL");
+    if (n_meshes && !meshes_in) fail(OOC_ERR_INVALID, "meshes are NULL");
     cudaStream_t st = c->own_stream;
-    const int stride = prm->geometry_only ? 9 : 21;
-    const size_t bytes = n_tris * stride * sizeof(float);
-    float* d_tris = ensure<float>(c->d_tris, bytes);
+    // one device buffer for every mesh's triangles (256-byte aligned slices)
+    std::vector<uint64_t> off(n_meshes + 1, 0);
+    for (uint64_t i = 0; i < n_meshes; i++) {
+      check_params(&meshes_in[i].params, meshes_in[i].n_tris);
+      if (meshes_in[i].n_tris && !meshes_in[i].tris) fail(OOC_ERR_INVALID, "triangles are NULL");
+      const uint64_t bytes = meshes_in[i].n_tris * (meshes_in[i].params.geometry_only ? 9 : 21) * 4;
+      off[i + 1] = off[i] + (bytes + 255) / 256 * 256;
+    }
+    unsigned char* d_all = ensure<unsigned char>(c->d_tris, off[n_meshes]);
+    std::vector<Emitter> outs(n_meshes);
+    std::vector<MeshWork> meshes;
+    meshes.reserve(n_meshes);
+    for (uint64_t i = 0; i < n_meshes; i++) {
+      outs[i].sink = sink;
+      outs[i].user = user;
+      outs[i].mesh = i;
+      meshes.emplace_back(make_plan(&meshes_in[i].params), &outs[i]);
+      meshes.back().prm = &meshes_in[i].params;
+      meshes.back().d_tris = reinterpret_cast<const float*>(d_all + off[i]);
+      meshes.back().n_tris = meshes_in[i].n_tris;
+    }
     {
       PhaseScope all(c, PH_ALL, st);
       {
         PhaseScope ph(c, PH_COPY, st);
-        if (bytes) ck(cudaMemcpyAsync(d_tris, tris_host, bytes, cudaMemcpyHostToDevice, st), "H2D triangles");
+        for (uint64_t i = 0; i < n_meshes; i++) {
+          const uint64_t bytes = meshes_in[i].n_tris * (meshes_in[i].params.geometry_only ? 9 : 21) * 4;
+          if (bytes) ck(cudaMemcpyAsync(d_all + off[i], meshes_in[i].tris, bytes, cudaMemcpyHostToDevice, st), "H2D");
+        }
       }
-      Emitter out;
-      out.device = false;
-      out.sink = sink;
-      out.user = user;
-      build_core(c, prm, d_tris, n_tris, st, out, info);
+      build_meshes(c, st, meshes, false);
     }
     ck(cudaStreamSynchronize(st), "build");
+    if (infos)
+      for (uint64_t i = 0; i < n_meshes; i++) fill_info(meshes[i], &infos[i]);
     finish_timing(c);
   });
 }
@@ -801,14 +1102,21 @@ int ooc_build_device(ooc_ctx* c, const ooc_build_params* prm, const float* tris_
     check_params(prm, n_tris);
     if (n_tris && !tris_device) fail(OOC_ERR_INVALID, "triangles are NULL");
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+    Emitter out;
+    out.device = true;
+    std::vector<MeshWork> meshes;
+    meshes.emplace_back(make_plan(prm), &out);
+    meshes[0].prm = prm;
+    meshes[0].d_tris = tris_device;
+    meshes[0].n_tris = n_tris;
     {
       PhaseScope all(c, PH_ALL, st);
-      Emitter out;
-      out.device = true;
-      build_core(c, prm, tris_device, n_tris, st, out, info);
+      build_meshes(c, st, meshes, true);
+      finish_device_output(c, st, meshes[0], out);
     }
     ck(cudaStreamSynchronize(st), "build");
     ck(cudaGetLastError(), "build kernels");
+    fill_info(meshes[0], info);
     finish_timing(c);
   });
 }

@@ -357,9 +357,7 @@ __device__ __forceinline__ uint64_t item_triangle(const VoxJob& j, uint64_t i) {
 // Pass 0, one thread per item: items with at most small_vol (<= 64) candidates
 // are voxelized here and leave their pass mask; larger ones get a warp-task
 // count (32 columns per task).
-__global__ void k_vox_small_occ(VoxJob j) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= j.n_items) return;
+__device__ __forceinline__ void vox_small_occ_item(const VoxJob& j, uint64_t i) {
   const uint64_t t = item_triangle(j, i);
   const TriVerts tv = load_verts(j.tris, t, j.stride);
   int lo[3], hi[3];
@@ -389,10 +387,13 @@ __global__ void k_vox_small_occ(VoxJob j) {
   if (j.item_mask) j.item_mask[i] = mask;
 }
 
-// Pass 1 for small items: rank the voxels their pass mask names.
-__global__ void k_vox_small_win(VoxJob j) {
+__global__ void k_vox_small_occ(VoxJob j) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= j.n_items) return;
+  if (i < j.n_items) vox_small_occ_item(j, i);
+}
+
+// Pass 1 for small items: rank the voxels their pass mask names.
+__device__ __forceinline__ void vox_small_win_item(const VoxJob& j, uint64_t i) {
   uint64_t mask = j.item_mask[i];
   if (!mask) return;
   const uint32_t t = (uint32_t)item_triangle(j, i);
@@ -406,6 +407,30 @@ __global__ void k_vox_small_win(VoxJob j) {
     const uint32_t x = col / by, y = col - x * by;
     const uint32_t m = morton_local(lx + x, ly + y, lz + z);
     atomicMin(&j.winners[leaf_rank(j, m)], t);
+  }
+}
+
+__global__ void k_vox_small_win(VoxJob j) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < j.n_items) vox_small_win_item(j, i);
+}
+
+// Columns 32*k .. 32*k+31 of large item i (one per lane).
+template <int PASS>
+__device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint64_t k, int lane) {
+  if (PASS == 1 && !j.winners) return;  // binary-mode stripe in a mixed batch: no winner pass
+  const uint64_t t = item_triangle(j, i);
+  const TriVerts tv = load_verts(j.tris, t, j.stride);
+  int lo[3], hi[3];
+  if (!item_box(j, tv, lo, hi)) return;  // cannot happen: the task count came from the same box
+  const uint64_t bx = (uint64_t)(hi[0] - lo[0] + 1), by = (uint64_t)(hi[1] - lo[1] + 1);
+  const uint64_t c = k * 32 + (uint64_t)lane;
+  if (c < bx * by) {
+    TriSetup s;
+    tri_setup(tv, j.u, s);
+    const int x = lo[0] + (int)(c % bx);
+    const int y = lo[1] + (int)(c / bx);
+    vox_column<PASS>(j, s, (uint32_t)t, x, y, lo[2], hi[2]);
   }
 }
 
@@ -425,19 +450,7 @@ __global__ void __launch_bounds__(256) k_vox_large(VoxJob j) {
       if (j.task_off[mid] <= task) lo_i = mid;
       else hi_i = mid;
     }
-    const uint64_t t = item_triangle(j, lo_i);
-    const TriVerts tv = load_verts(j.tris, t, j.stride);
-    int lo[3], hi[3];
-    if (!item_box(j, tv, lo, hi)) continue;  // cannot happen: the task count came from the same box
-    const uint64_t bx = (uint64_t)(hi[0] - lo[0] + 1), by = (uint64_t)(hi[1] - lo[1] + 1);
-    const uint64_t c = (task - j.task_off[lo_i]) * 32 + lane;
-    if (c < bx * by) {
-      TriSetup s;
-      tri_setup(tv, j.u, s);
-      const int x = lo[0] + (int)(c % bx);
-      const int y = lo[1] + (int)(c / bx);
-      vox_column<PASS>(j, s, (uint32_t)t, x, y, lo[2], hi[2]);
-    }
+    vox_large_task<PASS>(j, lo_i, task - j.task_off[lo_i], lane);
   }
 }
 
@@ -492,9 +505,7 @@ __device__ __forceinline__ uint32_t child_mask(const uint32_t* __restrict__ bits
 
 // Keys of all levels in one launch, one thread per 256-bit block (blocks are
 // 8 aligned words and never straddle two levels).
-__global__ void k_compact(Pyramid p, uint64_t total_blocks, uint32_t* __restrict__ keys) {
-  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= total_blocks) return;
+__device__ __forceinline__ void compact_block(const Pyramid& p, uint64_t b, uint32_t* __restrict__ keys) {
   const uint4* q = reinterpret_cast<const uint4*>(p.bits + 8 * b);
   const uint4 q0 = q[0], q1 = q[1];
   if (!(q0.x | q0.y | q0.z | q0.w | q1.x | q1.y | q1.z | q1.w)) return;
@@ -512,6 +523,11 @@ __global__ void k_compact(Pyramid p, uint64_t total_blocks, uint32_t* __restrict
       word &= word - 1;
     }
   }
+}
+
+__global__ void k_compact(Pyramid p, uint64_t total_blocks, uint32_t* __restrict__ keys) {
+  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < total_blocks) compact_block(p, b, keys);
 }
 
 // ===========================================================================
@@ -595,16 +611,19 @@ __device__ bool leaf_value(const EmitJob& e, uint64_t li, uint32_t key, float ou
 }
 
 // Leaf payloads into the per-node cache (needed before the -levels averages).
-__global__ void k_leaf_payload(Pyramid p, EmitJob e) {
+__device__ __forceinline__ void leaf_payload(const Pyramid& p, const EmitJob& e, uint64_t i) {
   const Level& L = p.lv[p.depth];
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= L.n) return;
   float v[6];
   if (leaf_value(e, i, e.keys[L.koff + i], v)) {
     float* out = e.cache + (L.koff + i) * 6;
 #pragma unroll
     for (int q = 0; q < 6; q++) out[q] = v[q];
   }
+}
+
+__global__ void k_leaf_payload(Pyramid p, EmitJob e) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < p.lv[p.depth].n) leaf_payload(p, e, i);
 }
 
 // ===========================================================================
@@ -770,11 +789,9 @@ __device__ __forceinline__ void top_down_node(const Pyramid& p, const EmitJob& e
 
 // Leaf records, one thread per leaf: the parent (level depth-1) already knows
 // where its child group and data run start.
-__global__ void k_top_down_leaves(Pyramid p, EmitJob e) {
+__device__ __forceinline__ void top_down_leaf(const Pyramid& p, const EmitJob& e, uint64_t i) {
   const Level& L = p.lv[p.depth];
   const Level& P = p.lv[p.depth - 1];
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= L.n) return;
   const uint64_t gi = L.koff + i;
   const uint32_t k = e.keys[gi];
   const uint32_t pk = k >> 3;
@@ -798,6 +815,11 @@ __global__ void k_top_down_leaves(Pyramid p, EmitJob e) {
   store_data_record(e, di, e.stripe_base + k, v);
 }
 
+__global__ void k_top_down_leaves(Pyramid p, EmitJob e) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < p.lv[p.depth].n) top_down_leaf(p, e, i);
+}
+
 __global__ void k_top_down(Pyramid p, EmitJob e, int l) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < p.lv[l].n) top_down_node(p, e, l, i);
@@ -818,14 +840,15 @@ __global__ void k_top_down_top(Pyramid p, EmitJob e, int l_lo, uint64_t node_bas
 
 // Stripe root: child mask and payload for the host, and (with -levels, or a
 // one-voxel stripe in payload mode) the root's own data record.
-__global__ void k_root_info(Pyramid p, EmitJob e, uint64_t data_base, uint32_t* out) {
+__device__ void root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base, uint32_t* out) {
+  const uint64_t r0 = p.lv[0].koff;  // global node index of the stripe root
   float c[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
   if (p.depth >= 1) {
     if (e.levels)
-      for (int q = 0; q < 6; q++) c[q] = e.cache[q];
+      for (int q = 0; q < 6; q++) c[q] = e.cache[r0 * 6 + q];
   } else if (!e.binary) {
     if (e.cache) {
-      for (int q = 0; q < 6; q++) c[q] = e.cache[q];
+      for (int q = 0; q < 6; q++) c[q] = e.cache[r0 * 6 + q];
     } else {
       leaf_value(e, 0, 0, c);
     }
@@ -833,11 +856,13 @@ __global__ void k_root_info(Pyramid p, EmitJob e, uint64_t data_base, uint32_t* 
   out[0] = p.depth >= 1 ? child_mask(p.bits, p.lv[1], 0) : 0u;
   for (int q = 0; q < 6; q++) out[1 + q] = __float_as_uint(c[q]);
   if (p.depth >= 1) {
-    if (e.levels) store_data_record(e, data_base + e.dsize[0] - 1, 0, c);
+    if (e.levels) store_data_record(e, data_base + e.dsize[r0] - 1, 0, c);
   } else if (!e.binary) {
     store_data_record(e, data_base, e.stripe_base, c);
   }
 }
+
+__global__ void k_root_info(Pyramid p, EmitJob e, uint64_t data_base, uint32_t* out) { root_info(p, e, data_base, out); }
 
 // Per-level node counts from the scan: out[l] = first node of level l, out[depth+1] = total.
 __global__ void k_level_bases(Pyramid p, uint64_t total_blocks, uint32_t* out) {
@@ -852,6 +877,182 @@ __global__ void k_scatter_records(const uint64_t* __restrict__ src, uint64_t n, 
   const uint64_t* s = src + i * (1 + words);
   uint64_t* d = dst + s[0] * words;
   for (int q = 0; q < words; q++) d[q] = s[1 + q];
+}
+
+
+// ===========================================================================
+// Batched forms: every stripe of a batch in one launch.  A chunk table gives
+// each CTA one stripe and a run of at most kChunk elements; the CTA copies that
+// stripe's job into shared memory and runs the per-element bodies above.
+// ===========================================================================
+template <typename T>
+__device__ __forceinline__ void stage(T& dst, const T& src) {
+  static_assert(sizeof(T) % 4 == 0, "staged structs are word-sized");
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(&src);
+  uint32_t* d = reinterpret_cast<uint32_t*>(&dst);
+  for (uint32_t q = threadIdx.x; q < sizeof(T) / 4; q += blockDim.x) d[q] = s[q];
+}
+
+template <int PASS>
+__global__ void __launch_bounds__(kChunk) kb_vox_small(const VoxJob* __restrict__ jobs, const Chunk* __restrict__ chunks) {
+  __shared__ VoxJob sj;
+  const Chunk ch = chunks[blockIdx.x];
+  stage(sj, jobs[ch.stripe]);
+  __syncthreads();
+  if (threadIdx.x >= ch.count) return;
+  if (PASS == 0) vox_small_occ_item(sj, ch.first + threadIdx.x);
+  else vox_small_win_item(sj, ch.first + threadIdx.x);
+}
+
+template <int PASS>
+__global__ void __launch_bounds__(256) kb_vox_large(const VoxJob* __restrict__ jobs, const uint64_t* __restrict__ item_beg,
+                                                    uint32_t n_stripes, const uint64_t* __restrict__ task_off,
+                                                    uint64_t total_items, unsigned long long* counter) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t total = task_off[total_items];
+  for (;;) {
+    unsigned long long task = 0;
+    if (lane == 0) task = atomicAdd(counter, 1ull);
+    task = __shfl_sync(FULL, task, 0);
+    if (task >= total) break;
+    uint64_t lo_i = 0, hi_i = total_items;  // task_off[lo_i] <= task < task_off[hi_i]
+    while (hi_i - lo_i > 1) {
+      const uint64_t mid = (lo_i + hi_i) >> 1;
+      if (task_off[mid] <= task) lo_i = mid;
+      else hi_i = mid;
+    }
+    uint32_t s0 = 0, s1 = n_stripes;  // item_beg[s0] <= lo_i < item_beg[s1]
+    while (s1 - s0 > 1) {
+      const uint32_t mid = (s0 + s1) >> 1;
+      if (item_beg[mid] <= lo_i) s0 = mid;
+      else s1 = mid;
+    }
+    vox_large_task<PASS>(jobs[s0], lo_i - item_beg[s0], task - task_off[lo_i], lane);
+  }
+}
+
+__global__ void __launch_bounds__(kChunk) kb_pyramid(const Pyramid* __restrict__ pyrs, const Chunk* __restrict__ chunks) {
+  __shared__ Pyramid sp;
+  const Chunk ch = chunks[blockIdx.x];
+  stage(sp, pyrs[ch.stripe]);
+  __syncthreads();
+  if (threadIdx.x < ch.count) pyramid_block(sp, (int)ch.level, ch.first + threadIdx.x);
+}
+
+__global__ void kb_pyramid_top(const Pyramid* __restrict__ pyrs, int l_hi) {
+  __shared__ Pyramid sp;
+  stage(sp, pyrs[blockIdx.x]);
+  __syncthreads();
+  for (int l = l_hi < sp.depth ? l_hi : sp.depth; l >= 0; l--) {
+    for (uint64_t b = threadIdx.x; b < sp.lv[l].nblocks; b += blockDim.x) pyramid_block(sp, l, b);
+    __syncthreads();
+  }
+}
+
+// chunk.first is a global block index inside the stripe's pyramid
+__global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__ pyrs, const Chunk* __restrict__ chunks,
+                                                     uint32_t* __restrict__ keys) {
+  __shared__ Pyramid sp;
+  const Chunk ch = chunks[blockIdx.x];
+  stage(sp, pyrs[ch.stripe]);
+  __syncthreads();
+  if (threadIdx.x < ch.count) compact_block(sp, ch.first + threadIdx.x, keys);
+}
+
+__global__ void kb_level_bases(const Pyramid* __restrict__ pyrs, uint32_t n_stripes, uint32_t* __restrict__ out) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_stripes) return;
+  const Pyramid& p = pyrs[s];
+  uint32_t* o = out + (uint64_t)s * (kMaxLevels + 1);
+  for (int l = 0; l <= p.depth; l++) o[l] = p.scan[p.lv[l].off_b];
+  o[p.depth + 1] = p.scan[p.lv[p.depth].off_b + p.lv[p.depth].nblocks];
+}
+
+__global__ void __launch_bounds__(kChunk) kb_leaf_payload(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits,
+                                                          const Chunk* __restrict__ chunks) {
+  __shared__ Pyramid sp;
+  __shared__ EmitJob se;
+  const Chunk ch = chunks[blockIdx.x];
+  stage(sp, pyrs[ch.stripe]);
+  stage(se, emits[ch.stripe]);
+  __syncthreads();
+  if (threadIdx.x < ch.count) leaf_payload(sp, se, ch.first + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(kChunk) kb_bottom_up(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits,
+                                                       const Chunk* __restrict__ chunks) {
+  __shared__ Pyramid sp;
+  __shared__ EmitJob se;
+  const Chunk ch = chunks[blockIdx.x];
+  stage(sp, pyrs[ch.stripe]);
+  stage(se, emits[ch.stripe]);
+  __syncthreads();
+  if (threadIdx.x < ch.count) bottom_up_node(sp, se, (int)ch.level, ch.first + threadIdx.x);
+}
+
+// One CTA per stripe: bottom-up of levels l_small .. 0.
+__global__ void kb_bottom_up_top(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits) {
+  __shared__ Pyramid sp;
+  __shared__ EmitJob se;
+  stage(sp, pyrs[blockIdx.x]);
+  stage(se, emits[blockIdx.x]);
+  __syncthreads();
+  if (sp.depth < 1 || sp.lv[sp.depth].n == 0) return;
+  for (int l = se.l_small; l >= 0; l--) {
+    for (uint64_t i = threadIdx.x; i < sp.lv[l].n; i += blockDim.x) bottom_up_node(sp, se, l, i);
+    __syncthreads();
+  }
+}
+
+// One CTA per stripe: the root starts at the stripe's bases; parents of levels 0 .. min(l_small, depth-2).
+__global__ void kb_top_down_top(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits) {
+  __shared__ Pyramid sp;
+  __shared__ EmitJob se;
+  stage(sp, pyrs[blockIdx.x]);
+  stage(se, emits[blockIdx.x]);
+  __syncthreads();
+  if (sp.depth < 1 || sp.lv[sp.depth].n == 0) return;
+  if (threadIdx.x == 0) {
+    se.start[sp.lv[0].koff] = se.node_base;
+    se.dstart[sp.lv[0].koff] = se.data_base;
+  }
+  __syncthreads();
+  const int last = se.l_small < sp.depth - 2 ? se.l_small : sp.depth - 2;
+  for (int l = 0; l <= last; l++) {
+    for (uint64_t i = threadIdx.x; i < sp.lv[l].n; i += blockDim.x) top_down_node(sp, se, l, i);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kChunk) kb_top_down(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits,
+                                                      const Chunk* __restrict__ chunks) {
+  __shared__ Pyramid sp;
+  __shared__ EmitJob se;
+  const Chunk ch = chunks[blockIdx.x];
+  stage(sp, pyrs[ch.stripe]);
+  stage(se, emits[ch.stripe]);
+  __syncthreads();
+  if (threadIdx.x < ch.count) top_down_node(sp, se, (int)ch.level, ch.first + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(kChunk) kb_top_down_leaves(const Pyramid* __restrict__ pyrs,
+                                                             const EmitJob* __restrict__ emits,
+                                                             const Chunk* __restrict__ chunks) {
+  __shared__ Pyramid sp;
+  __shared__ EmitJob se;
+  const Chunk ch = chunks[blockIdx.x];
+  stage(sp, pyrs[ch.stripe]);
+  stage(se, emits[ch.stripe]);
+  __syncthreads();
+  if (threadIdx.x < ch.count) top_down_leaf(sp, se, ch.first + threadIdx.x);
+}
+
+__global__ void kb_root_info(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits, uint32_t n_stripes,
+                             uint32_t* __restrict__ out) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_stripes) return;
+  if (pyrs[s].lv[pyrs[s].depth].n == 0) return;
+  root_info(pyrs[s], emits[s], emits[s].data_base, out + (uint64_t)s * 16);
 }
 
 }  // namespace
@@ -977,6 +1178,96 @@ void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t
   if (n == 0) return;
   KScope k("scatter_records", st);
   k_scatter_records<<<grid_for(n, 128), 128, 0, st>>>(src, n, words, dst);
+}
+
+
+// ---- batched launch wrappers ----
+void launch_b_vox_small(const VoxJob* jobs, const Chunk* chunks, uint64_t n_chunks, int pass, cudaStream_t st) {
+  if (n_chunks == 0) return;
+  KScope k(pass == 0 ? "vox_small_occupancy" : "vox_small_winner", st);
+  if (pass == 0) kb_vox_small<0><<<(unsigned)n_chunks, kChunk, 0, st>>>(jobs, chunks);
+  else kb_vox_small<1><<<(unsigned)n_chunks, kChunk, 0, st>>>(jobs, chunks);
+}
+
+void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n_stripes, const uint64_t* task_off,
+                        uint64_t total_items, unsigned long long* counter, int pass, cudaStream_t st, int num_sms) {
+  if (total_items == 0) return;
+  cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+  const unsigned grid = (unsigned)num_sms * 8;
+  KScope k(pass == 0 ? "vox_large_occupancy" : "vox_large_winner", st);
+  if (pass == 0) kb_vox_large<0><<<grid, 256, 0, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter);
+  else kb_vox_large<1><<<grid, 256, 0, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter);
+}
+
+void launch_b_pyramid(const Pyramid* pyrs, const Chunk* chunks, uint64_t n_chunks, cudaStream_t st) {
+  if (n_chunks == 0) return;
+  KScope k("pyramid", st);
+  kb_pyramid<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, chunks);
+}
+
+void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cudaStream_t st) {
+  if (n_stripes == 0) return;
+  KScope k("pyramid_top", st);
+  kb_pyramid_top<<<n_stripes, 512, 0, st>>>(pyrs, l_hi);
+}
+
+void launch_b_compact(const Pyramid* pyrs, const Chunk* chunks, uint64_t n_chunks, uint32_t* keys, cudaStream_t st) {
+  if (n_chunks == 0) return;
+  KScope k("compact", st);
+  kb_compact<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, chunks, keys);
+}
+
+void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, cudaStream_t st) {
+  if (n_stripes == 0) return;
+  KScope k("level_bases", st);
+  kb_level_bases<<<grid_for(n_stripes, 128), 128, 0, st>>>(pyrs, n_stripes, out);
+}
+
+void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const Chunk* chunks, uint64_t n_chunks,
+                           cudaStream_t st) {
+  if (n_chunks == 0) return;
+  KScope k("leaf_payload", st);
+  kb_leaf_payload<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, emits, chunks);
+}
+
+void launch_b_bottom_up(const Pyramid* pyrs, const EmitJob* emits, const Chunk* chunks, uint64_t n_chunks,
+                        cudaStream_t st) {
+  if (n_chunks == 0) return;
+  KScope k("bottom_up", st);
+  kb_bottom_up<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, emits, chunks);
+}
+
+void launch_b_bottom_up_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, cudaStream_t st) {
+  if (n_stripes == 0) return;
+  KScope k("bottom_up_top", st);
+  kb_bottom_up_top<<<n_stripes, 256, 0, st>>>(pyrs, emits);
+}
+
+void launch_b_top_down_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, cudaStream_t st) {
+  if (n_stripes == 0) return;
+  KScope k("top_down_top", st);
+  kb_top_down_top<<<n_stripes, 256, 0, st>>>(pyrs, emits);
+}
+
+void launch_b_top_down(const Pyramid* pyrs, const EmitJob* emits, const Chunk* chunks, uint64_t n_chunks,
+                       cudaStream_t st) {
+  if (n_chunks == 0) return;
+  KScope k("top_down", st);
+  kb_top_down<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, emits, chunks);
+}
+
+void launch_b_top_down_leaves(const Pyramid* pyrs, const EmitJob* emits, const Chunk* chunks, uint64_t n_chunks,
+                              cudaStream_t st) {
+  if (n_chunks == 0) return;
+  KScope k("top_down_leaves", st);
+  kb_top_down_leaves<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, emits, chunks);
+}
+
+void launch_b_root_info(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, uint32_t* out,
+                        cudaStream_t st) {
+  if (n_stripes == 0) return;
+  KScope k("root_info", st);
+  kb_root_info<<<grid_for(n_stripes, 128), 128, 0, st>>>(pyrs, emits, n_stripes, out);
 }
 
 }  // namespace ooc

@@ -1,0 +1,57 @@
+"""ooc_build_batch: many meshes of different gridsizes, modes and flags in one call.
+
+Each mesh's octree must equal the oracle's (and so ooc_build's) on that mesh alone.
+"""
+import numpy as np
+import pytest
+
+import pyoracle
+from ooc_svo_builder_gb300 import make_params, octree, tri
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_meshes(seed=5, count=24):
+    rng = np.random.default_rng(seed)
+    meshes, params, oracle_args = [], [], []
+    for i in range(count):
+        payload = bool(rng.integers(0, 2))
+        N = int(rng.choice([1, 8, 32, 64, 128, 256]))
+        limit = 2 if (N == 256 and rng.random() < 0.5) else 2048
+        levels = bool(rng.integers(0, 2))
+        color = str(rng.choice(["model", "fixed", "linear", "normal"])) if payload else "model"
+        kind = rng.integers(0, 3)
+        if kind == 0:
+            t = tri.icosphere_tris(int(rng.integers(1, 4)), payload=payload, seed=int(rng.integers(0, 1000)))
+        elif kind == 1:
+            t = tri.random_tris(int(rng.integers(1, 400)), int(rng.integers(0, 1000)), payload, lo=-0.1, hi=1.1,
+                                max_edge=float(rng.uniform(0.01, 0.5)))
+        else:
+            t = np.zeros((0, 21 if payload else 9), np.float32)
+        meshes.append(t)
+        params.append(make_params(N, limit, geometry_only=not payload, color=color, levels=levels))
+        oracle_args.append(dict(gridsize=N, memory_limit_mb=limit, color=color, levels=levels))
+    return meshes, params, oracle_args
+
+
+def test_batch_matches_single_mesh_builds(builder):
+    meshes, params, args = mixed_meshes()
+    results = builder.build_batch(meshes, params)
+    assert len(results) == len(meshes)
+    for t, r, a in zip(meshes, results, args):
+        nodes, data, info = pyoracle.build(t, a["gridsize"], a["memory_limit_mb"], color=a["color"],
+                                           levels=a["levels"])
+        d = octree.diff(r.tree, octree.Octree(a["gridsize"], nodes, data))
+        assert not d, "\n".join(d)
+        assert r.info["n_filled"] == info["n_filled"]
+        assert r.info["n_partitions"] == info["n_partitions"]
+
+
+def test_batch_split_into_sub_batches(builder):
+    # many 256^3 meshes exceed no budget; the call must still give per-mesh results in order
+    meshes = [tri.random_tris(300, 700 + i, i % 2 == 1, max_edge=0.2) for i in range(6)]
+    params = [make_params(256, 2048 if i % 3 else 2, geometry_only=(i % 2 == 0)) for i in range(6)]
+    results = builder.build_batch(meshes, params)
+    for i, (t, r) in enumerate(zip(meshes, results)):
+        nodes, data, _ = pyoracle.build(t, 256, 2048 if i % 3 else 2)
+        assert not octree.diff(r.tree, octree.Octree(256, nodes, data))
