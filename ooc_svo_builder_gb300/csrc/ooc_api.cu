@@ -386,16 +386,12 @@ int pyramid_levels(int Ds, Level* lv, uint64_t& words, uint64_t& blocks) {
   return Ds;
 }
 
-void add_chunks(std::vector<Chunk>& v, uint32_t stripe, uint32_t level, uint64_t first, uint64_t count) {
-  for (uint64_t k = 0; k < count; k += kChunk) {
-    Chunk c;
-    c.stripe = stripe;
-    c.level = level;
-    c.first = first + k;
-    c.count = (uint32_t)std::min<uint64_t>(kChunk, count - k);
-    c.pad = 0;
-    v.push_back(c);
-  }
+// CTA prefix of one batched launch: stripe s gets ceil(count(s) / kChunk) CTAs.
+template <typename F>
+std::vector<uint64_t> cta_prefix(uint32_t n, F count) {
+  std::vector<uint64_t> beg(n + 1, 0);
+  for (uint32_t s = 0; s < n; s++) beg[s + 1] = beg[s] + (count(s) + kChunk - 1) / kChunk;
+  return beg;
 }
 
 // Upload host vectors into one device buffer through pinned staging; returns device pointers.
@@ -454,8 +450,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   uint32_t* d_root = ensure<uint32_t>(c->d_rootinfo, ((uint64_t)n * 16 + 64) * 4);
   uint32_t* flag = d_root + (uint64_t)n * 16;
 
-  std::vector<Chunk> ch_items, ch_pay_items, ch_compact;
-  std::vector<std::vector<Chunk>> ch_pyr(max_depth + 1);
   constexpr int kTopPyramidLevel = 5;  // levels 0..5 have at most 512 blocks: one CTA per stripe
   for (uint32_t s = 0; s < n; s++) {
     const StripeRef& r = sb[s];
@@ -488,20 +482,24 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     j.task_counter = counter;
     j.item_mask = m.pl.binary ? nullptr : item_mask + item_beg[s];
     j.item_box = m.pl.binary ? nullptr : item_box + item_beg[s];
-    add_chunks(ch_items, s, 0, 0, r.n_items);
-    if (!m.pl.binary) add_chunks(ch_pay_items, s, 0, 0, r.n_items);
-    for (int l = P.depth; l > kTopPyramidLevel; l--) add_chunks(ch_pyr[P.depth - l], s, (uint32_t)l, 0, P.lv[l].nblocks);
-    add_chunks(ch_compact, s, 0, P.lv[0].off_b, P.lv[P.depth].off_b + P.lv[P.depth].nblocks - P.lv[0].off_b);
   }
+  const std::vector<uint64_t> cp_items = cta_prefix(n, [&](uint32_t s) { return sb[s].n_items; });
+  std::vector<std::vector<uint64_t>> cp_pyr;
+  for (int r = 0; r <= max_depth - kTopPyramidLevel - 1; r++)
+    cp_pyr.push_back(cta_prefix(n, [&](uint32_t s) -> uint64_t {
+      const int l = pyr[s].depth - r;
+      return l > kTopPyramidLevel ? pyr[s].lv[l].nblocks : 0;
+    }));
 
   Uploader up1;
   const size_t o_vj = up1.add(vj.data(), n * sizeof(VoxJob));
   const size_t o_pyr = up1.add(pyr.data(), n * sizeof(Pyramid));
   const size_t o_beg = up1.add(item_beg.data(), (n + 1) * 8);
-  const size_t o_chi = up1.add(ch_items.data(), ch_items.size() * sizeof(Chunk));
-  std::vector<size_t> o_chp(ch_pyr.size());
-  for (size_t r = 0; r < ch_pyr.size(); r++) o_chp[r] = up1.add(ch_pyr[r].data(), ch_pyr[r].size() * sizeof(Chunk));
+  const size_t o_cpi = up1.add(cp_items.data(), (n + 1) * 8);
+  std::vector<size_t> o_cpp(cp_pyr.size());
+  for (size_t r = 0; r < cp_pyr.size(); r++) o_cpp[r] = up1.add(cp_pyr[r].data(), (n + 1) * 8);
   unsigned char* t1 = up1.run(c, c->d_tables1, c->h_tables1, st);
+  auto dp1 = [&](size_t off) { return reinterpret_cast<const uint64_t*>(t1 + off); };
   const VoxJob* d_vj = reinterpret_cast<const VoxJob*>(t1 + o_vj);
   const Pyramid* d_pyr = reinterpret_cast<const Pyramid*>(t1 + o_pyr);
   const uint64_t* d_beg = reinterpret_cast<const uint64_t*>(t1 + o_beg);
@@ -512,15 +510,14 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     ck(cudaMemsetAsync(bits, 0, words * 4, st), "memset bits");
     ck(cudaMemsetAsync(task_off + items, 0, 8, st), "memset task_off");
     ck(cudaMemsetAsync(flag, 0, 4, st), "memset flag");
-    launch_b_vox_small(d_vj, reinterpret_cast<const Chunk*>(t1 + o_chi), ch_items.size(), 0, st);
+    launch_b_vox_small(d_vj, dp1(o_cpi), n, cp_items[n], 0, st);
     scan_u64_exclusive(task_off, items + 1, taskpart, st);
     launch_b_vox_large(d_vj, d_beg, n, task_off, items, counter, 0, st, c->num_sms);
   }
   {
     PhaseScope ph(c, PH_PYR, st);
     ck(cudaMemsetAsync(scan + blocks, 0, 4, st), "memset scan");
-    for (size_t r = 0; r < ch_pyr.size(); r++)
-      launch_b_pyramid(d_pyr, reinterpret_cast<const Chunk*>(t1 + o_chp[r]), ch_pyr[r].size(), st);
+    for (size_t r = 0; r < cp_pyr.size(); r++) launch_b_pyramid(d_pyr, dp1(o_cpp[r]), n, cp_pyr[r][n], (int)r, st);
     launch_b_pyramid_top(d_pyr, n, kTopPyramidLevel, st);
     scan_u32_exclusive(scan, blocks + 1, scanpart, st);
     launch_b_level_bases(d_pyr, n, d_root, st);
@@ -617,8 +614,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     ensure<unsigned char>(c->d_data, out_data * 32);
   }
   std::vector<EmitJob> ej(n);
-  std::vector<Chunk> ch_leaves, ch_leafpay;
-  std::vector<std::vector<Chunk>> ch_bu(max_depth + 1), ch_td(max_depth + 1);
   for (uint32_t s = 0; s < n; s++) {
     const MeshWork& m = meshes[sb[s].mesh];
     const Pyramid& P = pyr[s];
@@ -671,47 +666,67 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     int ls = 0;
     while (ls + 1 <= P.depth - 1 && P.lv[ls + 1].n <= 256) ls++;
     e.l_small = ls;
-    if (P.depth >= 1) add_chunks(ch_leaves, s, (uint32_t)P.depth, 0, q.n_leaf);  // a depth-0 root is the leaf
-    if (m.pl.levels && !m.pl.binary) add_chunks(ch_leafpay, s, (uint32_t)P.depth, 0, q.n_leaf);
-    for (int l = P.depth - 1; l > ls; l--) add_chunks(ch_bu[P.depth - l], s, (uint32_t)l, 0, P.lv[l].n);
-    for (int l = std::min(ls, P.depth - 2) + 1; l <= P.depth - 2; l++) add_chunks(ch_td[l], s, (uint32_t)l, 0, P.lv[l].n);
   }
+  auto live = [&](uint32_t s) { return !pl[s].empty; };
+  const std::vector<uint64_t> cp_compact = cta_prefix(n, [&](uint32_t s) {
+    return pyr[s].lv[pyr[s].depth].off_b + pyr[s].lv[pyr[s].depth].nblocks - pyr[s].lv[0].off_b;
+  });
+  const std::vector<uint64_t> cp_pay = cta_prefix(n, [&](uint32_t s) -> uint64_t {
+    return meshes[sb[s].mesh].pl.binary ? 0 : sb[s].n_items;
+  });
+  const std::vector<uint64_t> cp_leafpay = cta_prefix(n, [&](uint32_t s) -> uint64_t {
+    const Plan& mp = meshes[sb[s].mesh].pl;
+    return (live(s) && mp.levels && !mp.binary) ? pl[s].n_leaf : 0;
+  });
+  const std::vector<uint64_t> cp_leaves = cta_prefix(n, [&](uint32_t s) -> uint64_t {
+    return (live(s) && pyr[s].depth >= 1) ? pl[s].n_leaf : 0;  // a depth-0 root is the leaf
+  });
+  std::vector<std::vector<uint64_t>> cp_bu(max_depth + 1), cp_td(max_depth + 1);
+  for (int r = 1; r <= max_depth; r++)
+    cp_bu[r] = cta_prefix(n, [&](uint32_t s) -> uint64_t {
+      const int l = pyr[s].depth - r;
+      return (live(s) && l > ej[s].l_small && l >= 0) ? pyr[s].lv[l].n : 0;
+    });
+  for (int l = 0; l <= max_depth; l++)
+    cp_td[l] = cta_prefix(n, [&](uint32_t s) -> uint64_t {
+      const int last_top = std::min(ej[s].l_small, pyr[s].depth - 2);
+      return (live(s) && l > last_top && l <= pyr[s].depth - 2) ? pyr[s].lv[l].n : 0;
+    });
   Uploader up2;
   const size_t o_vj2 = up2.add(vj.data(), n * sizeof(VoxJob));
   const size_t o_pyr2 = up2.add(pyr.data(), n * sizeof(Pyramid));
   const size_t o_ej = up2.add(ej.data(), n * sizeof(EmitJob));
-  const size_t o_cc = up2.add(ch_compact.data(), ch_compact.size() * sizeof(Chunk));
-  const size_t o_cpi = up2.add(ch_pay_items.data(), ch_pay_items.size() * sizeof(Chunk));
-  const size_t o_cl = up2.add(ch_leaves.data(), ch_leaves.size() * sizeof(Chunk));
-  const size_t o_clp = up2.add(ch_leafpay.data(), ch_leafpay.size() * sizeof(Chunk));
-  std::vector<size_t> o_bu(ch_bu.size()), o_td(ch_td.size());
-  for (size_t r = 0; r < ch_bu.size(); r++) o_bu[r] = up2.add(ch_bu[r].data(), ch_bu[r].size() * sizeof(Chunk));
-  for (size_t r = 0; r < ch_td.size(); r++) o_td[r] = up2.add(ch_td[r].data(), ch_td[r].size() * sizeof(Chunk));
+  const size_t o_cc = up2.add(cp_compact.data(), (n + 1) * 8);
+  const size_t o_cpay = up2.add(cp_pay.data(), (n + 1) * 8);
+  const size_t o_clp = up2.add(cp_leafpay.data(), (n + 1) * 8);
+  const size_t o_cl = up2.add(cp_leaves.data(), (n + 1) * 8);
+  std::vector<size_t> o_bu(cp_bu.size(), 0), o_td(cp_td.size(), 0);
+  for (size_t r = 1; r < cp_bu.size(); r++) o_bu[r] = up2.add(cp_bu[r].data(), (n + 1) * 8);
+  for (size_t l = 0; l < cp_td.size(); l++) o_td[l] = up2.add(cp_td[l].data(), (n + 1) * 8);
   unsigned char* t2 = up2.run(c, c->d_tables2, c->h_tables2, st);
+  auto dp2 = [&](size_t off) { return reinterpret_cast<const uint64_t*>(t2 + off); };
   const VoxJob* d_vj2 = reinterpret_cast<const VoxJob*>(t2 + o_vj2);
   const Pyramid* d_pyr2 = reinterpret_cast<const Pyramid*>(t2 + o_pyr2);
   const EmitJob* d_ej = reinterpret_cast<const EmitJob*>(t2 + o_ej);
 
   {
     PhaseScope ph(c, PH_PYR, st);
-    launch_b_compact(d_pyr2, reinterpret_cast<const Chunk*>(t2 + o_cc), ch_compact.size(), keys, st);
+    launch_b_compact(d_pyr2, dp2(o_cc), n, cp_compact[n], keys, st);
   }
   if (any_payload) {
     PhaseScope ph(c, PH_VOX, st);
     ck(cudaMemsetAsync(winners, 0xff, total_nodes * 4, st), "memset winners");
-    launch_b_vox_small(d_vj2, reinterpret_cast<const Chunk*>(t2 + o_cpi), ch_pay_items.size(), 1, st);
+    launch_b_vox_small(d_vj2, dp2(o_cpay), n, cp_pay[n], 1, st);
     launch_b_vox_large(d_vj2, d_beg, n, task_off, items, counter, 1, st, c->num_sms);
-    launch_b_leaf_payload(d_pyr2, d_ej, reinterpret_cast<const Chunk*>(t2 + o_clp), ch_leafpay.size(), st);
+    launch_b_leaf_payload(d_pyr2, d_ej, dp2(o_clp), n, cp_leafpay[n], st);
   }
   {
     PhaseScope ph(c, PH_TREE, st);
-    for (size_t r = 1; r < ch_bu.size(); r++)
-      launch_b_bottom_up(d_pyr2, d_ej, reinterpret_cast<const Chunk*>(t2 + o_bu[r]), ch_bu[r].size(), st);
+    for (size_t r = 1; r < cp_bu.size(); r++) launch_b_bottom_up(d_pyr2, d_ej, dp2(o_bu[r]), n, cp_bu[r][n], (int)r, st);
     launch_b_bottom_up_top(d_pyr2, d_ej, n, st);
     launch_b_top_down_top(d_pyr2, d_ej, n, st);
-    for (size_t l = 0; l < ch_td.size(); l++)
-      launch_b_top_down(d_pyr2, d_ej, reinterpret_cast<const Chunk*>(t2 + o_td[l]), ch_td[l].size(), st);
-    launch_b_top_down_leaves(d_pyr2, d_ej, reinterpret_cast<const Chunk*>(t2 + o_cl), ch_leaves.size(), st);
+    for (size_t l = 0; l < cp_td.size(); l++) launch_b_top_down(d_pyr2, d_ej, dp2(o_td[l]), n, cp_td[l][n], (int)l, st);
+    launch_b_top_down_leaves(d_pyr2, d_ej, dp2(o_cl), n, cp_leaves[n], st);
     launch_b_root_info(d_pyr2, d_ej, n, d_root, st);
     ck(cudaMemcpyAsync(lvl, d_root, ((uint64_t)n * 16 + 1) * 4, cudaMemcpyDeviceToHost, st), "root info");
   }

@@ -893,15 +893,36 @@ __device__ __forceinline__ void stage(T& dst, const T& src) {
   for (uint32_t q = threadIdx.x; q < sizeof(T) / 4; q += blockDim.x) d[q] = s[q];
 }
 
-template <int PASS>
-__global__ void __launch_bounds__(kChunk) kb_vox_small(const VoxJob* __restrict__ jobs, const Chunk* __restrict__ chunks) {
-  __shared__ VoxJob sj;
-  const Chunk ch = chunks[blockIdx.x];
-  stage(sj, jobs[ch.stripe]);
+// CTA b belongs to the stripe s with cta_beg[s] <= b < cta_beg[s+1]; it
+// handles elements kChunk * (b - cta_beg[s]) .. + kChunk - 1 of that stripe.
+__device__ __forceinline__ uint32_t cta_stripe(const uint64_t* __restrict__ cta_beg, uint32_t n, uint64_t& local) {
+  __shared__ uint32_t s_stripe;
+  if (threadIdx.x == 0) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (cta_beg[mid] <= blockIdx.x) lo = mid;
+      else hi = mid;
+    }
+    s_stripe = lo;
+  }
   __syncthreads();
-  if (threadIdx.x >= ch.count) return;
-  if (PASS == 0) vox_small_occ_item(sj, ch.first + threadIdx.x);
-  else vox_small_win_item(sj, ch.first + threadIdx.x);
+  const uint32_t s = s_stripe;
+  local = (uint64_t)(blockIdx.x - cta_beg[s]) * kChunk + threadIdx.x;
+  return s;
+}
+
+template <int PASS>
+__global__ void __launch_bounds__(kChunk) kb_vox_small(const VoxJob* __restrict__ jobs,
+                                                       const uint64_t* __restrict__ cta_beg, uint32_t n) {
+  __shared__ VoxJob sj;
+  uint64_t i;
+  const uint32_t s = cta_stripe(cta_beg, n, i);
+  stage(sj, jobs[s]);
+  __syncthreads();
+  if (i >= sj.n_items) return;
+  if (PASS == 0) vox_small_occ_item(sj, i);
+  else vox_small_win_item(sj, i);
 }
 
 template <int PASS>
@@ -931,12 +952,16 @@ __global__ void __launch_bounds__(256) kb_vox_large(const VoxJob* __restrict__ j
   }
 }
 
-__global__ void __launch_bounds__(kChunk) kb_pyramid(const Pyramid* __restrict__ pyrs, const Chunk* __restrict__ chunks) {
+// Level depth - r of every stripe that has CTAs in this launch.
+__global__ void __launch_bounds__(kChunk) kb_pyramid(const Pyramid* __restrict__ pyrs,
+                                                     const uint64_t* __restrict__ cta_beg, uint32_t n, int r) {
   __shared__ Pyramid sp;
-  const Chunk ch = chunks[blockIdx.x];
-  stage(sp, pyrs[ch.stripe]);
+  uint64_t b;
+  const uint32_t s = cta_stripe(cta_beg, n, b);
+  stage(sp, pyrs[s]);
   __syncthreads();
-  if (threadIdx.x < ch.count) pyramid_block(sp, (int)ch.level, ch.first + threadIdx.x);
+  const int l = sp.depth - r;
+  if (b < sp.lv[l].nblocks) pyramid_block(sp, l, b);
 }
 
 __global__ void kb_pyramid_top(const Pyramid* __restrict__ pyrs, int l_hi) {
@@ -949,14 +974,17 @@ __global__ void kb_pyramid_top(const Pyramid* __restrict__ pyrs, int l_hi) {
   }
 }
 
-// chunk.first is a global block index inside the stripe's pyramid
-__global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__ pyrs, const Chunk* __restrict__ chunks,
+// Every block of every level of the stripe.
+__global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__ pyrs,
+                                                     const uint64_t* __restrict__ cta_beg, uint32_t n,
                                                      uint32_t* __restrict__ keys) {
   __shared__ Pyramid sp;
-  const Chunk ch = chunks[blockIdx.x];
-  stage(sp, pyrs[ch.stripe]);
+  uint64_t b;
+  const uint32_t s = cta_stripe(cta_beg, n, b);
+  stage(sp, pyrs[s]);
   __syncthreads();
-  if (threadIdx.x < ch.count) compact_block(sp, ch.first + threadIdx.x, keys);
+  const uint64_t first = sp.lv[0].off_b, end = sp.lv[sp.depth].off_b + sp.lv[sp.depth].nblocks;
+  if (first + b < end) compact_block(sp, first + b, keys);
 }
 
 __global__ void kb_level_bases(const Pyramid* __restrict__ pyrs, uint32_t n_stripes, uint32_t* __restrict__ out) {
@@ -968,26 +996,31 @@ __global__ void kb_level_bases(const Pyramid* __restrict__ pyrs, uint32_t n_stri
   o[p.depth + 1] = p.scan[p.lv[p.depth].off_b + p.lv[p.depth].nblocks];
 }
 
-__global__ void __launch_bounds__(kChunk) kb_leaf_payload(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits,
-                                                          const Chunk* __restrict__ chunks) {
+__global__ void __launch_bounds__(kChunk) kb_leaf_payload(const Pyramid* __restrict__ pyrs,
+                                                          const EmitJob* __restrict__ emits,
+                                                          const uint64_t* __restrict__ cta_beg, uint32_t n) {
   __shared__ Pyramid sp;
   __shared__ EmitJob se;
-  const Chunk ch = chunks[blockIdx.x];
-  stage(sp, pyrs[ch.stripe]);
-  stage(se, emits[ch.stripe]);
+  uint64_t i;
+  const uint32_t s = cta_stripe(cta_beg, n, i);
+  stage(sp, pyrs[s]);
+  stage(se, emits[s]);
   __syncthreads();
-  if (threadIdx.x < ch.count) leaf_payload(sp, se, ch.first + threadIdx.x);
+  if (i < sp.lv[sp.depth].n) leaf_payload(sp, se, i);
 }
 
+// Level depth - r of every stripe that has CTAs in this launch.
 __global__ void __launch_bounds__(kChunk) kb_bottom_up(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits,
-                                                       const Chunk* __restrict__ chunks) {
+                                                       const uint64_t* __restrict__ cta_beg, uint32_t n, int r) {
   __shared__ Pyramid sp;
   __shared__ EmitJob se;
-  const Chunk ch = chunks[blockIdx.x];
-  stage(sp, pyrs[ch.stripe]);
-  stage(se, emits[ch.stripe]);
+  uint64_t i;
+  const uint32_t s = cta_stripe(cta_beg, n, i);
+  stage(sp, pyrs[s]);
+  stage(se, emits[s]);
   __syncthreads();
-  if (threadIdx.x < ch.count) bottom_up_node(sp, se, (int)ch.level, ch.first + threadIdx.x);
+  const int l = sp.depth - r;
+  if (i < sp.lv[l].n) bottom_up_node(sp, se, l, i);
 }
 
 // One CTA per stripe: bottom-up of levels l_small .. 0.
@@ -1024,27 +1057,30 @@ __global__ void kb_top_down_top(const Pyramid* __restrict__ pyrs, const EmitJob*
   }
 }
 
+// Parents of absolute level l of every stripe that has CTAs in this launch.
 __global__ void __launch_bounds__(kChunk) kb_top_down(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits,
-                                                      const Chunk* __restrict__ chunks) {
+                                                      const uint64_t* __restrict__ cta_beg, uint32_t n, int l) {
   __shared__ Pyramid sp;
   __shared__ EmitJob se;
-  const Chunk ch = chunks[blockIdx.x];
-  stage(sp, pyrs[ch.stripe]);
-  stage(se, emits[ch.stripe]);
+  uint64_t i;
+  const uint32_t s = cta_stripe(cta_beg, n, i);
+  stage(sp, pyrs[s]);
+  stage(se, emits[s]);
   __syncthreads();
-  if (threadIdx.x < ch.count) top_down_node(sp, se, (int)ch.level, ch.first + threadIdx.x);
+  if (i < sp.lv[l].n) top_down_node(sp, se, l, i);
 }
 
 __global__ void __launch_bounds__(kChunk) kb_top_down_leaves(const Pyramid* __restrict__ pyrs,
                                                              const EmitJob* __restrict__ emits,
-                                                             const Chunk* __restrict__ chunks) {
+                                                             const uint64_t* __restrict__ cta_beg, uint32_t n) {
   __shared__ Pyramid sp;
   __shared__ EmitJob se;
-  const Chunk ch = chunks[blockIdx.x];
-  stage(sp, pyrs[ch.stripe]);
-  stage(se, emits[ch.stripe]);
+  uint64_t i;
+  const uint32_t s = cta_stripe(cta_beg, n, i);
+  stage(sp, pyrs[s]);
+  stage(se, emits[s]);
   __syncthreads();
-  if (threadIdx.x < ch.count) top_down_leaf(sp, se, ch.first + threadIdx.x);
+  if (i < sp.lv[sp.depth].n) top_down_leaf(sp, se, i);
 }
 
 __global__ void kb_root_info(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits, uint32_t n_stripes,
@@ -1182,11 +1218,12 @@ void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t
 
 
 // ---- batched launch wrappers ----
-void launch_b_vox_small(const VoxJob* jobs, const Chunk* chunks, uint64_t n_chunks, int pass, cudaStream_t st) {
-  if (n_chunks == 0) return;
+void launch_b_vox_small(const VoxJob* jobs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, int pass,
+                        cudaStream_t st) {
+  if (ctas == 0) return;
   KScope k(pass == 0 ? "vox_small_occupancy" : "vox_small_winner", st);
-  if (pass == 0) kb_vox_small<0><<<(unsigned)n_chunks, kChunk, 0, st>>>(jobs, chunks);
-  else kb_vox_small<1><<<(unsigned)n_chunks, kChunk, 0, st>>>(jobs, chunks);
+  if (pass == 0) kb_vox_small<0><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n);
+  else kb_vox_small<1><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n);
 }
 
 void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n_stripes, const uint64_t* task_off,
@@ -1199,10 +1236,11 @@ void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n
   else kb_vox_large<1><<<grid, 256, 0, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter);
 }
 
-void launch_b_pyramid(const Pyramid* pyrs, const Chunk* chunks, uint64_t n_chunks, cudaStream_t st) {
-  if (n_chunks == 0) return;
-  KScope k("pyramid", st);
-  kb_pyramid<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, chunks);
+void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, int r,
+                      cudaStream_t st) {
+  if (ctas == 0) return;
+  KScope k(r == 0 ? "pyramid_leaf" : "pyramid", st);
+  kb_pyramid<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, r);
 }
 
 void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cudaStream_t st) {
@@ -1211,10 +1249,11 @@ void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cud
   kb_pyramid_top<<<n_stripes, 512, 0, st>>>(pyrs, l_hi);
 }
 
-void launch_b_compact(const Pyramid* pyrs, const Chunk* chunks, uint64_t n_chunks, uint32_t* keys, cudaStream_t st) {
-  if (n_chunks == 0) return;
+void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t* keys,
+                      cudaStream_t st) {
+  if (ctas == 0) return;
   KScope k("compact", st);
-  kb_compact<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, chunks, keys);
+  kb_compact<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys);
 }
 
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, cudaStream_t st) {
@@ -1223,18 +1262,18 @@ void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out
   kb_level_bases<<<grid_for(n_stripes, 128), 128, 0, st>>>(pyrs, n_stripes, out);
 }
 
-void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const Chunk* chunks, uint64_t n_chunks,
-                           cudaStream_t st) {
-  if (n_chunks == 0) return;
+void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
+                           uint64_t ctas, cudaStream_t st) {
+  if (ctas == 0) return;
   KScope k("leaf_payload", st);
-  kb_leaf_payload<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, emits, chunks);
+  kb_leaf_payload<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n);
 }
 
-void launch_b_bottom_up(const Pyramid* pyrs, const EmitJob* emits, const Chunk* chunks, uint64_t n_chunks,
-                        cudaStream_t st) {
-  if (n_chunks == 0) return;
-  KScope k("bottom_up", st);
-  kb_bottom_up<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, emits, chunks);
+void launch_b_bottom_up(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas,
+                        int r, cudaStream_t st) {
+  if (ctas == 0) return;
+  KScope k(r == 1 ? "bottom_up_leaf_parents" : "bottom_up", st);
+  kb_bottom_up<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, r);
 }
 
 void launch_b_bottom_up_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, cudaStream_t st) {
@@ -1249,18 +1288,18 @@ void launch_b_top_down_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n
   kb_top_down_top<<<n_stripes, 256, 0, st>>>(pyrs, emits);
 }
 
-void launch_b_top_down(const Pyramid* pyrs, const EmitJob* emits, const Chunk* chunks, uint64_t n_chunks,
-                       cudaStream_t st) {
-  if (n_chunks == 0) return;
+void launch_b_top_down(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas,
+                       int l, cudaStream_t st) {
+  if (ctas == 0) return;
   KScope k("top_down", st);
-  kb_top_down<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, emits, chunks);
+  kb_top_down<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, l);
 }
 
-void launch_b_top_down_leaves(const Pyramid* pyrs, const EmitJob* emits, const Chunk* chunks, uint64_t n_chunks,
-                              cudaStream_t st) {
-  if (n_chunks == 0) return;
+void launch_b_top_down_leaves(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
+                              uint64_t ctas, cudaStream_t st) {
+  if (ctas == 0) return;
   KScope k("top_down_leaves", st);
-  kb_top_down_leaves<<<(unsigned)n_chunks, kChunk, 0, st>>>(pyrs, emits, chunks);
+  kb_top_down_leaves<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n);
 }
 
 void launch_b_root_info(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, uint32_t* out,
