@@ -510,14 +510,15 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     ck(cudaMemsetAsync(bits, 0, words * 4, st), "memset bits");
     ck(cudaMemsetAsync(task_off + items, 0, 8, st), "memset task_off");
     ck(cudaMemsetAsync(flag, 0, 4, st), "memset flag");
-    launch_b_vox_small(d_vj, dp1(o_cpi), n, cp_items[n], 0, st);
+    launch_b_vox_small(d_vj, dp1(o_cpi), n, cp_items[n], 0, n == 1 ? &vj[0] : nullptr, st);
     scan_u64_exclusive(task_off, items + 1, taskpart, st);
     launch_b_vox_large(d_vj, d_beg, n, task_off, items, counter, 0, st, c->num_sms);
   }
   {
     PhaseScope ph(c, PH_PYR, st);
     ck(cudaMemsetAsync(scan + blocks, 0, 4, st), "memset scan");
-    for (size_t r = 0; r < cp_pyr.size(); r++) launch_b_pyramid(d_pyr, dp1(o_cpp[r]), n, cp_pyr[r][n], (int)r, st);
+    for (size_t r = 0; r < cp_pyr.size(); r++)
+      launch_b_pyramid(d_pyr, dp1(o_cpp[r]), n, cp_pyr[r][n], (int)r, n == 1 ? &pyr[0] : nullptr, st);
     launch_b_pyramid_top(d_pyr, n, kTopPyramidLevel, st);
     scan_u32_exclusive(scan, blocks + 1, scanpart, st);
     launch_b_level_bases(d_pyr, n, d_root, st);
@@ -708,25 +709,29 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const VoxJob* d_vj2 = reinterpret_cast<const VoxJob*>(t2 + o_vj2);
   const Pyramid* d_pyr2 = reinterpret_cast<const Pyramid*>(t2 + o_pyr2);
   const EmitJob* d_ej = reinterpret_cast<const EmitJob*>(t2 + o_ej);
+  const Pyramid* sp1 = n == 1 ? &pyr[0] : nullptr;  // one-stripe launches take the jobs as parameters
+  const EmitJob* se1 = n == 1 ? &ej[0] : nullptr;
 
   {
     PhaseScope ph(c, PH_PYR, st);
-    launch_b_compact(d_pyr2, dp2(o_cc), n, cp_compact[n], keys, st);
+    launch_b_compact(d_pyr2, dp2(o_cc), n, cp_compact[n], keys, n == 1 ? &pyr[0] : nullptr, st);
   }
   if (any_payload) {
     PhaseScope ph(c, PH_VOX, st);
     ck(cudaMemsetAsync(winners, 0xff, total_nodes * 4, st), "memset winners");
-    launch_b_vox_small(d_vj2, dp2(o_cpay), n, cp_pay[n], 1, st);
+    launch_b_vox_small(d_vj2, dp2(o_cpay), n, cp_pay[n], 1, n == 1 ? &vj[0] : nullptr, st);
     launch_b_vox_large(d_vj2, d_beg, n, task_off, items, counter, 1, st, c->num_sms);
-    launch_b_leaf_payload(d_pyr2, d_ej, dp2(o_clp), n, cp_leafpay[n], st);
+    launch_b_leaf_payload(d_pyr2, d_ej, dp2(o_clp), n, cp_leafpay[n], sp1, se1, st);
   }
   {
     PhaseScope ph(c, PH_TREE, st);
-    for (size_t r = 1; r < cp_bu.size(); r++) launch_b_bottom_up(d_pyr2, d_ej, dp2(o_bu[r]), n, cp_bu[r][n], (int)r, st);
+    for (size_t r = 1; r < cp_bu.size(); r++)
+      launch_b_bottom_up(d_pyr2, d_ej, dp2(o_bu[r]), n, cp_bu[r][n], (int)r, sp1, se1, st);
     launch_b_bottom_up_top(d_pyr2, d_ej, n, st);
     launch_b_top_down_top(d_pyr2, d_ej, n, st);
-    for (size_t l = 0; l < cp_td.size(); l++) launch_b_top_down(d_pyr2, d_ej, dp2(o_td[l]), n, cp_td[l][n], (int)l, st);
-    launch_b_top_down_leaves(d_pyr2, d_ej, dp2(o_cl), n, cp_leaves[n], st);
+    for (size_t l = 0; l < cp_td.size(); l++)
+      launch_b_top_down(d_pyr2, d_ej, dp2(o_td[l]), n, cp_td[l][n], (int)l, sp1, se1, st);
+    launch_b_top_down_leaves(d_pyr2, d_ej, dp2(o_cl), n, cp_leaves[n], sp1, se1, st);
     launch_b_root_info(d_pyr2, d_ej, n, d_root, st);
     ck(cudaMemcpyAsync(lvl, d_root, ((uint64_t)n * 16 + 1) * 4, cudaMemcpyDeviceToHost, st), "root info");
   }

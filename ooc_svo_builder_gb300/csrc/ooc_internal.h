@@ -134,33 +134,34 @@ void launch_root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base, ui
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st);
 
 // ---- batched launches: per-stripe jobs in device arrays; `cta_beg` (n + 1 entries) maps CTAs to stripes ----
+// `single` (may be NULL): the job of a one-stripe launch, passed as a kernel parameter.
 void launch_b_vox_small(const VoxJob* jobs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, int pass,
-                        cudaStream_t st);
+                        const VoxJob* single, cudaStream_t st);
 // Large items of every stripe; task_off is the batch-wide exclusive scan (total_items + 1 entries),
 // item_beg[s] the first batch item of stripe s (ascending).
 void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n_stripes, const uint64_t* task_off,
                         uint64_t total_items, unsigned long long* counter, int pass, cudaStream_t st, int num_sms);
 // Level depth - r of each stripe.
 void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, int r,
-                      cudaStream_t st);
+                      const Pyramid* single, cudaStream_t st);
 // One CTA per stripe: levels min(l_hi, depth) .. 0.
 void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cudaStream_t st);
 void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t* keys,
-                      cudaStream_t st);
+                      const Pyramid* single, cudaStream_t st);
 // out[s * (kMaxLevels + 1) + l] = global node index of level l's first node, l = 0..depth+1.
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, cudaStream_t st);
 void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
-                           uint64_t ctas, cudaStream_t st);
+                           uint64_t ctas, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 // Level depth - r of each stripe.
 void launch_b_bottom_up(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas,
-                        int r, cudaStream_t st);
+                        int r, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 void launch_b_bottom_up_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, cudaStream_t st);
 void launch_b_top_down_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, cudaStream_t st);
 // Parents of absolute level l.
 void launch_b_top_down(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas,
-                       int l, cudaStream_t st);
+                       int l, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 void launch_b_top_down_leaves(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
-                              uint64_t ctas, cudaStream_t st);
+                              uint64_t ctas, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 // out[s * 16 + 0..6] = stripe s's root child mask and cache.
 void launch_b_root_info(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, uint32_t* out,
                         cudaStream_t st);

@@ -5,6 +5,8 @@
 // reference's x86-64 build.
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "ooc_device.cuh"
 #include "ooc_internal.h"
 
@@ -912,17 +914,27 @@ __device__ __forceinline__ uint32_t cta_stripe(const uint64_t* __restrict__ cta_
   return s;
 }
 
-template <int PASS>
+// A one-stripe launch (SINGLE) takes the stripe's job as a kernel parameter
+// and indexes elements directly; a batch launch finds its stripe first and
+// stages the job in shared memory.
+template <int PASS, bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_vox_small(const VoxJob* __restrict__ jobs,
-                                                       const uint64_t* __restrict__ cta_beg, uint32_t n) {
-  __shared__ VoxJob sj;
-  uint64_t i;
-  const uint32_t s = cta_stripe(cta_beg, n, i);
-  stage(sj, jobs[s]);
-  __syncthreads();
-  if (i >= sj.n_items) return;
-  if (PASS == 0) vox_small_occ_item(sj, i);
-  else vox_small_win_item(sj, i);
+                                                       const uint64_t* __restrict__ cta_beg, uint32_t n, VoxJob j0) {
+  if constexpr (SINGLE) {
+    const uint64_t i = (uint64_t)blockIdx.x * kChunk + threadIdx.x;
+    if (i >= j0.n_items) return;
+    if (PASS == 0) vox_small_occ_item(j0, i);
+    else vox_small_win_item(j0, i);
+  } else {
+    __shared__ VoxJob sj;
+    uint64_t i;
+    const uint32_t s = cta_stripe(cta_beg, n, i);
+    stage(sj, jobs[s]);
+    __syncthreads();
+    if (i >= sj.n_items) return;
+    if (PASS == 0) vox_small_occ_item(sj, i);
+    else vox_small_win_item(sj, i);
+  }
 }
 
 template <int PASS>
@@ -953,15 +965,22 @@ __global__ void __launch_bounds__(256) kb_vox_large(const VoxJob* __restrict__ j
 }
 
 // Level depth - r of every stripe that has CTAs in this launch.
+template <bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_pyramid(const Pyramid* __restrict__ pyrs,
-                                                     const uint64_t* __restrict__ cta_beg, uint32_t n, int r) {
-  __shared__ Pyramid sp;
-  uint64_t b;
-  const uint32_t s = cta_stripe(cta_beg, n, b);
-  stage(sp, pyrs[s]);
-  __syncthreads();
-  const int l = sp.depth - r;
-  if (b < sp.lv[l].nblocks) pyramid_block(sp, l, b);
+                                                     const uint64_t* __restrict__ cta_beg, uint32_t n, int r, Pyramid p0) {
+  if constexpr (SINGLE) {
+    const uint64_t b = (uint64_t)blockIdx.x * kChunk + threadIdx.x;
+    const int l = p0.depth - r;
+    if (b < p0.lv[l].nblocks) pyramid_block(p0, l, b);
+  } else {
+    __shared__ Pyramid sp;
+    uint64_t b;
+    const uint32_t s = cta_stripe(cta_beg, n, b);
+    stage(sp, pyrs[s]);
+    __syncthreads();
+    const int l = sp.depth - r;
+    if (b < sp.lv[l].nblocks) pyramid_block(sp, l, b);
+  }
 }
 
 __global__ void kb_pyramid_top(const Pyramid* __restrict__ pyrs, int l_hi) {
@@ -974,17 +993,26 @@ __global__ void kb_pyramid_top(const Pyramid* __restrict__ pyrs, int l_hi) {
   }
 }
 
+__device__ __forceinline__ void compact_stripe_block(const Pyramid& p, uint64_t b, uint32_t* __restrict__ keys) {
+  const uint64_t first = p.lv[0].off_b, end = p.lv[p.depth].off_b + p.lv[p.depth].nblocks;
+  if (first + b < end) compact_block(p, first + b, keys);
+}
+
 // Every block of every level of the stripe.
+template <bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__ pyrs,
                                                      const uint64_t* __restrict__ cta_beg, uint32_t n,
-                                                     uint32_t* __restrict__ keys) {
-  __shared__ Pyramid sp;
-  uint64_t b;
-  const uint32_t s = cta_stripe(cta_beg, n, b);
-  stage(sp, pyrs[s]);
-  __syncthreads();
-  const uint64_t first = sp.lv[0].off_b, end = sp.lv[sp.depth].off_b + sp.lv[sp.depth].nblocks;
-  if (first + b < end) compact_block(sp, first + b, keys);
+                                                     uint32_t* __restrict__ keys, Pyramid p0) {
+  if constexpr (SINGLE) {
+    compact_stripe_block(p0, (uint64_t)blockIdx.x * kChunk + threadIdx.x, keys);
+  } else {
+    __shared__ Pyramid sp;
+    uint64_t b;
+    const uint32_t s = cta_stripe(cta_beg, n, b);
+    stage(sp, pyrs[s]);
+    __syncthreads();
+    compact_stripe_block(sp, b, keys);
+  }
 }
 
 __global__ void kb_level_bases(const Pyramid* __restrict__ pyrs, uint32_t n_stripes, uint32_t* __restrict__ out) {
@@ -996,31 +1024,39 @@ __global__ void kb_level_bases(const Pyramid* __restrict__ pyrs, uint32_t n_stri
   o[p.depth + 1] = p.scan[p.lv[p.depth].off_b + p.lv[p.depth].nblocks];
 }
 
-__global__ void __launch_bounds__(kChunk) kb_leaf_payload(const Pyramid* __restrict__ pyrs,
-                                                          const EmitJob* __restrict__ emits,
-                                                          const uint64_t* __restrict__ cta_beg, uint32_t n) {
-  __shared__ Pyramid sp;
-  __shared__ EmitJob se;
-  uint64_t i;
-  const uint32_t s = cta_stripe(cta_beg, n, i);
-  stage(sp, pyrs[s]);
-  stage(se, emits[s]);
-  __syncthreads();
-  if (i < sp.lv[sp.depth].n) leaf_payload(sp, se, i);
+// Kinds of per-node launches that take (Pyramid, EmitJob) pairs.
+enum NodeOp { OP_LEAF_PAYLOAD = 0, OP_BOTTOM_UP = 1, OP_TOP_DOWN = 2, OP_LEAVES = 3 };
+
+template <int OP>
+__device__ __forceinline__ void node_op(const Pyramid& p, const EmitJob& e, int arg, uint64_t i) {
+  if (OP == OP_LEAF_PAYLOAD) {
+    if (i < p.lv[p.depth].n) leaf_payload(p, e, i);
+  } else if (OP == OP_BOTTOM_UP) {
+    const int l = p.depth - arg;  // arg = distance from the leaf level
+    if (i < p.lv[l].n) bottom_up_node(p, e, l, i);
+  } else if (OP == OP_TOP_DOWN) {
+    if (i < p.lv[arg].n) top_down_node(p, e, arg, i);  // arg = absolute parent level
+  } else {
+    if (i < p.lv[p.depth].n) top_down_leaf(p, e, i);
+  }
 }
 
-// Level depth - r of every stripe that has CTAs in this launch.
-__global__ void __launch_bounds__(kChunk) kb_bottom_up(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits,
-                                                       const uint64_t* __restrict__ cta_beg, uint32_t n, int r) {
-  __shared__ Pyramid sp;
-  __shared__ EmitJob se;
-  uint64_t i;
-  const uint32_t s = cta_stripe(cta_beg, n, i);
-  stage(sp, pyrs[s]);
-  stage(se, emits[s]);
-  __syncthreads();
-  const int l = sp.depth - r;
-  if (i < sp.lv[l].n) bottom_up_node(sp, se, l, i);
+template <int OP, bool SINGLE>
+__global__ void __launch_bounds__(kChunk) kb_nodes(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits,
+                                                   const uint64_t* __restrict__ cta_beg, uint32_t n, int arg, Pyramid p0,
+                                                   EmitJob e0) {
+  if constexpr (SINGLE) {
+    node_op<OP>(p0, e0, arg, (uint64_t)blockIdx.x * kChunk + threadIdx.x);
+  } else {
+    __shared__ Pyramid sp;
+    __shared__ EmitJob se;
+    uint64_t i;
+    const uint32_t s = cta_stripe(cta_beg, n, i);
+    stage(sp, pyrs[s]);
+    stage(se, emits[s]);
+    __syncthreads();
+    node_op<OP>(sp, se, arg, i);
+  }
 }
 
 // One CTA per stripe: bottom-up of levels l_small .. 0.
@@ -1055,32 +1091,6 @@ __global__ void kb_top_down_top(const Pyramid* __restrict__ pyrs, const EmitJob*
     for (uint64_t i = threadIdx.x; i < sp.lv[l].n; i += blockDim.x) top_down_node(sp, se, l, i);
     __syncthreads();
   }
-}
-
-// Parents of absolute level l of every stripe that has CTAs in this launch.
-__global__ void __launch_bounds__(kChunk) kb_top_down(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits,
-                                                      const uint64_t* __restrict__ cta_beg, uint32_t n, int l) {
-  __shared__ Pyramid sp;
-  __shared__ EmitJob se;
-  uint64_t i;
-  const uint32_t s = cta_stripe(cta_beg, n, i);
-  stage(sp, pyrs[s]);
-  stage(se, emits[s]);
-  __syncthreads();
-  if (i < sp.lv[l].n) top_down_node(sp, se, l, i);
-}
-
-__global__ void __launch_bounds__(kChunk) kb_top_down_leaves(const Pyramid* __restrict__ pyrs,
-                                                             const EmitJob* __restrict__ emits,
-                                                             const uint64_t* __restrict__ cta_beg, uint32_t n) {
-  __shared__ Pyramid sp;
-  __shared__ EmitJob se;
-  uint64_t i;
-  const uint32_t s = cta_stripe(cta_beg, n, i);
-  stage(sp, pyrs[s]);
-  stage(se, emits[s]);
-  __syncthreads();
-  if (i < sp.lv[sp.depth].n) top_down_leaf(sp, se, i);
 }
 
 __global__ void kb_root_info(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits, uint32_t n_stripes,
@@ -1219,11 +1229,19 @@ void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t
 
 // ---- batched launch wrappers ----
 void launch_b_vox_small(const VoxJob* jobs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, int pass,
-                        cudaStream_t st) {
+                        const VoxJob* single, cudaStream_t st) {
   if (ctas == 0) return;
   KScope k(pass == 0 ? "vox_small_occupancy" : "vox_small_winner", st);
-  if (pass == 0) kb_vox_small<0><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n);
-  else kb_vox_small<1><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n);
+  VoxJob j0;
+  std::memset(&j0, 0, sizeof(j0));
+  if (single) j0 = *single;
+  if (pass == 0) {
+    if (single) kb_vox_small<0, true><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n, j0);
+    else kb_vox_small<0, false><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n, j0);
+  } else {
+    if (single) kb_vox_small<1, true><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n, j0);
+    else kb_vox_small<1, false><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n, j0);
+  }
 }
 
 void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n_stripes, const uint64_t* task_off,
@@ -1237,10 +1255,14 @@ void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n
 }
 
 void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, int r,
-                      cudaStream_t st) {
+                      const Pyramid* single, cudaStream_t st) {
   if (ctas == 0) return;
   KScope k(r == 0 ? "pyramid_leaf" : "pyramid", st);
-  kb_pyramid<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, r);
+  Pyramid p0;
+  std::memset(&p0, 0, sizeof(p0));
+  if (single) p0 = *single;
+  if (single) kb_pyramid<true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, r, p0);
+  else kb_pyramid<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, r, p0);
 }
 
 void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cudaStream_t st) {
@@ -1250,10 +1272,14 @@ void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cud
 }
 
 void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t* keys,
-                      cudaStream_t st) {
+                      const Pyramid* single, cudaStream_t st) {
   if (ctas == 0) return;
   KScope k("compact", st);
-  kb_compact<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys);
+  Pyramid p0;
+  std::memset(&p0, 0, sizeof(p0));
+  if (single) p0 = *single;
+  if (single) kb_compact<true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys, p0);
+  else kb_compact<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys, p0);
 }
 
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, cudaStream_t st) {
@@ -1262,18 +1288,35 @@ void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out
   kb_level_bases<<<grid_for(n_stripes, 128), 128, 0, st>>>(pyrs, n_stripes, out);
 }
 
-void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
-                           uint64_t ctas, cudaStream_t st) {
+namespace {
+template <int OP>
+void launch_nodes(const char* name, const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
+                  uint64_t ctas, int arg, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
   if (ctas == 0) return;
-  KScope k("leaf_payload", st);
-  kb_leaf_payload<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n);
+  KScope k(name, st);
+  Pyramid p0;
+  EmitJob e0;
+  std::memset(&p0, 0, sizeof(p0));
+  std::memset(&e0, 0, sizeof(e0));
+  if (sp && se) {
+    p0 = *sp;
+    e0 = *se;
+    kb_nodes<OP, true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, arg, p0, e0);
+  } else {
+    kb_nodes<OP, false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, arg, p0, e0);
+  }
+}
+}  // namespace
+
+void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
+                           uint64_t ctas, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
+  launch_nodes<OP_LEAF_PAYLOAD>("leaf_payload", pyrs, emits, cta_beg, n, ctas, 0, sp, se, st);
 }
 
 void launch_b_bottom_up(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas,
-                        int r, cudaStream_t st) {
-  if (ctas == 0) return;
-  KScope k(r == 1 ? "bottom_up_leaf_parents" : "bottom_up", st);
-  kb_bottom_up<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, r);
+                        int r, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
+  launch_nodes<OP_BOTTOM_UP>(r == 1 ? "bottom_up_leaf_parents" : "bottom_up", pyrs, emits, cta_beg, n, ctas, r, sp,
+                             se, st);
 }
 
 void launch_b_bottom_up_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, cudaStream_t st) {
@@ -1289,17 +1332,13 @@ void launch_b_top_down_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n
 }
 
 void launch_b_top_down(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas,
-                       int l, cudaStream_t st) {
-  if (ctas == 0) return;
-  KScope k("top_down", st);
-  kb_top_down<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, l);
+                       int l, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
+  launch_nodes<OP_TOP_DOWN>("top_down", pyrs, emits, cta_beg, n, ctas, l, sp, se, st);
 }
 
 void launch_b_top_down_leaves(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
-                              uint64_t ctas, cudaStream_t st) {
-  if (ctas == 0) return;
-  KScope k("top_down_leaves", st);
-  kb_top_down_leaves<<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n);
+                              uint64_t ctas, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
+  launch_nodes<OP_LEAVES>("top_down_leaves", pyrs, emits, cta_beg, n, ctas, 0, sp, se, st);
 }
 
 void launch_b_root_info(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, uint32_t* out,
