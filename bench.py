@@ -305,6 +305,94 @@ def run_ours(args, world, rank, local):
     return line
 
 
+def run_batch(args, world, rank, local):
+    """Configuration 4: the batched form against the plain per-mesh path, both through the C ABI
+    from pinned host triangles to host octree bytes."""
+    import ctypes
+    import torch
+    import ooc_svo_builder_gb300 as ooc
+
+    torch.cuda.set_device(local)
+    meshes = tri.batch_meshes(args.n_meshes, seed=4)
+    n = len(meshes)
+    total_tris = sum(m[0].shape[0] for m in meshes)
+    offs = [0]
+    for t, _, _ in meshes:
+        offs.append(offs[-1] + (t.nbytes + 255) // 256 * 256)
+    pinned = torch.empty(offs[-1], dtype=torch.uint8).pin_memory()
+    host = pinned.numpy()
+    arr = (ooc.Mesh * n)()
+    params = []
+    for i, (t, N, payload) in enumerate(meshes):
+        host[offs[i]:offs[i] + t.nbytes] = t.reshape(-1).view(np.uint8)
+        p = ooc.make_params(N, 2048, geometry_only=not payload)
+        params.append(p)
+        arr[i].tris = pinned.data_ptr() + offs[i]
+        arr[i].n_tris = t.shape[0]
+        arr[i].params = p
+    infos = (ooc.BuildInfo * n)()
+    cb = ooc.BATCH_SINK(lambda user, mesh, kind, ptr, nb: 0)
+    cb1 = ooc.SINK(lambda user, kind, ptr, nb: 0)
+    b = ooc.Builder(local)
+
+    for _ in range(max(1, args.warmup)):
+        b.build_batch_ptrs(arr, n, cb, infos)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.build_batch_ptrs(arr, n, cb, infos)
+    t_batch = (time.perf_counter() - t0) / args.steps
+    launches = b.kernel_launches()
+    n_nodes = sum(int(infos[i].n_nodes) for i in range(n))
+
+    # plain path: one ooc_build per mesh
+    for i in range(min(n, 64)):
+        b.build_ptr(arr[i].tris, arr[i].n_tris, params[i], cb1)
+    t0 = time.perf_counter()
+    for i in range(n):
+        b.build_ptr(arr[i].tris, arr[i].n_tris, params[i], cb1)
+    t_plain = time.perf_counter() - t0
+
+    # parity sample: the batch's bytes equal the plain path's for every 64th mesh
+    sample = list(range(0, n, 64))
+    got = {i: {0: [], 1: []} for i in sample}
+
+    def collect(user, mesh, kind, ptr, nb):
+        if mesh in got:
+            got[mesh][kind].append(ctypes.string_at(ptr, nb))
+        return 0
+
+    b.build_batch_ptrs(arr, n, ooc.BATCH_SINK(collect), infos)
+    identical = True
+    for i in sample:
+        want = {0: [], 1: []}
+
+        def collect1(user, kind, ptr, nb, want=want):
+            want[kind].append(ctypes.string_at(ptr, nb))
+            return 0
+
+        b.build_ptr(arr[i].tris, arr[i].n_tris, params[i], ooc.SINK(collect1))
+        for k in (0, 1):
+            identical = identical and b"".join(got[i][k]) == b"".join(want[k])
+    b.close()
+    value = n / t_batch
+    return {
+        "metric": "meshes/s", "value": value, "unit": "meshes/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_batch * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "configuration 4: %d meshes, log-uniform 64..200k triangles (icospheres and soups), "
+                               "gridsize 64/128/256/512, binary or payload 50/50, one ooc_build_batch call" % n,
+                   "name": "batch4096", "n_meshes": n, "n_triangles": total_tris},
+        "mtri_per_s": total_tris / t_batch / 1e6, "svo_nodes_per_s": n_nodes / t_batch,
+        "plain_meshes_per_s": n / t_plain, "speedup_vs_plain": t_plain / t_batch,
+        "parity_sample": {"meshes": len(sample), "identical_to_plain": identical},
+        "e2e": {"value": value, "unit": "meshes/s", "h2d_bytes_per_step": int(sum(m[0].nbytes for m in meshes)),
+                "d2h_bytes_per_step": int(sum(int(infos[i].n_nodes) * 24 + int(infos[i].n_data) * 32
+                                              for i in range(n)))},
+        "gpu_launches": launches,
+    }
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return None
@@ -333,7 +421,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="heightfield1024", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="heightfield1024", choices=sorted(WORKLOADS) + ["batch4096"])
+    ap.add_argument("--n-meshes", type=int, default=4096, help="meshes of the batch4096 workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")
@@ -343,6 +432,8 @@ def main():
     world, rank, local = dist_setup(args.gpus)
     if args.impl == "reference":
         line = run_reference(args, world, rank)
+    elif args.workload == "batch4096":
+        line = run_batch(args, world, rank, local)
     else:
         line = run_ours(args, world, rank, local)
     if rank == 0 and line is not None:

@@ -114,22 +114,6 @@ void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const floa
 void launch_vox_small(const VoxJob& j, int pass, cudaStream_t st);
 void launch_vox_large(const VoxJob& j, int pass, cudaStream_t st, int num_sms);
 
-void launch_pyramid(const Pyramid& p, int level, cudaStream_t st);
-void launch_pyramid_top(const Pyramid& p, int l_hi, cudaStream_t st);  // levels l_hi..0 in one CTA
-void launch_compact(const Pyramid& p, uint64_t total_blocks, uint32_t* keys, cudaStream_t st);
-void launch_level_bases(const Pyramid& p, uint64_t total_blocks, uint32_t* out, cudaStream_t st);
-void launch_leaf_payload(const Pyramid& p, const EmitJob& e, cudaStream_t st);
-void launch_bottom_up(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st);
-void launch_bottom_up_top(const Pyramid& p, const EmitJob& e, int l_hi, cudaStream_t st);
-// Parents of level `level` (at most depth-2) write their children's records.
-void launch_top_down(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st);
-// Leaf records (and payload data records), one thread per leaf.
-void launch_top_down_leaves(const Pyramid& p, const EmitJob& e, cudaStream_t st);
-void launch_top_down_top(const Pyramid& p, const EmitJob& e, int l_lo, uint64_t node_base, uint64_t data_base,
-                         cudaStream_t st);
-// Writes the stripe root's child mask and cache to out[0..6] and its own data
-// record (with -levels, or the payload of a one-voxel stripe).
-void launch_root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base, uint32_t* out, cudaStream_t st);
 // src holds n entries of (index, `words` u64 values); dst[index*words + q] = value q.
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st);
 

@@ -271,7 +271,6 @@ __global__ void k_part_emit(const float* __restrict__ tris, int stride, uint64_t
         }
 }
 
-
 // ===========================================================================
 // Voxelization (voxelizer.cpp:168-306)
 //
@@ -480,19 +479,6 @@ __device__ __forceinline__ void pyramid_block(const Pyramid& p, int l, uint64_t 
   if (l > 0) p.bits[p.lv[l - 1].off_w + b] = pw;
 }
 
-__global__ void k_pyramid(Pyramid p, int l) {
-  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < p.lv[l].nblocks) pyramid_block(p, l, b);
-}
-
-// Levels l_hi .. 0 in one CTA (they are small); the barrier orders the levels.
-__global__ void k_pyramid_top(Pyramid p, int l_hi) {
-  for (int l = l_hi; l >= 0; l--) {
-    for (uint64_t b = threadIdx.x; b < p.lv[l].nblocks; b += blockDim.x) pyramid_block(p, l, b);
-    __syncthreads();
-  }
-}
-
 // Global node index of bit `b` of a level: the concatenated scan already
 // counts every node of the shallower levels.
 __device__ __forceinline__ uint64_t node_index(const uint32_t* __restrict__ bits, const uint32_t* __restrict__ scan,
@@ -525,11 +511,6 @@ __device__ __forceinline__ void compact_block(const Pyramid& p, uint64_t b, uint
       word &= word - 1;
     }
   }
-}
-
-__global__ void k_compact(Pyramid p, uint64_t total_blocks, uint32_t* __restrict__ keys) {
-  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < total_blocks) compact_block(p, b, keys);
 }
 
 // ===========================================================================
@@ -623,11 +604,6 @@ __device__ __forceinline__ void leaf_payload(const Pyramid& p, const EmitJob& e,
   }
 }
 
-__global__ void k_leaf_payload(Pyramid p, EmitJob e) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < p.lv[p.depth].n) leaf_payload(p, e, i);
-}
-
 // ===========================================================================
 // Octree layout.  Subtree sizes bottom-up, then top-down the index of the
 // first node / data record written inside every subtree; the reference writes
@@ -695,19 +671,6 @@ __device__ __forceinline__ void bottom_up_node(const Pyramid& p, const EmitJob& 
   e.dsize[gi] = dsz;
   e.first_child[gi] = (uint32_t)c0;
   if (e.levels) average_children(e, mask, c0, child_leaf, e.cache + gi * 6);
-}
-
-__global__ void k_bottom_up(Pyramid p, EmitJob e, int l) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < p.lv[l].n) bottom_up_node(p, e, l, i);
-}
-
-// Levels l_hi .. 0 in one CTA.
-__global__ void k_bottom_up_top(Pyramid p, EmitJob e, int l_hi) {
-  for (int l = l_hi; l >= 0; l--) {
-    for (uint64_t i = threadIdx.x; i < p.lv[l].n; i += blockDim.x) bottom_up_node(p, e, l, i);
-    __syncthreads();
-  }
 }
 
 __device__ __forceinline__ void store_data_record(const EmitJob& e, uint64_t idx, uint64_t morton, const float* v) {
@@ -817,29 +780,6 @@ __device__ __forceinline__ void top_down_leaf(const Pyramid& p, const EmitJob& e
   store_data_record(e, di, e.stripe_base + k, v);
 }
 
-__global__ void k_top_down_leaves(Pyramid p, EmitJob e) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < p.lv[p.depth].n) top_down_leaf(p, e, i);
-}
-
-__global__ void k_top_down(Pyramid p, EmitJob e, int l) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < p.lv[l].n) top_down_node(p, e, l, i);
-}
-
-// Parents of levels 0 .. l_lo in one CTA; the stripe root starts at the bases.
-__global__ void k_top_down_top(Pyramid p, EmitJob e, int l_lo, uint64_t node_base, uint64_t data_base) {
-  if (threadIdx.x == 0) {
-    e.start[0] = node_base;
-    e.dstart[0] = data_base;
-  }
-  __syncthreads();
-  for (int l = 0; l <= l_lo; l++) {
-    for (uint64_t i = threadIdx.x; i < p.lv[l].n; i += blockDim.x) top_down_node(p, e, l, i);
-    __syncthreads();
-  }
-}
-
 // Stripe root: child mask and payload for the host, and (with -levels, or a
 // one-voxel stripe in payload mode) the root's own data record.
 __device__ void root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base, uint32_t* out) {
@@ -864,15 +804,6 @@ __device__ void root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base
   }
 }
 
-__global__ void k_root_info(Pyramid p, EmitJob e, uint64_t data_base, uint32_t* out) { root_info(p, e, data_base, out); }
-
-// Per-level node counts from the scan: out[l] = first node of level l, out[depth+1] = total.
-__global__ void k_level_bases(Pyramid p, uint64_t total_blocks, uint32_t* out) {
-  const int l = threadIdx.x;
-  if (l <= p.depth) out[l] = p.scan[p.lv[l].off_b];
-  if (l == p.depth + 1) out[l] = p.scan[total_blocks];
-}
-
 __global__ void k_scatter_records(const uint64_t* __restrict__ src, uint64_t n, int words, uint64_t* __restrict__ dst) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -880,7 +811,6 @@ __global__ void k_scatter_records(const uint64_t* __restrict__ src, uint64_t n, 
   uint64_t* d = dst + s[0] * words;
   for (int q = 0; q < words; q++) d[q] = s[1 + q];
 }
-
 
 // ===========================================================================
 // Batched forms: every stripe of a batch in one launch.  A chunk table gives
@@ -1156,76 +1086,11 @@ void launch_vox_large(const VoxJob& j, int pass, cudaStream_t st, int num_sms) {
   else k_vox_large<1><<<grid, 256, 0, st>>>(j);
 }
 
-void launch_pyramid(const Pyramid& p, int level, cudaStream_t st) {
-  KScope k(level == p.depth ? "pyramid_leaf" : "pyramid", st);
-  k_pyramid<<<grid_for(p.lv[level].nblocks, 256), 256, 0, st>>>(p, level);
-}
-
-void launch_pyramid_top(const Pyramid& p, int l_hi, cudaStream_t st) {
-  KScope k("pyramid_top", st);
-  k_pyramid_top<<<1, 1024, 0, st>>>(p, l_hi);
-}
-
-void launch_compact(const Pyramid& p, uint64_t total_blocks, uint32_t* keys, cudaStream_t st) {
-  KScope k("compact", st);
-  k_compact<<<grid_for(total_blocks, 256), 256, 0, st>>>(p, total_blocks, keys);
-}
-
-void launch_level_bases(const Pyramid& p, uint64_t total_blocks, uint32_t* out, cudaStream_t st) {
-  KScope k("level_bases", st);
-  k_level_bases<<<1, 32, 0, st>>>(p, total_blocks, out);
-}
-
-void launch_leaf_payload(const Pyramid& p, const EmitJob& e, cudaStream_t st) {
-  const uint64_t n = p.lv[p.depth].n;
-  if (n == 0) return;
-  KScope k("leaf_payload", st);
-  k_leaf_payload<<<grid_for(n, 256), 256, 0, st>>>(p, e);
-}
-
-void launch_bottom_up(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st) {
-  const uint64_t n = p.lv[level].n;
-  if (n == 0) return;
-  KScope k(level == p.depth - 1 ? "bottom_up_leaf_parents" : "bottom_up", st);
-  k_bottom_up<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
-}
-
-void launch_bottom_up_top(const Pyramid& p, const EmitJob& e, int l_hi, cudaStream_t st) {
-  KScope k("bottom_up_top", st);
-  k_bottom_up_top<<<1, 1024, 0, st>>>(p, e, l_hi);
-}
-
-void launch_top_down(const Pyramid& p, const EmitJob& e, int level, cudaStream_t st) {
-  const uint64_t n = p.lv[level].n;
-  if (n == 0) return;
-  KScope k("top_down", st);
-  k_top_down<<<grid_for(n, 256), 256, 0, st>>>(p, e, level);
-}
-
-void launch_top_down_leaves(const Pyramid& p, const EmitJob& e, cudaStream_t st) {
-  const uint64_t n = p.lv[p.depth].n;
-  if (n == 0 || p.depth < 1) return;
-  KScope k("top_down_leaves", st);
-  k_top_down_leaves<<<grid_for(n, 256), 256, 0, st>>>(p, e);
-}
-
-void launch_top_down_top(const Pyramid& p, const EmitJob& e, int l_lo, uint64_t node_base, uint64_t data_base,
-                         cudaStream_t st) {
-  KScope k("top_down_top", st);
-  k_top_down_top<<<1, 1024, 0, st>>>(p, e, l_lo, node_base, data_base);
-}
-
-void launch_root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base, uint32_t* out, cudaStream_t st) {
-  KScope k("root_info", st);
-  k_root_info<<<1, 1, 0, st>>>(p, e, data_base, out);
-}
-
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st) {
   if (n == 0) return;
   KScope k("scatter_records", st);
   k_scatter_records<<<grid_for(n, 128), 128, 0, st>>>(src, n, words, dst);
 }
-
 
 // ---- batched launch wrappers ----
 void launch_b_vox_small(const VoxJob* jobs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, int pass,

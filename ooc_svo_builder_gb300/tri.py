@@ -118,7 +118,7 @@ def face_normals(v0: np.ndarray, v1: np.ndarray, v2: np.ndarray) -> np.ndarray:
     sq = (c[:, 0] * c[:, 0] + c[:, 1] * c[:, 1]) + c[:, 2] * c[:, 2]
     with np.errstate(divide="ignore", invalid="ignore"):
         r = np.float32(1.0) / np.sqrt(sq)
-    return (c * r[:, None]).astype(np.float32)
+        return (c * r[:, None]).astype(np.float32)
 
 
 def pack(v0, v1, v2, normals=None, colors=None) -> np.ndarray:
@@ -139,12 +139,13 @@ def pack(v0, v1, v2, normals=None, colors=None) -> np.ndarray:
 # Seeded synthetic meshes
 # --------------------------------------------------------------------------
 
-def icosphere(subdiv: int, radius: float = 0.4, center=(0.5, 0.5, 0.5), jitter: float = 0.002,
-              seed: int = 1):
-    """Icosphere with 20 * 4**subdiv faces; every unique vertex moves radially by N(0, jitter).
+_UNIT_ICOSPHERES: dict = {}
 
-    Returns (vertices[V, 3] float64 on the unit sphere scaled and jittered, faces[F, 3]).
-    """
+
+def _unit_icosphere(subdiv: int):
+    """Vertices on the unit sphere and faces of the subdivided icosahedron (cached per level)."""
+    if subdiv in _UNIT_ICOSPHERES:
+        return _UNIT_ICOSPHERES[subdiv]
     t = (1.0 + 5.0 ** 0.5) / 2.0
     verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t),
              (0, -1, -t), (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
@@ -170,6 +171,17 @@ def icosphere(subdiv: int, radius: float = 0.4, center=(0.5, 0.5, 0.5), jitter: 
         F = np.concatenate([
             np.stack([F[:, 0], m01, m20], 1), np.stack([F[:, 1], m12, m01], 1),
             np.stack([F[:, 2], m20, m12], 1), np.stack([m01, m12, m20], 1)], axis=0)
+    _UNIT_ICOSPHERES[subdiv] = (V, F)
+    return V, F
+
+
+def icosphere(subdiv: int, radius: float = 0.4, center=(0.5, 0.5, 0.5), jitter: float = 0.002,
+              seed: int = 1):
+    """Icosphere with 20 * 4**subdiv faces; every unique vertex moves radially by N(0, jitter).
+
+    Returns (vertices[V, 3] float64 on the unit sphere scaled and jittered, faces[F, 3]).
+    """
+    V, F = _unit_icosphere(subdiv)
     rng = np.random.default_rng(seed)
     r = radius + rng.normal(0.0, jitter, size=V.shape[0])
     P = np.asarray(center, np.float64)[None, :] + V * r[:, None]
@@ -296,3 +308,30 @@ def random_tris(n_tris: int, seed: int, payload: bool, lo: float = 0.0, hi: floa
 def to_binary(tris: np.ndarray) -> np.ndarray:
     """Drop normals and colours: [T, 21] -> [T, 9]."""
     return np.ascontiguousarray(tris[:, :9])
+
+
+def batch_meshes(n_meshes: int = 4096, seed: int = 4, tri_min: int = 64, tri_max: int = 200_000,
+                 gridsizes=(64, 128, 256, 512)):
+    """Configuration 4's mesh set: (triangles, gridsize, payload) per mesh.
+
+    Triangle counts are log-uniform in [tri_min, tri_max]; half the meshes are
+    icospheres (subdivision 1..7, the one closest below the drawn count), half
+    soups as in configuration 3 at that count; gridsize uniform in `gridsizes`;
+    binary or payload mode at 50/50.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_meshes):
+        T = int(round(float(np.exp(rng.uniform(np.log(tri_min), np.log(tri_max))))))
+        N = int(rng.choice(gridsizes))
+        payload = bool(rng.integers(0, 2))
+        sub_seed = int(rng.integers(0, 2**31 - 1))
+        if rng.random() < 0.5:
+            s = int(np.clip(np.floor(np.log(max(T, 80) / 20.0) / np.log(4.0)), 1, 7))
+            tris = icosphere_tris(s, radius=float(rng.uniform(0.2, 0.45)), jitter=0.002, seed=sub_seed,
+                                  payload=payload)
+        else:
+            tris = soup_tris(T, N, seed=sub_seed, sigma=1.0, n_spheres=max(1, min(200, T // 500)),
+                             payload=payload)
+        out.append((tris, N, payload))
+    return out
