@@ -114,6 +114,11 @@ struct ooc_ctx {
       d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo, d_itemmask,
       d_firstchild, d_itembox;
   PinBuf h_nodes, h_data, h_misc, h_recs, h_tables1, h_tables2;
+  // double-buffered outputs of pipelined sub-batches
+  DevBuf d_out_nodes[2], d_out_data[2];
+  PinBuf h_out_nodes[2], h_out_data[2], h_root[2];
+  cudaEvent_t ev_compute[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr};
+  cudaStream_t copy_stream = nullptr;
   DevBuf d_tables1, d_tables2;
   std::vector<DevBuf> d_mesh_items;
   uint64_t batch_budget_bytes = 4ull << 30;  // occupancy pyramids of one sub-batch
@@ -353,11 +358,22 @@ struct MeshWork {
   std::vector<uint32_t> part_off;  // P > 1: items of partition p are part_off[p] .. part_off[p+1)
   const uint32_t* items = nullptr;
   Emitter* out = nullptr;
-  TopBuilder top;
+  TopBuilder top;            // emits the records above the stripes, in file order
   uint64_t next_stripe = 0;  // stripes before this one have been pushed into `top`
+  Emitter dry;
+  TopBuilder layout;         // the same grouping run ahead on placeholders: file positions only
+  uint64_t layout_next = 0;
   uint64_t filled = 0;
   uint64_t n_items = 0;
-  MeshWork(const Plan& p, Emitter* o) : pl(p), out(o), top(p.Ls, p.levels != 0, o) {}
+  MeshWork(const Plan& p, Emitter* o)
+      : pl(p), out(o), top(p.Ls, p.levels != 0, o), layout(p.Ls, p.levels != 0, nullptr) {
+    dry.dry = true;
+  }
+  MeshWork(const MeshWork&) = delete;
+  MeshWork(MeshWork&& o) noexcept
+      : prm(o.prm), pl(o.pl), d_tris(o.d_tris), n_tris(o.n_tris), part_off(std::move(o.part_off)), items(o.items),
+        out(o.out), top(o.top), next_stripe(o.next_stripe), dry(o.dry), layout(o.layout),
+        layout_next(o.layout_next), filled(o.filled), n_items(o.n_items) {}
 };
 
 struct StripeRef {
@@ -419,8 +435,17 @@ struct Uploader {
   }
 };
 
+// A launched sub-batch whose records are still on their way to the host.
+struct Pending {
+  bool active = false;
+  int slot = 0;
+  std::vector<StripeRef> sb;
+  std::vector<Placed> pl;
+  std::vector<int> depth;
+};
+
 void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, const std::vector<StripeRef>& sb,
-                   bool device_mode) {
+                   bool device_mode, Pending& out_pending, int slot) {
   const uint32_t n = (uint32_t)sb.size();
   // ---- geometry of every stripe ----
   std::vector<Pyramid> pyr(n);
@@ -550,35 +575,23 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   }
   // node indices are 32-bit within a sub-batch (the block scan is u32)
   if (summed != total_nodes) fail(OOC_ERR_LIMIT, "more than 2^32 nodes in one sub-batch; lower the batch budget");
-  // dry run of the host-side grouping: where every stripe's records start
-  {
-    Emitter dry;
-    dry.dry = true;
-    std::vector<TopBuilder> tops;
-    std::vector<uint64_t> cursor(meshes.size());
-    std::vector<int> have(meshes.size(), -1);
-    for (uint32_t s = 0; s < n; s++) {
-      const uint32_t mi = sb[s].mesh;
-      if (have[mi] < 0) {
-        have[mi] = (int)tops.size();
-        tops.push_back(meshes[mi].top);
-        tops.back().out = &dry;
-        cursor[mi] = meshes[mi].next_stripe;
-      }
-      TopBuilder& tb = tops[have[mi]];
-      for (; cursor[mi] < sb[s].stripe; cursor[mi]++) tb.push(tb.top, TNode());
-      pl[s].node_base = tb.node_pos;
-      pl[s].data_base = tb.data_pos;
-      if (pl[s].empty) {
-        tb.push(tb.top, TNode());
-      } else {
-        tb.node_pos += pl[s].node_span;
-        tb.data_pos += pl[s].data_span;
-        TNode ph;
-        ph.off = 0;  // any non-null node
-        tb.push(tb.top, ph);
-      }
-      cursor[mi]++;
+  // the grouping above the stripes, run ahead on placeholders: where every stripe's records start
+  for (uint32_t s = 0; s < n; s++) {
+    MeshWork& m = meshes[sb[s].mesh];
+    TopBuilder& tb = m.layout;
+    tb.out = &m.dry;
+    for (; m.layout_next < sb[s].stripe; m.layout_next++) tb.push(tb.top, TNode());
+    m.layout_next++;
+    pl[s].node_base = tb.node_pos;
+    pl[s].data_base = tb.data_pos;
+    if (pl[s].empty) {
+      tb.push(tb.top, TNode());
+    } else {
+      tb.node_pos += pl[s].node_span;
+      tb.data_pos += pl[s].data_span;
+      TNode ph;
+      ph.off = 0;  // any non-null node
+      tb.push(tb.top, ph);
     }
   }
   // ---- per-node arrays and output windows ----
@@ -611,8 +624,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       out_nodes += pl[s].node_span;
       out_data += pl[s].data_span;
     }
-    ensure<uint64_t>(c->d_nodes, out_nodes * 24);
-    ensure<unsigned char>(c->d_data, out_data * 32);
+    ensure<uint64_t>(c->d_out_nodes[slot], out_nodes * 24);
+    ensure<unsigned char>(c->d_out_data[slot], out_data * 32);
   }
   std::vector<EmitJob> ej(n);
   for (uint32_t s = 0; s < n; s++) {
@@ -650,8 +663,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       e.node_win_len = q.node_base + q.node_span;
       e.data_win_len = q.data_base + q.data_span;
     } else {
-      e.node_win = static_cast<uint64_t*>(c->d_nodes.p) + q.out_node_off * 3;
-      e.data_win = static_cast<unsigned char*>(c->d_data.p) + q.out_data_off * 32;
+      e.node_win = static_cast<uint64_t*>(c->d_out_nodes[slot].p) + q.out_node_off * 3;
+      e.data_win = static_cast<unsigned char*>(c->d_out_data[slot].p) + q.out_data_off * 32;
       e.node_win_base = q.node_base;
       e.data_win_base = q.data_base;
       e.node_win_len = q.node_span;
@@ -733,26 +746,46 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       launch_b_top_down(d_pyr2, d_ej, dp2(o_td[l]), n, cp_td[l][n], (int)l, sp1, se1, st);
     launch_b_top_down_leaves(d_pyr2, d_ej, dp2(o_cl), n, cp_leaves[n], sp1, se1, st);
     launch_b_root_info(d_pyr2, d_ej, n, d_root, st);
-    ck(cudaMemcpyAsync(lvl, d_root, ((uint64_t)n * 16 + 1) * 4, cudaMemcpyDeviceToHost, st), "root info");
+    uint32_t* hr = ensure_pinned<uint32_t>(c->h_root[slot], ((uint64_t)n * 16 + 1) * 4);
+    ck(cudaMemcpyAsync(hr, d_root, ((uint64_t)n * 16 + 1) * 4, cudaMemcpyDeviceToHost, st), "root info");
   }
+  ck(cudaEventRecord(c->ev_compute[slot], st), "event");
   if (!device_mode) {
-    PhaseScope ph(c, PH_COPY, st);
-    void* hn = ensure_pinned<void>(c->h_nodes, out_nodes * 24);
-    void* hd = ensure_pinned<void>(c->h_data, out_data * 32);
-    if (out_nodes) ck(cudaMemcpyAsync(hn, c->d_nodes.p, out_nodes * 24, cudaMemcpyDeviceToHost, st), "D2H nodes");
-    if (out_data) ck(cudaMemcpyAsync(hd, c->d_data.p, out_data * 32, cudaMemcpyDeviceToHost, st), "D2H data");
+    // the records travel to the host on the copy stream while the next sub-batch computes
+    PhaseScope ph(c, PH_COPY, c->copy_stream);
+    ck(cudaStreamWaitEvent(c->copy_stream, c->ev_compute[slot], 0), "wait");
+    void* hn = ensure_pinned<void>(c->h_out_nodes[slot], out_nodes * 24);
+    void* hd = ensure_pinned<void>(c->h_out_data[slot], out_data * 32);
+    if (out_nodes)
+      ck(cudaMemcpyAsync(hn, c->d_out_nodes[slot].p, out_nodes * 24, cudaMemcpyDeviceToHost, c->copy_stream), "D2H");
+    if (out_data)
+      ck(cudaMemcpyAsync(hd, c->d_out_data[slot].p, out_data * 32, cudaMemcpyDeviceToHost, c->copy_stream), "D2H");
   }
-  ck(cudaStreamSynchronize(st), "sub-batch");
-  ck(cudaGetLastError(), "sub-batch kernels");
-  if (lvl[(uint64_t)n * 16] != 0)
-    fail(OOC_ERR_DEVICE, "internal layout check failed (flag " + std::to_string(lvl[(uint64_t)n * 16]) + ")");
+  ck(cudaEventRecord(c->ev_done[slot], device_mode ? st : c->copy_stream), "event");
+  out_pending.active = true;
+  out_pending.slot = slot;
+  out_pending.sb = sb;
+  out_pending.pl = pl;
+  out_pending.depth.resize(n);
+  for (uint32_t s = 0; s < n; s++) out_pending.depth[s] = pyr[s].depth;
+}
 
-  // ---- hand the stripes to their meshes, in file order ----
+// Wait for a sub-batch's records and hand its stripes to their meshes, in file order.
+void finish_sub_batch(ooc_ctx* c, std::vector<MeshWork>& meshes, Pending& pd, bool device_mode) {
+  if (!pd.active) return;
+  pd.active = false;
+  const int slot = pd.slot;
+  const uint32_t n = (uint32_t)pd.sb.size();
+  ck(cudaEventSynchronize(c->ev_done[slot]), "sub-batch");
+  ck(cudaGetLastError(), "sub-batch kernels");
+  const uint32_t* hr = static_cast<const uint32_t*>(c->h_root[slot].p);
+  if (hr[(uint64_t)n * 16] != 0)
+    fail(OOC_ERR_DEVICE, "internal layout check failed (flag " + std::to_string(hr[(uint64_t)n * 16]) + ")");
   for (uint32_t s = 0; s < n; s++) {
-    MeshWork& m = meshes[sb[s].mesh];
-    for (; m.next_stripe < sb[s].stripe; m.next_stripe++) m.top.push(m.top.top, TNode());
+    MeshWork& m = meshes[pd.sb[s].mesh];
+    for (; m.next_stripe < pd.sb[s].stripe; m.next_stripe++) m.top.push(m.top.top, TNode());
     m.next_stripe++;
-    const Placed& q = pl[s];
+    const Placed& q = pd.pl[s];
     if (q.node_base != m.top.node_pos || q.data_base != m.top.data_pos)
       fail(OOC_ERR_DEVICE, "internal placement mismatch");
     if (q.empty) {
@@ -761,19 +794,19 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     }
     m.filled += q.n_leaf;
     if (!device_mode) {
-      const char* hn = static_cast<const char*>(c->h_nodes.p) + q.out_node_off * 24;
-      const char* hd = static_cast<const char*>(c->h_data.p) + q.out_data_off * 32;
+      const char* hn = static_cast<const char*>(c->h_out_nodes[slot].p) + q.out_node_off * 24;
+      const char* hd = static_cast<const char*>(c->h_out_data[slot].p) + q.out_data_off * 32;
       if (q.node_span) m.out->span(OOC_STREAM_NODES, hn, q.node_span * 24);
       if (q.data_span) m.out->span(OOC_STREAM_DATA, hd, q.data_span * 32);
     }
     m.top.node_pos += q.node_span;
     m.top.data_pos += q.data_span;
-    const uint32_t* h_root = lvl + (uint64_t)s * 16;
+    const uint32_t* h_root = hr + (uint64_t)s * 16;
     TNode r;
     const uint32_t mask = h_root[0];
     float cf[6];
     std::memcpy(cf, h_root + 1, sizeof(cf));
-    if (pyr[s].depth >= 1) {
+    if (pd.depth[s] >= 1) {
       r.data = m.pl.levels ? q.data_base + q.data_span - 1 : 0;
       r.cb = q.node_base + q.total - 1 - (uint64_t)__builtin_popcount(mask);
       r.off = offsets_from_mask(mask);
@@ -840,11 +873,23 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bo
       float white[6] = {1, 1, 1, 0, 0, 0};
       m.out->data(m.top.data_pos++, 0, white);
     }
+    m.layout.data_pos = m.top.data_pos;
   }
   // stripes with items, in mesh order and Morton order, split by the pyramid budget
   std::vector<StripeRef> sb;
   uint64_t budget_words = 0;
   const uint64_t budget = c->batch_budget_bytes / 4;
+  Pending pend[2];
+  int k = 0;
+  // launch sub-batch k, then finish k-1 while k computes
+  auto flush = [&]() {
+    run_sub_batch(c, st, meshes, sb, device_mode, pend[k & 1], k & 1);
+    if (device_mode) finish_sub_batch(c, meshes, pend[k & 1], true);
+    else finish_sub_batch(c, meshes, pend[(k + 1) & 1], false);
+    k++;
+    sb.clear();
+    budget_words = 0;
+  };
   for (uint32_t mi = 0; mi < meshes.size(); mi++) {
     MeshWork& m = meshes[mi];
     for (uint64_t s = 0; s < m.pl.n_stripes; s++) {
@@ -855,16 +900,14 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bo
       Level tmp[kMaxLevels];
       uint64_t w = 0, b = 0;
       pyramid_levels(m.pl.Ds, tmp, w, b);
-      if (!sb.empty() && budget_words + w > budget) {
-        run_sub_batch(c, st, meshes, sb, device_mode);
-        sb.clear();
-        budget_words = 0;
-      }
+      if (!sb.empty() && budget_words + w > budget) flush();
       sb.push_back(StripeRef{mi, s, part, ibeg, cnt});
       budget_words += w;
     }
   }
-  if (!sb.empty()) run_sub_batch(c, st, meshes, sb, device_mode);
+  if (!sb.empty()) flush();
+  finish_sub_batch(c, meshes, pend[0], device_mode);
+  finish_sub_batch(c, meshes, pend[1], device_mode);
   for (MeshWork& m : meshes) {
     for (; m.next_stripe < m.pl.n_stripes; m.next_stripe++) m.top.push(m.top.top, TNode());
     // finalizeTree: the root is written last (OctreeBuilder.cpp:34-55)
@@ -995,7 +1038,12 @@ int ooc_ctx_create(int32_t device, ooc_ctx** out) {
   c->device = device;
   if (cudaSetDevice(device) != cudaSuccess ||
       cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_compute[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_compute[1], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_done[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_done[1], cudaEventDisableTiming) != cudaSuccess) {
     delete c;
     return OOC_ERR_DEVICE;
   }
@@ -1016,6 +1064,19 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   PinBuf* pins[] = {&c->h_nodes, &c->h_data, &c->h_misc, &c->h_recs, &c->h_tables1, &c->h_tables2};
   for (PinBuf* b : pins)
     if (b->p) cudaFreeHost(b->p);
+  for (int i = 0; i < 2; i++) {
+    if (c->d_out_nodes[i].p) cudaFree(c->d_out_nodes[i].p);
+    if (c->d_out_data[i].p) cudaFree(c->d_out_data[i].p);
+    if (c->h_out_nodes[i].p) cudaFreeHost(c->h_out_nodes[i].p);
+    if (c->h_out_data[i].p) cudaFreeHost(c->h_out_data[i].p);
+    if (c->h_root[i].p) cudaFreeHost(c->h_root[i].p);
+    if (c->ev_compute[i]) cudaEventDestroy(c->ev_compute[i]);
+    if (c->ev_done[i]) cudaEventDestroy(c->ev_done[i]);
+  }
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
   if (c->d_tables1.p) cudaFree(c->d_tables1.p);
   if (c->d_tables2.p) cudaFree(c->d_tables2.p);
   for (DevBuf& b : c->d_mesh_items)
