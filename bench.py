@@ -393,6 +393,101 @@ def run_batch(args, world, rank, local):
     }
 
 
+def serve_stream(srv, pool, rate: float, duration: float, seed: int, drain_s: float) -> dict:
+    """Drive one Poisson arrival stream through a server; latencies from the server's own clock."""
+    import threading
+
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * duration * 1.5) + 16))
+    arrivals = arrivals[arrivals < duration]
+    picks = rng.integers(0, len(pool), size=len(arrivals))
+    results = []
+    submitted = [0]
+    stop = threading.Event()
+
+    def collect():
+        while not stop.is_set() or len(results) < submitted[0]:
+            r = srv.poll(50, copy=False)
+            if r is not None:
+                results.append(r)
+            elif stop.is_set() and time.perf_counter() > t_end:
+                return
+
+    t_end = float("inf")
+    th = threading.Thread(target=collect)
+    th.start()
+    t0 = time.perf_counter()
+    for a, k in zip(arrivals, picks):
+        while True:
+            dt = t0 + a - time.perf_counter()
+            if dt <= 0:
+                break
+            time.sleep(min(dt, 0.0005) if dt > 0.0002 else 0)
+        ptr, n, params, N = pool[k]
+        srv.submit_ptr(ptr, n, params, N)
+        submitted[0] += 1
+    t_end = time.perf_counter() + drain_s
+    stop.set()
+    th.join()
+    lat = np.array([(r["t_done_us"] - r["t_submit_us"]) / 1e3 for r in results])
+    done = np.array([r["t_done_us"] for r in results])
+    sub = np.array([r["t_submit_us"] for r in results])
+    span = (done.max() - sub.min()) / 1e6 if len(results) else float("nan")
+    return {"offered_req_s": rate, "requests": int(submitted[0]), "completed": len(results),
+            "failed": int(sum(r["status"] != 0 for r in results)),
+            "meshes_per_s": len(results) / span if len(results) else 0.0,
+            "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+            "mean_batch": float(np.mean([r["batch_size"] for r in results])) if results else None,
+            "output_gb": float(sum(r["bytes"] for r in results) / 1e9)}
+
+
+def run_serve(args, world, rank, local):
+    """Configuration 5: Poisson request streams through the serving loop (continuous batching,
+    footprint admission) and, on the same streams, through the plain path (one request at a time)."""
+    import torch
+    import ooc_svo_builder_gb300 as ooc
+
+    torch.cuda.set_device(local)
+    meshes = tri.batch_meshes(args.n_meshes, seed=5, gridsizes=(128, 256, 512, 1024, 2048))
+    offs = [0]
+    for t, _, _ in meshes:
+        offs.append(offs[-1] + (t.nbytes + 255) // 256 * 256)
+    pinned = torch.empty(offs[-1], dtype=torch.uint8).pin_memory()
+    host = pinned.numpy()
+    pool = []
+    for i, (t, N, payload) in enumerate(meshes):
+        host[offs[i]:offs[i] + t.nbytes] = t.reshape(-1).view(np.uint8)
+        pool.append((pinned.data_ptr() + offs[i], t.shape[0], ooc.make_params(N, 2048, geometry_only=not payload), N))
+    rates = [float(r) for r in args.rates.split(",")]
+    arms = {"served": dict(engines=args.engines, max_batch=256, memory_budget=120 << 30),
+            "plain": dict(engines=1, max_batch=1, memory_budget=120 << 30)}
+    out = {}
+    for arm, cfg in arms.items():
+        with ooc.Server(local, **cfg) as srv:
+            serve_stream(srv, pool, min(rates), min(2.0, args.duration), seed=99, drain_s=30.0)  # warm-up
+            out[arm] = [serve_stream(srv, pool, r, args.duration, seed=5 + int(r), drain_s=args.drain)
+                        for r in rates]
+    top = out["served"][-1]
+    return {
+        "metric": "served meshes/s", "value": top["meshes_per_s"], "unit": "meshes/s", "n_gpus": world,
+        "steps": top["completed"], "warmup": 1, "ms_per_step": 1e3 / max(top["meshes_per_s"], 1e-9),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "configuration 5: Poisson arrivals at %s req/s, %.0f s each, meshes drawn from a "
+                               "pool of %d configuration-4 meshes with gridsizes 128..2048; 120 GB admission "
+                               "budget; pinned host triangles in, host octree bytes out"
+                               % (args.rates, args.duration, len(pool)),
+                   "name": "serve", "engines": args.engines, "max_batch": 256},
+        "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
+        "rates": out["served"], "plain": out["plain"],
+        "speedup_vs_plain": [s["meshes_per_s"] / max(p["meshes_per_s"], 1e-9)
+                             for s, p in zip(out["served"], out["plain"])],
+        "e2e": {"value": top["meshes_per_s"], "unit": "meshes/s",
+                "h2d_bytes_per_step": int(np.mean([t.nbytes for t, _, _ in meshes])),
+                "d2h_bytes_per_step": int(top["output_gb"] * 1e9 / max(top["completed"], 1))},
+    }
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return None
@@ -421,8 +516,13 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="heightfield1024", choices=sorted(WORKLOADS) + ["batch4096"])
-    ap.add_argument("--n-meshes", type=int, default=4096, help="meshes of the batch4096 workload")
+    ap.add_argument("--workload", default="heightfield1024", choices=sorted(WORKLOADS) + ["batch4096", "serve"])
+    ap.add_argument("--n-meshes", type=int, default=None,
+                    help="meshes of the batch4096 workload (4096) or of the serve pool (512)")
+    ap.add_argument("--rates", default="200,500,1000,2000", help="serve: offered request rates, req/s")
+    ap.add_argument("--duration", type=float, default=5.0, help="serve: seconds of arrivals per rate")
+    ap.add_argument("--drain", type=float, default=60.0, help="serve: seconds to wait for the queue to drain")
+    ap.add_argument("--engines", type=int, default=2, help="serve: engines of the served arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")
@@ -433,7 +533,11 @@ def main():
     if args.impl == "reference":
         line = run_reference(args, world, rank)
     elif args.workload == "batch4096":
+        args.n_meshes = args.n_meshes or 4096
         line = run_batch(args, world, rank, local)
+    elif args.workload == "serve":
+        args.n_meshes = args.n_meshes or 512
+        line = run_serve(args, world, rank, local)
     else:
         line = run_ours(args, world, rank, local)
     if rank == 0 and line is not None:

@@ -43,6 +43,7 @@ extern "C" {
 #define OOC_ERR_IO 4       /* file could not be read or written                  */
 #define OOC_ERR_SINK 5     /* the caller's sink returned non-zero                */
 #define OOC_ERR_LIMIT 6    /* input beyond the fixed limits of ooc_voxelize_occupancy_noalloc */
+#define OOC_ERR_TIMEOUT 7  /* ooc_server_poll: nothing completed within the timeout                */
 
 /* Colour modes of svo_builder's -c flag (main.cpp:23, 154-179). */
 #define OOC_COLOR_MODEL 0
@@ -186,6 +187,49 @@ int ooc_kernel_time(const ooc_ctx* ctx, int32_t index, const char** name, float*
 #define OOC_NOALLOC_MAX_GRIDSIZE 1024
 int ooc_voxelize_occupancy_noalloc(const ooc_build_params* params, const float* tris_device, uint64_t n_tris,
                                    uint32_t* occupancy_device, uint64_t occupancy_words, void* stream);
+
+/* ---- Serving loop (no counterpart in the reference) ----
+ * Requests (meshes) are admitted by their computed HBM footprint -- triangles,
+ * the occupancy pyramids of their stripes, and per-node arrays for an
+ * estimate of their nodes -- against `memory_budget`, and run in continuously
+ * formed batches: each of `engines` contexts (own streams and scratch) takes,
+ * whenever it is free, every queued request that fits (at most max_batch) and
+ * builds them in one ooc_build_batch call.  Each result is byte-identical to
+ * ooc_build on that mesh alone. */
+typedef struct ooc_server ooc_server;
+
+typedef struct {
+  int32_t device;
+  int32_t engines;        /* batches in flight at once, >= 1                       */
+  uint32_t max_batch;     /* requests per batch, >= 1 (1: every request alone)     */
+  uint32_t reserved;      /* must be 0                                             */
+  uint64_t memory_budget; /* bytes of HBM the requests in flight may hold          */
+} ooc_server_config;
+
+typedef struct {
+  uint64_t id;
+  int32_t status;         /* OOC_OK or the build's error code                      */
+  int32_t reserved;
+  const void* nodes;      /* node file bytes (valid until ooc_server_release)      */
+  uint64_t nodes_bytes;
+  const void* data;       /* data file bytes                                       */
+  uint64_t data_bytes;
+  ooc_build_info info;
+  double t_submit_us;     /* times in microseconds since the server started        */
+  double t_start_us;
+  double t_done_us;
+  uint64_t batch_size;    /* requests in the batch this one ran in                 */
+} ooc_result;
+
+int ooc_server_create(const ooc_server_config* cfg, ooc_server** out);
+/* Queue one mesh; its triangles (host memory) must stay valid until its result is polled. */
+int ooc_server_submit(ooc_server* server, const ooc_mesh* mesh, uint64_t* id);
+/* Next completed request (OOC_OK), or OOC_ERR_TIMEOUT after `timeout_ms`. */
+int ooc_server_poll(ooc_server* server, int32_t timeout_ms, ooc_result* out);
+/* Free a polled result's buffers. */
+int ooc_server_release(ooc_server* server, uint64_t id);
+/* Finish queued requests, then stop the engines and free everything. */
+void ooc_server_destroy(ooc_server* server);
 
 /* File front end used by the svo_builder CLIs: reads <base>.tri/.tridata and
  * writes <base><gridsize>_<npartitions>.octree/.octreenodes/.octreedata

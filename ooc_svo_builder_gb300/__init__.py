@@ -20,7 +20,8 @@ LIB_PATH = os.path.join(PKG, "libooc_svo_gpu.so")
 
 OOC_OK = 0
 ERRORS = {1: "OOC_ERR_INVALID", 2: "OOC_ERR_OOM", 3: "OOC_ERR_DEVICE", 4: "OOC_ERR_IO", 5: "OOC_ERR_SINK",
-          6: "OOC_ERR_LIMIT"}
+          6: "OOC_ERR_LIMIT", 7: "OOC_ERR_TIMEOUT"}
+OOC_ERR_TIMEOUT = 7
 NOALLOC_MAX_TRIANGLES = 1048576
 NOALLOC_MAX_GRIDSIZE = 1024
 COLOR_MODES = {"model": 0, "fixed": 1, "linear": 2, "normal": 3}
@@ -30,7 +31,8 @@ PHASES = ("partition", "voxelize", "pyramid", "octree", "copies", "build")
 EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_partitions", "ooc_build",
            "ooc_build_device", "ooc_result_device", "ooc_result_copy", "ooc_set_phase_timing", "ooc_phase_times",
            "ooc_kernel_launches", "ooc_build_files", "ooc_set_kernel_timing", "ooc_kernel_time",
-           "ooc_voxelize_occupancy_noalloc", "ooc_build_batch")
+           "ooc_voxelize_occupancy_noalloc", "ooc_build_batch", "ooc_server_create", "ooc_server_submit",
+           "ooc_server_poll", "ooc_server_release", "ooc_server_destroy")
 
 
 class BuildParams(ctypes.Structure):
@@ -52,6 +54,18 @@ BATCH_SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ct
 
 class Mesh(ctypes.Structure):
     _fields_ = [("tris", ctypes.c_void_p), ("n_tris", ctypes.c_uint64), ("params", BuildParams)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("engines", ctypes.c_int32), ("max_batch", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("memory_budget", ctypes.c_uint64)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("nodes", ctypes.c_void_p), ("nodes_bytes", ctypes.c_uint64), ("data", ctypes.c_void_p),
+                ("data_bytes", ctypes.c_uint64), ("info", BuildInfo), ("t_submit_us", ctypes.c_double),
+                ("t_start_us", ctypes.c_double), ("t_done_us", ctypes.c_double), ("batch_size", ctypes.c_uint64)]
 
 
 class OocError(RuntimeError):
@@ -107,6 +121,16 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_build_batch.argtypes = [ctypes.c_void_p, P(Mesh), ctypes.c_uint64, BATCH_SINK, ctypes.c_void_p,
                                     P(BuildInfo)]
     lib.ooc_build_batch.restype = ctypes.c_int
+    lib.ooc_server_create.argtypes = [P(ServerConfig), P(ctypes.c_void_p)]
+    lib.ooc_server_create.restype = ctypes.c_int
+    lib.ooc_server_submit.argtypes = [ctypes.c_void_p, P(Mesh), P(ctypes.c_uint64)]
+    lib.ooc_server_submit.restype = ctypes.c_int
+    lib.ooc_server_poll.argtypes = [ctypes.c_void_p, ctypes.c_int32, P(Result)]
+    lib.ooc_server_poll.restype = ctypes.c_int
+    lib.ooc_server_release.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+    lib.ooc_server_release.restype = ctypes.c_int
+    lib.ooc_server_destroy.argtypes = [ctypes.c_void_p]
+    lib.ooc_server_destroy.restype = None
     lib.ooc_voxelize_occupancy_noalloc.argtypes = [P(BuildParams), ctypes.c_void_p, ctypes.c_uint64,
                                                    ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
     lib.ooc_voxelize_occupancy_noalloc.restype = ctypes.c_int
@@ -309,3 +333,75 @@ class Builder:
         self._check(self.lib.ooc_build_files(self.h, tri_path.encode(), ctypes.byref(params), out, 4096,
                                              ctypes.byref(info)))
         return out.value.decode(), _info_dict(info)
+
+
+class Server:
+    """The serving loop: submit meshes, poll completed octrees (see ooc_server_* in the C ABI)."""
+
+    def __init__(self, device: int = 0, engines: int = 2, max_batch: int = 256, memory_budget: int = 120 << 30):
+        self.lib = load_library()
+        cfg = ServerConfig(device, engines, max_batch, 0, memory_budget)
+        h = ctypes.c_void_p()
+        rc = self.lib.ooc_server_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != OOC_OK:
+            raise OocError(rc, "ooc_server_create failed")
+        self.h = h
+        self._keep = {}
+
+    def submit(self, tris: np.ndarray, params: BuildParams) -> int:
+        tris = np.ascontiguousarray(tris, dtype=np.float32)
+        width = 9 if params.geometry_only else 21
+        if tris.ndim != 2 or tris.shape[1] != width:
+            raise ValueError("triangles must be [T, %d] float32" % width)
+        m = Mesh()
+        m.tris = tris.ctypes.data
+        m.n_tris = tris.shape[0]
+        m.params = params
+        rid = ctypes.c_uint64()
+        rc = self.lib.ooc_server_submit(self.h, ctypes.byref(m), ctypes.byref(rid))
+        if rc != OOC_OK:
+            raise OocError(rc, "ooc_server_submit failed")
+        self._keep[rid.value] = (tris, int(params.gridsize))
+        return rid.value
+
+    def submit_ptr(self, tris_ptr: int, n_tris: int, params: BuildParams, gridsize: int) -> int:
+        """Queue triangles given by address (e.g. pinned memory kept alive by the caller)."""
+        m = Mesh()
+        m.tris = tris_ptr
+        m.n_tris = n_tris
+        m.params = params
+        rid = ctypes.c_uint64()
+        rc = self.lib.ooc_server_submit(self.h, ctypes.byref(m), ctypes.byref(rid))
+        if rc != OOC_OK:
+            raise OocError(rc, "ooc_server_submit failed")
+        self._keep[rid.value] = (None, gridsize)
+        return rid.value
+
+    def poll(self, timeout_ms: int = 100, copy: bool = True):
+        """Next completed request as a dict (None on timeout); `copy` returns its octree."""
+        r = Result()
+        rc = self.lib.ooc_server_poll(self.h, timeout_ms, ctypes.byref(r))
+        if rc == OOC_ERR_TIMEOUT:
+            return None
+        if rc != OOC_OK:
+            raise OocError(rc, "ooc_server_poll failed")
+        _, gridsize = self._keep.pop(r.id)
+        out = {"id": r.id, "status": r.status, "info": _info_dict(r.info), "t_submit_us": r.t_submit_us,
+               "t_start_us": r.t_start_us, "t_done_us": r.t_done_us, "batch_size": r.batch_size,
+               "bytes": r.nodes_bytes + r.data_bytes}
+        if copy and r.status == OOC_OK:
+            out["tree"] = _octree.from_bytes(gridsize, ctypes.string_at(r.nodes, r.nodes_bytes),
+                                             ctypes.string_at(r.data, r.data_bytes))
+        self.lib.ooc_server_release(self.h, r.id)
+        return out
+
+    def close(self):
+        if self.h:
+            self.lib.ooc_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-Xptxas", "-v"]
 CUDA_SOURCES = ["ooc_kernels.cu", "ooc_api.cu", "ooc_noalloc.cu"]
-CXX_SOURCES = ["ooc_files.cpp"]
+CXX_SOURCES = ["ooc_files.cpp", "ooc_server.cpp"]
 
 
 def _nvcc() -> str:
@@ -83,7 +83,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         for out in ex.map(lambda c: _run(c, log), jobs):
             pass
     if force or jobs or not os.path.exists(LIB):
-        _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"], log)
+        _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lpthread"], log)
     main = os.path.join(CSRC, "svo_builder_main.cpp")
     for name, extra in (("svo_builder", []), ("svo_builder_binary", ["-DOOC_CLI_BINARY"])):
         exe = os.path.join(BIN, name)

@@ -1,0 +1,299 @@
+// Serving loop: requests are admitted by their computed HBM footprint and
+// run in continuously formed batches.
+//
+// Each engine is a library context with its own streams.  An engine that is
+// free takes every queued request that fits the remaining memory budget (up to
+// max_batch) and builds them with one ooc_build_batch call; requests that
+// arrive meanwhile wait for the next free engine.  With two or more engines,
+// one batch's device work overlaps the next batch's, and each batch's copies
+// overlap its own sub-batches' compute.  Results stay in host memory until the
+// caller releases them.  The server uses only the public C ABI.
+#include <algorithm>
+#include <chrono>
+#include <cstdlib>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "ooc_svo_gpu.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+// Growable host buffer.  realloc of a large block remaps its pages instead of
+// copying them, so appending a result piece by piece costs one copy.
+struct Bytes {
+  char* p = nullptr;
+  size_t n = 0, cap = 0;
+  Bytes() = default;
+  Bytes(const Bytes&) = delete;
+  Bytes& operator=(const Bytes&) = delete;
+  ~Bytes() { std::free(p); }
+  bool append(const void* src, size_t k) {
+    if (n + k > cap) {
+      size_t nc = std::max<size_t>(std::max<size_t>(cap + cap / 2, n + k), 1 << 16);
+      char* q = static_cast<char*>(std::realloc(p, nc));
+      if (!q) return false;
+      p = q;
+      cap = nc;
+    }
+    std::memcpy(p + n, src, k);
+    n += k;
+    return true;
+  }
+  void clear() { n = 0; }
+};
+
+struct Request {
+  uint64_t id = 0;
+  ooc_mesh mesh;
+  uint64_t footprint = 0;
+  Bytes nodes, data;
+  ooc_build_info info;
+  int32_t status = OOC_OK;
+  double t_submit = 0, t_start = 0, t_done = 0;
+  uint64_t batch_size = 0;
+};
+
+// The per-mesh checks ooc_build makes on its parameters, so that a request
+// that would fail is refused at submission and never shares a batch.
+bool valid(const ooc_mesh& m) {
+  const ooc_build_params& p = m.params;
+  const uint64_t N = p.gridsize;
+  if (N == 0 || (N & (N - 1)) != 0 || N > 65536) return false;
+  if (p.memory_limit_mb < 1 || (p.geometry_only != 0 && p.geometry_only != 1)) return false;
+  if (p.color_mode < 0 || p.color_mode > 3 || p.reserved != 0) return false;
+  if (m.n_tris >= (1ull << 32) || (m.n_tris && !m.tris)) return false;
+  return ooc_estimate_partitions(N, p.memory_limit_mb) <= (1ull << 21);
+}
+
+// HBM a request may hold while it is in flight: its triangles, the occupancy
+// pyramids of its stripes, and per-node arrays plus output records for an
+// estimate of its nodes (about twice the surface area in voxels, times 1.5
+// for the inner levels).
+uint64_t footprint(const ooc_mesh& m) {
+  const ooc_build_params& p = m.params;
+  const uint64_t N = p.gridsize;
+  const uint64_t stride = p.geometry_only ? 9 : 21;
+  uint64_t bytes = m.n_tris * stride * 4;
+  int D = 0;
+  while ((1ull << D) < N) D++;
+  const uint64_t P = ooc_estimate_partitions(N, p.memory_limit_mb);
+  int kP = 0;
+  while ((1ull << (3 * kP)) < P) kP++;
+  const int Ds = std::min(D - kP, 10);
+  uint64_t words = 0;
+  for (int l = 0; l <= Ds; l++) words += (((1ull << (3 * l)) + 31) / 32 + 7) / 8 * 8;
+  const uint64_t stripes = (N * N * N) >> (3 * Ds);
+  bytes += words * 4 * stripes;
+  const float u = (p.bbox_max[0] - p.bbox_min[0]) / (float)N;
+  double area = 0.0;
+  for (uint64_t t = 0; t < m.n_tris; t++) {
+    const float* v = m.tris + t * stride;
+    const double ax = v[3] - v[0], ay = v[4] - v[1], az = v[5] - v[2];
+    const double bx = v[6] - v[0], by = v[7] - v[1], bz = v[8] - v[2];
+    const double cx = ay * bz - az * by, cy = az * bx - ax * bz, cz = ax * by - ay * bx;
+    area += 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+  }
+  const double voxels = std::min<double>(2.0 * area / (double)u / (double)u + 2.0 * (double)m.n_tris,
+                                         (double)N * (double)N * (double)N);
+  bytes += (uint64_t)(voxels * 1.5 * 120.0);
+  return bytes;
+}
+
+}  // namespace
+
+struct ooc_server {
+  ooc_server_config cfg;
+  std::vector<ooc_ctx*> engines;
+  std::vector<std::thread> threads;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Request*> queue;
+  std::deque<Request*> done;
+  std::unordered_map<uint64_t, Request*> held;  // polled, not yet released
+  uint64_t next_id = 1;
+  uint64_t in_flight = 0;
+  bool stop = false;
+  Clock::time_point t0 = Clock::now();
+
+  double now_us() const { return std::chrono::duration<double, std::micro>(Clock::now() - t0).count(); }
+
+  bool fits(const Request* r) const { return in_flight == 0 || in_flight + r->footprint <= cfg.memory_budget; }
+
+  static int sink(void* user, uint64_t mesh, int32_t kind, const void* bytes, uint64_t n) {
+    std::vector<Request*>& batch = *static_cast<std::vector<Request*>*>(user);
+    Bytes& dst = kind == OOC_STREAM_NODES ? batch[mesh]->nodes : batch[mesh]->data;
+    return dst.append(bytes, n) ? 0 : 1;
+  }
+
+  // One ooc_build_batch call; results land in the requests.
+  static int run(ooc_ctx* ctx, std::vector<Request*>& batch) {
+    std::vector<ooc_mesh> meshes(batch.size());
+    std::vector<ooc_build_info> infos(batch.size());
+    for (size_t i = 0; i < batch.size(); i++) {
+      meshes[i] = batch[i]->mesh;
+      batch[i]->nodes.clear();
+      batch[i]->data.clear();
+    }
+    const int rc = ooc_build_batch(ctx, meshes.data(), meshes.size(), &ooc_server::sink, &batch, infos.data());
+    for (size_t i = 0; i < batch.size(); i++) {
+      batch[i]->status = rc;
+      batch[i]->info = infos[i];
+    }
+    return rc;
+  }
+
+  void engine_loop(ooc_ctx* ctx) {
+    for (;;) {
+      std::vector<Request*> batch;
+      uint64_t taken = 0;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_work.wait(lk, [&] { return stop || (!queue.empty() && fits(queue.front())); });
+        if (stop && queue.empty()) return;
+        while (!queue.empty() && batch.size() < cfg.max_batch && fits(queue.front())) {
+          Request* r = queue.front();
+          queue.pop_front();
+          in_flight += r->footprint;
+          taken += r->footprint;
+          batch.push_back(r);
+        }
+      }
+      if (batch.empty()) {  // shutting down while another engine still holds the budget
+        std::this_thread::sleep_for(std::chrono::microseconds(100));
+        continue;
+      }
+      const double ts = now_us();
+      for (Request* r : batch) {
+        r->t_start = ts;
+        r->batch_size = batch.size();
+      }
+      if (run(ctx, batch) != OOC_OK && batch.size() > 1) {
+        // A failure (out of memory, too many triangle/partition pairs) belongs
+        // to some request of the batch: run each alone so that only it fails.
+        for (Request* r : batch) {
+          std::vector<Request*> one(1, r);
+          run(ctx, one);
+          r->batch_size = 1;
+        }
+      }
+      const double td = now_us();
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        in_flight -= taken;
+        for (Request* r : batch) {
+          r->t_done = td;
+          done.push_back(r);
+        }
+      }
+      cv_done.notify_all();
+      cv_work.notify_all();
+    }
+  }
+};
+
+extern "C" {
+
+int ooc_server_create(const ooc_server_config* cfg, ooc_server** out) {
+  if (!cfg || !out || cfg->engines < 1 || cfg->max_batch < 1 || cfg->memory_budget == 0) return OOC_ERR_INVALID;
+  *out = nullptr;
+  ooc_server* s = new (std::nothrow) ooc_server();
+  if (!s) return OOC_ERR_OOM;
+  s->cfg = *cfg;
+  for (int i = 0; i < cfg->engines; i++) {
+    ooc_ctx* c = nullptr;
+    const int rc = ooc_ctx_create(cfg->device, &c);
+    if (rc != OOC_OK) {
+      for (ooc_ctx* e : s->engines) ooc_ctx_destroy(e);
+      delete s;
+      return rc;
+    }
+    s->engines.push_back(c);
+  }
+  for (ooc_ctx* c : s->engines) s->threads.emplace_back([s, c] { s->engine_loop(c); });
+  *out = s;
+  return OOC_OK;
+}
+
+int ooc_server_submit(ooc_server* s, const ooc_mesh* mesh, uint64_t* id) {
+  if (!s || !mesh || !valid(*mesh)) return OOC_ERR_INVALID;
+  const double t = s->now_us();
+  Request* r = new (std::nothrow) Request();
+  if (!r) return OOC_ERR_OOM;
+  r->mesh = *mesh;
+  r->footprint = footprint(*mesh);
+  r->t_submit = t;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    r->id = s->next_id++;
+    s->queue.push_back(r);
+  }
+  if (id) *id = r->id;
+  s->cv_work.notify_one();
+  return OOC_OK;
+}
+
+int ooc_server_poll(ooc_server* s, int32_t timeout_ms, ooc_result* out) {
+  if (!s || !out) return OOC_ERR_INVALID;
+  Request* r = nullptr;
+  {
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms),
+                             [&] { return !s->done.empty(); }))
+      return OOC_ERR_TIMEOUT;
+    r = s->done.front();
+    s->done.pop_front();
+    s->held[r->id] = r;
+  }
+  std::memset(out, 0, sizeof(*out));
+  out->id = r->id;
+  out->status = r->status;
+  out->nodes = r->nodes.p;
+  out->nodes_bytes = r->nodes.n;
+  out->data = r->data.p;
+  out->data_bytes = r->data.n;
+  out->info = r->info;
+  out->t_submit_us = r->t_submit;
+  out->t_start_us = r->t_start;
+  out->t_done_us = r->t_done;
+  out->batch_size = r->batch_size;
+  return OOC_OK;
+}
+
+int ooc_server_release(ooc_server* s, uint64_t id) {
+  if (!s) return OOC_ERR_INVALID;
+  Request* r = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->held.find(id);
+    if (it == s->held.end()) return OOC_ERR_INVALID;
+    r = it->second;
+    s->held.erase(it);
+  }
+  delete r;
+  return OOC_OK;
+}
+
+void ooc_server_destroy(ooc_server* s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  for (std::thread& t : s->threads) t.join();
+  for (ooc_ctx* c : s->engines) ooc_ctx_destroy(c);
+  for (Request* r : s->queue) delete r;
+  for (Request* r : s->done) delete r;
+  for (auto& kv : s->held) delete kv.second;
+  delete s;
+}
+
+}  // extern "C"

@@ -1,0 +1,31 @@
+"""Serving loop: argument checks that need no GPU (nothing here creates an engine)."""
+import ctypes
+
+import ooc_svo_builder_gb300 as ooc
+
+
+def test_server_create_rejects_bad_config():
+    lib = ooc.load_library()
+    h = ctypes.c_void_p()
+    for cfg in (ooc.ServerConfig(0, 0, 8, 0, 1 << 30),   # no engines
+                ooc.ServerConfig(0, 1, 0, 0, 1 << 30),   # batches of zero requests
+                ooc.ServerConfig(0, 1, 8, 0, 0)):        # no memory budget
+        assert lib.ooc_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+    assert lib.ooc_server_create(None, ctypes.byref(h)) == 1
+
+
+def test_server_calls_reject_null():
+    lib = ooc.load_library()
+    r = ooc.Result()
+    m = ooc.Mesh()
+    rid = ctypes.c_uint64()
+    assert lib.ooc_server_submit(None, ctypes.byref(m), ctypes.byref(rid)) == 1
+    assert lib.ooc_server_poll(None, 0, ctypes.byref(r)) == 1
+    assert lib.ooc_server_release(None, 1) == 1
+    lib.ooc_server_destroy(None)
+
+
+def test_result_struct_layout():
+    # ooc_result: id, status, reserved, nodes, nodes_bytes, data, data_bytes, info (6 x u64), 3 doubles, batch_size
+    assert ctypes.sizeof(ooc.Result) == 8 + 4 + 4 + 8 * 4 + 48 + 24 + 8
+    assert ctypes.sizeof(ooc.ServerConfig) == 24
