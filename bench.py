@@ -358,7 +358,7 @@ def run_batch(args, world, rank, local):
     got = {i: {0: [], 1: []} for i in sample}
 
     def collect(user, mesh, kind, ptr, nb):
-        if mesh in got:
+        if mesh in got and kind < 2:
             got[mesh][kind].append(ctypes.string_at(ptr, nb))
         return 0
 
@@ -462,12 +462,22 @@ def run_serve(args, world, rank, local):
     rates = [float(r) for r in args.rates.split(",")]
     arms = {"served": dict(engines=args.engines, max_batch=256, memory_budget=120 << 30),
             "plain": dict(engines=1, max_batch=1, memory_budget=120 << 30)}
+    # warm-up set: the requests with the largest grids, then a spread of the rest
+    order = sorted(range(len(pool)), key=lambda i: -pool[i][3] * pool[i][1])
+    warm = order[:16] + order[16::max(1, len(pool) // 64)]
     out = {}
     for arm, cfg in arms.items():
-        with ooc.Server(local, **cfg) as srv:
-            serve_stream(srv, pool, min(rates), min(2.0, args.duration), seed=99, drain_s=30.0)  # warm-up
-            out[arm] = [serve_stream(srv, pool, r, args.duration, seed=5 + int(r), drain_s=args.drain)
-                        for r in rates]
+        out[arm] = []
+        for r in rates:
+            # a fresh server per rate: a backlog left by an overloaded rate does not carry over
+            with ooc.Server(local, **cfg) as srv:
+                for i in warm:
+                    srv.submit_ptr(*pool[i])
+                for _ in warm:
+                    while srv.poll(1000, copy=False) is None:
+                        pass
+                out[arm].append(serve_stream(srv, pool, r, args.duration, seed=5 + int(r), drain_s=args.drain))
+            print("serve %s %.0f req/s: %s" % (arm, r, json.dumps(out[arm][-1])), file=sys.stderr, flush=True)
     top = out["served"][-1]
     return {
         "metric": "served meshes/s", "value": top["meshes_per_s"], "unit": "meshes/s", "n_gpus": world,

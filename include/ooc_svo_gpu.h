@@ -54,6 +54,7 @@ extern "C" {
 /* Which file a sink call carries. */
 #define OOC_STREAM_NODES 0
 #define OOC_STREAM_DATA 1
+#define OOC_STREAM_END 2   /* ooc_batch_sink_fn only: the mesh is complete (bytes NULL, nbytes 0) */
 
 typedef struct ooc_ctx ooc_ctx;
 
@@ -109,7 +110,10 @@ typedef struct {
 } ooc_mesh;
 
 /* Like ooc_sink_fn, with the index of the mesh whose file the bytes belong to.
- * Each mesh's files arrive in file order; meshes may interleave. */
+ * Each mesh's files arrive in file order; meshes may interleave.  Meshes
+ * complete in index order, each as soon as its last stripe is built: after a
+ * mesh's last piece the sink is called once with kind OOC_STREAM_END (bytes
+ * NULL, nbytes 0), and that mesh's ooc_build_info is final at that moment. */
 typedef int (*ooc_batch_sink_fn)(void* user, uint64_t mesh, int32_t kind, const void* bytes, uint64_t nbytes);
 
 /* Many meshes with their own gridsize, mode and flags in one call: every stripe
@@ -228,7 +232,8 @@ int ooc_server_submit(ooc_server* server, const ooc_mesh* mesh, uint64_t* id);
 int ooc_server_poll(ooc_server* server, int32_t timeout_ms, ooc_result* out);
 /* Free a polled result's buffers. */
 int ooc_server_release(ooc_server* server, uint64_t id);
-/* Finish queued requests, then stop the engines and free everything. */
+/* Drop the requests not yet started, let running batches finish, then stop
+ * the engines and free everything (results not yet released included). */
 void ooc_server_destroy(ooc_server* server);
 
 /* File front end used by the svo_builder CLIs: reads <base>.tri/.tridata and

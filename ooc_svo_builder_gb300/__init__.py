@@ -22,6 +22,7 @@ OOC_OK = 0
 ERRORS = {1: "OOC_ERR_INVALID", 2: "OOC_ERR_OOM", 3: "OOC_ERR_DEVICE", 4: "OOC_ERR_IO", 5: "OOC_ERR_SINK",
           6: "OOC_ERR_LIMIT", 7: "OOC_ERR_TIMEOUT"}
 OOC_ERR_TIMEOUT = 7
+OOC_STREAM_NODES, OOC_STREAM_DATA, OOC_STREAM_END = 0, 1, 2
 NOALLOC_MAX_TRIANGLES = 1048576
 NOALLOC_MAX_GRIDSIZE = 1024
 COLOR_MODES = {"model": 0, "fixed": 1, "linear": 2, "normal": 3}
@@ -284,13 +285,20 @@ class Builder:
             arr[i].params = p
         parts = [{0: [], 1: []} for _ in meshes]
 
+        ends = []
+
         def _collect(user, mesh, kind, ptr, n):
-            parts[mesh][kind].append(ctypes.string_at(ptr, n))
+            if kind == OOC_STREAM_END:
+                ends.append(mesh)
+            else:
+                parts[mesh][kind].append(ctypes.string_at(ptr, n))
             return 0
 
         cb = BATCH_SINK(_collect)
         infos = (BuildInfo * max(1, len(meshes)))()
         self._check(self.lib.ooc_build_batch(self.h, arr, len(meshes), cb, None, infos))
+        if ends != list(range(len(meshes))):
+            raise OocError(3, "meshes did not complete once each, in order: %r" % ends[:16])
         return [BuildResult(_octree.from_bytes(int(params_list[i].gridsize), b"".join(parts[i][0]),
                                                b"".join(parts[i][1])), _info_dict(infos[i]))
                 for i in range(len(meshes))]

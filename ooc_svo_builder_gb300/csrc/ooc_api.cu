@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -97,6 +98,23 @@ T* ensure_pinned(PinBuf& b, size_t bytes) {
   return static_cast<T*>(b.p);
 }
 
+// Bounded pinned staging for the records a sub-batch copies back: its device
+// bytes travel through kRingK chunks of kRingChunk bytes on the copy stream,
+// and a chunk is refilled as soon as the host has handed it to the sink.  The
+// pinned memory a context holds is therefore fixed, whatever a batch emits.
+constexpr int kRingK = 4;
+constexpr uint64_t kRingChunk = 32ull << 20;
+
+struct D2HRing {
+  PinBuf buf;
+  cudaEvent_t ev[kRingK] = {};
+  const char* src = nullptr;
+  uint64_t len = 0, n_chunks = 0;
+  uint64_t issued = 0;    // chunks whose copy has been queued
+  uint64_t released = 0;  // chunks handed to the sink and free again
+  size_t t_begin = 0;     // timing event before the first chunk
+};
+
 constexpr int kPhases = 6;
 enum Phase { PH_BIN = 0, PH_VOX = 1, PH_PYR = 2, PH_TREE = 3, PH_COPY = 4, PH_ALL = 5 };
 
@@ -116,8 +134,9 @@ struct ooc_ctx {
   PinBuf h_nodes, h_data, h_misc, h_recs, h_tables1, h_tables2;
   // double-buffered outputs of pipelined sub-batches
   DevBuf d_out_nodes[2], d_out_data[2];
-  PinBuf h_out_nodes[2], h_out_data[2], h_root[2];
-  cudaEvent_t ev_compute[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr};
+  PinBuf h_root[2];
+  D2HRing ring[2][2];  // [slot][OOC_STREAM_NODES / OOC_STREAM_DATA]
+  cudaEvent_t ev_compute[2] = {nullptr, nullptr};
   cudaStream_t copy_stream = nullptr;
   DevBuf d_tables1, d_tables2;
   std::vector<DevBuf> d_mesh_items;
@@ -168,6 +187,54 @@ struct PhaseScope {
     }
   }
 };
+
+void ring_issue(ooc_ctx* c, D2HRing& r) {
+  const uint64_t j = r.issued++;
+  const uint64_t off = j * kRingChunk;
+  const uint64_t n = std::min(kRingChunk, r.len - off);
+  char* dst = static_cast<char*>(r.buf.p) + (j % kRingK) * kRingChunk;
+  ck(cudaMemcpyAsync(dst, r.src + off, n, cudaMemcpyDeviceToHost, c->copy_stream), "D2H");
+  ck(cudaEventRecord(r.ev[j % kRingK], c->copy_stream), "event");
+  if (c->timing && r.issued == r.n_chunks) {
+    const size_t e = c->ev_used;
+    ck(cudaEventRecord(next_event(c), c->copy_stream), "cudaEventRecord");
+    c->marks.push_back({(size_t)PH_COPY, r.t_begin, e});
+  }
+}
+
+// Queue the first chunks of `len` device bytes (the copy stream already waits for their producer).
+void ring_start(ooc_ctx* c, D2HRing& r, const void* src, uint64_t len) {
+  r.src = static_cast<const char*>(src);
+  r.len = len;
+  r.n_chunks = (len + kRingChunk - 1) / kRingChunk;
+  r.issued = r.released = 0;
+  if (!len) return;
+  ensure_pinned<char>(r.buf, std::min<uint64_t>(len, kRingK * kRingChunk));
+  for (int k = 0; k < kRingK; k++)
+    if (!r.ev[k]) ck(cudaEventCreateWithFlags(&r.ev[k], cudaEventDisableTiming), "cudaEventCreate");
+  if (c->timing) {
+    r.t_begin = c->ev_used;
+    ck(cudaEventRecord(next_event(c), c->copy_stream), "cudaEventRecord");
+  }
+  while (r.issued < r.n_chunks && r.issued < (uint64_t)kRingK) ring_issue(c, r);
+}
+
+// Hand bytes [a, b) to `out` in order; calls over one sub-batch cover its bytes in increasing order.
+template <typename F>
+void ring_take(ooc_ctx* c, D2HRing& r, uint64_t a, uint64_t b, F&& out) {
+  while (a < b) {
+    const uint64_t j = a / kRingChunk;
+    if (j >= r.issued || j < r.released) fail(OOC_ERR_DEVICE, "internal copy-back order");
+    ck(cudaEventSynchronize(r.ev[j % kRingK]), "D2H");
+    const uint64_t end = std::min(b, (j + 1) * kRingChunk);
+    out(static_cast<const char*>(r.buf.p) + (j % kRingK) * kRingChunk + (a - j * kRingChunk), end - a);
+    a = end;
+    if (a == (j + 1) * kRingChunk || a == r.len) {
+      r.released = j + 1;
+      if (r.issued < r.n_chunks) ring_issue(c, r);
+    }
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Node records and the host-side grouping above the stripes.
@@ -365,6 +432,7 @@ struct MeshWork {
   uint64_t layout_next = 0;
   uint64_t filled = 0;
   uint64_t n_items = 0;
+  int64_t last_stripe = -1;  // last stripe with items (-1: none)
   MeshWork(const Plan& p, Emitter* o)
       : pl(p), out(o), top(p.Ls, p.levels != 0, o), layout(p.Ls, p.levels != 0, nullptr) {
     dry.dry = true;
@@ -373,7 +441,7 @@ struct MeshWork {
   MeshWork(MeshWork&& o) noexcept
       : prm(o.prm), pl(o.pl), d_tris(o.d_tris), n_tris(o.n_tris), part_off(std::move(o.part_off)), items(o.items),
         out(o.out), top(o.top), next_stripe(o.next_stripe), dry(o.dry), layout(o.layout),
-        layout_next(o.layout_next), filled(o.filled), n_items(o.n_items) {}
+        layout_next(o.layout_next), filled(o.filled), n_items(o.n_items), last_stripe(o.last_stripe) {}
 };
 
 struct StripeRef {
@@ -752,16 +820,10 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   ck(cudaEventRecord(c->ev_compute[slot], st), "event");
   if (!device_mode) {
     // the records travel to the host on the copy stream while the next sub-batch computes
-    PhaseScope ph(c, PH_COPY, c->copy_stream);
     ck(cudaStreamWaitEvent(c->copy_stream, c->ev_compute[slot], 0), "wait");
-    void* hn = ensure_pinned<void>(c->h_out_nodes[slot], out_nodes * 24);
-    void* hd = ensure_pinned<void>(c->h_out_data[slot], out_data * 32);
-    if (out_nodes)
-      ck(cudaMemcpyAsync(hn, c->d_out_nodes[slot].p, out_nodes * 24, cudaMemcpyDeviceToHost, c->copy_stream), "D2H");
-    if (out_data)
-      ck(cudaMemcpyAsync(hd, c->d_out_data[slot].p, out_data * 32, cudaMemcpyDeviceToHost, c->copy_stream), "D2H");
+    ring_start(c, c->ring[slot][OOC_STREAM_NODES], c->d_out_nodes[slot].p, out_nodes * 24);
+    ring_start(c, c->ring[slot][OOC_STREAM_DATA], c->d_out_data[slot].p, out_data * 32);
   }
-  ck(cudaEventRecord(c->ev_done[slot], device_mode ? st : c->copy_stream), "event");
   out_pending.active = true;
   out_pending.slot = slot;
   out_pending.sb = sb;
@@ -776,7 +838,7 @@ void finish_sub_batch(ooc_ctx* c, std::vector<MeshWork>& meshes, Pending& pd, bo
   pd.active = false;
   const int slot = pd.slot;
   const uint32_t n = (uint32_t)pd.sb.size();
-  ck(cudaEventSynchronize(c->ev_done[slot]), "sub-batch");
+  ck(cudaEventSynchronize(c->ev_compute[slot]), "sub-batch");
   ck(cudaGetLastError(), "sub-batch kernels");
   const uint32_t* hr = static_cast<const uint32_t*>(c->h_root[slot].p);
   if (hr[(uint64_t)n * 16] != 0)
@@ -794,10 +856,10 @@ void finish_sub_batch(ooc_ctx* c, std::vector<MeshWork>& meshes, Pending& pd, bo
     }
     m.filled += q.n_leaf;
     if (!device_mode) {
-      const char* hn = static_cast<const char*>(c->h_out_nodes[slot].p) + q.out_node_off * 24;
-      const char* hd = static_cast<const char*>(c->h_out_data[slot].p) + q.out_data_off * 32;
-      if (q.node_span) m.out->span(OOC_STREAM_NODES, hn, q.node_span * 24);
-      if (q.data_span) m.out->span(OOC_STREAM_DATA, hd, q.data_span * 32);
+      ring_take(c, c->ring[slot][OOC_STREAM_NODES], q.out_node_off * 24, (q.out_node_off + q.node_span) * 24,
+                [&](const void* p, uint64_t n) { m.out->span(OOC_STREAM_NODES, p, n); });
+      ring_take(c, c->ring[slot][OOC_STREAM_DATA], q.out_data_off * 32, (q.out_data_off + q.data_span) * 32,
+                [&](const void* p, uint64_t n) { m.out->span(OOC_STREAM_DATA, p, n); });
     }
     m.top.node_pos += q.node_span;
     m.top.data_pos += q.data_span;
@@ -859,8 +921,19 @@ void bin_mesh(ooc_ctx* c, cudaStream_t st, MeshWork& m, DevBuf& items_buf) {
   m.items = items;
 }
 
-// Whole path for a list of meshes (triangles already on the device).
-void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bool device_mode) {
+// Last records of a mesh whose stripes are all done: empty stripes after the
+// last one with items, then the root, written last (finalizeTree,
+// OctreeBuilder.cpp:34-55).
+void finalize_mesh(MeshWork& m) {
+  for (; m.next_stripe < m.pl.n_stripes; m.next_stripe++) m.top.push(m.top.top, TNode());
+  m.out->node(m.top.node_pos++, m.top.buf[0][0]);
+}
+
+// Whole path for a list of meshes (triangles already on the device).  Meshes
+// complete in order, each as soon as the sub-batch holding its last stripe is
+// finished; `on_done(i)` runs right after mesh i's last record.
+void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bool device_mode,
+                  const std::function<void(size_t)>& on_done = nullptr) {
   if (c->d_mesh_items.size() < meshes.size()) c->d_mesh_items.resize(meshes.size());
   for (size_t i = 0; i < meshes.size(); i++) {
     MeshWork& m = meshes[i];
@@ -879,6 +952,22 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bo
   std::vector<StripeRef> sb;
   uint64_t budget_words = 0;
   const uint64_t budget = c->batch_budget_bytes / 4;
+  auto items_of = [&](const MeshWork& m, uint64_t s) -> uint64_t {
+    const uint64_t part = s / m.pl.stripes_per_part;
+    return m.pl.P > 1 ? (uint64_t)m.part_off[part + 1] - m.part_off[part] : m.n_tris;
+  };
+  for (MeshWork& m : meshes)
+    for (int64_t s = (int64_t)m.pl.n_stripes - 1; s >= 0 && m.last_stripe < 0; s--)
+      if (items_of(m, (uint64_t)s)) m.last_stripe = s;
+  size_t n_done = 0;
+  auto complete = [&]() {
+    while (n_done < meshes.size() && (int64_t)meshes[n_done].next_stripe > meshes[n_done].last_stripe) {
+      finalize_mesh(meshes[n_done]);
+      if (on_done) on_done(n_done);
+      n_done++;
+    }
+  };
+  complete();
   Pending pend[2];
   int k = 0;
   // launch sub-batch k, then finish k-1 while k computes
@@ -886,6 +975,7 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bo
     run_sub_batch(c, st, meshes, sb, device_mode, pend[k & 1], k & 1);
     if (device_mode) finish_sub_batch(c, meshes, pend[k & 1], true);
     else finish_sub_batch(c, meshes, pend[(k + 1) & 1], false);
+    complete();
     k++;
     sb.clear();
     budget_words = 0;
@@ -895,7 +985,7 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bo
     for (uint64_t s = 0; s < m.pl.n_stripes; s++) {
       const uint64_t part = s / m.pl.stripes_per_part;
       const uint64_t ibeg = m.pl.P > 1 ? m.part_off[part] : 0;
-      const uint64_t cnt = m.pl.P > 1 ? (uint64_t)m.part_off[part + 1] - m.part_off[part] : m.n_tris;
+      const uint64_t cnt = items_of(m, s);
       if (cnt == 0) continue;  // main.cpp:330: partitions without triangles are skipped
       Level tmp[kMaxLevels];
       uint64_t w = 0, b = 0;
@@ -908,11 +998,8 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bo
   if (!sb.empty()) flush();
   finish_sub_batch(c, meshes, pend[0], device_mode);
   finish_sub_batch(c, meshes, pend[1], device_mode);
-  for (MeshWork& m : meshes) {
-    for (; m.next_stripe < m.pl.n_stripes; m.next_stripe++) m.top.push(m.top.top, TNode());
-    // finalizeTree: the root is written last (OctreeBuilder.cpp:34-55)
-    m.out->node(m.top.node_pos++, m.top.buf[0][0]);
-  }
+  complete();
+  if (n_done != meshes.size()) fail(OOC_ERR_DEVICE, "internal: mesh left unfinished");
 }
 
 void fill_info(const MeshWork& m, ooc_build_info* info) {
@@ -986,6 +1073,8 @@ void kernel_end(void* user, const char* name, cudaStream_t st) {
 
 void begin_build(ooc_ctx* c) {
   ck(cudaSetDevice(c->device), "cudaSetDevice");
+  // a build that failed part-way may have left copies queued into the staging buffers
+  ck(cudaStreamSynchronize(c->copy_stream), "cudaStreamSynchronize");
   c->err.clear();
   c->marks.clear();
   c->kmarks.clear();
@@ -1041,9 +1130,7 @@ int ooc_ctx_create(int32_t device, ooc_ctx** out) {
       cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_compute[0], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_compute[1], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_done[0], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_done[1], cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&c->ev_compute[1], cudaEventDisableTiming) != cudaSuccess) {
     delete c;
     return OOC_ERR_DEVICE;
   }
@@ -1055,6 +1142,7 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->own_stream) cudaStreamSynchronize(c->own_stream);
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   DevBuf* bufs[] = {&c->d_tris, &c->d_items, &c->d_hist, &c->d_axis, &c->d_bits, &c->d_scan, &c->d_scanpart,
                     &c->d_keys, &c->d_size, &c->d_dsize, &c->d_start, &c->d_dstart, &c->d_cache, &c->d_winners,
                     &c->d_taskoff, &c->d_taskpart, &c->d_counter, &c->d_nodes, &c->d_data, &c->d_recs,
@@ -1067,16 +1155,15 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   for (int i = 0; i < 2; i++) {
     if (c->d_out_nodes[i].p) cudaFree(c->d_out_nodes[i].p);
     if (c->d_out_data[i].p) cudaFree(c->d_out_data[i].p);
-    if (c->h_out_nodes[i].p) cudaFreeHost(c->h_out_nodes[i].p);
-    if (c->h_out_data[i].p) cudaFreeHost(c->h_out_data[i].p);
+    for (D2HRing& r : c->ring[i]) {
+      if (r.buf.p) cudaFreeHost(r.buf.p);
+      for (cudaEvent_t e : r.ev)
+        if (e) cudaEventDestroy(e);
+    }
     if (c->h_root[i].p) cudaFreeHost(c->h_root[i].p);
     if (c->ev_compute[i]) cudaEventDestroy(c->ev_compute[i]);
-    if (c->ev_done[i]) cudaEventDestroy(c->ev_done[i]);
   }
-  if (c->copy_stream) {
-    cudaStreamSynchronize(c->copy_stream);
-    cudaStreamDestroy(c->copy_stream);
-  }
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->d_tables1.p) cudaFree(c->d_tables1.p);
   if (c->d_tables2.p) cudaFree(c->d_tables2.p);
   for (DevBuf& b : c->d_mesh_items)
@@ -1107,7 +1194,7 @@ struct SingleSink {
 };
 int single_sink(void* user, uint64_t, int32_t kind, const void* bytes, uint64_t n) {
   SingleSink* s = static_cast<SingleSink*>(user);
-  return s->sink(s->user, kind, bytes, n);
+  return kind == OOC_STREAM_END ? 0 : s->sink(s->user, kind, bytes, n);
 }
 }  // namespace
 
@@ -1167,11 +1254,12 @@ int ooc_build_batch(ooc_ctx* c, const ooc_mesh* meshes_in, uint64_t n_meshes, oo
           if (bytes) ck(cudaMemcpyAsync(d_all + off[i], meshes_in[i].tris, bytes, cudaMemcpyHostToDevice, st), "H2D");
         }
       }
-      build_meshes(c, st, meshes, false);
+      build_meshes(c, st, meshes, false, [&](size_t i) {
+        if (infos) fill_info(meshes[i], &infos[i]);
+        if (sink(user, i, OOC_STREAM_END, nullptr, 0) != 0) fail(OOC_ERR_SINK, "sink returned an error");
+      });
     }
     ck(cudaStreamSynchronize(st), "build");
-    if (infos)
-      for (uint64_t i = 0; i < n_meshes; i++) fill_info(meshes[i], &infos[i]);
     finish_timing(c);
   });
 }

@@ -127,27 +127,52 @@ struct ooc_server {
 
   bool fits(const Request* r) const { return in_flight == 0 || in_flight + r->footprint <= cfg.memory_budget; }
 
+  // A request is complete (and can be polled, then released by the caller)
+  // as soon as its mesh is; the engine does not touch it afterwards.
+  void publish(Request* r, int32_t status) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      r->status = status;
+      r->t_done = now_us();
+      done.push_back(r);
+    }
+    cv_done.notify_all();
+  }
+
+  struct Call {
+    ooc_server* s;
+    std::vector<Request*> reqs;
+    std::vector<ooc_build_info> infos;
+    std::vector<char>* published;  // by index into the engine's batch
+    std::vector<size_t> index;
+  };
+
   static int sink(void* user, uint64_t mesh, int32_t kind, const void* bytes, uint64_t n) {
-    std::vector<Request*>& batch = *static_cast<std::vector<Request*>*>(user);
-    Bytes& dst = kind == OOC_STREAM_NODES ? batch[mesh]->nodes : batch[mesh]->data;
+    Call& call = *static_cast<Call*>(user);
+    Request* r = call.reqs[mesh];
+    if (kind == OOC_STREAM_END) {
+      r->info = call.infos[mesh];
+      (*call.published)[call.index[mesh]] = 1;
+      call.s->publish(r, OOC_OK);
+      return 0;
+    }
+    Bytes& dst = kind == OOC_STREAM_NODES ? r->nodes : r->data;
     return dst.append(bytes, n) ? 0 : 1;
   }
 
-  // One ooc_build_batch call; results land in the requests.
-  static int run(ooc_ctx* ctx, std::vector<Request*>& batch) {
-    std::vector<ooc_mesh> meshes(batch.size());
-    std::vector<ooc_build_info> infos(batch.size());
-    for (size_t i = 0; i < batch.size(); i++) {
-      meshes[i] = batch[i]->mesh;
-      batch[i]->nodes.clear();
-      batch[i]->data.clear();
+  // One ooc_build_batch call over batch[index...]; each request is published when its mesh completes.
+  int run(ooc_ctx* ctx, const std::vector<Request*>& batch, const std::vector<size_t>& index,
+          std::vector<char>& published) {
+    Call call{this, {}, std::vector<ooc_build_info>(index.size()), &published, index};
+    std::vector<ooc_mesh> meshes(index.size());
+    for (size_t i = 0; i < index.size(); i++) {
+      Request* r = batch[index[i]];
+      call.reqs.push_back(r);
+      meshes[i] = r->mesh;
+      r->nodes.clear();
+      r->data.clear();
     }
-    const int rc = ooc_build_batch(ctx, meshes.data(), meshes.size(), &ooc_server::sink, &batch, infos.data());
-    for (size_t i = 0; i < batch.size(); i++) {
-      batch[i]->status = rc;
-      batch[i]->info = infos[i];
-    }
-    return rc;
+    return ooc_build_batch(ctx, meshes.data(), meshes.size(), &ooc_server::sink, &call, call.infos.data());
   }
 
   void engine_loop(ooc_ctx* ctx) {
@@ -175,25 +200,28 @@ struct ooc_server {
         r->t_start = ts;
         r->batch_size = batch.size();
       }
-      if (run(ctx, batch) != OOC_OK && batch.size() > 1) {
+      std::vector<char> published(batch.size(), 0);
+      std::vector<size_t> all(batch.size());
+      for (size_t i = 0; i < batch.size(); i++) all[i] = i;
+      const int rc = run(ctx, batch, all, published);
+      if (rc != OOC_OK) {
         // A failure (out of memory, too many triangle/partition pairs) belongs
-        // to some request of the batch: run each alone so that only it fails.
-        for (Request* r : batch) {
-          std::vector<Request*> one(1, r);
-          run(ctx, one);
-          r->batch_size = 1;
+        // to one request: the ones not yet complete run again alone, so that
+        // only the failing one reports it.
+        for (size_t i = 0; i < batch.size(); i++) {
+          if (published[i]) continue;
+          int rc1 = rc;
+          if (batch.size() > 1) {
+            batch[i]->batch_size = 1;
+            rc1 = run(ctx, batch, std::vector<size_t>(1, i), published);
+          }
+          if (!published[i]) publish(batch[i], rc1 != OOC_OK ? rc1 : OOC_ERR_DEVICE);
         }
       }
-      const double td = now_us();
       {
         std::lock_guard<std::mutex> lk(mu);
         in_flight -= taken;
-        for (Request* r : batch) {
-          r->t_done = td;
-          done.push_back(r);
-        }
       }
-      cv_done.notify_all();
       cv_work.notify_all();
     }
   }
@@ -286,11 +314,12 @@ void ooc_server_destroy(ooc_server* s) {
   {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop = true;
+    for (Request* r : s->queue) delete r;  // never started
+    s->queue.clear();
   }
   s->cv_work.notify_all();
   for (std::thread& t : s->threads) t.join();
   for (ooc_ctx* c : s->engines) ooc_ctx_destroy(c);
-  for (Request* r : s->queue) delete r;
   for (Request* r : s->done) delete r;
   for (auto& kv : s->held) delete kv.second;
   delete s;
