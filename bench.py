@@ -306,8 +306,9 @@ def run_ours(args, world, rank, local):
 
 
 def run_batch(args, world, rank, local):
-    """Configuration 4: the batched form against the plain per-mesh path, both through the C ABI
-    from pinned host triangles to host octree bytes."""
+    """Configuration 4: the batched form against the plain per-mesh path, through the C ABI from pinned
+    host triangles, with octrees delivered to host memory (ooc_build_batch vs ooc_build per mesh) and
+    kept resident in HBM (ooc_build_batch_device over all meshes vs one mesh per call)."""
     import ctypes
     import torch
     import ooc_svo_builder_gb300 as ooc
@@ -335,25 +336,48 @@ def run_batch(args, world, rank, local):
     cb1 = ooc.SINK(lambda user, kind, ptr, nb: 0)
     b = ooc.Builder(local)
 
-    for _ in range(max(1, args.warmup)):
-        b.build_batch_ptrs(arr, n, cb, infos)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        b.build_batch_ptrs(arr, n, cb, infos)
-    t_batch = (time.perf_counter() - t0) / args.steps
+    def timed(fn, warm, reps):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        return (time.perf_counter() - t0) / reps
+
+    # host output
+    t_batch = timed(lambda: b.build_batch_ptrs(arr, n, cb, infos), max(1, args.warmup), args.steps)
     launches = b.kernel_launches()
     n_nodes = sum(int(infos[i].n_nodes) for i in range(n))
+    out_bytes = sum(int(infos[i].n_nodes) * 24 + int(infos[i].n_data) * 32 for i in range(n))
 
-    # plain path: one ooc_build per mesh
+    def plain_host():
+        for i in range(n):
+            b.build_ptr(arr[i].tris, arr[i].n_tris, params[i], cb1)
     for i in range(min(n, 64)):
         b.build_ptr(arr[i].tris, arr[i].n_tris, params[i], cb1)
-    t0 = time.perf_counter()
-    for i in range(n):
-        b.build_ptr(arr[i].tris, arr[i].n_tris, params[i], cb1)
-    t_plain = time.perf_counter() - t0
+    t_plain = timed(plain_host, 0, 1)
 
-    # parity sample: the batch's bytes equal the plain path's for every 64th mesh
+    # device-resident output into one HBM arena
+    arena_buf = torch.empty(out_bytes + 512 * n + (64 << 20), dtype=torch.uint8, device="cuda")
+    arena = ooc.DeviceArena(arena_buf.data_ptr(), arena_buf.numel(), 0)
+    dinfos = (ooc.BuildInfo * n)()
+
+    def batch_dev():
+        arena.used = 0
+        b.build_batch_device_ptrs(arr, n, arena, dinfos)
+    t_batch_dev = timed(batch_dev, max(1, args.warmup), args.steps)
+    launches_dev = b.kernel_launches()
+    one = (ooc.Mesh * 1)()
+
+    def plain_dev():
+        for i in range(n):
+            one[0] = arr[i]
+            arena.used = 0
+            b.build_batch_device_ptrs(one, 1, arena, dinfos)
+    t_plain_dev = timed(plain_dev, 0, 1)
+
+    # parity sample: for every 64th mesh, the batch's host bytes and its arena bytes equal ooc_build's
     sample = list(range(0, n, 64))
     got = {i: {0: [], 1: []} for i in sample}
 
@@ -363,7 +387,9 @@ def run_batch(args, world, rank, local):
         return 0
 
     b.build_batch_ptrs(arr, n, ooc.BATCH_SINK(collect), infos)
-    identical = True
+    batch_dev()
+    layout, _ = ooc.arena_layout(dinfos, n)
+    identical = dev_identical = True
     for i in sample:
         want = {0: [], 1: []}
 
@@ -372,24 +398,33 @@ def run_batch(args, world, rank, local):
             return 0
 
         b.build_ptr(arr[i].tris, arr[i].n_tris, params[i], ooc.SINK(collect1))
-        for k in (0, 1):
-            identical = identical and b"".join(got[i][k]) == b"".join(want[k])
+        w = (b"".join(want[0]), b"".join(want[1]))
+        identical = identical and (b"".join(got[i][0]), b"".join(got[i][1])) == w
+        no, nb, do, db = layout[i]
+        d = (arena_buf[no:no + nb].cpu().numpy().tobytes(), arena_buf[do:do + db].cpu().numpy().tobytes())
+        dev_identical = dev_identical and d == w
     b.close()
-    value = n / t_batch
+    value = n / t_batch_dev
     return {
         "metric": "meshes/s", "value": value, "unit": "meshes/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t_batch * 1e3, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": t_batch_dev * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "configuration 4: %d meshes, log-uniform 64..200k triangles (icospheres and soups), "
-                               "gridsize 64/128/256/512, binary or payload 50/50, one ooc_build_batch call" % n,
-                   "name": "batch4096", "n_meshes": n, "n_triangles": total_tris},
-        "mtri_per_s": total_tris / t_batch / 1e6, "svo_nodes_per_s": n_nodes / t_batch,
-        "plain_meshes_per_s": n / t_plain, "speedup_vs_plain": t_plain / t_batch,
-        "parity_sample": {"meshes": len(sample), "identical_to_plain": identical},
-        "e2e": {"value": value, "unit": "meshes/s", "h2d_bytes_per_step": int(sum(m[0].nbytes for m in meshes)),
-                "d2h_bytes_per_step": int(sum(int(infos[i].n_nodes) * 24 + int(infos[i].n_data) * 32
-                                              for i in range(n)))},
-        "gpu_launches": launches,
+                               "gridsize 64/128/256/512, binary or payload 50/50, one batch call per step; "
+                               "value = octrees resident in HBM (ooc_build_batch_device), e2e = octrees "
+                               "copied back to host memory (ooc_build_batch)" % n,
+                   "name": "batch4096", "n_meshes": n, "n_triangles": total_tris,
+                   "l2": "inputs larger than L2 (%.1f GB of triangles per step)" % (offs[-1] / 1e9)},
+        "mtri_per_s": total_tris / t_batch_dev / 1e6, "svo_nodes_per_s": n_nodes / t_batch_dev,
+        "resident": {"batched_meshes_per_s": n / t_batch_dev, "plain_meshes_per_s": n / t_plain_dev,
+                     "speedup_vs_plain": t_plain_dev / t_batch_dev},
+        "host": {"batched_meshes_per_s": n / t_batch, "plain_meshes_per_s": n / t_plain,
+                 "speedup_vs_plain": t_plain / t_batch},
+        "parity_sample": {"meshes": len(sample), "host_identical_to_plain": identical,
+                          "resident_identical_to_plain": dev_identical},
+        "e2e": {"value": n / t_batch, "unit": "meshes/s", "h2d_bytes_per_step": int(sum(m[0].nbytes for m in meshes)),
+                "d2h_bytes_per_step": int(out_bytes)},
+        "gpu_launches": launches_dev, "gpu_launches_host_output": launches,
     }
 
 
@@ -460,8 +495,12 @@ def run_serve(args, world, rank, local):
         host[offs[i]:offs[i] + t.nbytes] = t.reshape(-1).view(np.uint8)
         pool.append((pinned.data_ptr() + offs[i], t.shape[0], ooc.make_params(N, 2048, geometry_only=not payload), N))
     rates = [float(r) for r in args.rates.split(",")]
-    arms = {"served": dict(engines=args.engines, max_batch=256, memory_budget=120 << 30),
-            "plain": dict(engines=1, max_batch=1, memory_budget=120 << 30)}
+    # served: continuous batching over engines; plain: one request at a time through the same library.
+    # resident: octrees stay in HBM (released by the poller); host: copied back to host memory.
+    arms = {"served_resident": dict(engines=args.engines, max_batch=256, memory_budget=120 << 30, resident=True),
+            "plain_resident": dict(engines=1, max_batch=1, memory_budget=120 << 30, resident=True),
+            "served_host": dict(engines=args.engines, max_batch=256, memory_budget=120 << 30),
+            "plain_host": dict(engines=1, max_batch=1, memory_budget=120 << 30)}
     # warm-up set: the requests with the largest grids, then a spread of the rest
     order = sorted(range(len(pool)), key=lambda i: -pool[i][3] * pool[i][1])
     warm = order[:16] + order[16::max(1, len(pool) // 64)]
@@ -478,7 +517,12 @@ def run_serve(args, world, rank, local):
                         pass
                 out[arm].append(serve_stream(srv, pool, r, args.duration, seed=5 + int(r), drain_s=args.drain))
             print("serve %s %.0f req/s: %s" % (arm, r, json.dumps(out[arm][-1])), file=sys.stderr, flush=True)
-    top = out["served"][-1]
+    top = out["served_resident"][-1]
+    top_host = out["served_host"][-1]
+
+    def ratio(a, b):
+        return [x["meshes_per_s"] / max(y["meshes_per_s"], 1e-9) for x, y in zip(out[a], out[b])]
+
     return {
         "metric": "served meshes/s", "value": top["meshes_per_s"], "unit": "meshes/s", "n_gpus": world,
         "steps": top["completed"], "warmup": 1, "ms_per_step": 1e3 / max(top["meshes_per_s"], 1e-9),
@@ -487,14 +531,16 @@ def run_serve(args, world, rank, local):
                                "pool of %d configuration-4 meshes with gridsizes 128..2048; 120 GB admission "
                                "budget; pinned host triangles in, host octree bytes out"
                                % (args.rates, args.duration, len(pool)),
-                   "name": "serve", "engines": args.engines, "max_batch": 256},
+                   "name": "serve", "engines": args.engines, "max_batch": 256,
+                   "value_arm": "served_resident: octrees resident in HBM, released by the poller"},
         "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
-        "rates": out["served"], "plain": out["plain"],
-        "speedup_vs_plain": [s["meshes_per_s"] / max(p["meshes_per_s"], 1e-9)
-                             for s, p in zip(out["served"], out["plain"])],
-        "e2e": {"value": top["meshes_per_s"], "unit": "meshes/s",
+        "arms": out,
+        "speedup_vs_plain_resident": ratio("served_resident", "plain_resident"),
+        "speedup_vs_plain_host": ratio("served_host", "plain_host"),
+        "e2e": {"value": top_host["meshes_per_s"], "unit": "meshes/s", "p50_ms": top_host["p50_ms"],
+                "p99_ms": top_host["p99_ms"], "note": "results copied back to host memory",
                 "h2d_bytes_per_step": int(np.mean([t.nbytes for t, _, _ in meshes])),
-                "d2h_bytes_per_step": int(top["output_gb"] * 1e9 / max(top["completed"], 1))},
+                "d2h_bytes_per_step": int(top_host["output_gb"] * 1e9 / max(top_host["completed"], 1))},
     }
 
 
@@ -531,7 +577,7 @@ def main():
                     help="meshes of the batch4096 workload (4096) or of the serve pool (512)")
     ap.add_argument("--rates", default="200,500,1000,2000", help="serve: offered request rates, req/s")
     ap.add_argument("--duration", type=float, default=5.0, help="serve: seconds of arrivals per rate")
-    ap.add_argument("--drain", type=float, default=60.0, help="serve: seconds to wait for the queue to drain")
+    ap.add_argument("--drain", type=float, default=10.0, help="serve: seconds to wait for the queue to drain")
     ap.add_argument("--engines", type=int, default=2, help="serve: engines of the served arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,

@@ -125,6 +125,41 @@ typedef int (*ooc_batch_sink_fn)(void* user, uint64_t mesh, int32_t kind, const 
 int ooc_build_batch(ooc_ctx* ctx, const ooc_mesh* meshes, uint64_t n_meshes, ooc_batch_sink_fn sink, void* user,
                     ooc_build_info* infos);
 
+/* ---- Batched build into device memory (no counterpart in the reference) ----
+ * Like ooc_build_batch (host triangles in), but every mesh's node and data
+ * files are written straight into device memory that the caller provides:
+ * `alloc` is called once per mesh, in mesh order, as soon as the mesh's sizes
+ * are known and before any of its records are written.  It returns two device
+ * pointers (8-byte aligned) through `nodes` and `data`; `stream` is the
+ * cudaStream_t the library writes them on, so memory allocated stream-ordered
+ * on it (cudaMallocAsync) may be used.  `ready` (may be NULL) is called once
+ * per mesh, in mesh order, when every byte of its files has been written.  The
+ * files are byte-identical to what ooc_build writes for that mesh alone.
+ * Both callbacks return 0, or non-zero to abort the call. */
+typedef int (*ooc_alloc_fn)(void* user, uint64_t mesh, uint64_t nodes_bytes, uint64_t data_bytes, void* stream,
+                            void** nodes, void** data);
+typedef int (*ooc_ready_fn)(void* user, uint64_t mesh);
+int ooc_build_batch_device(ooc_ctx* ctx, const ooc_mesh* meshes, uint64_t n_meshes, ooc_alloc_fn alloc,
+                           ooc_ready_fn ready, void* user, ooc_build_info* infos);
+
+/* A bump allocator over one caller-owned device buffer, usable as `alloc`
+ * with `user` = the arena: each file starts on a 256-byte boundary; a full
+ * arena fails the call with OOC_ERR_OOM. */
+typedef struct {
+  void* base;
+  uint64_t capacity;
+  uint64_t used;
+} ooc_device_arena;
+int ooc_arena_alloc(void* arena, uint64_t mesh, uint64_t nodes_bytes, uint64_t data_bytes, void* stream,
+                    void** nodes, void** data);
+
+/* Bytes of occupancy pyramids one sub-batch may hold (default 4 GiB, at least
+ * 4096): the stripes of a batch call run in sub-batches of at most this much
+ * pyramid (a single stripe larger than it runs alone).  Output is the same for
+ * every budget. */
+int ooc_set_batch_budget(ooc_ctx* ctx, uint64_t bytes);
+uint64_t ooc_batch_budget(const ooc_ctx* ctx);
+
 /* Same path from triangles already in device memory; the octree stays in
  * device memory (see ooc_result_device).  `stream` is a cudaStream_t (NULL:
  * the context's own stream); all work is ordered on it and the call returns
@@ -194,26 +229,33 @@ int ooc_voxelize_occupancy_noalloc(const ooc_build_params* params, const float* 
 
 /* ---- Serving loop (no counterpart in the reference) ----
  * Requests (meshes) are admitted by their computed HBM footprint -- triangles,
- * the occupancy pyramids of their stripes, and per-node arrays for an
- * estimate of their nodes -- against `memory_budget`, and run in continuously
- * formed batches: each of `engines` contexts (own streams and scratch) takes,
- * whenever it is free, every queued request that fits (at most max_batch) and
- * builds them in one ooc_build_batch call.  Each result is byte-identical to
- * ooc_build on that mesh alone. */
+ * the occupancy pyramids of their stripes, and per-node arrays plus output
+ * for an estimate of their nodes -- against `memory_budget`, and run in
+ * continuously formed batches: each of `engines` contexts (own streams and
+ * scratch) takes, whenever it is free, every queued request that fits (at
+ * most max_batch) and builds them in one batch call (ooc_build_batch, or
+ * ooc_build_batch_device for results resident in device memory).  A request
+ * completes as soon as its mesh does, not when its batch does.  Each result is
+ * byte-identical to ooc_build on that mesh alone.  Device-resident results
+ * hold their HBM until released, and count against `memory_budget` until
+ * then. */
 typedef struct ooc_server ooc_server;
+
+#define OOC_RESULT_HOST 0    /* results are copied back into host memory            */
+#define OOC_RESULT_DEVICE 1  /* results stay resident in device memory (HBM)         */
 
 typedef struct {
   int32_t device;
-  int32_t engines;        /* batches in flight at once, >= 1                       */
-  uint32_t max_batch;     /* requests per batch, >= 1 (1: every request alone)     */
-  uint32_t reserved;      /* must be 0                                             */
-  uint64_t memory_budget; /* bytes of HBM the requests in flight may hold          */
+  int32_t engines;         /* batches in flight at once, >= 1                       */
+  uint32_t max_batch;      /* requests per batch, >= 1 (1: every request alone)     */
+  int32_t result_location; /* OOC_RESULT_HOST or OOC_RESULT_DEVICE                  */
+  uint64_t memory_budget;  /* bytes of HBM the requests in flight may hold          */
 } ooc_server_config;
 
 typedef struct {
   uint64_t id;
   int32_t status;         /* OOC_OK or the build's error code                      */
-  int32_t reserved;
+  int32_t location;       /* OOC_RESULT_HOST or OOC_RESULT_DEVICE: where the bytes are */
   const void* nodes;      /* node file bytes (valid until ooc_server_release)      */
   uint64_t nodes_bytes;
   const void* data;       /* data file bytes                                       */
@@ -230,6 +272,8 @@ int ooc_server_create(const ooc_server_config* cfg, ooc_server** out);
 int ooc_server_submit(ooc_server* server, const ooc_mesh* mesh, uint64_t* id);
 /* Next completed request (OOC_OK), or OOC_ERR_TIMEOUT after `timeout_ms`. */
 int ooc_server_poll(ooc_server* server, int32_t timeout_ms, ooc_result* out);
+/* Copy a polled result's files into host memory (either location). */
+int ooc_server_read(ooc_server* server, uint64_t id, void* nodes_host, void* data_host);
 /* Free a polled result's buffers. */
 int ooc_server_release(ooc_server* server, uint64_t id);
 /* Drop the requests not yet started, let running batches finish, then stop

@@ -33,7 +33,8 @@ EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_
            "ooc_build_device", "ooc_result_device", "ooc_result_copy", "ooc_set_phase_timing", "ooc_phase_times",
            "ooc_kernel_launches", "ooc_build_files", "ooc_set_kernel_timing", "ooc_kernel_time",
            "ooc_voxelize_occupancy_noalloc", "ooc_build_batch", "ooc_server_create", "ooc_server_submit",
-           "ooc_server_poll", "ooc_server_release", "ooc_server_destroy")
+           "ooc_server_poll", "ooc_server_release", "ooc_server_destroy", "ooc_build_batch_device",
+           "ooc_arena_alloc", "ooc_set_batch_budget", "ooc_batch_budget", "ooc_server_read")
 
 
 class BuildParams(ctypes.Structure):
@@ -57,16 +58,39 @@ class Mesh(ctypes.Structure):
     _fields_ = [("tris", ctypes.c_void_p), ("n_tris", ctypes.c_uint64), ("params", BuildParams)]
 
 
+RESULT_HOST, RESULT_DEVICE = 0, 1
+
+
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("engines", ctypes.c_int32), ("max_batch", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32), ("memory_budget", ctypes.c_uint64)]
+                ("result_location", ctypes.c_int32), ("memory_budget", ctypes.c_uint64)]
 
 
 class Result(ctypes.Structure):
-    _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int32), ("reserved", ctypes.c_int32),
+    _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int32), ("location", ctypes.c_int32),
                 ("nodes", ctypes.c_void_p), ("nodes_bytes", ctypes.c_uint64), ("data", ctypes.c_void_p),
                 ("data_bytes", ctypes.c_uint64), ("info", BuildInfo), ("t_submit_us", ctypes.c_double),
                 ("t_start_us", ctypes.c_double), ("t_done_us", ctypes.c_double), ("batch_size", ctypes.c_uint64)]
+
+
+class DeviceArena(ctypes.Structure):
+    _fields_ = [("base", ctypes.c_void_p), ("capacity", ctypes.c_uint64), ("used", ctypes.c_uint64)]
+
+
+ALLOC = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p))
+READY = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64)
+
+
+def arena_layout(infos, n: int):
+    """Offsets of each mesh's node and data files in an arena filled by ooc_arena_alloc (mesh order,
+    256-byte aligned files)."""
+    out, off = [], 0
+    for i in range(n):
+        nb, db = int(infos[i].n_nodes) * 24, int(infos[i].n_data) * 32
+        out.append((off, nb, off + (nb + 255) // 256 * 256, db))
+        off += (nb + 255) // 256 * 256 + (db + 255) // 256 * 256
+    return out, off
 
 
 class OocError(RuntimeError):
@@ -122,12 +146,22 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_build_batch.argtypes = [ctypes.c_void_p, P(Mesh), ctypes.c_uint64, BATCH_SINK, ctypes.c_void_p,
                                     P(BuildInfo)]
     lib.ooc_build_batch.restype = ctypes.c_int
+    lib.ooc_build_batch_device.argtypes = [ctypes.c_void_p, P(Mesh), ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, P(BuildInfo)]
+    lib.ooc_build_batch_device.restype = ctypes.c_int
+    lib.ooc_arena_alloc.restype = ctypes.c_int
+    lib.ooc_set_batch_budget.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+    lib.ooc_set_batch_budget.restype = ctypes.c_int
+    lib.ooc_batch_budget.argtypes = [ctypes.c_void_p]
+    lib.ooc_batch_budget.restype = ctypes.c_uint64
     lib.ooc_server_create.argtypes = [P(ServerConfig), P(ctypes.c_void_p)]
     lib.ooc_server_create.restype = ctypes.c_int
     lib.ooc_server_submit.argtypes = [ctypes.c_void_p, P(Mesh), P(ctypes.c_uint64)]
     lib.ooc_server_submit.restype = ctypes.c_int
     lib.ooc_server_poll.argtypes = [ctypes.c_void_p, ctypes.c_int32, P(Result)]
     lib.ooc_server_poll.restype = ctypes.c_int
+    lib.ooc_server_read.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
+    lib.ooc_server_read.restype = ctypes.c_int
     lib.ooc_server_release.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
     lib.ooc_server_release.restype = ctypes.c_int
     lib.ooc_server_destroy.argtypes = [ctypes.c_void_p]
@@ -303,6 +337,55 @@ class Builder:
                                                b"".join(parts[i][1])), _info_dict(infos[i]))
                 for i in range(len(meshes))]
 
+    def set_batch_budget(self, nbytes: int) -> None:
+        self._check(self.lib.ooc_set_batch_budget(self.h, nbytes))
+
+    def batch_budget(self) -> int:
+        return int(self.lib.ooc_batch_budget(self.h))
+
+    def build_batch_device(self, meshes, params_list, capacity: int = 1 << 30) -> list:
+        """Many meshes in one call, each octree written into device memory (one arena, a torch
+        buffer of `capacity` bytes); returns one BuildResult per mesh after copying the arena back."""
+        import torch
+        arr, keep = self._mesh_array(meshes, params_list)
+        arena_buf = torch.empty(capacity, dtype=torch.uint8, device="cuda")
+        arena = DeviceArena(arena_buf.data_ptr(), capacity, 0)
+        infos = (BuildInfo * max(1, len(meshes)))()
+        ready = []
+        cb = READY(lambda user, mesh: ready.append(mesh) or 0)
+        fn = ctypes.cast(self.lib.ooc_arena_alloc, ctypes.c_void_p)
+        self._check(self.lib.ooc_build_batch_device(self.h, arr, len(meshes), fn, cb, ctypes.byref(arena), infos))
+        if ready != list(range(len(meshes))):
+            raise OocError(3, "meshes were not ready once each, in order")
+        layout, used = arena_layout(infos, len(meshes))
+        if used != arena.used:
+            raise OocError(3, "arena layout differs from the allocator's")
+        host = arena_buf[:used].cpu().numpy().tobytes()
+        return [BuildResult(_octree.from_bytes(int(params_list[i].gridsize), host[no:no + nb], host[do:do + db]),
+                            _info_dict(infos[i])) for i, (no, nb, do, db) in enumerate(layout)]
+
+    def build_batch_device_ptrs(self, mesh_array, n_meshes: int, arena: "DeviceArena", infos) -> None:
+        """Low-level device batch call into an arena (ooc_arena_alloc), no ready callback."""
+        fn = ctypes.cast(self.lib.ooc_arena_alloc, ctypes.c_void_p)
+        self._check(self.lib.ooc_build_batch_device(self.h, mesh_array, n_meshes, fn, None, ctypes.byref(arena),
+                                                    infos))
+
+    def _mesh_array(self, meshes, params_list):
+        if len(meshes) != len(params_list):
+            raise ValueError("one BuildParams per mesh")
+        keep = []
+        arr = (Mesh * max(1, len(meshes)))()
+        for i, (t, p) in enumerate(zip(meshes, params_list)):
+            t = np.ascontiguousarray(t, dtype=np.float32)
+            width = 9 if p.geometry_only else 21
+            if t.ndim != 2 or t.shape[1] != width:
+                raise ValueError("mesh %d: triangles must be [T, %d] float32" % (i, width))
+            keep.append(t)
+            arr[i].tris = t.ctypes.data
+            arr[i].n_tris = t.shape[0]
+            arr[i].params = p
+        return arr, keep
+
     def build_batch_ptrs(self, mesh_array, n_meshes: int, sink, infos) -> None:
         """Low-level batch call: a ctypes Mesh array, a BATCH_SINK and a BuildInfo array."""
         self._check(self.lib.ooc_build_batch(self.h, mesh_array, n_meshes, sink, None, infos))
@@ -346,9 +429,11 @@ class Builder:
 class Server:
     """The serving loop: submit meshes, poll completed octrees (see ooc_server_* in the C ABI)."""
 
-    def __init__(self, device: int = 0, engines: int = 2, max_batch: int = 256, memory_budget: int = 120 << 30):
+    def __init__(self, device: int = 0, engines: int = 2, max_batch: int = 256, memory_budget: int = 120 << 30,
+                 resident: bool = False):
+        """`resident`: results stay in device memory (read with poll(copy=True) or ooc_server_read)."""
         self.lib = load_library()
-        cfg = ServerConfig(device, engines, max_batch, 0, memory_budget)
+        cfg = ServerConfig(device, engines, max_batch, RESULT_DEVICE if resident else RESULT_HOST, memory_budget)
         h = ctypes.c_void_p()
         rc = self.lib.ooc_server_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc != OOC_OK:
@@ -396,10 +481,14 @@ class Server:
         _, gridsize = self._keep.pop(r.id)
         out = {"id": r.id, "status": r.status, "info": _info_dict(r.info), "t_submit_us": r.t_submit_us,
                "t_start_us": r.t_start_us, "t_done_us": r.t_done_us, "batch_size": r.batch_size,
-               "bytes": r.nodes_bytes + r.data_bytes}
+               "bytes": r.nodes_bytes + r.data_bytes, "location": r.location}
         if copy and r.status == OOC_OK:
-            out["tree"] = _octree.from_bytes(gridsize, ctypes.string_at(r.nodes, r.nodes_bytes),
-                                             ctypes.string_at(r.data, r.data_bytes))
+            nodes = np.empty(r.nodes_bytes, np.uint8)
+            data = np.empty(r.data_bytes, np.uint8)
+            rc = self.lib.ooc_server_read(self.h, r.id, nodes.ctypes.data, data.ctypes.data)
+            if rc != OOC_OK:
+                raise OocError(rc, "ooc_server_read failed")
+            out["tree"] = _octree.from_bytes(gridsize, nodes.tobytes(), data.tobytes())
         self.lib.ooc_server_release(self.h, r.id)
         return out
 

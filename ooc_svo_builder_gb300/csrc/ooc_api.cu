@@ -433,6 +433,13 @@ struct MeshWork {
   uint64_t filled = 0;
   uint64_t n_items = 0;
   int64_t last_stripe = -1;  // last stripe with items (-1: none)
+  uint64_t index = 0;        // in the batch
+  // caller-owned device destination (output to device destinations)
+  void* dst_nodes = nullptr;
+  void* dst_data = nullptr;
+  bool dst_ready = false;
+  uint64_t total_nodes = 0, total_data = 0;
+  uint64_t carried_nodes = 0, carried_data = 0;  // records parked in the carry buffers
   MeshWork(const Plan& p, Emitter* o)
       : pl(p), out(o), top(p.Ls, p.levels != 0, o), layout(p.Ls, p.levels != 0, nullptr) {
     dry.dry = true;
@@ -441,7 +448,10 @@ struct MeshWork {
   MeshWork(MeshWork&& o) noexcept
       : prm(o.prm), pl(o.pl), d_tris(o.d_tris), n_tris(o.n_tris), part_off(std::move(o.part_off)), items(o.items),
         out(o.out), top(o.top), next_stripe(o.next_stripe), dry(o.dry), layout(o.layout),
-        layout_next(o.layout_next), filled(o.filled), n_items(o.n_items), last_stripe(o.last_stripe) {}
+        layout_next(o.layout_next), filled(o.filled), n_items(o.n_items), last_stripe(o.last_stripe),
+        index(o.index), dst_nodes(o.dst_nodes), dst_data(o.dst_data), dst_ready(o.dst_ready),
+        total_nodes(o.total_nodes), total_data(o.total_data), carried_nodes(o.carried_nodes),
+        carried_data(o.carried_data) {}
 };
 
 struct StripeRef {
@@ -503,6 +513,50 @@ struct Uploader {
   }
 };
 
+// Where the records of the stripes go: host sink (through the copy-back ring),
+// the context's own device files (one mesh), or a device destination per mesh
+// that the caller provides once the mesh's sizes are known.
+enum OutMode { OUT_HOST, OUT_CTX, OUT_DEST };
+struct OutSpec {
+  OutMode mode = OUT_HOST;
+  ooc_alloc_fn alloc = nullptr;
+  ooc_ready_fn ready = nullptr;
+  void* user = nullptr;
+  mutable size_t alloc_next = 0;  // destinations are asked for in mesh order
+};
+
+// Sizes of a mesh's files from the placement run-ahead (every stripe with items
+// already placed), then its destination from the caller.  Records parked in the
+// carry buffers (stripes of earlier sub-batches) move there first.
+void ensure_dest(ooc_ctx* c, cudaStream_t st, MeshWork& m, const OutSpec& os) {
+  if (m.dst_ready) return;
+  TopBuilder& tb = m.layout;
+  tb.out = &m.dry;
+  for (; m.layout_next < m.pl.n_stripes; m.layout_next++) tb.push(tb.top, TNode());
+  m.total_nodes = tb.node_pos + 1;  // the root
+  m.total_data = tb.data_pos;
+  void* dn = nullptr;
+  void* dd = nullptr;
+  if (os.alloc(os.user, m.index, m.total_nodes * 24, m.total_data * 32, st, &dn, &dd) != 0 || !dn || !dd)
+    fail(OOC_ERR_OOM, "destination allocation failed for mesh " + std::to_string(m.index));
+  if ((reinterpret_cast<uintptr_t>(dn) | reinterpret_cast<uintptr_t>(dd)) & 7)
+    fail(OOC_ERR_INVALID, "destinations must be 8-byte aligned");
+  m.dst_nodes = dn;
+  m.dst_data = dd;
+  m.dst_ready = true;
+  if (m.carried_nodes)
+    ck(cudaMemcpyAsync(dn, c->d_nodes.p, m.carried_nodes * 24, cudaMemcpyDeviceToDevice, st), "carry");
+  if (m.carried_data)
+    ck(cudaMemcpyAsync(dd, c->d_data.p, m.carried_data * 32, cudaMemcpyDeviceToDevice, st), "carry");
+}
+
+// Destinations of meshes up to `idx`, in mesh order: the ones before it that
+// have not had theirs are meshes without items (every stripe of a mesh with
+// items precedes the stripes of later meshes, so it has been placed).
+void alloc_through(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, size_t idx, const OutSpec& os) {
+  for (; os.alloc_next <= idx; os.alloc_next++) ensure_dest(c, st, meshes[os.alloc_next], os);
+}
+
 // A launched sub-batch whose records are still on their way to the host.
 struct Pending {
   bool active = false;
@@ -513,7 +567,7 @@ struct Pending {
 };
 
 void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, const std::vector<StripeRef>& sb,
-                   bool device_mode, Pending& out_pending, int slot) {
+                   const OutSpec& os, Pending& out_pending, int slot) {
   const uint32_t n = (uint32_t)sb.size();
   // ---- geometry of every stripe ----
   std::vector<Pyramid> pyr(n);
@@ -677,7 +731,25 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   float* cache = any_levels ? ensure<float>(c->d_cache, total_nodes * 24) : nullptr;
   uint32_t* winners = any_payload ? ensure<uint32_t>(c->d_winners, total_nodes * 4) : nullptr;
   uint64_t out_nodes = 0, out_data = 0;
-  if (device_mode) {
+  if (os.mode == OUT_DEST) {
+    // meshes whose last stripe is here get their destination; the others park
+    // their records in the carry buffers until then
+    for (uint32_t s = 0; s < n; s++) {
+      MeshWork& m = meshes[sb[s].mesh];
+      if ((int64_t)sb[s].stripe == m.last_stripe) alloc_through(c, st, meshes, sb[s].mesh, os);
+    }
+    uint64_t need_n = 0, need_d = 0;
+    for (uint32_t s = 0; s < n; s++) {
+      MeshWork& m = meshes[sb[s].mesh];
+      if (m.dst_ready) continue;
+      m.carried_nodes = std::max(m.carried_nodes, pl[s].node_base + pl[s].node_span);
+      m.carried_data = std::max(m.carried_data, pl[s].data_base + pl[s].data_span);
+      need_n = std::max(need_n, m.carried_nodes);
+      need_d = std::max(need_d, m.carried_data);
+    }
+    if (need_n) ensure_keep<uint64_t>(c->d_nodes, need_n * 24, need_n * 24, st);
+    if (need_d) ensure_keep<unsigned char>(c->d_data, need_d * 32, need_d * 32, st);
+  } else if (os.mode == OUT_CTX) {
     uint64_t need_n = 0, need_d = 0;
     for (uint32_t s = 0; s < n; s++) {
       need_n = std::max(need_n, pl[s].node_base + pl[s].node_span);
@@ -723,7 +795,14 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     e.flag = flag;
     e.node_base = q.node_base;
     e.data_base = q.data_base;
-    if (device_mode) {
+    if (os.mode == OUT_DEST && m.dst_ready) {
+      e.node_win = static_cast<uint64_t*>(m.dst_nodes);
+      e.data_win = static_cast<unsigned char*>(m.dst_data);
+      e.node_win_base = 0;
+      e.data_win_base = 0;
+      e.node_win_len = m.total_nodes;
+      e.data_win_len = m.total_data;
+    } else if (os.mode != OUT_HOST) {
       e.node_win = static_cast<uint64_t*>(c->d_nodes.p);
       e.data_win = static_cast<unsigned char*>(c->d_data.p);
       e.node_win_base = 0;
@@ -818,7 +897,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     ck(cudaMemcpyAsync(hr, d_root, ((uint64_t)n * 16 + 1) * 4, cudaMemcpyDeviceToHost, st), "root info");
   }
   ck(cudaEventRecord(c->ev_compute[slot], st), "event");
-  if (!device_mode) {
+  if (os.mode == OUT_HOST) {
     // the records travel to the host on the copy stream while the next sub-batch computes
     ck(cudaStreamWaitEvent(c->copy_stream, c->ev_compute[slot], 0), "wait");
     ring_start(c, c->ring[slot][OOC_STREAM_NODES], c->d_out_nodes[slot].p, out_nodes * 24);
@@ -833,7 +912,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
 }
 
 // Wait for a sub-batch's records and hand its stripes to their meshes, in file order.
-void finish_sub_batch(ooc_ctx* c, std::vector<MeshWork>& meshes, Pending& pd, bool device_mode) {
+void finish_sub_batch(ooc_ctx* c, std::vector<MeshWork>& meshes, Pending& pd, const OutSpec& os) {
   if (!pd.active) return;
   pd.active = false;
   const int slot = pd.slot;
@@ -855,7 +934,7 @@ void finish_sub_batch(ooc_ctx* c, std::vector<MeshWork>& meshes, Pending& pd, bo
       continue;
     }
     m.filled += q.n_leaf;
-    if (!device_mode) {
+    if (os.mode == OUT_HOST) {
       ring_take(c, c->ring[slot][OOC_STREAM_NODES], q.out_node_off * 24, (q.out_node_off + q.node_span) * 24,
                 [&](const void* p, uint64_t n) { m.out->span(OOC_STREAM_NODES, p, n); });
       ring_take(c, c->ring[slot][OOC_STREAM_DATA], q.out_data_off * 32, (q.out_data_off + q.data_span) * 32,
@@ -931,9 +1010,10 @@ void finalize_mesh(MeshWork& m) {
 
 // Whole path for a list of meshes (triangles already on the device).  Meshes
 // complete in order, each as soon as the sub-batch holding its last stripe is
-// finished; `on_done(i)` runs right after mesh i's last record.
-void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bool device_mode,
-                  const std::function<void(size_t)>& on_done = nullptr) {
+// finished; `on_done(list)` runs right after the last records of the meshes
+// that have just completed.
+void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, const OutSpec& os,
+                  const std::function<void(const std::vector<size_t>&)>& on_done = nullptr) {
   if (c->d_mesh_items.size() < meshes.size()) c->d_mesh_items.resize(meshes.size());
   for (size_t i = 0; i < meshes.size(); i++) {
     MeshWork& m = meshes[i];
@@ -960,21 +1040,24 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bo
     for (int64_t s = (int64_t)m.pl.n_stripes - 1; s >= 0 && m.last_stripe < 0; s--)
       if (items_of(m, (uint64_t)s)) m.last_stripe = s;
   size_t n_done = 0;
+  std::vector<size_t> just_done;
   auto complete = [&]() {
+    just_done.clear();
     while (n_done < meshes.size() && (int64_t)meshes[n_done].next_stripe > meshes[n_done].last_stripe) {
       finalize_mesh(meshes[n_done]);
-      if (on_done) on_done(n_done);
+      just_done.push_back(n_done);
       n_done++;
     }
+    if (on_done && !just_done.empty()) on_done(just_done);
   };
   complete();
   Pending pend[2];
   int k = 0;
   // launch sub-batch k, then finish k-1 while k computes
   auto flush = [&]() {
-    run_sub_batch(c, st, meshes, sb, device_mode, pend[k & 1], k & 1);
-    if (device_mode) finish_sub_batch(c, meshes, pend[k & 1], true);
-    else finish_sub_batch(c, meshes, pend[(k + 1) & 1], false);
+    run_sub_batch(c, st, meshes, sb, os, pend[k & 1], k & 1);
+    if (os.mode == OUT_CTX) finish_sub_batch(c, meshes, pend[k & 1], os);
+    else finish_sub_batch(c, meshes, pend[(k + 1) & 1], os);
     complete();
     k++;
     sb.clear();
@@ -996,8 +1079,8 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, bo
     }
   }
   if (!sb.empty()) flush();
-  finish_sub_batch(c, meshes, pend[0], device_mode);
-  finish_sub_batch(c, meshes, pend[1], device_mode);
+  finish_sub_batch(c, meshes, pend[k & 1], os);  // the older of the two first
+  finish_sub_batch(c, meshes, pend[(k + 1) & 1], os);
   complete();
   if (n_done != meshes.size()) fail(OOC_ERR_DEVICE, "internal: mesh left unfinished");
 }
@@ -1217,51 +1300,154 @@ int ooc_build(ooc_ctx* c, const ooc_build_params* prm, const float* tris_host, u
   return ooc_build_batch(c, &m, 1, single_sink, &ss, info);
 }
 
+namespace {
+// The meshes of a batch call, their triangles in one device buffer (256-byte
+// aligned slices); the H2D copies are queued on `st` by upload().
+struct BatchInput {
+  std::vector<uint64_t> off;
+  std::vector<Emitter> outs;
+  std::vector<MeshWork> meshes;
+  unsigned char* d_all = nullptr;
+
+  BatchInput(ooc_ctx* c, const ooc_mesh* in, uint64_t n, bool device_records) : off(n + 1, 0), outs(n) {
+    if (n && !in) fail(OOC_ERR_INVALID, "meshes are NULL");
+    for (uint64_t i = 0; i < n; i++) {
+      check_params(&in[i].params, in[i].n_tris);
+      if (in[i].n_tris && !in[i].tris) fail(OOC_ERR_INVALID, "triangles are NULL");
+      off[i + 1] = off[i] + (bytes(in[i]) + 255) / 256 * 256;
+    }
+    d_all = ensure<unsigned char>(c->d_tris, off[n]);
+    meshes.reserve(n);
+    for (uint64_t i = 0; i < n; i++) {
+      outs[i].device = device_records;
+      outs[i].mesh = i;
+      meshes.emplace_back(make_plan(&in[i].params), &outs[i]);
+      meshes.back().prm = &in[i].params;
+      meshes.back().d_tris = reinterpret_cast<const float*>(d_all + off[i]);
+      meshes.back().n_tris = in[i].n_tris;
+      meshes.back().index = i;
+    }
+  }
+  static uint64_t bytes(const ooc_mesh& m) { return m.n_tris * (m.params.geometry_only ? 9 : 21) * 4; }
+  void upload(ooc_ctx* c, const ooc_mesh* in, cudaStream_t st) {
+    PhaseScope ph(c, PH_COPY, st);
+    for (size_t i = 0; i < meshes.size(); i++)
+      if (bytes(in[i])) ck(cudaMemcpyAsync(d_all + off[i], in[i].tris, bytes(in[i]), cudaMemcpyHostToDevice, st), "H2D");
+  }
+};
+}  // namespace
+
 int ooc_build_batch(ooc_ctx* c, const ooc_mesh* meshes_in, uint64_t n_meshes, ooc_batch_sink_fn sink, void* user,
                     ooc_build_info* infos) {
   return guarded(c, [&] {
     begin_build(c);
     if (!sink) fail(OOC_ERR_INVALID, "sink is NULL");
-    if (n_meshes && !meshes_in) fail(OOC_ERR_INVALID, "meshes are NULL");
     cudaStream_t st = c->own_stream;
-    // one device buffer for every mesh's triangles (256-byte aligned slices)
-    std::vector<uint64_t> off(n_meshes + 1, 0);
-    for (uint64_t i = 0; i < n_meshes; i++) {
-      check_params(&meshes_in[i].params, meshes_in[i].n_tris);
-      if (meshes_in[i].n_tris && !meshes_in[i].tris) fail(OOC_ERR_INVALID, "triangles are NULL");
-      const uint64_t bytes = meshes_in[i].n_tris * (meshes_in[i].params.geometry_only ? 9 : 21) * 4;
-      off[i + 1] = off[i] + (bytes + 255) / 256 * 256;
-    }
-    unsigned char* d_all = ensure<unsigned char>(c->d_tris, off[n_meshes]);
-    std::vector<Emitter> outs(n_meshes);
-    std::vector<MeshWork> meshes;
-    meshes.reserve(n_meshes);
-    for (uint64_t i = 0; i < n_meshes; i++) {
-      outs[i].sink = sink;
-      outs[i].user = user;
-      outs[i].mesh = i;
-      meshes.emplace_back(make_plan(&meshes_in[i].params), &outs[i]);
-      meshes.back().prm = &meshes_in[i].params;
-      meshes.back().d_tris = reinterpret_cast<const float*>(d_all + off[i]);
-      meshes.back().n_tris = meshes_in[i].n_tris;
+    BatchInput b(c, meshes_in, n_meshes, false);
+    for (Emitter& e : b.outs) {
+      e.sink = sink;
+      e.user = user;
     }
     {
       PhaseScope all(c, PH_ALL, st);
-      {
-        PhaseScope ph(c, PH_COPY, st);
-        for (uint64_t i = 0; i < n_meshes; i++) {
-          const uint64_t bytes = meshes_in[i].n_tris * (meshes_in[i].params.geometry_only ? 9 : 21) * 4;
-          if (bytes) ck(cudaMemcpyAsync(d_all + off[i], meshes_in[i].tris, bytes, cudaMemcpyHostToDevice, st), "H2D");
+      b.upload(c, meshes_in, st);
+      OutSpec os;
+      os.mode = OUT_HOST;
+      build_meshes(c, st, b.meshes, os, [&](const std::vector<size_t>& done) {
+        for (size_t i : done) {
+          if (infos) fill_info(b.meshes[i], &infos[i]);
+          if (sink(user, i, OOC_STREAM_END, nullptr, 0) != 0) fail(OOC_ERR_SINK, "sink returned an error");
         }
-      }
-      build_meshes(c, st, meshes, false, [&](size_t i) {
-        if (infos) fill_info(meshes[i], &infos[i]);
-        if (sink(user, i, OOC_STREAM_END, nullptr, 0) != 0) fail(OOC_ERR_SINK, "sink returned an error");
       });
     }
     ck(cudaStreamSynchronize(st), "build");
     finish_timing(c);
   });
+}
+
+int ooc_build_batch_device(ooc_ctx* c, const ooc_mesh* meshes_in, uint64_t n_meshes, ooc_alloc_fn alloc,
+                           ooc_ready_fn ready, void* user, ooc_build_info* infos) {
+  return guarded(c, [&] {
+    begin_build(c);
+    if (!alloc) fail(OOC_ERR_INVALID, "alloc is NULL");
+    cudaStream_t st = c->own_stream;
+    BatchInput b(c, meshes_in, n_meshes, true);
+    OutSpec os;
+    os.mode = OUT_DEST;
+    os.alloc = alloc;
+    os.ready = ready;
+    os.user = user;
+    {
+      PhaseScope all(c, PH_ALL, st);
+      b.upload(c, meshes_in, st);
+      // records written on the host (levels above the stripes, header records,
+      // the root) land in the destinations by one scatter per group of meshes
+      build_meshes(c, st, b.meshes, os, [&](const std::vector<size_t>& done) {
+        std::vector<uint64_t> nrec, drec;
+        for (size_t i : done) {
+          MeshWork& m = b.meshes[i];
+          alloc_through(c, c->copy_stream, b.meshes, i, os);  // a mesh without items gets its destination here
+          if (m.top.node_pos != m.total_nodes || m.top.data_pos != m.total_data)
+            fail(OOC_ERR_DEVICE, "internal size mismatch for mesh " + std::to_string(i));
+          Emitter& e = b.outs[i];
+          const uint64_t dn = reinterpret_cast<uintptr_t>(m.dst_nodes), dd = reinterpret_cast<uintptr_t>(m.dst_data);
+          for (size_t r = 0; r < e.node_recs.size(); r += 4) {
+            if (e.node_recs[r] >= m.total_nodes) fail(OOC_ERR_DEVICE, "internal node record position");
+            nrec.insert(nrec.end(), {dn + e.node_recs[r] * 24, e.node_recs[r + 1], e.node_recs[r + 2], e.node_recs[r + 3]});
+          }
+          for (size_t r = 0; r < e.data_recs.size(); r += 5) {
+            if (e.data_recs[r] >= m.total_data) fail(OOC_ERR_DEVICE, "internal data record position");
+            drec.insert(drec.end(), {dd + e.data_recs[r] * 32, e.data_recs[r + 1], e.data_recs[r + 2],
+                                     e.data_recs[r + 3], e.data_recs[r + 4]});
+          }
+          std::vector<uint64_t>().swap(e.node_recs);
+          std::vector<uint64_t>().swap(e.data_recs);
+          if (infos) fill_info(m, &infos[i]);
+        }
+        const size_t words = nrec.size() + drec.size();
+        if (words) {
+          uint64_t* h = ensure_pinned<uint64_t>(c->h_recs, words * 8);
+          std::memcpy(h, nrec.data(), nrec.size() * 8);
+          std::memcpy(h + nrec.size(), drec.data(), drec.size() * 8);
+          uint64_t* d = ensure<uint64_t>(c->d_recs, words * 8);
+          ck(cudaMemcpyAsync(d, h, words * 8, cudaMemcpyHostToDevice, c->copy_stream), "records");
+          launch_scatter_to(d, nrec.size() / 4, 3, c->copy_stream);
+          launch_scatter_to(d + nrec.size(), drec.size() / 5, 4, c->copy_stream);
+        }
+        // the meshes' stripes were finished before their sub-batch's event; the scatter is this stream's
+        ck(cudaStreamSynchronize(c->copy_stream), "records");
+        ck(cudaGetLastError(), "scatter");
+        if (ready)
+          for (size_t i : done)
+            if (ready(user, i) != 0) fail(OOC_ERR_SINK, "ready callback returned an error");
+      });
+    }
+    ck(cudaStreamSynchronize(st), "build");
+    finish_timing(c);
+  });
+}
+
+int ooc_set_batch_budget(ooc_ctx* c, uint64_t bytes) {
+  if (!c || bytes < 4096) return OOC_ERR_INVALID;
+  c->batch_budget_bytes = bytes;
+  return OOC_OK;
+}
+
+uint64_t ooc_batch_budget(const ooc_ctx* c) { return c ? c->batch_budget_bytes : 0; }
+
+int ooc_arena_alloc(void* arena, uint64_t mesh, uint64_t nodes_bytes, uint64_t data_bytes, void* stream,
+                    void** nodes, void** data) {
+  (void)mesh;
+  (void)stream;
+  ooc_device_arena* a = static_cast<ooc_device_arena*>(arena);
+  if (!a || !nodes || !data) return OOC_ERR_INVALID;
+  const uint64_t n = (nodes_bytes + 255) / 256 * 256, d = (data_bytes + 255) / 256 * 256;
+  if (a->used + n + d > a->capacity) return OOC_ERR_OOM;
+  char* base = static_cast<char*>(a->base) + a->used;
+  *nodes = base;
+  *data = base + n;
+  a->used += n + d;
+  return OOC_OK;
 }
 
 int ooc_build_device(ooc_ctx* c, const ooc_build_params* prm, const float* tris_device, uint64_t n_tris,
@@ -1280,7 +1466,9 @@ int ooc_build_device(ooc_ctx* c, const ooc_build_params* prm, const float* tris_
     meshes[0].n_tris = n_tris;
     {
       PhaseScope all(c, PH_ALL, st);
-      build_meshes(c, st, meshes, true);
+      OutSpec os;
+      os.mode = OUT_CTX;
+      build_meshes(c, st, meshes, os);
       finish_device_output(c, st, meshes[0], out);
     }
     ck(cudaStreamSynchronize(st), "build");

@@ -116,6 +116,7 @@ void launch_vox_large(const VoxJob& j, int pass, cudaStream_t st, int num_sms);
 
 // src holds n entries of (index, `words` u64 values); dst[index*words + q] = value q.
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st);
+void launch_scatter_to(const uint64_t* src, uint64_t n, int words, cudaStream_t st);
 
 // ---- batched launches: per-stripe jobs in device arrays; `cta_beg` (n + 1 entries) maps CTAs to stripes ----
 // `single` (may be NULL): the job of a one-stripe launch, passed as a kernel parameter.

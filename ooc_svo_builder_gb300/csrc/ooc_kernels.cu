@@ -812,6 +812,15 @@ __global__ void k_scatter_records(const uint64_t* __restrict__ src, uint64_t n, 
   for (int q = 0; q < words; q++) d[q] = s[1 + q];
 }
 
+// Records with their own destination: src[i] = {address, words...}.
+__global__ void k_scatter_to(const uint64_t* __restrict__ src, uint64_t n, int words) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t* s = src + i * (1 + words);
+  uint64_t* d = reinterpret_cast<uint64_t*>(s[0]);
+  for (int q = 0; q < words; q++) d[q] = s[1 + q];
+}
+
 // ===========================================================================
 // Batched forms: every stripe of a batch in one launch.  A chunk table gives
 // each CTA one stripe and a run of at most kChunk elements; the CTA copies that
@@ -1090,6 +1099,12 @@ void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t
   if (n == 0) return;
   KScope k("scatter_records", st);
   k_scatter_records<<<grid_for(n, 128), 128, 0, st>>>(src, n, words, dst);
+}
+
+void launch_scatter_to(const uint64_t* src, uint64_t n, int words, cudaStream_t st) {
+  if (n == 0) return;
+  KScope k("scatter_records", st);
+  k_scatter_to<<<grid_for(n, 128), 128, 0, st>>>(src, n, words);
 }
 
 // ---- batched launch wrappers ----

@@ -3,16 +3,20 @@
 //
 // Each engine is a library context with its own streams.  An engine that is
 // free takes every queued request that fits the remaining memory budget (up to
-// max_batch) and builds them with one ooc_build_batch call; requests that
-// arrive meanwhile wait for the next free engine.  With two or more engines,
-// one batch's device work overlaps the next batch's, and each batch's copies
-// overlap its own sub-batches' compute.  Results stay in host memory until the
-// caller releases them.  The server uses only the public C ABI.
+// max_batch) and builds them with one batch call; requests that arrive
+// meanwhile wait for the next free engine.  With two or more engines, one
+// batch's device work overlaps the next batch's.  A request completes as soon
+// as its own mesh does.  Results either come back to host memory (through the
+// library's copy-back ring) or stay resident in device memory, allocated
+// stream-ordered from the device's memory pool, until the caller releases
+// them.  Apart from that allocation the server uses only the public C ABI.
+#include <cuda_runtime.h>
+
 #include <algorithm>
 #include <chrono>
-#include <cstdlib>
 #include <cmath>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -54,7 +58,10 @@ struct Request {
   uint64_t id = 0;
   ooc_mesh mesh;
   uint64_t footprint = 0;
-  Bytes nodes, data;
+  Bytes nodes, data;                          // host results
+  void* d_nodes = nullptr;                    // device results
+  void* d_data = nullptr;
+  uint64_t d_nodes_bytes = 0, d_data_bytes = 0;
   ooc_build_info info;
   int32_t status = OOC_OK;
   double t_submit = 0, t_start = 0, t_done = 0;
@@ -113,13 +120,14 @@ struct ooc_server {
   ooc_server_config cfg;
   std::vector<ooc_ctx*> engines;
   std::vector<std::thread> threads;
+  cudaStream_t release_stream = nullptr;  // device results are freed on it
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Request*> queue;
   std::deque<Request*> done;
   std::unordered_map<uint64_t, Request*> held;  // polled, not yet released
   uint64_t next_id = 1;
-  uint64_t in_flight = 0;
+  uint64_t in_flight = 0;  // admitted footprints, plus device results not yet released
   bool stop = false;
   Clock::time_point t0 = Clock::now();
 
@@ -134,6 +142,7 @@ struct ooc_server {
       std::lock_guard<std::mutex> lk(mu);
       r->status = status;
       r->t_done = now_us();
+      if (status == OOC_OK) in_flight += r->d_nodes_bytes + r->d_data_bytes;  // held until released
       done.push_back(r);
     }
     cv_done.notify_all();
@@ -147,20 +156,50 @@ struct ooc_server {
     std::vector<size_t> index;
   };
 
+  static void mark(Call& call, uint64_t mesh) {
+    Request* r = call.reqs[mesh];
+    r->info = call.infos[mesh];
+    (*call.published)[call.index[mesh]] = 1;
+    call.s->publish(r, OOC_OK);
+  }
+
   static int sink(void* user, uint64_t mesh, int32_t kind, const void* bytes, uint64_t n) {
     Call& call = *static_cast<Call*>(user);
     Request* r = call.reqs[mesh];
     if (kind == OOC_STREAM_END) {
-      r->info = call.infos[mesh];
-      (*call.published)[call.index[mesh]] = 1;
-      call.s->publish(r, OOC_OK);
+      mark(call, mesh);
       return 0;
     }
     Bytes& dst = kind == OOC_STREAM_NODES ? r->nodes : r->data;
     return dst.append(bytes, n) ? 0 : 1;
   }
 
-  // One ooc_build_batch call over batch[index...]; each request is published when its mesh completes.
+  static int alloc(void* user, uint64_t mesh, uint64_t nodes_bytes, uint64_t data_bytes, void* stream, void** nodes,
+                   void** data) {
+    Call& call = *static_cast<Call*>(user);
+    Request* r = call.reqs[mesh];
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaMallocAsync(&r->d_nodes, nodes_bytes, st) != cudaSuccess) return 1;
+    if (cudaMallocAsync(&r->d_data, data_bytes, st) != cudaSuccess) return 1;
+    r->d_nodes_bytes = nodes_bytes;
+    r->d_data_bytes = data_bytes;
+    *nodes = r->d_nodes;
+    *data = r->d_data;
+    return 0;
+  }
+
+  static int ready(void* user, uint64_t mesh) {
+    mark(*static_cast<Call*>(user), mesh);
+    return 0;
+  }
+
+  void free_device(Request* r) {
+    if (r->d_nodes) cudaFreeAsync(r->d_nodes, release_stream);
+    if (r->d_data) cudaFreeAsync(r->d_data, release_stream);
+    r->d_nodes = r->d_data = nullptr;
+  }
+
+  // One batch call over batch[index...]; each request is published when its mesh completes.
   int run(ooc_ctx* ctx, const std::vector<Request*>& batch, const std::vector<size_t>& index,
           std::vector<char>& published) {
     Call call{this, {}, std::vector<ooc_build_info>(index.size()), &published, index};
@@ -172,10 +211,28 @@ struct ooc_server {
       r->nodes.clear();
       r->data.clear();
     }
-    return ooc_build_batch(ctx, meshes.data(), meshes.size(), &ooc_server::sink, &call, call.infos.data());
+    int rc;
+    if (cfg.result_location == OOC_RESULT_DEVICE) {
+      rc = ooc_build_batch_device(ctx, meshes.data(), meshes.size(), &ooc_server::alloc, &ooc_server::ready, &call,
+                                  call.infos.data());
+      if (rc != OOC_OK) {
+        // the failed call may have left writes queued into the destinations
+        cudaSetDevice(cfg.device);
+        cudaDeviceSynchronize();
+        for (size_t i = 0; i < index.size(); i++)
+          if (!published[index[i]]) {
+            free_device(call.reqs[i]);
+            call.reqs[i]->d_nodes_bytes = call.reqs[i]->d_data_bytes = 0;
+          }
+      }
+    } else {
+      rc = ooc_build_batch(ctx, meshes.data(), meshes.size(), &ooc_server::sink, &call, call.infos.data());
+    }
+    return rc;
   }
 
   void engine_loop(ooc_ctx* ctx) {
+    cudaSetDevice(cfg.device);
     for (;;) {
       std::vector<Request*> batch;
       uint64_t taken = 0;
@@ -231,6 +288,7 @@ extern "C" {
 
 int ooc_server_create(const ooc_server_config* cfg, ooc_server** out) {
   if (!cfg || !out || cfg->engines < 1 || cfg->max_batch < 1 || cfg->memory_budget == 0) return OOC_ERR_INVALID;
+  if (cfg->result_location != OOC_RESULT_HOST && cfg->result_location != OOC_RESULT_DEVICE) return OOC_ERR_INVALID;
   *out = nullptr;
   ooc_server* s = new (std::nothrow) ooc_server();
   if (!s) return OOC_ERR_OOM;
@@ -244,6 +302,18 @@ int ooc_server_create(const ooc_server_config* cfg, ooc_server** out) {
       return rc;
     }
     s->engines.push_back(c);
+  }
+  if (cfg->result_location == OOC_RESULT_DEVICE) {
+    // keep freed result memory in the pool instead of returning it to the driver at every synchronisation
+    cudaMemPool_t pool;
+    uint64_t keep = ~0ull;
+    if (cudaSetDevice(cfg->device) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, cfg->device) != cudaSuccess ||
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->release_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      for (ooc_ctx* e : s->engines) ooc_ctx_destroy(e);
+      delete s;
+      return OOC_ERR_DEVICE;
+    }
   }
   for (ooc_ctx* c : s->engines) s->threads.emplace_back([s, c] { s->engine_loop(c); });
   *out = s;
@@ -283,15 +353,46 @@ int ooc_server_poll(ooc_server* s, int32_t timeout_ms, ooc_result* out) {
   std::memset(out, 0, sizeof(*out));
   out->id = r->id;
   out->status = r->status;
-  out->nodes = r->nodes.p;
-  out->nodes_bytes = r->nodes.n;
-  out->data = r->data.p;
-  out->data_bytes = r->data.n;
+  out->location = s->cfg.result_location;
+  if (s->cfg.result_location == OOC_RESULT_DEVICE) {
+    out->nodes = r->d_nodes;
+    out->nodes_bytes = r->status == OOC_OK ? r->d_nodes_bytes : 0;
+    out->data = r->d_data;
+    out->data_bytes = r->status == OOC_OK ? r->d_data_bytes : 0;
+  } else {
+    out->nodes = r->nodes.p;
+    out->nodes_bytes = r->nodes.n;
+    out->data = r->data.p;
+    out->data_bytes = r->data.n;
+  }
   out->info = r->info;
   out->t_submit_us = r->t_submit;
   out->t_start_us = r->t_start;
   out->t_done_us = r->t_done;
   out->batch_size = r->batch_size;
+  return OOC_OK;
+}
+
+int ooc_server_read(ooc_server* s, uint64_t id, void* nodes_host, void* data_host) {
+  if (!s) return OOC_ERR_INVALID;
+  Request* r = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->held.find(id);
+    if (it == s->held.end()) return OOC_ERR_INVALID;
+    r = it->second;
+  }
+  if (r->status != OOC_OK) return r->status;
+  if (s->cfg.result_location == OOC_RESULT_DEVICE) {
+    if (cudaSetDevice(s->cfg.device) != cudaSuccess) return OOC_ERR_DEVICE;
+    if (nodes_host && cudaMemcpy(nodes_host, r->d_nodes, r->d_nodes_bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return OOC_ERR_DEVICE;
+    if (data_host && cudaMemcpy(data_host, r->d_data, r->d_data_bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return OOC_ERR_DEVICE;
+  } else {
+    if (nodes_host) std::memcpy(nodes_host, r->nodes.p, r->nodes.n);
+    if (data_host) std::memcpy(data_host, r->data.p, r->data.n);
+  }
   return OOC_OK;
 }
 
@@ -304,8 +405,14 @@ int ooc_server_release(ooc_server* s, uint64_t id) {
     if (it == s->held.end()) return OOC_ERR_INVALID;
     r = it->second;
     s->held.erase(it);
+    if (r->status == OOC_OK) s->in_flight -= r->d_nodes_bytes + r->d_data_bytes;
+  }
+  if (r->d_nodes || r->d_data) {
+    cudaSetDevice(s->cfg.device);
+    s->free_device(r);
   }
   delete r;
+  s->cv_work.notify_all();
   return OOC_OK;
 }
 
@@ -320,8 +427,19 @@ void ooc_server_destroy(ooc_server* s) {
   s->cv_work.notify_all();
   for (std::thread& t : s->threads) t.join();
   for (ooc_ctx* c : s->engines) ooc_ctx_destroy(c);
-  for (Request* r : s->done) delete r;
-  for (auto& kv : s->held) delete kv.second;
+  if (s->release_stream) cudaSetDevice(s->cfg.device);
+  for (Request* r : s->done) {
+    s->free_device(r);
+    delete r;
+  }
+  for (auto& kv : s->held) {
+    s->free_device(kv.second);
+    delete kv.second;
+  }
+  if (s->release_stream) {
+    cudaStreamSynchronize(s->release_stream);
+    cudaStreamDestroy(s->release_stream);
+  }
   delete s;
 }
 

@@ -55,3 +55,33 @@ def test_batch_split_into_sub_batches(builder):
     for i, (t, r) in enumerate(zip(meshes, results)):
         nodes, data, _ = pyoracle.build(t, 256, 2048 if i % 3 else 2)
         assert not octree.diff(r.tree, octree.Octree(256, nodes, data))
+
+
+def test_batch_device_matches_single_mesh_builds(builder):
+    # octrees written straight into device memory equal the oracle's, mesh by mesh
+    meshes, params, args = mixed_meshes(seed=6, count=32)
+    results = builder.build_batch_device(meshes, params)
+    for t, r, a in zip(meshes, results, args):
+        nodes, data, info = pyoracle.build(t, a["gridsize"], a["memory_limit_mb"], color=a["color"],
+                                           levels=a["levels"])
+        d = octree.diff(r.tree, octree.Octree(a["gridsize"], nodes, data))
+        assert not d, "\n".join(d)
+        assert r.info["n_filled"] == info["n_filled"]
+
+
+def test_batch_device_meshes_straddling_sub_batches(builder):
+    # a small pyramid budget splits meshes across sub-batches: their early
+    # stripes wait in the carry buffers until the mesh's destination exists
+    meshes = [tri.random_tris(400, 900 + i, i % 2 == 1, max_edge=0.3) for i in range(5)]
+    params = [make_params(256, 2, geometry_only=(i % 2 == 0), levels=(i == 3)) for i in range(5)]
+    old = builder.batch_budget()
+    try:
+        builder.set_batch_budget(700_000)  # two 128^3 stripes (300 KB of pyramid each) per sub-batch
+        results = builder.build_batch_device(meshes, params)
+        host = builder.build_batch(meshes, params)
+    finally:
+        builder.set_batch_budget(old)
+    for i, (t, r) in enumerate(zip(meshes, results)):
+        nodes, data, _ = pyoracle.build(t, 256, 2, levels=(i == 3))
+        assert not octree.diff(r.tree, octree.Octree(256, nodes, data))
+        assert not octree.diff(host[i].tree, r.tree)

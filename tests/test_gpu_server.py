@@ -31,10 +31,11 @@ def request_mix(seed=9, count=40):
     return out
 
 
-def test_results_alone_equal_results_in_the_mix(builder):
+@pytest.mark.parametrize("resident", [False, True], ids=["host", "device"])
+def test_results_alone_equal_results_in_the_mix(builder, resident):
     reqs = request_mix()
     alone = [builder.build(t, p).tree for t, p in reqs]
-    with ooc.Server(0, engines=2, max_batch=16, memory_budget=8 << 30) as srv:
+    with ooc.Server(0, engines=2, max_batch=16, memory_budget=8 << 30, resident=resident) as srv:
         ids = [srv.submit(t, p) for t, p in reqs]
         got = {}
         deadline = time.time() + 120
@@ -47,16 +48,18 @@ def test_results_alone_equal_results_in_the_mix(builder):
     for rid, want in zip(ids, alone):
         r = got[rid]
         assert r["status"] == 0
+        assert r["location"] == (1 if resident else 0)
         d = octree.diff(r["tree"], want)
         assert not d, "\n".join(d)
         assert r["t_submit_us"] <= r["t_start_us"] <= r["t_done_us"]
 
 
-def test_arrivals_while_busy_join_later_batches(builder):
+@pytest.mark.parametrize("resident", [False, True], ids=["host", "device"])
+def test_arrivals_while_busy_join_later_batches(builder, resident):
     # a submitting thread keeps adding requests while the engines are running
     reqs = request_mix(seed=11, count=30)
     alone = [builder.build(t, p).tree for t, p in reqs]
-    with ooc.Server(0, engines=2, max_batch=8, memory_budget=8 << 30) as srv:
+    with ooc.Server(0, engines=2, max_batch=8, memory_budget=8 << 30, resident=resident) as srv:
         ids = [None] * len(reqs)
 
         def feed():

@@ -9,7 +9,8 @@ def test_server_create_rejects_bad_config():
     h = ctypes.c_void_p()
     for cfg in (ooc.ServerConfig(0, 0, 8, 0, 1 << 30),   # no engines
                 ooc.ServerConfig(0, 1, 0, 0, 1 << 30),   # batches of zero requests
-                ooc.ServerConfig(0, 1, 8, 0, 0)):        # no memory budget
+                ooc.ServerConfig(0, 1, 8, 0, 0),         # no memory budget
+                ooc.ServerConfig(0, 1, 8, 2, 1 << 30)):  # unknown result location
         assert lib.ooc_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
     assert lib.ooc_server_create(None, ctypes.byref(h)) == 1
 
@@ -22,6 +23,7 @@ def test_server_calls_reject_null():
     assert lib.ooc_server_submit(None, ctypes.byref(m), ctypes.byref(rid)) == 1
     assert lib.ooc_server_poll(None, 0, ctypes.byref(r)) == 1
     assert lib.ooc_server_release(None, 1) == 1
+    assert lib.ooc_server_read(None, 1, None, None) == 1
     lib.ooc_server_destroy(None)
 
 
