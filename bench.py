@@ -49,6 +49,9 @@ WORKLOADS = {
                      desc="configuration 3: svo_builder_binary -s 4096 -l 2048 (64 partitions) on a 20M-triangle "
                           "soup: half small triangles on 200 spheres, half log-normal edges (median 4 voxels, "
                           "sigma 1.0, clipped at 512)"),
+    "soup1024": dict(gridsize=1024, limit=2048, payload=False, color="model",
+                     desc="profiling case of the configuration-3 soup: svo_builder_binary -s 1024 -l 2048 (one "
+                          "partition) on a 4M-triangle soup of the same distribution"),
 }
 
 
@@ -59,6 +62,8 @@ def make_mesh(name: str) -> np.ndarray:
         return tri.icosphere_tris(5, radius=0.4, jitter=0.002, seed=1)
     if name == "soup4096":
         return tri.soup_tris(20_000_000, 4096, seed=3, sigma=1.0)
+    if name == "soup1024":
+        return tri.soup_tris(4_000_000, 1024, seed=3, sigma=1.0)
     raise SystemExit("unknown workload " + name)
 
 
@@ -368,6 +373,16 @@ def run_batch(args, world, rank, local):
         b.build_batch_device_ptrs(arr, n, arena, dinfos)
     t_batch_dev = timed(batch_dev, max(1, args.warmup), args.steps)
     launches_dev = b.kernel_launches()
+    # one more call with CUDA-event phase and per-kernel timing (not part of the timed steps)
+    b.set_phase_timing(True)
+    b.set_kernel_timing("*")
+    t0 = time.perf_counter()
+    batch_dev()
+    wall_dev = time.perf_counter() - t0
+    phases_dev = b.phase_times()
+    kernels_dev = {k: round(v[0], 3) for k, v in sorted(b.kernel_times().items(), key=lambda kv: -kv[1][0])}
+    b.set_phase_timing(False)
+    b.set_kernel_timing(None)
     one = (ooc.Mesh * 1)()
 
     def plain_dev():
@@ -417,7 +432,8 @@ def run_batch(args, world, rank, local):
                    "l2": "inputs larger than L2 (%.1f GB of triangles per step)" % (offs[-1] / 1e9)},
         "mtri_per_s": total_tris / t_batch_dev / 1e6, "svo_nodes_per_s": n_nodes / t_batch_dev,
         "resident": {"batched_meshes_per_s": n / t_batch_dev, "plain_meshes_per_s": n / t_plain_dev,
-                     "speedup_vs_plain": t_plain_dev / t_batch_dev},
+                     "speedup_vs_plain": t_plain_dev / t_batch_dev,
+                     "timed_call": {"wall_ms": wall_dev * 1e3, "phases_ms": phases_dev, "kernels_ms": kernels_dev}},
         "host": {"batched_meshes_per_s": n / t_batch, "plain_meshes_per_s": n / t_plain,
                  "speedup_vs_plain": t_plain / t_batch},
         "parity_sample": {"meshes": len(sample), "host_identical_to_plain": identical,

@@ -138,6 +138,8 @@ struct ooc_ctx {
   D2HRing ring[2][2];  // [slot][OOC_STREAM_NODES / OOC_STREAM_DATA]
   cudaEvent_t ev_compute[2] = {nullptr, nullptr};
   cudaStream_t copy_stream = nullptr;
+  cudaStream_t h2d_stream = nullptr;     // batch uploads, overlapping the sub-batches that do not need them yet
+  std::vector<cudaEvent_t> up_events;    // recorded on h2d_stream as groups of meshes arrive
   DevBuf d_tables1, d_tables2;
   std::vector<DevBuf> d_mesh_items;
   uint64_t batch_budget_bytes = 4ull << 30;  // occupancy pyramids of one sub-batch
@@ -433,6 +435,7 @@ struct MeshWork {
   uint64_t filled = 0;
   uint64_t n_items = 0;
   int64_t last_stripe = -1;  // last stripe with items (-1: none)
+  cudaEvent_t uploaded = nullptr;  // the triangles are on the device once this has completed (null: already)
   uint64_t index = 0;        // in the batch
   // caller-owned device destination (output to device destinations)
   void* dst_nodes = nullptr;
@@ -449,6 +452,7 @@ struct MeshWork {
       : prm(o.prm), pl(o.pl), d_tris(o.d_tris), n_tris(o.n_tris), part_off(std::move(o.part_off)), items(o.items),
         out(o.out), top(o.top), next_stripe(o.next_stripe), dry(o.dry), layout(o.layout),
         layout_next(o.layout_next), filled(o.filled), n_items(o.n_items), last_stripe(o.last_stripe),
+        uploaded(o.uploaded),
         index(o.index), dst_nodes(o.dst_nodes), dst_data(o.dst_data), dst_ready(o.dst_ready),
         total_nodes(o.total_nodes), total_data(o.total_data), carried_nodes(o.carried_nodes),
         carried_data(o.carried_data) {}
@@ -851,7 +855,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   for (int l = 0; l <= max_depth; l++)
     cp_td[l] = cta_prefix(n, [&](uint32_t s) -> uint64_t {
       const int last_top = std::min(ej[s].l_small, pyr[s].depth - 2);
-      return (live(s) && l > last_top && l <= pyr[s].depth - 2) ? pyr[s].lv[l].n : 0;
+      return (live(s) && l > last_top && l <= pyr[s].depth - 2) ? pyr[s].lv[l + 1].n : 0;  // one thread per child
     });
   Uploader up2;
   const size_t o_vj2 = up2.add(vj.data(), n * sizeof(VoxJob));
@@ -1017,8 +1021,12 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, co
   if (c->d_mesh_items.size() < meshes.size()) c->d_mesh_items.resize(meshes.size());
   for (size_t i = 0; i < meshes.size(); i++) {
     MeshWork& m = meshes[i];
-    if (m.pl.P > 1) bin_mesh(c, st, m, c->d_mesh_items[i]);
-    else m.n_items = m.n_tris;
+    if (m.pl.P > 1) {
+      if (m.uploaded) ck(cudaStreamWaitEvent(st, m.uploaded, 0), "wait upload");
+      bin_mesh(c, st, m, c->d_mesh_items[i]);
+    } else {
+      m.n_items = m.n_tris;
+    }
     // data file header records (OctreeBuilder.cpp:22-28)
     float zero[6] = {0, 0, 0, 0, 0, 0};
     m.out->data(m.top.data_pos++, 0, zero);
@@ -1055,6 +1063,8 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, co
   int k = 0;
   // launch sub-batch k, then finish k-1 while k computes
   auto flush = [&]() {
+    // uploads arrive in mesh order: the sub-batch's last mesh being there covers the others
+    if (meshes[sb.back().mesh].uploaded) ck(cudaStreamWaitEvent(st, meshes[sb.back().mesh].uploaded, 0), "wait upload");
     run_sub_batch(c, st, meshes, sb, os, pend[k & 1], k & 1);
     if (os.mode == OUT_CTX) finish_sub_batch(c, meshes, pend[k & 1], os);
     else finish_sub_batch(c, meshes, pend[(k + 1) & 1], os);
@@ -1158,6 +1168,7 @@ void begin_build(ooc_ctx* c) {
   ck(cudaSetDevice(c->device), "cudaSetDevice");
   // a build that failed part-way may have left copies queued into the staging buffers
   ck(cudaStreamSynchronize(c->copy_stream), "cudaStreamSynchronize");
+  ck(cudaStreamSynchronize(c->h2d_stream), "cudaStreamSynchronize");
   c->err.clear();
   c->marks.clear();
   c->kmarks.clear();
@@ -1212,6 +1223,7 @@ int ooc_ctx_create(int32_t device, ooc_ctx** out) {
       cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->h2d_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_compute[0], cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_compute[1], cudaEventDisableTiming) != cudaSuccess) {
     delete c;
@@ -1226,6 +1238,7 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   cudaSetDevice(c->device);
   if (c->own_stream) cudaStreamSynchronize(c->own_stream);
   if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+  if (c->h2d_stream) cudaStreamSynchronize(c->h2d_stream);
   DevBuf* bufs[] = {&c->d_tris, &c->d_items, &c->d_hist, &c->d_axis, &c->d_bits, &c->d_scan, &c->d_scanpart,
                     &c->d_keys, &c->d_size, &c->d_dsize, &c->d_start, &c->d_dstart, &c->d_cache, &c->d_winners,
                     &c->d_taskoff, &c->d_taskpart, &c->d_counter, &c->d_nodes, &c->d_data, &c->d_recs,
@@ -1247,6 +1260,8 @@ void ooc_ctx_destroy(ooc_ctx* c) {
     if (c->ev_compute[i]) cudaEventDestroy(c->ev_compute[i]);
   }
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  if (c->h2d_stream) cudaStreamDestroy(c->h2d_stream);
+  for (cudaEvent_t e : c->up_events) cudaEventDestroy(e);
   if (c->d_tables1.p) cudaFree(c->d_tables1.p);
   if (c->d_tables2.p) cudaFree(c->d_tables2.p);
   for (DevBuf& b : c->d_mesh_items)
@@ -1329,10 +1344,30 @@ struct BatchInput {
     }
   }
   static uint64_t bytes(const ooc_mesh& m) { return m.n_tris * (m.params.geometry_only ? 9 : 21) * 4; }
+  // Queue the uploads on the context's upload stream, with an event after
+  // every group of about 16 MB, so each sub-batch waits only for its meshes.
   void upload(ooc_ctx* c, const ooc_mesh* in, cudaStream_t st) {
-    PhaseScope ph(c, PH_COPY, st);
-    for (size_t i = 0; i < meshes.size(); i++)
-      if (bytes(in[i])) ck(cudaMemcpyAsync(d_all + off[i], in[i].tris, bytes(in[i]), cudaMemcpyHostToDevice, st), "H2D");
+    ck(cudaEventRecord(c->ev_compute[0], st), "event");  // the device buffer is free once earlier work on st is done
+    ck(cudaStreamWaitEvent(c->h2d_stream, c->ev_compute[0], 0), "wait");
+    PhaseScope ph(c, PH_COPY, c->h2d_stream);
+    size_t used = 0, group = 0;
+    uint64_t acc = 0;
+    for (size_t i = 0; i < meshes.size(); i++) {
+      if (bytes(in[i]))
+        ck(cudaMemcpyAsync(d_all + off[i], in[i].tris, bytes(in[i]), cudaMemcpyHostToDevice, c->h2d_stream), "H2D");
+      acc += bytes(in[i]);
+      if (acc >= (16ull << 20) || i + 1 == meshes.size()) {
+        if (used == c->up_events.size()) {
+          cudaEvent_t e;
+          ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+          c->up_events.push_back(e);
+        }
+        cudaEvent_t e = c->up_events[used++];
+        ck(cudaEventRecord(e, c->h2d_stream), "event");
+        for (; group <= i; group++) meshes[group].uploaded = e;
+        acc = 0;
+      }
+    }
   }
 };
 }  // namespace

@@ -208,4 +208,53 @@ __device__ __forceinline__ float plane_xy(const TriSetup& s, float px, float py)
   return __fadd_rn(__fmul_rn(s.n[0], px), __fmul_rn(s.n[1], py));
 }
 
+// The whole per-voxel test of voxelizer.cpp:266-287 at one voxel corner.
+__device__ __forceinline__ bool pass_voxel(const TriSetup& s, float px, float py, float pz) {
+  return pass_xy(s, px, py) && pass_z(s, plane_xy(s, px, py), px, py, pz);
+}
+
+// The projection tests that do not depend on x (YZ) and on y (ZX).
+__device__ __forceinline__ bool pass_yz(const TriSetup& s, float py, float pz) {
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    if (__fadd_rn(dot2(s.yz[k][0], s.yz[k][1], py, pz), s.dyz[k]) < 0.0f) return false;
+  return true;
+}
+__device__ __forceinline__ bool pass_zx(const TriSetup& s, float pz, float px) {
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    if (__fadd_rn(dot2(s.zx[k][0], s.zx[k][1], pz, px), s.dzx[k]) < 0.0f) return false;
+  return true;
+}
+
+// Where the plane test of voxel p stands along axis w, whose normal component is nw:
+// 0 it passes, -1 the passing run lies at larger w, +1 at smaller w.  Every
+// operand of the test is a rounded sum or product of one monotone input, so
+// along any line the rounded plane value moves monotonically with the sign of
+// nw, the two offsets keep their order, and the passing voxels form one run;
+// outside it both factors have the sign that says which side it is on.
+__device__ __forceinline__ int plane_side(const TriSetup& s, float px, float py, float pz, float nw) {
+  const float nDOTp = __fadd_rn(plane_xy(s, px, py), __fmul_rn(s.n[2], pz));
+  const float a = __fadd_rn(nDOTp, s.d1), b = __fadd_rn(nDOTp, s.d2);
+  if (!(__fmul_rn(a, b) > 0.0f)) return 0;
+  return ((a > 0.0f) == (nw > 0.0f)) ? 1 : -1;
+}
+
+// True when the monotone-run argument above holds for this triangle: every
+// constant of the test finite and small enough that no sum or product of the
+// test overflows or turns into NaN (voxel coordinates are below 2^60 too).
+__device__ __forceinline__ bool monotone_setup(const TriSetup& s, float coord_max) {
+  const float lim = 1.0e18f;
+  bool ok = fabsf(s.d1) < lim && fabsf(s.d2) < lim && coord_max < lim;
+#pragma unroll
+  for (int a = 0; a < 3; a++) ok = ok && fabsf(s.n[a]) < lim;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    ok = ok && fabsf(s.xy[k][0]) < lim && fabsf(s.xy[k][1]) < lim && fabsf(s.dxy[k]) < lim;
+    ok = ok && fabsf(s.yz[k][0]) < lim && fabsf(s.yz[k][1]) < lim && fabsf(s.dyz[k]) < lim;
+    ok = ok && fabsf(s.zx[k][0]) < lim && fabsf(s.zx[k][1]) < lim && fabsf(s.dzx[k]) < lim;
+  }
+  return ok;  // NaN fails every comparison
+}
+
 }  // namespace ooc

@@ -355,9 +355,147 @@ __device__ __forceinline__ uint64_t item_triangle(const VoxJob& j, uint64_t i) {
   return j.item_tri ? (uint64_t)j.item_tri[j.ibeg + i] : j.ibeg + i;
 }
 
+// ---------------------------------------------------------------------------
+// Large items walk lines along the axis of their largest normal component.  On
+// every line the voxels that pass the plane test form one run (plane_side), so
+// a line costs its run plus a few probes instead of its whole length; every
+// voxel of the run still gets the complete test, so the result is the
+// reference's candidate loop (voxelizer.cpp:257-305) voxel for voxel.
+// ---------------------------------------------------------------------------
+constexpr int kLinesPerLane = 16;
+constexpr uint64_t kLinesPerTask = 32 * kLinesPerLane;
+
+// Axis of the largest component of cross(e0, e1); the item count and the tasks
+// call this same function, so they agree on the lines of every item.
+__device__ __forceinline__ int walk_axis(const TriVerts& t) {
+  const float e0x = t.v[1][0] - t.v[0][0], e0y = t.v[1][1] - t.v[0][1], e0z = t.v[1][2] - t.v[0][2];
+  const float e1x = t.v[2][0] - t.v[1][0], e1y = t.v[2][1] - t.v[1][1], e1z = t.v[2][2] - t.v[1][2];
+  const float ax = fabsf(e0y * e1z - e0z * e1y), ay = fabsf(e0z * e1x - e0x * e1z), az = fabsf(e0x * e1y - e0y * e1x);
+  if (az >= ax && az >= ay) return 2;
+  return ax >= ay ? 0 : 1;
+}
+
+// Lines of a large item: the box extents across the walk axis.
+__device__ __forceinline__ uint64_t item_lines(int W, const int lo[3], const int hi[3]) {
+  const uint64_t ex = (uint64_t)(hi[0] - lo[0] + 1), ey = (uint64_t)(hi[1] - lo[1] + 1),
+                 ez = (uint64_t)(hi[2] - lo[2] + 1);
+  return W == 0 ? ey * ez : (W == 1 ? ex * ez : ex * ey);
+}
+
+// One line of a large item: pass 0 sets its bits, pass 1 offers the triangle
+// to every voxel it passes.  `dir` is the sign-carrying slope of the plane
+// value along the line (n_w * u) and `inv_dir` its reciprocal.
+template <int PASS>
+__device__ __forceinline__ void vox_line(const VoxJob& j, const TriSetup& s, uint32_t tri, int W, int ca, int cb,
+                                         int w0, int w1, bool mono, float dir, float inv_dir) {
+  const float fa = __fmul_rn((float)ca, j.u), fb = __fmul_rn((float)cb, j.u);
+  float px, py, pz;
+  auto corner = [&](int w) {
+    const float fw = __fmul_rn((float)w, j.u);
+    px = W == 0 ? fw : fa;
+    py = W == 1 ? fw : (W == 0 ? fa : fb);
+    pz = W == 2 ? fw : fb;
+  };
+  corner(w0);
+  // the projection test that does not depend on the walk coordinate
+  if (!(W == 2 ? pass_xy(s, px, py) : (W == 0 ? pass_yz(s, py, pz) : pass_zx(s, pz, px)))) return;
+  // the two that do (with the plane test they complete the voxel test)
+  auto rest = [&]() {
+    return W == 2 ? (pass_yz(s, py, pz) && pass_zx(s, pz, px))
+                  : (W == 0 ? (pass_xy(s, px, py) && pass_zx(s, pz, px)) : (pass_xy(s, px, py) && pass_yz(s, py, pz)));
+  };
+  // stripe-local Morton bits of the two fixed coordinates; the walk axis adds its own
+  const int sw = W == 0 ? j.sa[0] : (W == 1 ? j.sa[1] : j.sa[2]);
+  const uint32_t la = (uint32_t)(ca - (W == 0 ? j.sa[1] : j.sa[0])), lb = (uint32_t)(cb - (W == 2 ? j.sa[1] : j.sa[2]));
+  const uint32_t mab = W == 0 ? (spread3_10(la) << 1) | (spread3_10(lb) << 2)
+                              : (W == 1 ? spread3_10(la) | (spread3_10(lb) << 2) : spread3_10(la) | (spread3_10(lb) << 1));
+  uint32_t cur_w = 0xffffffffu, acc = 0;
+  auto emit = [&](int w) {
+    const uint32_t m = mab | (spread3_10((uint32_t)(w - sw)) << W);
+    if (PASS == 0) {
+      const uint32_t wd = m >> 5;
+      if (wd != cur_w) {
+        if (acc) atomicOr(&j.leafbits[cur_w], acc);
+        cur_w = wd;
+        acc = 0;
+      }
+      acc |= 1u << (m & 31);
+    } else {
+      atomicMin(&j.winners[leaf_rank(j, m)], tri);  // pass 0 set this voxel's bit
+    }
+  };
+  if (!mono) {  // every voxel of the line, complete test
+    for (int w = w0; w <= w1; w++) {
+      corner(w);
+      if (pass_z(s, plane_xy(s, px, py), px, py, pz) && rest()) emit(w);
+    }
+  } else {
+    auto side = [&](int w) {
+      corner(w);
+      return plane_side(s, px, py, pz, dir);
+    };
+    // start where the plane crosses the line's middle, then find one voxel of the run
+    const float off = (W == 0 ? 0.0f : s.n[0] * px) + (W == 1 ? 0.0f : s.n[1] * py) + (W == 2 ? 0.0f : s.n[2] * pz);
+    float west = -(off + 0.5f * (s.d1 + s.d2)) * inv_dir;
+    west = fminf(fmaxf(west, (float)w0), (float)w1);  // NaN becomes w0
+    int start = (int)west, walk = 0;                   // walk: +1 up only, -1 down only, 0 both ways
+    const int g0 = side(start);
+    if (g0 < 0) {  // the run lies above: first w with side >= 0
+      int lo = start, hi = -1, step = 1;
+      for (;;) {
+        const int nx = min(lo + step, w1);
+        if (side(nx) >= 0) {
+          hi = nx;
+          break;
+        }
+        if (nx == w1) return;
+        lo = nx;
+        step <<= 1;
+      }
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (side(mid) >= 0) hi = mid;
+        else lo = mid;
+      }
+      if (side(hi) != 0) return;  // the run falls between two voxels
+      start = hi;
+      walk = 1;
+    } else if (g0 > 0) {  // below: last w with side <= 0
+      int hi = start, lo = -1, step = 1;
+      for (;;) {
+        const int nx = max(hi - step, w0);
+        if (side(nx) <= 0) {
+          lo = nx;
+          break;
+        }
+        if (nx == w0) return;
+        hi = nx;
+        step <<= 1;
+      }
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (side(mid) <= 0) lo = mid;
+        else hi = mid;
+      }
+      if (side(lo) != 0) return;
+      start = lo;
+      walk = -1;
+    }
+    // px/py/pz hold `start`'s corner and its plane test passed
+    if (rest()) emit(start);
+    if (walk >= 0)
+      for (int w = start + 1; w <= w1 && side(w) == 0; w++)
+        if (rest()) emit(w);
+    if (walk <= 0)
+      for (int w = start - 1; w >= w0 && side(w) == 0; w--)
+        if (rest()) emit(w);
+  }
+  if (PASS == 0 && acc) atomicOr(&j.leafbits[cur_w], acc);
+}
+
 // Pass 0, one thread per item: items with at most small_vol (<= 64) candidates
 // are voxelized here and leave their pass mask; larger ones get a warp-task
-// count (32 columns per task).
+// count (kLinesPerTask lines per task).
 __device__ __forceinline__ void vox_small_occ_item(const VoxJob& j, uint64_t i) {
   const uint64_t t = item_triangle(j, i);
   const TriVerts tv = load_verts(j.tris, t, j.stride);
@@ -381,7 +519,7 @@ __device__ __forceinline__ void vox_small_occ_item(const VoxJob& j, uint64_t i) 
                         ((uint64_t)(lo[2] - j.sa[2]) << 20) | ((bx - 1) << 30) | ((by - 1) << 36) | ((bz - 1) << 42);
       }
     } else {
-      cost = (bx * by + 31) / 32;
+      cost = (item_lines(walk_axis(tv), lo, hi) + kLinesPerTask - 1) / kLinesPerTask;
     }
   }
   j.task_off[i] = cost;
@@ -416,7 +554,7 @@ __global__ void k_vox_small_win(VoxJob j) {
   if (i < j.n_items) vox_small_win_item(j, i);
 }
 
-// Columns 32*k .. 32*k+31 of large item i (one per lane).
+// Lines kLinesPerTask*k .. +kLinesPerTask-1 of large item i (lane, lane+32, ...).
 template <int PASS>
 __device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint64_t k, int lane) {
   if (PASS == 1 && !j.winners) return;  // binary-mode stripe in a mixed batch: no winner pass
@@ -424,20 +562,32 @@ __device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint
   const TriVerts tv = load_verts(j.tris, t, j.stride);
   int lo[3], hi[3];
   if (!item_box(j, tv, lo, hi)) return;  // cannot happen: the task count came from the same box
-  const uint64_t bx = (uint64_t)(hi[0] - lo[0] + 1), by = (uint64_t)(hi[1] - lo[1] + 1);
-  const uint64_t c = k * 32 + (uint64_t)lane;
-  if (c < bx * by) {
-    TriSetup s;
-    tri_setup(tv, j.u, s);
-    const int x = lo[0] + (int)(c % bx);
-    const int y = lo[1] + (int)(c / bx);
-    vox_column<PASS>(j, s, (uint32_t)t, x, y, lo[2], hi[2]);
+  const int W = walk_axis(tv);
+  // lines of one item number at most 1024^2 (a stripe's face): 32-bit arithmetic
+  const uint32_t ea = (uint32_t)(W == 0 ? hi[1] - lo[1] + 1 : hi[0] - lo[0] + 1);  // first axis across the walk
+  const uint32_t lines = (uint32_t)item_lines(W, lo, hi);
+  const uint32_t c0 = (uint32_t)k * (uint32_t)kLinesPerTask + (uint32_t)lane;
+  if (c0 >= lines) return;
+  TriSetup s;
+  tri_setup(tv, j.u, s);
+  const int top = max(hi[0], max(hi[1], hi[2]));
+  const bool mono = monotone_setup(s, fabsf(__fmul_rn((float)(top + 1), j.u)));
+  const float dir = (W == 0 ? s.n[0] : (W == 1 ? s.n[1] : s.n[2])) * j.u;
+  const float inv_dir = 1.0f / dir;
+  const int wlo = W == 0 ? lo[0] : (W == 1 ? lo[1] : lo[2]);
+  const int whi = W == 0 ? hi[0] : (W == 1 ? hi[1] : hi[2]);
+  const int alo = W == 0 ? lo[1] : lo[0], blo = W == 2 ? lo[1] : lo[2];
+#pragma unroll 1
+  for (int q = 0; q < kLinesPerLane; q++) {
+    const uint32_t c = c0 + 32u * q;
+    if (c >= lines) break;
+    vox_line<PASS>(j, s, (uint32_t)t, W, alo + (int)(c % ea), blo + (int)(c / ea), wlo, whi, mono, dir, inv_dir);
   }
 }
 
 // Persistent warps pull 32-column tasks of large items from a global counter.
 template <int PASS>
-__global__ void __launch_bounds__(256) k_vox_large(VoxJob j) {
+__global__ void __launch_bounds__(256, 4) k_vox_large(VoxJob j) {
   const int lane = threadIdx.x & 31;
   const uint64_t total = j.task_off[j.n_items];
   for (;;) {
@@ -752,6 +902,34 @@ __device__ __forceinline__ void top_down_node(const Pyramid& p, const EmitJob& e
   }
 }
 
+// The same for one child: node i of level l+1 (an internal node) finds its
+// parent's run starts and adds its earlier siblings' subtree sizes (siblings
+// are consecutive in the key order), so the launch reads and writes the
+// child level contiguously.
+__device__ __forceinline__ void top_down_child(const Pyramid& p, const EmitJob& e, int l, uint64_t i) {
+  const Level& C = p.lv[l + 1];
+  const uint64_t c = C.koff + i;
+  const uint32_t kc = e.keys[c];
+  const uint32_t pk = kc >> 3;
+  const uint64_t pidx = node_index(p.bits, p.scan, p.lv[l], pk);
+  const uint64_t f = e.first_child[pidx];
+  const uint64_t rank = c - f;
+  const uint32_t pmask = child_mask(p.bits, C, pk);
+  uint64_t run_s = e.start[pidx], run_d = e.dstart[pidx];
+  const uint64_t cb = run_s + (uint64_t)e.size[pidx] - 1 - (uint64_t)__popc(pmask);
+  for (uint64_t q = f; q < c; q++) {
+    run_s += (uint64_t)e.size[q] - 1;
+    run_d += e.dsize[q];
+  }
+  const uint32_t mc = child_mask(p.bits, p.lv[l + 2], kc);
+  const uint64_t szc = e.size[c], dszc = e.dsize[c];
+  e.start[c] = run_s;
+  e.dstart[c] = run_d;
+  const uint64_t di = run_d + dszc - 1;
+  store_node_record(e, cb + rank, e.levels ? di : 0, run_s + szc - 1 - (uint64_t)__popc(mc), child_offsets(mc));
+  if (e.levels) store_data_record(e, di, 0, e.cache + c * 6);
+}
+
 // Leaf records, one thread per leaf: the parent (level depth-1) already knows
 // where its child group and data run start.
 __device__ __forceinline__ void top_down_leaf(const Pyramid& p, const EmitJob& e, uint64_t i) {
@@ -877,7 +1055,7 @@ __global__ void __launch_bounds__(kChunk) kb_vox_small(const VoxJob* __restrict_
 }
 
 template <int PASS>
-__global__ void __launch_bounds__(256) kb_vox_large(const VoxJob* __restrict__ jobs, const uint64_t* __restrict__ item_beg,
+__global__ void __launch_bounds__(256, 4) kb_vox_large(const VoxJob* __restrict__ jobs, const uint64_t* __restrict__ item_beg,
                                                     uint32_t n_stripes, const uint64_t* __restrict__ task_off,
                                                     uint64_t total_items, unsigned long long* counter) {
   const int lane = threadIdx.x & 31;
@@ -974,7 +1152,7 @@ __device__ __forceinline__ void node_op(const Pyramid& p, const EmitJob& e, int 
     const int l = p.depth - arg;  // arg = distance from the leaf level
     if (i < p.lv[l].n) bottom_up_node(p, e, l, i);
   } else if (OP == OP_TOP_DOWN) {
-    if (i < p.lv[arg].n) top_down_node(p, e, arg, i);  // arg = absolute parent level
+    if (i < p.lv[arg + 1].n) top_down_child(p, e, arg, i);  // arg = absolute parent level
   } else {
     if (i < p.lv[p.depth].n) top_down_leaf(p, e, i);
   }

@@ -68,6 +68,44 @@ def test_large_triangles(builder):
     assert_same(*run_both(builder, t, 128))
 
 
+def _large_plane_cases(seed):
+    """Large triangles whose lines along the walk axis stress the run search: planes exactly
+    on voxel faces and axis-aligned, nearly parallel to an axis, tiny normal components,
+    collinear and zero-area triangles spanning the grid."""
+    rng = np.random.default_rng(seed)
+    out = []
+    g = np.float32(1.0 / 64)
+    for axis in range(3):  # axis-aligned planes on and between voxel faces
+        for c in (0.0, 17 * g, 17.5 * g, 1.0 - g, 1.0):
+            v = rng.random((3, 3), dtype=np.float32)
+            v[:, axis] = c
+            out.append(v.reshape(9))
+    for _ in range(60):  # nearly parallel to an axis: one normal component tiny
+        v = rng.random((3, 3), dtype=np.float32)
+        axis = int(rng.integers(0, 3))
+        v[1, axis] = v[0, axis] + np.float32(rng.choice([1e-7, 1e-5, 1e-3, -1e-6]))
+        v[2, axis] = v[0, axis] + np.float32(rng.choice([0.0, 2e-7, -1e-4]))
+        out.append(v.reshape(9))
+    for _ in range(40):  # generic large triangles with grid-aligned vertices
+        out.append((rng.integers(0, 65, size=9) * g).astype(np.float32))
+    a = rng.random((20, 3), dtype=np.float32)
+    b = rng.random((20, 3), dtype=np.float32)
+    out.extend(np.stack([a, (a + b) * np.float32(0.5), b], 1).reshape(20, 9))  # collinear, long
+    out.extend(np.stack([a, a, b], 1).reshape(20, 9))
+    return np.asarray(out, dtype=np.float32)
+
+
+@pytest.mark.parametrize("scale", [1.0, 1e-3, 1e4])
+def test_large_plane_runs(builder, scale):
+    t = _large_plane_cases(17) * np.float32(scale)
+    s = float(np.float32(scale))
+    assert_same(*run_both(builder, t, 64, bbox_max=(s, s, s)))
+    rng = np.random.default_rng(3)
+    col = rng.random((t.shape[0], 12), dtype=np.float32)
+    tp = np.concatenate([t, col], 1).astype(np.float32)
+    assert_same(*run_both(builder, tp, 128, limit=1, levels=True, bbox_max=(s, s, s)))
+
+
 def test_overlapping_first_writer(builder):
     # many coincident triangles with different colours: the payload must come
     # from the first one in stream order (voxelizer.cpp:263)
