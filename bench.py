@@ -340,6 +340,14 @@ def run_batch(args, world, rank, local):
     cb = ooc.BATCH_SINK(lambda user, mesh, kind, ptr, nb: 0)
     cb1 = ooc.SINK(lambda user, kind, ptr, nb: 0)
     b = ooc.Builder(local)
+    # the autotuner picks the launch choices on every 16th mesh (untimed)
+    sample_idx = list(range(0, n, 16))
+    sample = (ooc.Mesh * len(sample_idx))()
+    for q, i in enumerate(sample_idx):
+        sample[q] = arr[i]
+    t0 = time.perf_counter()
+    tuning = b.autotune(mesh_array=sample, n_meshes=len(sample_idx)).as_dict()
+    tune_s = time.perf_counter() - t0
 
     def timed(fn, warm, reps):
         for _ in range(warm):
@@ -436,6 +444,7 @@ def run_batch(args, world, rank, local):
                      "timed_call": {"wall_ms": wall_dev * 1e3, "phases_ms": phases_dev, "kernels_ms": kernels_dev}},
         "host": {"batched_meshes_per_s": n / t_batch, "plain_meshes_per_s": n / t_plain,
                  "speedup_vs_plain": t_plain / t_batch},
+        "tuning": dict(tuning, sample_meshes=len(sample_idx), seconds=round(tune_s, 2)),
         "parity_sample": {"meshes": len(sample), "host_identical_to_plain": identical,
                           "resident_identical_to_plain": dev_identical},
         "e2e": {"value": n / t_batch, "unit": "meshes/s", "h2d_bytes_per_step": int(sum(m[0].nbytes for m in meshes)),

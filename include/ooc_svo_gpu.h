@@ -153,6 +153,28 @@ typedef struct {
 int ooc_arena_alloc(void* arena, uint64_t mesh, uint64_t nodes_bytes, uint64_t data_bytes, void* stream,
                     void** nodes, void** data);
 
+/* ---- Tuning and the autotuner (no counterpart in the reference) ----
+ * Launch choices of the voxelizer and the batch engine.  Every value gives the
+ * same output; they only change speed. */
+typedef struct {
+  uint32_t small_vol;         /* triangles whose box has at most this many voxels run one per thread (1..64) */
+  uint32_t lines_per_lane;    /* lines of a large triangle each lane of a warp task walks (1..64);
+                                 the work-queue chunk is 32 x this many lines */
+  uint32_t large_block;       /* threads per CTA of the large-triangle kernel: 64, 128 or 256 */
+  uint32_t large_ctas_per_sm; /* persistent CTAs per SM of the large-triangle kernel (1..16) */
+  uint64_t batch_budget;      /* occupancy-pyramid bytes per sub-batch (>= 4096), as ooc_set_batch_budget */
+  uint32_t graphs;            /* 1: replay each sub-batch's two launch sequences as CUDA graphs; 0: launch directly */
+  uint32_t reserved;          /* must be 0 */
+} ooc_tuning;
+
+int ooc_get_tuning(const ooc_ctx* ctx, ooc_tuning* out);
+/* OOC_ERR_INVALID for a value out of range. */
+int ooc_set_tuning(ooc_ctx* ctx, const ooc_tuning* tuning);
+/* Time builds of `sample` (host triangles, results resident in a scratch
+ * arena) over a coordinate search of the tuning values, keep the fastest in
+ * the context and return it in `best` (may be NULL). */
+int ooc_autotune(ooc_ctx* ctx, const ooc_mesh* sample, uint64_t n_meshes, ooc_tuning* best);
+
 /* Bytes of occupancy pyramids one sub-batch may hold (default 4 GiB, at least
  * 4096): the stripes of a batch call run in sub-batches of at most this much
  * pyramid (a single stripe larger than it runs alone).  Output is the same for

@@ -34,7 +34,8 @@ EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_
            "ooc_kernel_launches", "ooc_build_files", "ooc_set_kernel_timing", "ooc_kernel_time",
            "ooc_voxelize_occupancy_noalloc", "ooc_build_batch", "ooc_server_create", "ooc_server_submit",
            "ooc_server_poll", "ooc_server_release", "ooc_server_destroy", "ooc_build_batch_device",
-           "ooc_arena_alloc", "ooc_set_batch_budget", "ooc_batch_budget", "ooc_server_read")
+           "ooc_arena_alloc", "ooc_set_batch_budget", "ooc_batch_budget", "ooc_server_read", "ooc_get_tuning",
+           "ooc_set_tuning", "ooc_autotune")
 
 
 class BuildParams(ctypes.Structure):
@@ -71,6 +72,15 @@ class Result(ctypes.Structure):
                 ("nodes", ctypes.c_void_p), ("nodes_bytes", ctypes.c_uint64), ("data", ctypes.c_void_p),
                 ("data_bytes", ctypes.c_uint64), ("info", BuildInfo), ("t_submit_us", ctypes.c_double),
                 ("t_start_us", ctypes.c_double), ("t_done_us", ctypes.c_double), ("batch_size", ctypes.c_uint64)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("small_vol", ctypes.c_uint32), ("lines_per_lane", ctypes.c_uint32), ("large_block", ctypes.c_uint32),
+                ("large_ctas_per_sm", ctypes.c_uint32), ("batch_budget", ctypes.c_uint64), ("graphs", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
 class DeviceArena(ctypes.Structure):
@@ -154,6 +164,12 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_set_batch_budget.restype = ctypes.c_int
     lib.ooc_batch_budget.argtypes = [ctypes.c_void_p]
     lib.ooc_batch_budget.restype = ctypes.c_uint64
+    lib.ooc_get_tuning.argtypes = [ctypes.c_void_p, P(Tuning)]
+    lib.ooc_get_tuning.restype = ctypes.c_int
+    lib.ooc_set_tuning.argtypes = [ctypes.c_void_p, P(Tuning)]
+    lib.ooc_set_tuning.restype = ctypes.c_int
+    lib.ooc_autotune.argtypes = [ctypes.c_void_p, P(Mesh), ctypes.c_uint64, P(Tuning)]
+    lib.ooc_autotune.restype = ctypes.c_int
     lib.ooc_server_create.argtypes = [P(ServerConfig), P(ctypes.c_void_p)]
     lib.ooc_server_create.restype = ctypes.c_int
     lib.ooc_server_submit.argtypes = [ctypes.c_void_p, P(Mesh), P(ctypes.c_uint64)]
@@ -336,6 +352,25 @@ class Builder:
         return [BuildResult(_octree.from_bytes(int(params_list[i].gridsize), b"".join(parts[i][0]),
                                                b"".join(parts[i][1])), _info_dict(infos[i]))
                 for i in range(len(meshes))]
+
+    def tuning(self) -> "Tuning":
+        t = Tuning()
+        self._check(self.lib.ooc_get_tuning(self.h, ctypes.byref(t)))
+        return t
+
+    def set_tuning(self, t: "Tuning") -> None:
+        self._check(self.lib.ooc_set_tuning(self.h, ctypes.byref(t)))
+
+    def autotune(self, meshes=None, params_list=None, mesh_array=None, n_meshes: int = 0) -> "Tuning":
+        """Tune on a sample (host arrays, or a ctypes Mesh array); the context keeps the result."""
+        keep = None
+        if mesh_array is None:
+            mesh_array, keep = self._mesh_array(meshes, params_list)
+            n_meshes = len(meshes)
+        t = Tuning()
+        self._check(self.lib.ooc_autotune(self.h, mesh_array, n_meshes, ctypes.byref(t)))
+        del keep
+        return t
 
     def set_batch_budget(self, nbytes: int) -> None:
         self._check(self.lib.ooc_set_batch_budget(self.h, nbytes))

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <functional>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -142,7 +143,10 @@ struct ooc_ctx {
   std::vector<cudaEvent_t> up_events;    // recorded on h2d_stream as groups of meshes arrive
   DevBuf d_tables1, d_tables2;
   std::vector<DevBuf> d_mesh_items;
-  uint64_t batch_budget_bytes = 4ull << 30;  // occupancy pyramids of one sub-batch
+  ooc_tuning tuning = {64, 16, 256, 4, 4ull << 30, 0, 0};  // launch choices (ooc_set_tuning / ooc_autotune)
+  // executable graphs of captured launch sequences, by shape (launch count and kernels)
+  std::vector<std::pair<uint64_t, cudaGraphExec_t>> graph_execs;
+  DevBuf d_tune_arena;                               // autotuner outputs
   uint64_t res_nodes = 0, res_data = 0;
   bool res_valid = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -236,6 +240,72 @@ void ring_take(ooc_ctx* c, D2HRing& r, uint64_t a, uint64_t b, F&& out) {
       if (r.issued < r.n_chunks) ring_issue(c, r);
     }
   }
+}
+
+// Run `launches` on `st`, directly or captured into a CUDA graph and replayed.
+// Executable graphs are cached by shape (the sequence, its node count and its
+// kernels) and updated in place with the new launch parameters, so repeated
+// shapes skip instantiation.  The captured region neither allocates nor
+// synchronises; phase and kernel timing launch directly.
+template <typename F>
+void run_launches(ooc_ctx* c, cudaStream_t st, int which, F&& launches) {
+  if (!c->tuning.graphs || c->timing || g_hooks.begin) {
+    launches();
+    return;
+  }
+  ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+  cudaGraph_t graph = nullptr;
+  try {
+    launches();
+  } catch (...) {
+    cudaStreamEndCapture(st, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    throw;
+  }
+  ck(cudaStreamEndCapture(st, &graph), "cudaStreamEndCapture");
+  // shape key: which sequence, node count, and the kernels in capture order
+  size_t count = 0;
+  ck(cudaGraphGetNodes(graph, nullptr, &count), "cudaGraphGetNodes");
+  std::vector<cudaGraphNode_t> nodes(count);
+  if (count) ck(cudaGraphGetNodes(graph, nodes.data(), &count), "cudaGraphGetNodes");
+  uint64_t key = 1469598103934665603ull ^ (uint64_t)which ^ ((uint64_t)count << 8);
+  for (cudaGraphNode_t nd : nodes) {
+    cudaGraphNodeType ty;
+    ck(cudaGraphNodeGetType(nd, &ty), "cudaGraphNodeGetType");
+    uint64_t v = (uint64_t)ty;
+    if (ty == cudaGraphNodeTypeKernel) {
+      cudaKernelNodeParams kp;
+      ck(cudaGraphKernelNodeGetParams(nd, &kp), "cudaGraphKernelNodeGetParams");
+      v ^= reinterpret_cast<uintptr_t>(kp.func) << 4;
+    }
+    key = (key ^ v) * 1099511628211ull;
+  }
+  cudaGraphExec_t exec = nullptr;
+  for (auto& kv : c->graph_execs)
+    if (kv.first == key) exec = kv.second;
+  cudaError_t e = cudaSuccess;
+  if (exec) {
+    cudaGraphExecUpdateResultInfo info;
+    e = cudaGraphExecUpdate(exec, graph, &info);
+  }
+  if (!exec || e != cudaSuccess) {
+    cudaGetLastError();  // an update refused is a shape change, not an error
+    for (auto it = c->graph_execs.begin(); it != c->graph_execs.end(); ++it)
+      if (it->first == key) {
+        cudaGraphExecDestroy(it->second);
+        c->graph_execs.erase(it);
+        break;
+      }
+    if (c->graph_execs.size() >= 64) {  // keep the cache bounded: drop the oldest shape
+      cudaGraphExecDestroy(c->graph_execs.front().second);
+      c->graph_execs.erase(c->graph_execs.begin());
+    }
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e == cudaSuccess) c->graph_execs.push_back({key, exec});
+  }
+  cudaGraphDestroy(graph);
+  ck(e, "cudaGraphInstantiate");
+  ck(cudaGraphLaunch(exec, st), "cudaGraphLaunch");
 }
 
 // ---------------------------------------------------------------------------
@@ -627,7 +697,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     }
     j.u = m.pl.u;
     j.unit_div = m.pl.unit_div;
-    j.small_vol = 64;
+    j.small_vol = c->tuning.small_vol;
+    j.lines_per_lane = c->tuning.lines_per_lane;
     j.leafbits = bits + P.lv[P.depth].off_w;
     j.task_off = task_off + item_beg[s];
     j.task_counter = counter;
@@ -656,25 +727,28 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const uint64_t* d_beg = reinterpret_cast<const uint64_t*>(t1 + o_beg);
 
   uint32_t* lvl = ensure_pinned<uint32_t>(c->h_misc, ((uint64_t)n * 16 + 64) * 4);  // level bases, then root info
-  {
-    PhaseScope ph(c, PH_VOX, st);
-    ck(cudaMemsetAsync(bits, 0, words * 4, st), "memset bits");
-    ck(cudaMemsetAsync(task_off + items, 0, 8, st), "memset task_off");
-    ck(cudaMemsetAsync(flag, 0, 4, st), "memset flag");
-    launch_b_vox_small(d_vj, dp1(o_cpi), n, cp_items[n], 0, n == 1 ? &vj[0] : nullptr, st);
-    scan_u64_exclusive(task_off, items + 1, taskpart, st);
-    launch_b_vox_large(d_vj, d_beg, n, task_off, items, counter, 0, st, c->num_sms);
-  }
-  {
-    PhaseScope ph(c, PH_PYR, st);
-    ck(cudaMemsetAsync(scan + blocks, 0, 4, st), "memset scan");
-    for (size_t r = 0; r < cp_pyr.size(); r++)
-      launch_b_pyramid(d_pyr, dp1(o_cpp[r]), n, cp_pyr[r][n], (int)r, n == 1 ? &pyr[0] : nullptr, st);
-    launch_b_pyramid_top(d_pyr, n, kTopPyramidLevel, st);
-    scan_u32_exclusive(scan, blocks + 1, scanpart, st);
-    launch_b_level_bases(d_pyr, n, d_root, st);
-    ck(cudaMemcpyAsync(lvl, d_root, (uint64_t)n * (kMaxLevels + 1) * 4, cudaMemcpyDeviceToHost, st), "levels");
-  }
+  run_launches(c, st, 0, [&] {
+    {
+      PhaseScope ph(c, PH_VOX, st);
+      ck(cudaMemsetAsync(bits, 0, words * 4, st), "memset bits");
+      ck(cudaMemsetAsync(task_off + items, 0, 8, st), "memset task_off");
+      ck(cudaMemsetAsync(flag, 0, 4, st), "memset flag");
+      launch_b_vox_small(d_vj, dp1(o_cpi), n, cp_items[n], 0, n == 1 ? &vj[0] : nullptr, st);
+      scan_u64_exclusive(task_off, items + 1, taskpart, st);
+      launch_b_vox_large(d_vj, d_beg, n, task_off, items, counter, 0, st, c->num_sms, (int)c->tuning.large_block,
+                         (int)c->tuning.large_ctas_per_sm);
+    }
+    {
+      PhaseScope ph(c, PH_PYR, st);
+      ck(cudaMemsetAsync(scan + blocks, 0, 4, st), "memset scan");
+      for (size_t r = 0; r < cp_pyr.size(); r++)
+        launch_b_pyramid(d_pyr, dp1(o_cpp[r]), n, cp_pyr[r][n], (int)r, n == 1 ? &pyr[0] : nullptr, st);
+      launch_b_pyramid_top(d_pyr, n, kTopPyramidLevel, st);
+      scan_u32_exclusive(scan, blocks + 1, scanpart, st);
+      launch_b_level_bases(d_pyr, n, d_root, st);
+      ck(cudaMemcpyAsync(lvl, d_root, (uint64_t)n * (kMaxLevels + 1) * 4, cudaMemcpyDeviceToHost, st), "levels");
+    }
+  });
   ck(cudaStreamSynchronize(st), "level counts");
 
   // ---- counts, placement in the files ----
@@ -876,30 +950,33 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const Pyramid* sp1 = n == 1 ? &pyr[0] : nullptr;  // one-stripe launches take the jobs as parameters
   const EmitJob* se1 = n == 1 ? &ej[0] : nullptr;
 
-  {
-    PhaseScope ph(c, PH_PYR, st);
-    launch_b_compact(d_pyr2, dp2(o_cc), n, cp_compact[n], keys, n == 1 ? &pyr[0] : nullptr, st);
-  }
-  if (any_payload) {
-    PhaseScope ph(c, PH_VOX, st);
-    ck(cudaMemsetAsync(winners, 0xff, total_nodes * 4, st), "memset winners");
-    launch_b_vox_small(d_vj2, dp2(o_cpay), n, cp_pay[n], 1, n == 1 ? &vj[0] : nullptr, st);
-    launch_b_vox_large(d_vj2, d_beg, n, task_off, items, counter, 1, st, c->num_sms);
-    launch_b_leaf_payload(d_pyr2, d_ej, dp2(o_clp), n, cp_leafpay[n], sp1, se1, st);
-  }
-  {
-    PhaseScope ph(c, PH_TREE, st);
-    for (size_t r = 1; r < cp_bu.size(); r++)
-      launch_b_bottom_up(d_pyr2, d_ej, dp2(o_bu[r]), n, cp_bu[r][n], (int)r, sp1, se1, st);
-    launch_b_bottom_up_top(d_pyr2, d_ej, n, st);
-    launch_b_top_down_top(d_pyr2, d_ej, n, st);
-    for (size_t l = 0; l < cp_td.size(); l++)
-      launch_b_top_down(d_pyr2, d_ej, dp2(o_td[l]), n, cp_td[l][n], (int)l, sp1, se1, st);
-    launch_b_top_down_leaves(d_pyr2, d_ej, dp2(o_cl), n, cp_leaves[n], sp1, se1, st);
-    launch_b_root_info(d_pyr2, d_ej, n, d_root, st);
-    uint32_t* hr = ensure_pinned<uint32_t>(c->h_root[slot], ((uint64_t)n * 16 + 1) * 4);
-    ck(cudaMemcpyAsync(hr, d_root, ((uint64_t)n * 16 + 1) * 4, cudaMemcpyDeviceToHost, st), "root info");
-  }
+  uint32_t* hr = ensure_pinned<uint32_t>(c->h_root[slot], ((uint64_t)n * 16 + 1) * 4);
+  run_launches(c, st, 1, [&] {
+    {
+      PhaseScope ph(c, PH_PYR, st);
+      launch_b_compact(d_pyr2, dp2(o_cc), n, cp_compact[n], keys, n == 1 ? &pyr[0] : nullptr, st);
+    }
+    if (any_payload) {
+      PhaseScope ph(c, PH_VOX, st);
+      ck(cudaMemsetAsync(winners, 0xff, total_nodes * 4, st), "memset winners");
+      launch_b_vox_small(d_vj2, dp2(o_cpay), n, cp_pay[n], 1, n == 1 ? &vj[0] : nullptr, st);
+      launch_b_vox_large(d_vj2, d_beg, n, task_off, items, counter, 1, st, c->num_sms, (int)c->tuning.large_block,
+                         (int)c->tuning.large_ctas_per_sm);
+      launch_b_leaf_payload(d_pyr2, d_ej, dp2(o_clp), n, cp_leafpay[n], sp1, se1, st);
+    }
+    {
+      PhaseScope ph(c, PH_TREE, st);
+      for (size_t r = 1; r < cp_bu.size(); r++)
+        launch_b_bottom_up(d_pyr2, d_ej, dp2(o_bu[r]), n, cp_bu[r][n], (int)r, sp1, se1, st);
+      launch_b_bottom_up_top(d_pyr2, d_ej, n, st);
+      launch_b_top_down_top(d_pyr2, d_ej, n, st);
+      for (size_t l = 0; l < cp_td.size(); l++)
+        launch_b_top_down(d_pyr2, d_ej, dp2(o_td[l]), n, cp_td[l][n], (int)l, sp1, se1, st);
+      launch_b_top_down_leaves(d_pyr2, d_ej, dp2(o_cl), n, cp_leaves[n], sp1, se1, st);
+      launch_b_root_info(d_pyr2, d_ej, n, d_root, st);
+      ck(cudaMemcpyAsync(hr, d_root, ((uint64_t)n * 16 + 1) * 4, cudaMemcpyDeviceToHost, st), "root info");
+    }
+  });
   ck(cudaEventRecord(c->ev_compute[slot], st), "event");
   if (os.mode == OUT_HOST) {
     // the records travel to the host on the copy stream while the next sub-batch computes
@@ -1039,7 +1116,7 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, co
   // stripes with items, in mesh order and Morton order, split by the pyramid budget
   std::vector<StripeRef> sb;
   uint64_t budget_words = 0;
-  const uint64_t budget = c->batch_budget_bytes / 4;
+  const uint64_t budget = c->tuning.batch_budget / 4;
   auto items_of = [&](const MeshWork& m, uint64_t s) -> uint64_t {
     const uint64_t part = s / m.pl.stripes_per_part;
     return m.pl.P > 1 ? (uint64_t)m.part_off[part + 1] - m.part_off[part] : m.n_tris;
@@ -1261,6 +1338,7 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   }
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->h2d_stream) cudaStreamDestroy(c->h2d_stream);
+  for (auto& kv : c->graph_execs) cudaGraphExecDestroy(kv.second);
   for (cudaEvent_t e : c->up_events) cudaEventDestroy(e);
   if (c->d_tables1.p) cudaFree(c->d_tables1.p);
   if (c->d_tables2.p) cudaFree(c->d_tables2.p);
@@ -1464,11 +1542,109 @@ int ooc_build_batch_device(ooc_ctx* c, const ooc_mesh* meshes_in, uint64_t n_mes
 
 int ooc_set_batch_budget(ooc_ctx* c, uint64_t bytes) {
   if (!c || bytes < 4096) return OOC_ERR_INVALID;
-  c->batch_budget_bytes = bytes;
+  c->tuning.batch_budget = bytes;
   return OOC_OK;
 }
 
-uint64_t ooc_batch_budget(const ooc_ctx* c) { return c ? c->batch_budget_bytes : 0; }
+uint64_t ooc_batch_budget(const ooc_ctx* c) { return c ? c->tuning.batch_budget : 0; }
+
+namespace {
+bool tuning_ok(const ooc_tuning& t) {
+  return t.small_vol >= 1 && t.small_vol <= 64 && t.lines_per_lane >= 1 && t.lines_per_lane <= 64 &&
+         (t.large_block == 64 || t.large_block == 128 || t.large_block == 256) && t.large_ctas_per_sm >= 1 &&
+         t.large_ctas_per_sm <= 16 && t.batch_budget >= 4096 && t.graphs <= 1 && t.reserved == 0;
+}
+
+struct TuneArena {
+  DevBuf* buf;
+  uint64_t used;
+};
+
+int tune_alloc(void* user, uint64_t, uint64_t nodes_bytes, uint64_t data_bytes, void*, void** nodes, void** data) {
+  TuneArena* a = static_cast<TuneArena*>(user);
+  const uint64_t n = (nodes_bytes + 255) / 256 * 256, d = (data_bytes + 255) / 256 * 256;
+  if (a->used + n + d > a->buf->cap) return 1;
+  *nodes = static_cast<char*>(a->buf->p) + a->used;
+  *data = static_cast<char*>(a->buf->p) + a->used + n;
+  a->used += n + d;
+  return 0;
+}
+
+int count_sink(void*, uint64_t, int32_t, const void*, uint64_t) { return 0; }
+}  // namespace
+
+int ooc_get_tuning(const ooc_ctx* c, ooc_tuning* out) {
+  if (!c || !out) return OOC_ERR_INVALID;
+  *out = c->tuning;
+  return OOC_OK;
+}
+
+int ooc_set_tuning(ooc_ctx* c, const ooc_tuning* t) {
+  if (!c || !t) return OOC_ERR_INVALID;
+  if (!tuning_ok(*t)) {
+    c->err = "tuning value out of range";
+    return OOC_ERR_INVALID;
+  }
+  c->tuning = *t;
+  return OOC_OK;
+}
+
+int ooc_autotune(ooc_ctx* c, const ooc_mesh* sample, uint64_t n, ooc_tuning* best) {
+  if (!c || (n && !sample)) return OOC_ERR_INVALID;
+  const ooc_tuning start = c->tuning;
+  // sizes of the sample's files, then one arena that holds them all
+  std::vector<ooc_build_info> infos(n > 0 ? n : 1);
+  int rc = ooc_build_batch(c, sample, n, count_sink, nullptr, infos.data());
+  if (rc != OOC_OK) return rc;
+  uint64_t bytes = 0;
+  for (uint64_t i = 0; i < n; i++)
+    bytes += (infos[i].n_nodes * 24 + 255) / 256 * 256 + (infos[i].n_data * 32 + 255) / 256 * 256;
+  rc = guarded(c, [&] { ensure<unsigned char>(c->d_tune_arena, bytes + 4096); });
+  if (rc != OOC_OK) return rc;
+  auto time_one = [&](const ooc_tuning& t, double& ms) -> int {
+    c->tuning = t;
+    double best_ms = 1e30;
+    for (int rep = 0; rep < 2; rep++) {
+      TuneArena a{&c->d_tune_arena, 0};
+      const auto t0 = std::chrono::steady_clock::now();
+      const int r = ooc_build_batch_device(c, sample, n, tune_alloc, nullptr, &a, infos.data());
+      if (r != OOC_OK) return r;
+      best_ms = std::min(best_ms, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+    }
+    ms = best_ms;
+    return OOC_OK;
+  };
+  ooc_tuning cur = start;
+  double cur_ms = 0.0;
+  rc = time_one(cur, cur_ms);  // warms the context's buffers too
+  if (rc == OOC_OK) rc = time_one(cur, cur_ms);
+  // one coordinate pass: each choice in turn, the others held at their best so far
+  const uint32_t lpl[] = {4, 8, 16, 32}, cps[] = {2, 4, 8}, blk[] = {128, 256}, svol[] = {16, 32, 48, 64}, gr[] = {0, 1};
+  const uint64_t bud[] = {1ull << 30, 2ull << 30, 4ull << 30, 8ull << 30};
+  auto try_values = [&](auto setter, const auto& values) {
+    for (const auto& v : values) {
+      if (rc != OOC_OK) return;
+      ooc_tuning t = cur;
+      setter(t, v);
+      if (std::memcmp(&t, &cur, sizeof(t)) == 0) continue;
+      double ms = 0.0;
+      rc = time_one(t, ms);
+      if (rc == OOC_OK && ms < cur_ms) {
+        cur = t;
+        cur_ms = ms;
+      }
+    }
+  };
+  try_values([](ooc_tuning& t, uint32_t v) { t.lines_per_lane = v; }, lpl);
+  try_values([](ooc_tuning& t, uint32_t v) { t.large_ctas_per_sm = v; }, cps);
+  try_values([](ooc_tuning& t, uint32_t v) { t.large_block = v; }, blk);
+  try_values([](ooc_tuning& t, uint32_t v) { t.small_vol = v; }, svol);
+  try_values([](ooc_tuning& t, uint64_t v) { t.batch_budget = v; }, bud);
+  try_values([](ooc_tuning& t, uint32_t v) { t.graphs = v; }, gr);
+  c->tuning = rc == OOC_OK ? cur : start;
+  if (best) *best = c->tuning;
+  return rc;
+}
 
 int ooc_arena_alloc(void* arena, uint64_t mesh, uint64_t nodes_bytes, uint64_t data_bytes, void* stream,
                     void** nodes, void** data) {

@@ -42,7 +42,8 @@ struct VoxJob {
   int pa[3], pb[3];         // partition box in grid coordinates (inclusive)
   int sa[3], sb[3];         // stripe box in grid coordinates (inclusive)
   float u, unit_div;
-  uint32_t small_vol;       // items with at most this many candidates run one per thread
+  uint32_t small_vol;       // items with at most this many candidates (<= 64) run one per thread
+  uint32_t lines_per_lane;  // lines of a large item each lane of a warp task walks (task = 32 x this)
   uint32_t* leafbits;       // level-Ds words
   // pass B (payload winners)
   const uint32_t* leafscan; // scan entries of level Ds (exclusive, minus its base)
@@ -125,7 +126,8 @@ void launch_b_vox_small(const VoxJob* jobs, const uint64_t* cta_beg, uint32_t n,
 // Large items of every stripe; task_off is the batch-wide exclusive scan (total_items + 1 entries),
 // item_beg[s] the first batch item of stripe s (ascending).
 void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n_stripes, const uint64_t* task_off,
-                        uint64_t total_items, unsigned long long* counter, int pass, cudaStream_t st, int num_sms);
+                        uint64_t total_items, unsigned long long* counter, int pass, cudaStream_t st, int num_sms,
+                        int block, int ctas_per_sm);
 // Level depth - r of each stripe.
 void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, int r,
                       const Pyramid* single, cudaStream_t st);

@@ -362,8 +362,6 @@ __device__ __forceinline__ uint64_t item_triangle(const VoxJob& j, uint64_t i) {
 // voxel of the run still gets the complete test, so the result is the
 // reference's candidate loop (voxelizer.cpp:257-305) voxel for voxel.
 // ---------------------------------------------------------------------------
-constexpr int kLinesPerLane = 16;
-constexpr uint64_t kLinesPerTask = 32 * kLinesPerLane;
 
 // Axis of the largest component of cross(e0, e1); the item count and the tasks
 // call this same function, so they agree on the lines of every item.
@@ -495,7 +493,7 @@ __device__ __forceinline__ void vox_line(const VoxJob& j, const TriSetup& s, uin
 
 // Pass 0, one thread per item: items with at most small_vol (<= 64) candidates
 // are voxelized here and leave their pass mask; larger ones get a warp-task
-// count (kLinesPerTask lines per task).
+// count (32 x lines_per_lane lines per task).
 __device__ __forceinline__ void vox_small_occ_item(const VoxJob& j, uint64_t i) {
   const uint64_t t = item_triangle(j, i);
   const TriVerts tv = load_verts(j.tris, t, j.stride);
@@ -519,7 +517,8 @@ __device__ __forceinline__ void vox_small_occ_item(const VoxJob& j, uint64_t i) 
                         ((uint64_t)(lo[2] - j.sa[2]) << 20) | ((bx - 1) << 30) | ((by - 1) << 36) | ((bz - 1) << 42);
       }
     } else {
-      cost = (item_lines(walk_axis(tv), lo, hi) + kLinesPerTask - 1) / kLinesPerTask;
+      const uint64_t per_task = 32ull * j.lines_per_lane;
+      cost = (item_lines(walk_axis(tv), lo, hi) + per_task - 1) / per_task;
     }
   }
   j.task_off[i] = cost;
@@ -554,7 +553,7 @@ __global__ void k_vox_small_win(VoxJob j) {
   if (i < j.n_items) vox_small_win_item(j, i);
 }
 
-// Lines kLinesPerTask*k .. +kLinesPerTask-1 of large item i (lane, lane+32, ...).
+// Lines 32*L*k .. 32*L*(k+1)-1 of large item i, L = lines_per_lane (lane, lane+32, ...).
 template <int PASS>
 __device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint64_t k, int lane) {
   if (PASS == 1 && !j.winners) return;  // binary-mode stripe in a mixed batch: no winner pass
@@ -566,7 +565,7 @@ __device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint
   // lines of one item number at most 1024^2 (a stripe's face): 32-bit arithmetic
   const uint32_t ea = (uint32_t)(W == 0 ? hi[1] - lo[1] + 1 : hi[0] - lo[0] + 1);  // first axis across the walk
   const uint32_t lines = (uint32_t)item_lines(W, lo, hi);
-  const uint32_t c0 = (uint32_t)k * (uint32_t)kLinesPerTask + (uint32_t)lane;
+  const uint32_t c0 = (uint32_t)k * 32u * j.lines_per_lane + (uint32_t)lane;
   if (c0 >= lines) return;
   TriSetup s;
   tri_setup(tv, j.u, s);
@@ -578,7 +577,7 @@ __device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint
   const int whi = W == 0 ? hi[0] : (W == 1 ? hi[1] : hi[2]);
   const int alo = W == 0 ? lo[1] : lo[0], blo = W == 2 ? lo[1] : lo[2];
 #pragma unroll 1
-  for (int q = 0; q < kLinesPerLane; q++) {
+  for (uint32_t q = 0; q < j.lines_per_lane; q++) {
     const uint32_t c = c0 + 32u * q;
     if (c >= lines) break;
     vox_line<PASS>(j, s, (uint32_t)t, W, alo + (int)(c % ea), blo + (int)(c / ea), wlo, whi, mono, dir, inv_dir);
@@ -1303,13 +1302,14 @@ void launch_b_vox_small(const VoxJob* jobs, const uint64_t* cta_beg, uint32_t n,
 }
 
 void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n_stripes, const uint64_t* task_off,
-                        uint64_t total_items, unsigned long long* counter, int pass, cudaStream_t st, int num_sms) {
+                        uint64_t total_items, unsigned long long* counter, int pass, cudaStream_t st, int num_sms,
+                        int block, int ctas_per_sm) {
   if (total_items == 0) return;
   cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
-  const unsigned grid = (unsigned)num_sms * 8;
+  const unsigned grid = (unsigned)num_sms * (unsigned)ctas_per_sm;
   KScope k(pass == 0 ? "vox_large_occupancy" : "vox_large_winner", st);
-  if (pass == 0) kb_vox_large<0><<<grid, 256, 0, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter);
-  else kb_vox_large<1><<<grid, 256, 0, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter);
+  if (pass == 0) kb_vox_large<0><<<grid, block, 0, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter);
+  else kb_vox_large<1><<<grid, block, 0, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter);
 }
 
 void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, int r,

@@ -98,6 +98,7 @@ extern "C" int ooc_voxelize_occupancy_noalloc(const ooc_build_params* params, co
   j.u = u;
   j.unit_div = 1.0f / u;  // voxelizer.cpp:164
   j.small_vol = 64;
+  j.lines_per_lane = 16;
   j.leafbits = occupancy_device;
   j.task_off = reinterpret_cast<uint64_t*>(scratch);
   uint64_t* partials = reinterpret_cast<uint64_t*>(scratch + kTaskWords);

@@ -5,6 +5,8 @@ Each mesh's octree must equal the oracle's (and so ooc_build's) on that mesh alo
 import numpy as np
 import pytest
 
+import ooc_svo_builder_gb300 as ooc
+
 import pyoracle
 from ooc_svo_builder_gb300 import make_params, octree, tri
 
@@ -85,3 +87,38 @@ def test_batch_device_meshes_straddling_sub_batches(builder):
         nodes, data, _ = pyoracle.build(t, 256, 2, levels=(i == 3))
         assert not octree.diff(r.tree, octree.Octree(256, nodes, data))
         assert not octree.diff(host[i].tree, r.tree)
+
+
+def test_every_tuning_gives_the_same_octrees(builder):
+    # launch choices change speed only: extreme values against the oracle
+    meshes, params, args = mixed_meshes(seed=8, count=12)
+    meshes.append(tri.random_tris(60, 5, True, lo=0.0, hi=1.0, max_edge=1.2))  # many large triangles
+    params.append(make_params(128, 2048, geometry_only=False))
+    args.append(dict(gridsize=128, memory_limit_mb=2048, color="model", levels=False))
+    old = builder.tuning()
+    want = []
+    for t, a in zip(meshes, args):
+        nodes, data, _ = pyoracle.build(t, a["gridsize"], a["memory_limit_mb"], color=a["color"], levels=a["levels"])
+        want.append(octree.Octree(a["gridsize"], nodes, data))
+    try:
+        for small_vol, lpl, block, cps, budget, graphs in [(1, 1, 64, 1, 4096, 1), (64, 64, 256, 16, 1 << 30, 0),
+                                                           (27, 3, 128, 2, 700_000, 1), (64, 16, 256, 4, 4 << 30, 1)]:
+            builder.set_tuning(ooc.Tuning(small_vol, lpl, block, cps, budget, graphs, 0))
+            for r, w in zip(builder.build_batch_device(meshes, params), want):
+                assert not octree.diff(r.tree, w)
+    finally:
+        builder.set_tuning(old)
+
+
+def test_autotune_keeps_a_valid_tuning(builder):
+    meshes = [tri.soup_tris(3000, 256, seed=s, sigma=1.0, n_spheres=2, payload=bool(s % 2)) for s in range(6)]
+    params = [make_params(256, 2048, geometry_only=not bool(s % 2)) for s in range(6)]
+    old = builder.tuning()
+    try:
+        t = builder.autotune(meshes, params)
+        assert 1 <= t.small_vol <= 64 and 1 <= t.lines_per_lane <= 64 and t.large_block in (64, 128, 256)
+        assert builder.tuning().as_dict() == t.as_dict()
+        for r, (m, p) in zip(builder.build_batch(meshes, params), zip(meshes, params)):
+            assert not octree.diff(r.tree, builder.build(m, p).tree)
+    finally:
+        builder.set_tuning(old)

@@ -31,3 +31,12 @@ def test_result_struct_layout():
     # ooc_result: id, status, reserved, nodes, nodes_bytes, data, data_bytes, info (6 x u64), 3 doubles, batch_size
     assert ctypes.sizeof(ooc.Result) == 8 + 4 + 4 + 8 * 4 + 48 + 24 + 8
     assert ctypes.sizeof(ooc.ServerConfig) == 24
+
+
+def test_tuning_calls_reject_null():
+    lib = ooc.load_library()
+    t = ooc.Tuning(64, 16, 256, 4, 1 << 30, 0, 0)
+    assert lib.ooc_set_tuning(None, ctypes.byref(t)) == 1
+    assert lib.ooc_get_tuning(None, ctypes.byref(t)) == 1
+    assert lib.ooc_autotune(None, None, 0, None) == 1
+    assert ctypes.sizeof(ooc.Tuning) == 32
