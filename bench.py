@@ -167,11 +167,21 @@ def cpu_port_time(tris, w, budget_s: float, max_runs: int, min_runs: int = 1):
     return statistics.mean(times), len(times)
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of a workload's dominant
+# kernel, from the ncu captures summarised under profiles/: (workload, kernel) -> (bytes, summary)
+NCU_TRAFFIC = {
+    ("heightfield1024", "vox_small_occupancy"): (179.7e6 + 34.1e6, "profiles/vox_small_heightfield1024.md"),
+}
+
+
 def algorithmic_bytes(kernel: str, n_tris: int, info: dict, S: int, payload: bool) -> float:
     """Minimum DRAM bytes one launch of `kernel` must move for this workload."""
     tri_bytes = 84 if payload else 36
     leaf_words = S // 32
-    if kernel in ("vox_small_occupancy", "vox_small_winner", "vox_large_occupancy", "vox_large_winner"):
+    if kernel == "vox_small_occupancy":
+        # vertices of every triangle (36 B) + its task count (8 B) + (payload) pass mask and box (16 B)
+        return n_tris * (36 + 8 + (16 if payload else 0))
+    if kernel in ("vox_small_winner", "vox_large_occupancy", "vox_large_winner"):
         # vertices of every triangle (36 B) + the task count per item (8 B)
         return n_tris * (36 + 8)
     if kernel == "pyramid":  # leaf level dominates: read bits, write parent bits + block counts
@@ -276,8 +286,12 @@ def run_ours(args, world, rank, local):
     launches_per_build = kt.get(dominant, (0, 1))[1] if dominant else 1
     alg_per_launch = alg / max(1, launches_per_build)
     achieved = alg_per_launch / (per_launch_ms / 1e3) / 1e9 if dom_n else None
+    traffic, traffic_src = args.traffic, "--traffic" if args.traffic else None
+    if traffic is None and (args.workload, dominant) in NCU_TRAFFIC:
+        traffic, traffic_src = NCU_TRAFFIC[(args.workload, dominant)]
     roofline = {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": args.traffic,
+                "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": traffic,
+                "traffic_source": traffic_src,
                 "peak_source": peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
                 "per_launch_ms": per_launch_ms, "algorithmic_bytes_per_launch": alg_per_launch}
 

@@ -302,6 +302,35 @@ int ooc_server_release(ooc_server* server, uint64_t id);
  * the engines and free everything (results not yet released included). */
 void ooc_server_destroy(ooc_server* server);
 
+/* ---- Octree check (replaces the reference's external viewer for checks) ----
+ * The invariants of the .octreenodes/.octreedata format (octree_io.h:48-83)
+ * that every correct build satisfies, checked on the GPU at any size: child
+ * groups written as consecutive slots before their parent (OctreeBuilder.cpp:
+ * 58-79), every node but the root (the last record) the child of exactly one
+ * node, leaves at depth log2(gridsize), data indices inside the data file
+ * (geometry-only leaves at the white entry 1), and each payload leaf's data
+ * record carrying the Morton code of its path from the root. */
+#define OOC_CHECK_CHILD_ORDER 1  /* a child group out of slot order, or not before its parent */
+#define OOC_CHECK_REFCOUNT 2     /* a node that is not the child of exactly one node          */
+#define OOC_CHECK_DEPTH 4        /* a leaf not at depth log2(gridsize), or an inner node there */
+#define OOC_CHECK_DATA_INDEX 8   /* a data index outside the data file                        */
+#define OOC_CHECK_MORTON 16      /* a payload leaf whose data Morton code is not its path     */
+
+typedef struct {
+  uint64_t n_nodes, n_data;
+  uint64_t n_leaves;   /* voxels (the root of an empty octree is not counted) */
+  uint64_t n_inner;
+  uint64_t first_bad;  /* lowest node index with a violation, ~0 when none */
+  uint32_t errors;     /* OOC_CHECK_* bits; 0 for a well-formed octree */
+  uint32_t max_depth;
+} ooc_octree_check;
+
+/* `nodes` and `data` are device pointers to the two files' bytes (8-byte
+ * aligned); `stream` is a cudaStream_t (NULL: the default stream).  Returns
+ * OOC_OK when the check ran; the verdict is `out->errors`. */
+int ooc_check_octree_device(const void* nodes, uint64_t n_nodes, const void* data, uint64_t n_data,
+                            uint64_t gridsize, int32_t geometry_only, void* stream, ooc_octree_check* out);
+
 /* File front end used by the svo_builder CLIs: reads <base>.tri/.tridata and
  * writes <base><gridsize>_<npartitions>.octree/.octreenodes/.octreedata
  * (main.cpp:296-398).  `out_base` receives the output base name (may be NULL). */

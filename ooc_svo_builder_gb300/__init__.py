@@ -35,7 +35,8 @@ EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_
            "ooc_voxelize_occupancy_noalloc", "ooc_build_batch", "ooc_server_create", "ooc_server_submit",
            "ooc_server_poll", "ooc_server_release", "ooc_server_destroy", "ooc_build_batch_device",
            "ooc_arena_alloc", "ooc_set_batch_budget", "ooc_batch_budget", "ooc_server_read", "ooc_get_tuning",
-           "ooc_set_tuning", "ooc_autotune")
+           "ooc_set_tuning", "ooc_autotune", "ooc_check_octree_device")
+CHECK_BITS = {1: "child group order", 2: "reference count", 4: "depth", 8: "data index", 16: "payload Morton code"}
 
 
 class BuildParams(ctypes.Structure):
@@ -81,6 +82,12 @@ class Tuning(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+class OctreeCheck(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_uint64), ("n_data", ctypes.c_uint64), ("n_leaves", ctypes.c_uint64),
+                ("n_inner", ctypes.c_uint64), ("first_bad", ctypes.c_uint64), ("errors", ctypes.c_uint32),
+                ("max_depth", ctypes.c_uint32)]
 
 
 class DeviceArena(ctypes.Structure):
@@ -170,6 +177,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_set_tuning.restype = ctypes.c_int
     lib.ooc_autotune.argtypes = [ctypes.c_void_p, P(Mesh), ctypes.c_uint64, P(Tuning)]
     lib.ooc_autotune.restype = ctypes.c_int
+    lib.ooc_check_octree_device.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
+                                            ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p, P(OctreeCheck)]
+    lib.ooc_check_octree_device.restype = ctypes.c_int
     lib.ooc_server_create.argtypes = [P(ServerConfig), P(ctypes.c_void_p)]
     lib.ooc_server_create.restype = ctypes.c_int
     lib.ooc_server_submit.argtypes = [ctypes.c_void_p, P(Mesh), P(ctypes.c_uint64)]
@@ -223,6 +233,20 @@ def voxelize_occupancy_noalloc(params: BuildParams, tris_device_ptr: int, n_tris
     return int(load_library().ooc_voxelize_occupancy_noalloc(
         ctypes.byref(params), ctypes.c_void_p(tris_device_ptr), n_tris, ctypes.c_void_p(occupancy_device_ptr),
         occupancy_words, ctypes.c_void_p(stream or None)))
+
+
+def check_octree_device(nodes_ptr: int, n_nodes: int, data_ptr: int, n_data: int, gridsize: int,
+                        geometry_only: bool, stream: int = 0) -> dict:
+    """Structural check of an octree in device memory (ooc_check_octree_device); `errors` lists
+    the violated invariants, empty for a well-formed octree."""
+    lib = load_library()
+    r = OctreeCheck()
+    rc = lib.ooc_check_octree_device(ctypes.c_void_p(nodes_ptr), n_nodes, ctypes.c_void_p(data_ptr), n_data, gridsize,
+                                     1 if geometry_only else 0, ctypes.c_void_p(stream or None), ctypes.byref(r))
+    if rc != OOC_OK:
+        raise OocError(rc, "ooc_check_octree_device failed")
+    return {"n_leaves": int(r.n_leaves), "n_inner": int(r.n_inner), "max_depth": int(r.max_depth),
+            "first_bad": int(r.first_bad), "errors": [v for b, v in CHECK_BITS.items() if r.errors & b]}
 
 
 @dataclass

@@ -24,7 +24,7 @@ BIN = os.path.join(PKG, "bin")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-Xptxas", "-v"]
-CUDA_SOURCES = ["ooc_kernels.cu", "ooc_api.cu", "ooc_noalloc.cu"]
+CUDA_SOURCES = ["ooc_kernels.cu", "ooc_api.cu", "ooc_noalloc.cu", "ooc_validate.cu"]
 CXX_SOURCES = ["ooc_files.cpp", "ooc_server.cpp"]
 
 
@@ -90,6 +90,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if force or not _newer(exe, [main, LIB, os.path.join(INCLUDE, "ooc_svo_gpu.h")]):
             _run(["g++", "-O2", "-std=c++17", *extra, "-I", INCLUDE, main, "-o", exe, "-L", PKG, "-looc_svo_gpu",
                   "-Wl,-rpath,$ORIGIN/.."], log)
+    check = os.path.join(CSRC, "octree_check_main.cpp")
+    exe = os.path.join(BIN, "octree_check")
+    if force or not _newer(exe, [check, LIB, os.path.join(INCLUDE, "ooc_svo_gpu.h")]):
+        _run([nvcc, "-O2", "-std=c++17", "-I", INCLUDE, check, "-o", exe, "-L", PKG, "-looc_svo_gpu",
+              "-Xlinker", "-rpath,$ORIGIN/.."], log)
     if verbose:
         sys.stdout.write("".join(log))
     return LIB

@@ -1,0 +1,47 @@
+"""Full-size configurations, through properties that need no oracle run: the octree check
+(structure, leaf count = filled voxels, depth) and the batched path against the plain one."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import ooc_svo_builder_gb300 as ooc
+from ooc_svo_builder_gb300 import make_params, tri
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def device_check(builder, info, N, binary):
+    nodes_ptr, data_ptr = builder.result_device()
+    return ooc.check_octree_device(nodes_ptr, info["n_nodes"], data_ptr, info["n_data"], N, binary)
+
+
+def test_configuration_3_full_size_is_well_formed(builder):
+    # svo_builder_binary -s 4096 -l 2048: 20M triangles, 64 partitions, 651M nodes
+    t = tri.soup_tris(20_000_000, 4096, seed=3, sigma=1.0)
+    d = torch.from_numpy(t).cuda()
+    info = builder.build_device(d.data_ptr(), t.shape[0], make_params(4096, 2048, geometry_only=True))
+    assert info["n_partitions"] == 64
+    c = device_check(builder, info, 4096, True)
+    assert c["errors"] == []
+    assert c["n_leaves"] == info["n_filled"] > 0
+    assert c["max_depth"] == 12
+    assert c["n_leaves"] + c["n_inner"] == info["n_nodes"]
+
+
+def test_configuration_2_full_size_batch_equals_plain(builder):
+    # svo_builder -s 1024 -c model on the 2,093,058-triangle heightfield: the batched call's
+    # files hash the same as the plain call's, and the tree is well formed
+    t = tri.heightfield_tris(1024, seed=2, payload=True)
+    p = make_params(1024, 2048, geometry_only=False)
+    plain = builder.build(t, p)
+    other = tri.icosphere_tris(3, seed=5, payload=True)
+    batch = builder.build_batch([other, t, other], [make_params(64, 2048, geometry_only=False), p,
+                                                   make_params(64, 2048, geometry_only=False)])
+    h = lambda tree: hashlib.sha256(tree.nodes.tobytes() + tree.data.tobytes()).hexdigest()
+    assert h(batch[1].tree) == h(plain.tree)
+    d = torch.from_numpy(t).cuda()
+    info = builder.build_device(d.data_ptr(), t.shape[0], p)
+    c = device_check(builder, info, 1024, False)
+    assert c["errors"] == [] and c["n_leaves"] == info["n_filled"] == plain.info["n_filled"]
