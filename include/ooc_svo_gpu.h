@@ -125,6 +125,12 @@ typedef int (*ooc_batch_sink_fn)(void* user, uint64_t mesh, int32_t kind, const 
 int ooc_build_batch(ooc_ctx* ctx, const ooc_mesh* meshes, uint64_t n_meshes, ooc_batch_sink_fn sink, void* user,
                     ooc_build_info* infos);
 
+/* Triangles already in device memory (n_tris * 9 or 21 floats), octree files
+ * delivered to the sink in host memory: the path of ooc_build without its
+ * upload (the file front end reads .tridata straight to the device). */
+int ooc_build_from_device(ooc_ctx* ctx, const ooc_build_params* params, const float* tris_device, uint64_t n_tris,
+                          ooc_sink_fn sink, void* user, ooc_build_info* info);
+
 /* ---- Batched build into device memory (no counterpart in the reference) ----
  * Like ooc_build_batch (host triangles in), but every mesh's node and data
  * files are written straight into device memory that the caller provides:

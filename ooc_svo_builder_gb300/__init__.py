@@ -35,7 +35,7 @@ EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_
            "ooc_voxelize_occupancy_noalloc", "ooc_build_batch", "ooc_server_create", "ooc_server_submit",
            "ooc_server_poll", "ooc_server_release", "ooc_server_destroy", "ooc_build_batch_device",
            "ooc_arena_alloc", "ooc_set_batch_budget", "ooc_batch_budget", "ooc_server_read", "ooc_get_tuning",
-           "ooc_set_tuning", "ooc_autotune", "ooc_check_octree_device")
+           "ooc_set_tuning", "ooc_autotune", "ooc_check_octree_device", "ooc_build_from_device")
 CHECK_BITS = {1: "child group order", 2: "reference count", 4: "depth", 8: "data index", 16: "payload Morton code"}
 
 
@@ -177,6 +177,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_set_tuning.restype = ctypes.c_int
     lib.ooc_autotune.argtypes = [ctypes.c_void_p, P(Mesh), ctypes.c_uint64, P(Tuning)]
     lib.ooc_autotune.restype = ctypes.c_int
+    lib.ooc_build_from_device.argtypes = [ctypes.c_void_p, P(BuildParams), ctypes.c_void_p, ctypes.c_uint64, SINK,
+                                          ctypes.c_void_p, P(BuildInfo)]
+    lib.ooc_build_from_device.restype = ctypes.c_int
     lib.ooc_check_octree_device.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64,
                                             ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p, P(OctreeCheck)]
     lib.ooc_check_octree_device.restype = ctypes.c_int

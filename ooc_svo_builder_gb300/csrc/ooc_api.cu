@@ -1689,6 +1689,36 @@ int ooc_build_device(ooc_ctx* c, const ooc_build_params* prm, const float* tris_
   });
 }
 
+int ooc_build_from_device(ooc_ctx* c, const ooc_build_params* prm, const float* tris_device, uint64_t n_tris,
+                          ooc_sink_fn sink, void* user, ooc_build_info* info) {
+  return guarded(c, [&] {
+    begin_build(c);
+    check_params(prm, n_tris);
+    if (!sink) fail(OOC_ERR_INVALID, "sink is NULL");
+    if (n_tris && !tris_device) fail(OOC_ERR_INVALID, "triangles are NULL");
+    cudaStream_t st = c->own_stream;
+    SingleSink ss{sink, user};
+    Emitter out;
+    out.sink = single_sink;
+    out.user = &ss;
+    std::vector<MeshWork> meshes;
+    meshes.emplace_back(make_plan(prm), &out);
+    meshes[0].prm = prm;
+    meshes[0].d_tris = tris_device;
+    meshes[0].n_tris = n_tris;
+    {
+      PhaseScope all(c, PH_ALL, st);
+      OutSpec os;
+      os.mode = OUT_HOST;
+      build_meshes(c, st, meshes, os);
+    }
+    ck(cudaStreamSynchronize(st), "build");
+    ck(cudaGetLastError(), "build kernels");
+    fill_info(meshes[0], info);
+    finish_timing(c);
+  });
+}
+
 int ooc_result_device(ooc_ctx* c, const void** nodes_device, const void** data_device) {
   if (!c) return OOC_ERR_INVALID;
   if (!c->res_valid) {

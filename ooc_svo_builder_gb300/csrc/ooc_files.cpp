@@ -2,10 +2,17 @@
 // .octreedata out, named and formatted as the reference does.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <fstream>
+#include <mutex>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "ooc_svo_gpu.h"
 
@@ -60,15 +67,123 @@ bool parse_tri_header(const std::string& filename, TriHeader& t, std::string& er
   return true;
 }
 
-struct FileSink {
-  FILE* nodes = nullptr;
-  FILE* data = nullptr;
+// .tridata straight into device memory: fixed-size chunks are read into two
+// pinned buffers in turn, and each chunk's upload overlaps the read of the
+// next, so no pinned copy of the whole file is made.
+bool read_to_device(const std::string& path, size_t bytes, void* dst, std::string& err) {
+  constexpr size_t kChunk = 64ull << 20;
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) {
+    err = "cannot open " + path;
+    return false;
+  }
+  void* pin[2] = {nullptr, nullptr};
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  cudaStream_t st = nullptr;
+  bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+  for (int i = 0; i < 2 && ok; i++)
+    ok = cudaMallocHost(&pin[i], std::min(kChunk, std::max<size_t>(bytes, 1))) == cudaSuccess &&
+         cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming) == cudaSuccess;
+  size_t off = 0;
+  for (int i = 0; ok && off < bytes; i ^= 1) {
+    const size_t n = std::min(kChunk, bytes - off);
+    ok = cudaEventSynchronize(done[i]) == cudaSuccess;  // the buffer's previous upload is done
+    if (ok && std::fread(pin[i], 1, n, f) != n) {
+      err = "short read of " + path;
+      ok = false;
+      break;
+    }
+    ok = ok && cudaMemcpyAsync(static_cast<char*>(dst) + off, pin[i], n, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+         cudaEventRecord(done[i], st) == cudaSuccess;
+    off += n;
+  }
+  if (st && cudaStreamSynchronize(st) != cudaSuccess) ok = false;
+  for (int i = 0; i < 2; i++) {
+    if (pin[i]) cudaFreeHost(pin[i]);
+    if (done[i]) cudaEventDestroy(done[i]);
+  }
+  if (st) cudaStreamDestroy(st);
+  std::fclose(f);
+  if (!ok && err.empty()) err = "device upload of " + path + " failed";
+  return ok;
+}
+
+// One writer thread per output file: the sink copies each piece into the
+// file's current 16 MiB buffer and hands full buffers to the thread, so the
+// two files are written in parallel and neither stalls the build.  At most
+// four buffers per file are in flight.
+class FileWriter {
+ public:
+  explicit FileWriter(FILE* f) : f_(f), th_([this] { loop(); }) {}
+  ~FileWriter() { finish(); }
+
+  bool put(const void* bytes, size_t n) {
+    const char* p = static_cast<const char*>(bytes);
+    while (n) {
+      if (cur_.size() == kBuf) flush_current();
+      const size_t k = std::min(n, kBuf - cur_.size());
+      cur_.insert(cur_.end(), p, p + k);
+      p += k;
+      n -= k;
+    }
+    return !failed_.load();
+  }
+
+  // Write what is left, stop the thread; true when every write succeeded.
+  bool finish() {
+    if (th_.joinable()) {
+      if (!cur_.empty()) flush_current();
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        stop_ = true;
+      }
+      cv_.notify_all();
+      th_.join();
+    }
+    return !failed_.load();
+  }
+
+ private:
+  static constexpr size_t kBuf = 16ull << 20;
+  static constexpr size_t kInFlight = 4;
+
+  void flush_current() {
+    std::unique_lock<std::mutex> lk(mu_);
+    cv_.wait(lk, [&] { return q_.size() < kInFlight; });
+    q_.push_back(std::move(cur_));
+    cur_ = std::vector<char>();
+    cur_.reserve(kBuf);
+    cv_.notify_all();
+  }
+
+  void loop() {
+    for (;;) {
+      std::vector<char> b;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return stop_ || !q_.empty(); });
+        if (q_.empty()) return;
+        b = std::move(q_.front());
+        q_.pop_front();
+      }
+      cv_.notify_all();
+      if (!b.empty() && std::fwrite(b.data(), 1, b.size(), f_) != b.size()) failed_ = true;
+    }
+  }
+
+  FILE* f_;
+  std::vector<char> cur_;
+  std::deque<std::vector<char>> q_;
+  std::mutex mu_;
+  std::condition_variable cv_;
+  bool stop_ = false;
+  std::atomic<bool> failed_{false};
+  std::thread th_;
 };
 
-int file_sink(void* user, int32_t kind, const void* bytes, uint64_t n) {
-  FileSink* s = static_cast<FileSink*>(user);
-  FILE* f = kind == OOC_STREAM_NODES ? s->nodes : s->data;
-  return fwrite(bytes, 1, (size_t)n, f) == (size_t)n ? 0 : 1;
+int writer_sink(void* user, int32_t kind, const void* bytes, uint64_t n) {
+  FileWriter** w = static_cast<FileWriter**>(user);
+  return w[kind == OOC_STREAM_NODES ? 0 : 1]->put(bytes, (size_t)n) ? 0 : 1;
 }
 
 }  // namespace
@@ -88,36 +203,31 @@ extern "C" int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_bui
   const int stride = prm.geometry_only ? 9 : 21;
   const size_t bytes = (size_t)h.n_triangles * stride * sizeof(float);
   void* tris = nullptr;
-  if (bytes && cudaMallocHost(&tris, bytes) != cudaSuccess) return OOC_ERR_OOM;
-  std::string data_path = h.base + ".tridata";
-  FILE* f = fopen(data_path.c_str(), "rb");
-  if (!f) {
-    if (tris) cudaFreeHost(tris);
-    return OOC_ERR_IO;
-  }
-  const size_t got = bytes ? fread(tris, 1, bytes, f) : 0;
-  fclose(f);
-  if (got != bytes) {
-    if (tris) cudaFreeHost(tris);
+  if (bytes && cudaMalloc(&tris, bytes) != cudaSuccess) return OOC_ERR_OOM;
+  if (bytes && !read_to_device(h.base + ".tridata", bytes, tris, err)) {
+    cudaFree(tris);
     return OOC_ERR_IO;
   }
   const uint64_t P = ooc_estimate_partitions(prm.gridsize, prm.memory_limit_mb);
   // <base><gridsize>_<npartitions> (partitioner.cpp:90, 141; main.cpp:325)
   const std::string base = h.base + std::to_string(prm.gridsize) + "_" + std::to_string(P);
-  FileSink sink;
-  sink.nodes = fopen((base + ".octreenodes").c_str(), "wb");
-  sink.data = fopen((base + ".octreedata").c_str(), "wb");
+  FILE* fn = std::fopen((base + ".octreenodes").c_str(), "wb");
+  FILE* fd = std::fopen((base + ".octreedata").c_str(), "wb");
   int rc = OOC_OK;
   ooc_build_info local;
   std::memset(&local, 0, sizeof(local));
-  if (!sink.nodes || !sink.data) {
+  if (!fn || !fd) {
     rc = OOC_ERR_IO;
   } else {
-    rc = ooc_build(ctx, &prm, static_cast<const float*>(tris), h.n_triangles, file_sink, &sink, &local);
+    FileWriter wn(fn), wd(fd);
+    FileWriter* w[2] = {&wn, &wd};
+    rc = ooc_build_from_device(ctx, &prm, static_cast<const float*>(tris), h.n_triangles, writer_sink, w, &local);
+    const bool ok_n = wn.finish(), ok_d = wd.finish();
+    if (rc == OOC_OK && !(ok_n && ok_d)) rc = OOC_ERR_IO;
   }
-  if (sink.nodes) fclose(sink.nodes);
-  if (sink.data) fclose(sink.data);
-  if (tris) cudaFreeHost(tris);
+  if (fn) std::fclose(fn);
+  if (fd) std::fclose(fd);
+  if (tris) cudaFree(tris);
   if (rc != OOC_OK) return rc;
   // writeOctreeHeader (octree_io.h:74-83)
   std::ofstream out((base + ".octree").c_str(), std::ios::out);
