@@ -313,41 +313,51 @@ __device__ __forceinline__ uint32_t leaf_rank(const VoxJob& j, uint32_t b) {
   return j.leafscan[blk] - j.leafscan_base + in_block_rank(j.leafbits + (uint64_t)blk * 8, b);
 }
 
-// One z column of pass 0 (set bits) or pass 1 (winners, re-testing set voxels).
-// Returns the column's pass bits (bit z - z0) for columns of at most 64 voxels.
-template <int PASS>
-__device__ __forceinline__ uint64_t vox_column(const VoxJob& j, const TriSetup& s, uint32_t tri, int x, int y, int z0,
-                                               int z1) {
+// One z column of a small item: sets its voxels' bits and returns the column's
+// pass bits (bit z - z0, columns of at most 64 voxels).  The halves of the YZ
+// and ZX edge functions that depend only on the column are formed once: each
+// is the same rounded product the per-voxel expression would form, and the
+// one addition that joins the halves is commutative, so every test is bit for
+// bit the reference's (voxelizer.cpp:266-287).
+__device__ __forceinline__ uint64_t vox_column(const VoxJob& j, const TriSetup& s, int x, int y, int z0, int z1) {
   const float px = __fmul_rn((float)x, j.u);
   const float py = __fmul_rn((float)y, j.u);
   if (!pass_xy(s, px, py)) return 0;
   const float nxy = plane_xy(s, px, py);
+  float yz_col[3], zx_col[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    yz_col[k] = __fmul_rn(s.yz[k][0], py);  // dot2(yz, (py, pz)) = yz0*py + yz1*pz
+    zx_col[k] = __fmul_rn(s.zx[k][1], px);  // dot2(zx, (pz, px)) = zx0*pz + zx1*px
+  }
   const uint32_t mxy = spread3_10((uint32_t)(x - j.sa[0])) | (spread3_10((uint32_t)(y - j.sa[1])) << 1);
   constexpr uint32_t ZBITS = 0x24924924u;  // Morton bit positions of z (2, 5, ..., 29)
   uint32_t mz = spread3_10((uint32_t)(z0 - j.sa[2])) << 2;
   uint32_t cur_w = 0xffffffffu, acc = 0;
   uint64_t col = 0;
   for (int z = z0; z <= z1; z++, mz = ((mz | ~ZBITS) + 4u) & ZBITS) {
+    const float pz = __fmul_rn((float)z, j.u);
+    const float nDOTp = __fadd_rn(nxy, __fmul_rn(s.n[2], pz));
+    if (__fmul_rn(__fadd_rn(nDOTp, s.d1), __fadd_rn(nDOTp, s.d2)) > 0.0f) continue;
+    bool pass = true;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      pass = pass && !(__fadd_rn(__fadd_rn(yz_col[k], __fmul_rn(s.yz[k][1], pz)), s.dyz[k]) < 0.0f);
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      pass = pass && !(__fadd_rn(__fadd_rn(__fmul_rn(s.zx[k][0], pz), zx_col[k]), s.dzx[k]) < 0.0f);
+    if (!pass) continue;
     const uint32_t m = mxy | mz;
-    if (PASS == 0) {
-      if (pass_z(s, nxy, px, py, __fmul_rn((float)z, j.u))) {
-        const uint32_t w = m >> 5;
-        if (w != cur_w) {
-          if (acc) atomicOr(&j.leafbits[cur_w], acc);
-          cur_w = w;
-          acc = 0;
-        }
-        acc |= 1u << (m & 31);
-        if (z - z0 < 64) col |= 1ull << (z - z0);
-      }
-    } else {
-      const uint32_t word = j.leafbits[m >> 5];
-      if ((word >> (m & 31)) & 1u) {
-        if (pass_z(s, nxy, px, py, __fmul_rn((float)z, j.u))) atomicMin(&j.winners[leaf_rank(j, m)], tri);
-      }
+    const uint32_t w = m >> 5;
+    if (w != cur_w) {
+      if (acc) atomicOr(&j.leafbits[cur_w], acc);
+      cur_w = w;
+      acc = 0;
     }
+    acc |= 1u << (m & 31);
+    if (z - z0 < 64) col |= 1ull << (z - z0);
   }
-  if (PASS == 0 && acc) atomicOr(&j.leafbits[cur_w], acc);
+  if (acc) atomicOr(&j.leafbits[cur_w], acc);
   return col;
 }
 
@@ -508,7 +518,7 @@ __device__ __forceinline__ void vox_small_occ_item(const VoxJob& j, uint64_t i) 
       uint32_t shift = 0;
       for (int x = lo[0]; x <= hi[0]; x++)
         for (int y = lo[1]; y <= hi[1]; y++) {
-          mask |= vox_column<0>(j, s, (uint32_t)t, x, y, lo[2], hi[2]) << shift;
+          mask |= vox_column(j, s, x, y, lo[2], hi[2]) << shift;
           shift += (uint32_t)bz;
         }
       if (j.item_mask && mask) {
@@ -1034,7 +1044,7 @@ __device__ __forceinline__ uint32_t cta_stripe(const uint64_t* __restrict__ cta_
 // and indexes elements directly; a batch launch finds its stripe first and
 // stages the job in shared memory.
 template <int PASS, bool SINGLE>
-__global__ void __launch_bounds__(kChunk) kb_vox_small(const VoxJob* __restrict__ jobs,
+__global__ void __launch_bounds__(kChunk, 4) kb_vox_small(const VoxJob* __restrict__ jobs,
                                                        const uint64_t* __restrict__ cta_beg, uint32_t n, VoxJob j0) {
   if constexpr (SINGLE) {
     const uint64_t i = (uint64_t)blockIdx.x * kChunk + threadIdx.x;
