@@ -538,6 +538,25 @@ def serve_stream(srv, pool, rate: float, duration: float, seed: int, drain_s: fl
             "output_gb": float(sum(r["bytes"] for r in results) / 1e9)}
 
 
+def serve_burst(srv, pool, n: int, seed: int) -> dict:
+    """Capacity: `n` requests submitted at once; meshes/s until the last completes."""
+    rng = np.random.default_rng(seed)
+    picks = rng.integers(0, len(pool), size=n)
+    t0 = time.perf_counter()
+    for k in picks:
+        srv.submit_ptr(*pool[k])
+    done = []
+    while len(done) < n:
+        r = srv.poll(1000, copy=False)
+        if r is not None:
+            done.append(r)
+    wall = time.perf_counter() - t0
+    lat = np.array([(r["t_done_us"] - r["t_submit_us"]) / 1e3 for r in done])
+    return {"requests": n, "meshes_per_s": n / wall, "seconds": wall, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "mean_batch": float(np.mean([r["batch_size"] for r in done])),
+            "failed": int(sum(r["status"] != 0 for r in done))}
+
+
 def run_serve(args, world, rank, local):
     """Configuration 5: Poisson request streams through the serving loop (continuous batching,
     footprint admission) and, on the same streams, through the plain path (one request at a time)."""
@@ -578,6 +597,17 @@ def run_serve(args, world, rank, local):
                         pass
                 out[arm].append(serve_stream(srv, pool, r, args.duration, seed=5 + int(r), drain_s=args.drain))
             print("serve %s %.0f req/s: %s" % (arm, r, json.dumps(out[arm][-1])), file=sys.stderr, flush=True)
+    # capacity of the resident arms: a burst of requests submitted at once
+    capacity = {}
+    for arm in ("served_resident", "plain_resident"):
+        with ooc.Server(local, **arms[arm]) as srv:
+            for i in warm:
+                srv.submit_ptr(*pool[i])
+            for _ in warm:
+                while srv.poll(1000, copy=False) is None:
+                    pass
+            capacity[arm] = serve_burst(srv, pool, args.burst, seed=77)
+        print("serve burst %s: %s" % (arm, json.dumps(capacity[arm])), file=sys.stderr, flush=True)
     top = out["served_resident"][-1]
     top_host = out["served_host"][-1]
 
@@ -597,6 +627,8 @@ def run_serve(args, world, rank, local):
         "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
         "arms": out,
         "speedup_vs_plain_resident": ratio("served_resident", "plain_resident"),
+        "capacity": dict(capacity, speedup_vs_plain=capacity["served_resident"]["meshes_per_s"] /
+                         max(capacity["plain_resident"]["meshes_per_s"], 1e-9)),
         "speedup_vs_plain_host": ratio("served_host", "plain_host"),
         "e2e": {"value": top_host["meshes_per_s"], "unit": "meshes/s", "p50_ms": top_host["p50_ms"],
                 "p99_ms": top_host["p99_ms"], "note": "results copied back to host memory",
@@ -667,6 +699,7 @@ def main():
     ap.add_argument("--duration", type=float, default=5.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--drain", type=float, default=10.0, help="serve: seconds to wait for the queue to drain")
     ap.add_argument("--engines", type=int, default=2, help="serve: engines of the served arm")
+    ap.add_argument("--burst", type=int, default=4096, help="serve: requests of the capacity burst")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-files", action="store_true", help="skip the file-to-file measurement")
     ap.add_argument("--ref-cores", type=int, default=0, help="reference arm: host processes (default: all cores)")
