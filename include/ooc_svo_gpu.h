@@ -170,7 +170,7 @@ typedef struct {
   uint32_t large_ctas_per_sm; /* persistent CTAs per SM of the large-triangle kernel (1..16) */
   uint64_t batch_budget;      /* occupancy-pyramid bytes per sub-batch (>= 4096), as ooc_set_batch_budget */
   uint32_t graphs;            /* 1: replay each sub-batch's two launch sequences as CUDA graphs; 0: launch directly */
-  uint32_t reserved;          /* must be 0 */
+  uint32_t light_per_thread;  /* elements each thread of the per-block and per-node kernels takes (1..16) */
 } ooc_tuning;
 
 int ooc_get_tuning(const ooc_ctx* ctx, ooc_tuning* out);

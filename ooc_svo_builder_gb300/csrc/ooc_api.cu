@@ -143,7 +143,7 @@ struct ooc_ctx {
   std::vector<cudaEvent_t> up_events;    // recorded on h2d_stream as groups of meshes arrive
   DevBuf d_tables1, d_tables2;
   std::vector<DevBuf> d_mesh_items;
-  ooc_tuning tuning = {64, 16, 256, 4, 4ull << 30, 0, 0};  // launch choices (ooc_set_tuning / ooc_autotune)
+  ooc_tuning tuning = {64, 16, 256, 4, 4ull << 30, 0, 8};  // launch choices (ooc_set_tuning / ooc_autotune)
   // executable graphs of captured launch sequences, by shape (launch count and kernels)
   std::vector<std::pair<uint64_t, cudaGraphExec_t>> graph_execs;
   DevBuf d_tune_arena;                               // autotuner outputs
@@ -554,12 +554,33 @@ int pyramid_levels(int Ds, Level* lv, uint64_t& words, uint64_t& blocks) {
   return Ds;
 }
 
-// CTA prefix of one batched launch: stripe s gets ceil(count(s) / kChunk) CTAs.
+// CTA prefix of one batched launch: stripe s gets ceil(count(s) / per_cta) CTAs.
 template <typename F>
-std::vector<uint64_t> cta_prefix(uint32_t n, F count) {
+std::vector<uint64_t> cta_prefix(uint32_t n, uint64_t per_cta, F count) {
   std::vector<uint64_t> beg(n + 1, 0);
-  for (uint32_t s = 0; s < n; s++) beg[s + 1] = beg[s] + (count(s) + kChunk - 1) / kChunk;
+  for (uint32_t s = 0; s < n; s++) beg[s + 1] = beg[s] + (count(s) + per_cta - 1) / per_cta;
   return beg;
+}
+
+// A per-block or per-node launch: its CTA prefix and the elements each thread
+// takes.  A thread takes as many elements (up to the tuning's limit) as still
+// leave about 16 CTAs per SM: few CTAs cost parallelism on small levels, many
+// cost the per-CTA staging on large ones.
+struct Light {
+  std::vector<uint64_t> beg;
+  uint32_t ept = 1;
+};
+
+template <typename F>
+Light light_prefix(const ooc_ctx* c, uint32_t n, F count) {
+  std::vector<uint64_t> cnt(n);
+  uint64_t total = 0;
+  for (uint32_t s = 0; s < n; s++) total += cnt[s] = count(s);
+  Light L;
+  const uint64_t fill = (uint64_t)c->num_sms * 16 * kChunk;
+  L.ept = (uint32_t)std::min<uint64_t>(c->tuning.light_per_thread, std::max<uint64_t>(1, total / fill));
+  L.beg = cta_prefix(n, (uint64_t)kChunk * L.ept, [&](uint32_t s) { return cnt[s]; });
+  return L;
 }
 
 // Upload host vectors into one device buffer through pinned staging; returns device pointers.
@@ -705,10 +726,10 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     j.item_mask = m.pl.binary ? nullptr : item_mask + item_beg[s];
     j.item_box = m.pl.binary ? nullptr : item_box + item_beg[s];
   }
-  const std::vector<uint64_t> cp_items = cta_prefix(n, [&](uint32_t s) { return sb[s].n_items; });
-  std::vector<std::vector<uint64_t>> cp_pyr;
+  const std::vector<uint64_t> cp_items = cta_prefix(n, kChunk, [&](uint32_t s) { return sb[s].n_items; });
+  std::vector<Light> cp_pyr;
   for (int r = 0; r <= max_depth - kTopPyramidLevel - 1; r++)
-    cp_pyr.push_back(cta_prefix(n, [&](uint32_t s) -> uint64_t {
+    cp_pyr.push_back(light_prefix(c, n, [&](uint32_t s) -> uint64_t {
       const int l = pyr[s].depth - r;
       return l > kTopPyramidLevel ? pyr[s].lv[l].nblocks : 0;
     }));
@@ -719,7 +740,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const size_t o_beg = up1.add(item_beg.data(), (n + 1) * 8);
   const size_t o_cpi = up1.add(cp_items.data(), (n + 1) * 8);
   std::vector<size_t> o_cpp(cp_pyr.size());
-  for (size_t r = 0; r < cp_pyr.size(); r++) o_cpp[r] = up1.add(cp_pyr[r].data(), (n + 1) * 8);
+  for (size_t r = 0; r < cp_pyr.size(); r++) o_cpp[r] = up1.add(cp_pyr[r].beg.data(), (n + 1) * 8);
   unsigned char* t1 = up1.run(c, c->d_tables1, c->h_tables1, st);
   auto dp1 = [&](size_t off) { return reinterpret_cast<const uint64_t*>(t1 + off); };
   const VoxJob* d_vj = reinterpret_cast<const VoxJob*>(t1 + o_vj);
@@ -742,7 +763,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       PhaseScope ph(c, PH_PYR, st);
       ck(cudaMemsetAsync(scan + blocks, 0, 4, st), "memset scan");
       for (size_t r = 0; r < cp_pyr.size(); r++)
-        launch_b_pyramid(d_pyr, dp1(o_cpp[r]), n, cp_pyr[r][n], (int)r, n == 1 ? &pyr[0] : nullptr, st);
+        launch_b_pyramid(d_pyr, dp1(o_cpp[r]), n, cp_pyr[r].beg[n], cp_pyr[r].ept, (int)r, n == 1 ? &pyr[0] : nullptr,
+                         st);
       launch_b_pyramid_top(d_pyr, n, kTopPyramidLevel, st);
       scan_u32_exclusive(scan, blocks + 1, scanpart, st);
       launch_b_level_bases(d_pyr, n, d_root, st);
@@ -907,27 +929,27 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     e.l_small = ls;
   }
   auto live = [&](uint32_t s) { return !pl[s].empty; };
-  const std::vector<uint64_t> cp_compact = cta_prefix(n, [&](uint32_t s) {
+  const Light cp_compact = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
     return pyr[s].lv[pyr[s].depth].off_b + pyr[s].lv[pyr[s].depth].nblocks - pyr[s].lv[0].off_b;
   });
-  const std::vector<uint64_t> cp_pay = cta_prefix(n, [&](uint32_t s) -> uint64_t {
+  const std::vector<uint64_t> cp_pay = cta_prefix(n, kChunk, [&](uint32_t s) -> uint64_t {
     return meshes[sb[s].mesh].pl.binary ? 0 : sb[s].n_items;
   });
-  const std::vector<uint64_t> cp_leafpay = cta_prefix(n, [&](uint32_t s) -> uint64_t {
+  const Light cp_leafpay = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
     const Plan& mp = meshes[sb[s].mesh].pl;
     return (live(s) && mp.levels && !mp.binary) ? pl[s].n_leaf : 0;
   });
-  const std::vector<uint64_t> cp_leaves = cta_prefix(n, [&](uint32_t s) -> uint64_t {
+  const Light cp_leaves = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
     return (live(s) && pyr[s].depth >= 1) ? pl[s].n_leaf : 0;  // a depth-0 root is the leaf
   });
-  std::vector<std::vector<uint64_t>> cp_bu(max_depth + 1), cp_td(max_depth + 1);
+  std::vector<Light> cp_bu(max_depth + 1), cp_td(max_depth + 1);
   for (int r = 1; r <= max_depth; r++)
-    cp_bu[r] = cta_prefix(n, [&](uint32_t s) -> uint64_t {
+    cp_bu[r] = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
       const int l = pyr[s].depth - r;
       return (live(s) && l > ej[s].l_small && l >= 0) ? pyr[s].lv[l].n : 0;
     });
   for (int l = 0; l <= max_depth; l++)
-    cp_td[l] = cta_prefix(n, [&](uint32_t s) -> uint64_t {
+    cp_td[l] = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
       const int last_top = std::min(ej[s].l_small, pyr[s].depth - 2);
       return (live(s) && l > last_top && l <= pyr[s].depth - 2) ? pyr[s].lv[l + 1].n : 0;  // one thread per child
     });
@@ -935,13 +957,13 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const size_t o_vj2 = up2.add(vj.data(), n * sizeof(VoxJob));
   const size_t o_pyr2 = up2.add(pyr.data(), n * sizeof(Pyramid));
   const size_t o_ej = up2.add(ej.data(), n * sizeof(EmitJob));
-  const size_t o_cc = up2.add(cp_compact.data(), (n + 1) * 8);
+  const size_t o_cc = up2.add(cp_compact.beg.data(), (n + 1) * 8);
   const size_t o_cpay = up2.add(cp_pay.data(), (n + 1) * 8);
-  const size_t o_clp = up2.add(cp_leafpay.data(), (n + 1) * 8);
-  const size_t o_cl = up2.add(cp_leaves.data(), (n + 1) * 8);
+  const size_t o_clp = up2.add(cp_leafpay.beg.data(), (n + 1) * 8);
+  const size_t o_cl = up2.add(cp_leaves.beg.data(), (n + 1) * 8);
   std::vector<size_t> o_bu(cp_bu.size(), 0), o_td(cp_td.size(), 0);
-  for (size_t r = 1; r < cp_bu.size(); r++) o_bu[r] = up2.add(cp_bu[r].data(), (n + 1) * 8);
-  for (size_t l = 0; l < cp_td.size(); l++) o_td[l] = up2.add(cp_td[l].data(), (n + 1) * 8);
+  for (size_t r = 1; r < cp_bu.size(); r++) o_bu[r] = up2.add(cp_bu[r].beg.data(), (n + 1) * 8);
+  for (size_t l = 0; l < cp_td.size(); l++) o_td[l] = up2.add(cp_td[l].beg.data(), (n + 1) * 8);
   unsigned char* t2 = up2.run(c, c->d_tables2, c->h_tables2, st);
   auto dp2 = [&](size_t off) { return reinterpret_cast<const uint64_t*>(t2 + off); };
   const VoxJob* d_vj2 = reinterpret_cast<const VoxJob*>(t2 + o_vj2);
@@ -954,7 +976,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   run_launches(c, st, 1, [&] {
     {
       PhaseScope ph(c, PH_PYR, st);
-      launch_b_compact(d_pyr2, dp2(o_cc), n, cp_compact[n], keys, n == 1 ? &pyr[0] : nullptr, st);
+      launch_b_compact(d_pyr2, dp2(o_cc), n, cp_compact.beg[n], cp_compact.ept, keys, n == 1 ? &pyr[0] : nullptr, st);
     }
     if (any_payload) {
       PhaseScope ph(c, PH_VOX, st);
@@ -962,17 +984,17 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       launch_b_vox_small(d_vj2, dp2(o_cpay), n, cp_pay[n], 1, n == 1 ? &vj[0] : nullptr, st);
       launch_b_vox_large(d_vj2, d_beg, n, task_off, items, counter, 1, st, c->num_sms, (int)c->tuning.large_block,
                          (int)c->tuning.large_ctas_per_sm);
-      launch_b_leaf_payload(d_pyr2, d_ej, dp2(o_clp), n, cp_leafpay[n], sp1, se1, st);
+      launch_b_leaf_payload(d_pyr2, d_ej, dp2(o_clp), n, cp_leafpay.beg[n], cp_leafpay.ept, sp1, se1, st);
     }
     {
       PhaseScope ph(c, PH_TREE, st);
       for (size_t r = 1; r < cp_bu.size(); r++)
-        launch_b_bottom_up(d_pyr2, d_ej, dp2(o_bu[r]), n, cp_bu[r][n], (int)r, sp1, se1, st);
+        launch_b_bottom_up(d_pyr2, d_ej, dp2(o_bu[r]), n, cp_bu[r].beg[n], cp_bu[r].ept, (int)r, sp1, se1, st);
       launch_b_bottom_up_top(d_pyr2, d_ej, n, st);
       launch_b_top_down_top(d_pyr2, d_ej, n, st);
       for (size_t l = 0; l < cp_td.size(); l++)
-        launch_b_top_down(d_pyr2, d_ej, dp2(o_td[l]), n, cp_td[l][n], (int)l, sp1, se1, st);
-      launch_b_top_down_leaves(d_pyr2, d_ej, dp2(o_cl), n, cp_leaves[n], sp1, se1, st);
+        launch_b_top_down(d_pyr2, d_ej, dp2(o_td[l]), n, cp_td[l].beg[n], cp_td[l].ept, (int)l, sp1, se1, st);
+      launch_b_top_down_leaves(d_pyr2, d_ej, dp2(o_cl), n, cp_leaves.beg[n], cp_leaves.ept, sp1, se1, st);
       launch_b_root_info(d_pyr2, d_ej, n, d_root, st);
       ck(cudaMemcpyAsync(hr, d_root, ((uint64_t)n * 16 + 1) * 4, cudaMemcpyDeviceToHost, st), "root info");
     }
@@ -1552,7 +1574,8 @@ namespace {
 bool tuning_ok(const ooc_tuning& t) {
   return t.small_vol >= 1 && t.small_vol <= 64 && t.lines_per_lane >= 1 && t.lines_per_lane <= 64 &&
          (t.large_block == 64 || t.large_block == 128 || t.large_block == 256) && t.large_ctas_per_sm >= 1 &&
-         t.large_ctas_per_sm <= 16 && t.batch_budget >= 4096 && t.graphs <= 1 && t.reserved == 0;
+         t.large_ctas_per_sm <= 16 && t.batch_budget >= 4096 && t.graphs <= 1 && t.light_per_thread >= 1 &&
+         t.light_per_thread <= 16;
 }
 
 struct TuneArena {
@@ -1619,7 +1642,8 @@ int ooc_autotune(ooc_ctx* c, const ooc_mesh* sample, uint64_t n, ooc_tuning* bes
   rc = time_one(cur, cur_ms);  // warms the context's buffers too
   if (rc == OOC_OK) rc = time_one(cur, cur_ms);
   // one coordinate pass: each choice in turn, the others held at their best so far
-  const uint32_t lpl[] = {4, 8, 16, 32}, cps[] = {2, 4, 8}, blk[] = {128, 256}, svol[] = {16, 32, 48, 64}, gr[] = {0, 1};
+  const uint32_t lpl[] = {4, 8, 16, 32}, cps[] = {2, 4, 8}, blk[] = {128, 256}, svol[] = {16, 32, 48, 64}, gr[] = {0, 1},
+                 ept[] = {1, 2, 4, 8};
   const uint64_t bud[] = {1ull << 30, 2ull << 30, 4ull << 30, 8ull << 30};
   auto try_values = [&](auto setter, const auto& values) {
     for (const auto& v : values) {
@@ -1640,6 +1664,7 @@ int ooc_autotune(ooc_ctx* c, const ooc_mesh* sample, uint64_t n, ooc_tuning* bes
   try_values([](ooc_tuning& t, uint32_t v) { t.large_block = v; }, blk);
   try_values([](ooc_tuning& t, uint32_t v) { t.small_vol = v; }, svol);
   try_values([](ooc_tuning& t, uint64_t v) { t.batch_budget = v; }, bud);
+  try_values([](ooc_tuning& t, uint32_t v) { t.light_per_thread = v; }, ept);
   try_values([](ooc_tuning& t, uint32_t v) { t.graphs = v; }, gr);
   c->tuning = rc == OOC_OK ? cur : start;
   if (best) *best = c->tuning;

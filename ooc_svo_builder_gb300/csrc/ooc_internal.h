@@ -129,26 +129,26 @@ void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n
                         uint64_t total_items, unsigned long long* counter, int pass, cudaStream_t st, int num_sms,
                         int block, int ctas_per_sm);
 // Level depth - r of each stripe.
-void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, int r,
+void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, int r,
                       const Pyramid* single, cudaStream_t st);
 // One CTA per stripe: levels min(l_hi, depth) .. 0.
 void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cudaStream_t st);
-void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t* keys,
+void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, uint32_t* keys,
                       const Pyramid* single, cudaStream_t st);
 // out[s * (kMaxLevels + 1) + l] = global node index of level l's first node, l = 0..depth+1.
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, cudaStream_t st);
 void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
-                           uint64_t ctas, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
+                           uint64_t ctas, uint32_t ept, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 // Level depth - r of each stripe.
-void launch_b_bottom_up(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas,
+void launch_b_bottom_up(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept,
                         int r, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 void launch_b_bottom_up_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, cudaStream_t st);
 void launch_b_top_down_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, cudaStream_t st);
 // Parents of absolute level l.
-void launch_b_top_down(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas,
+void launch_b_top_down(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept,
                        int l, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 void launch_b_top_down_leaves(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
-                              uint64_t ctas, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
+                              uint64_t ctas, uint32_t ept, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 // out[s * 16 + 0..6] = stripe s's root child mask and cache.
 void launch_b_root_info(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, uint32_t* out,
                         cudaStream_t st);

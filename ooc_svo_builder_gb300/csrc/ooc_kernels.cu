@@ -1021,9 +1021,11 @@ __device__ __forceinline__ void stage(T& dst, const T& src) {
   for (uint32_t q = threadIdx.x; q < sizeof(T) / 4; q += blockDim.x) d[q] = s[q];
 }
 
-// CTA b belongs to the stripe s with cta_beg[s] <= b < cta_beg[s+1]; it
-// handles elements kChunk * (b - cta_beg[s]) .. + kChunk - 1 of that stripe.
-__device__ __forceinline__ uint32_t cta_stripe(const uint64_t* __restrict__ cta_beg, uint32_t n, uint64_t& local) {
+// CTA b belongs to the stripe s with cta_beg[s] <= b < cta_beg[s+1]; it is
+// the stripe's CTA b - cta_beg[s] and covers the elements per CTA of its
+// launch from there (kChunk, or kChunk * ept for the per-block and per-node
+// launches, each thread taking one element of every kChunk-wide chunk).
+__device__ __forceinline__ uint32_t cta_stripe(const uint64_t* __restrict__ cta_beg, uint32_t n, uint64_t& cta) {
   __shared__ uint32_t s_stripe;
   if (threadIdx.x == 0) {
     uint32_t lo = 0, hi = n;
@@ -1036,7 +1038,7 @@ __device__ __forceinline__ uint32_t cta_stripe(const uint64_t* __restrict__ cta_
   }
   __syncthreads();
   const uint32_t s = s_stripe;
-  local = (uint64_t)(blockIdx.x - cta_beg[s]) * kChunk + threadIdx.x;
+  cta = (uint64_t)(blockIdx.x - cta_beg[s]);  // the CTA's index within its stripe
   return s;
 }
 
@@ -1053,10 +1055,11 @@ __global__ void __launch_bounds__(kChunk, 4) kb_vox_small(const VoxJob* __restri
     else vox_small_win_item(j0, i);
   } else {
     __shared__ VoxJob sj;
-    uint64_t i;
-    const uint32_t s = cta_stripe(cta_beg, n, i);
+    uint64_t cta;
+    const uint32_t s = cta_stripe(cta_beg, n, cta);
     stage(sj, jobs[s]);
     __syncthreads();
+    const uint64_t i = cta * kChunk + threadIdx.x;
     if (i >= sj.n_items) return;
     if (PASS == 0) vox_small_occ_item(sj, i);
     else vox_small_win_item(sj, i);
@@ -1093,19 +1096,25 @@ __global__ void __launch_bounds__(256, 4) kb_vox_large(const VoxJob* __restrict_
 // Level depth - r of every stripe that has CTAs in this launch.
 template <bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_pyramid(const Pyramid* __restrict__ pyrs,
-                                                     const uint64_t* __restrict__ cta_beg, uint32_t n, int r, Pyramid p0) {
+                                                     const uint64_t* __restrict__ cta_beg, uint32_t n, int r, uint32_t ept,
+                                                     Pyramid p0) {
   if constexpr (SINGLE) {
-    const uint64_t b = (uint64_t)blockIdx.x * kChunk + threadIdx.x;
     const int l = p0.depth - r;
-    if (b < p0.lv[l].nblocks) pyramid_block(p0, l, b);
+    for (uint32_t k = 0; k < ept; k++) {
+      const uint64_t b = ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x;
+      if (b < p0.lv[l].nblocks) pyramid_block(p0, l, b);
+    }
   } else {
     __shared__ Pyramid sp;
-    uint64_t b;
-    const uint32_t s = cta_stripe(cta_beg, n, b);
+    uint64_t cta;
+    const uint32_t s = cta_stripe(cta_beg, n, cta);
     stage(sp, pyrs[s]);
     __syncthreads();
     const int l = sp.depth - r;
-    if (b < sp.lv[l].nblocks) pyramid_block(sp, l, b);
+    for (uint32_t k = 0; k < ept; k++) {
+      const uint64_t b = (cta * ept + k) * kChunk + threadIdx.x;
+      if (b < sp.lv[l].nblocks) pyramid_block(sp, l, b);
+    }
   }
 }
 
@@ -1128,16 +1137,17 @@ __device__ __forceinline__ void compact_stripe_block(const Pyramid& p, uint64_t 
 template <bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__ pyrs,
                                                      const uint64_t* __restrict__ cta_beg, uint32_t n,
-                                                     uint32_t* __restrict__ keys, Pyramid p0) {
+                                                     uint32_t* __restrict__ keys, uint32_t ept, Pyramid p0) {
   if constexpr (SINGLE) {
-    compact_stripe_block(p0, (uint64_t)blockIdx.x * kChunk + threadIdx.x, keys);
+    for (uint32_t k = 0; k < ept; k++)
+      compact_stripe_block(p0, ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x, keys);
   } else {
     __shared__ Pyramid sp;
-    uint64_t b;
-    const uint32_t s = cta_stripe(cta_beg, n, b);
+    uint64_t cta;
+    const uint32_t s = cta_stripe(cta_beg, n, cta);
     stage(sp, pyrs[s]);
     __syncthreads();
-    compact_stripe_block(sp, b, keys);
+    for (uint32_t k = 0; k < ept; k++) compact_stripe_block(sp, (cta * ept + k) * kChunk + threadIdx.x, keys);
   }
 }
 
@@ -1169,19 +1179,19 @@ __device__ __forceinline__ void node_op(const Pyramid& p, const EmitJob& e, int 
 
 template <int OP, bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_nodes(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits,
-                                                   const uint64_t* __restrict__ cta_beg, uint32_t n, int arg, Pyramid p0,
-                                                   EmitJob e0) {
+                                                   const uint64_t* __restrict__ cta_beg, uint32_t n, int arg, uint32_t ept,
+                                                   Pyramid p0, EmitJob e0) {
   if constexpr (SINGLE) {
-    node_op<OP>(p0, e0, arg, (uint64_t)blockIdx.x * kChunk + threadIdx.x);
+    for (uint32_t k = 0; k < ept; k++) node_op<OP>(p0, e0, arg, ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x);
   } else {
     __shared__ Pyramid sp;
     __shared__ EmitJob se;
-    uint64_t i;
-    const uint32_t s = cta_stripe(cta_beg, n, i);
+    uint64_t cta;
+    const uint32_t s = cta_stripe(cta_beg, n, cta);
     stage(sp, pyrs[s]);
     stage(se, emits[s]);
     __syncthreads();
-    node_op<OP>(sp, se, arg, i);
+    for (uint32_t k = 0; k < ept; k++) node_op<OP>(sp, se, arg, (cta * ept + k) * kChunk + threadIdx.x);
   }
 }
 
@@ -1322,15 +1332,15 @@ void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n
   else kb_vox_large<1><<<grid, block, 0, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter);
 }
 
-void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, int r,
+void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, int r,
                       const Pyramid* single, cudaStream_t st) {
   if (ctas == 0) return;
   KScope k(r == 0 ? "pyramid_leaf" : "pyramid", st);
   Pyramid p0;
   std::memset(&p0, 0, sizeof(p0));
   if (single) p0 = *single;
-  if (single) kb_pyramid<true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, r, p0);
-  else kb_pyramid<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, r, p0);
+  if (single) kb_pyramid<true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, r, ept, p0);
+  else kb_pyramid<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, r, ept, p0);
 }
 
 void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cudaStream_t st) {
@@ -1339,15 +1349,15 @@ void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cud
   kb_pyramid_top<<<n_stripes, 512, 0, st>>>(pyrs, l_hi);
 }
 
-void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t* keys,
-                      const Pyramid* single, cudaStream_t st) {
+void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept,
+                      uint32_t* keys, const Pyramid* single, cudaStream_t st) {
   if (ctas == 0) return;
   KScope k("compact", st);
   Pyramid p0;
   std::memset(&p0, 0, sizeof(p0));
   if (single) p0 = *single;
-  if (single) kb_compact<true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys, p0);
-  else kb_compact<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys, p0);
+  if (single) kb_compact<true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys, ept, p0);
+  else kb_compact<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys, ept, p0);
 }
 
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, cudaStream_t st) {
@@ -1359,7 +1369,7 @@ void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out
 namespace {
 template <int OP>
 void launch_nodes(const char* name, const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
-                  uint64_t ctas, int arg, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
+                  uint64_t ctas, uint32_t ept, int arg, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
   if (ctas == 0) return;
   KScope k(name, st);
   Pyramid p0;
@@ -1369,22 +1379,22 @@ void launch_nodes(const char* name, const Pyramid* pyrs, const EmitJob* emits, c
   if (sp && se) {
     p0 = *sp;
     e0 = *se;
-    kb_nodes<OP, true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, arg, p0, e0);
+    kb_nodes<OP, true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, arg, ept, p0, e0);
   } else {
-    kb_nodes<OP, false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, arg, p0, e0);
+    kb_nodes<OP, false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, arg, ept, p0, e0);
   }
 }
 }  // namespace
 
 void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
-                           uint64_t ctas, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
-  launch_nodes<OP_LEAF_PAYLOAD>("leaf_payload", pyrs, emits, cta_beg, n, ctas, 0, sp, se, st);
+                           uint64_t ctas, uint32_t ept, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
+  launch_nodes<OP_LEAF_PAYLOAD>("leaf_payload", pyrs, emits, cta_beg, n, ctas, ept, 0, sp, se, st);
 }
 
 void launch_b_bottom_up(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas,
-                        int r, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
-  launch_nodes<OP_BOTTOM_UP>(r == 1 ? "bottom_up_leaf_parents" : "bottom_up", pyrs, emits, cta_beg, n, ctas, r, sp,
-                             se, st);
+                        uint32_t ept, int r, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
+  launch_nodes<OP_BOTTOM_UP>(r == 1 ? "bottom_up_leaf_parents" : "bottom_up", pyrs, emits, cta_beg, n, ctas, ept, r,
+                             sp, se, st);
 }
 
 void launch_b_bottom_up_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, cudaStream_t st) {
@@ -1400,13 +1410,13 @@ void launch_b_top_down_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n
 }
 
 void launch_b_top_down(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas,
-                       int l, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
-  launch_nodes<OP_TOP_DOWN>("top_down", pyrs, emits, cta_beg, n, ctas, l, sp, se, st);
+                       uint32_t ept, int l, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
+  launch_nodes<OP_TOP_DOWN>("top_down", pyrs, emits, cta_beg, n, ctas, ept, l, sp, se, st);
 }
 
 void launch_b_top_down_leaves(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
-                              uint64_t ctas, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
-  launch_nodes<OP_LEAVES>("top_down_leaves", pyrs, emits, cta_beg, n, ctas, 0, sp, se, st);
+                              uint64_t ctas, uint32_t ept, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
+  launch_nodes<OP_LEAVES>("top_down_leaves", pyrs, emits, cta_beg, n, ctas, ept, 0, sp, se, st);
 }
 
 void launch_b_root_info(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, uint32_t* out,

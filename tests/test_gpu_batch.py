@@ -101,9 +101,11 @@ def test_every_tuning_gives_the_same_octrees(builder):
         nodes, data, _ = pyoracle.build(t, a["gridsize"], a["memory_limit_mb"], color=a["color"], levels=a["levels"])
         want.append(octree.Octree(a["gridsize"], nodes, data))
     try:
-        for small_vol, lpl, block, cps, budget, graphs in [(1, 1, 64, 1, 4096, 1), (64, 64, 256, 16, 1 << 30, 0),
-                                                           (27, 3, 128, 2, 700_000, 1), (64, 16, 256, 4, 4 << 30, 1)]:
-            builder.set_tuning(ooc.Tuning(small_vol, lpl, block, cps, budget, graphs, 0))
+        for small_vol, lpl, block, cps, budget, graphs, ept in [(1, 1, 64, 1, 4096, 1, 1),
+                                                                (64, 64, 256, 16, 1 << 30, 0, 16),
+                                                                (27, 3, 128, 2, 700_000, 1, 3),
+                                                                (64, 16, 256, 4, 4 << 30, 1, 4)]:
+            builder.set_tuning(ooc.Tuning(small_vol, lpl, block, cps, budget, graphs, ept))
             for r, w in zip(builder.build_batch_device(meshes, params), want):
                 assert not octree.diff(r.tree, w)
     finally:
