@@ -49,6 +49,10 @@ WORKLOADS = {
                      desc="configuration 3: svo_builder_binary -s 4096 -l 2048 (64 partitions) on a 20M-triangle "
                           "soup: half small triangles on 200 spheres, half log-normal edges (median 4 voxels, "
                           "sigma 1.0, clipped at 512)"),
+    "soup2048": dict(gridsize=2048, limit=2048, payload=False, color="model",
+                     desc="profiling case of the batched stripe kernels: svo_builder_binary -s 2048 -l 2048 (8 "
+                          "partitions of 1024^3, one sub-batch) on a 1M-triangle soup of the configuration-3 "
+                          "distribution"),
     "soup1024": dict(gridsize=1024, limit=2048, payload=False, color="model",
                      desc="profiling case of the configuration-3 soup: svo_builder_binary -s 1024 -l 2048 (one "
                           "partition) on a 4M-triangle soup of the same distribution"),
@@ -64,6 +68,8 @@ def make_mesh(name: str) -> np.ndarray:
         return tri.soup_tris(20_000_000, 4096, seed=3, sigma=1.0)
     if name == "soup1024":
         return tri.soup_tris(4_000_000, 1024, seed=3, sigma=1.0)
+    if name == "soup2048":
+        return tri.soup_tris(1_000_000, 2048, seed=3, sigma=1.0)
     raise SystemExit("unknown workload " + name)
 
 
