@@ -100,13 +100,26 @@ def build(verbose: bool = False, force: bool = False) -> str:
     return LIB
 
 
+def reference_dir() -> str:
+    """Where the reference's sources are read from (OOC_REFERENCE, or the mount of this container)."""
+    return os.environ.get("OOC_REFERENCE", "/root/reference")
+
+
+def reference_present() -> bool:
+    return os.path.isdir(os.path.join(reference_dir(), "src", "svo_builder"))
+
+
+def build_reference(target: str = "ref") -> None:
+    """Compile the reference's own sources with the oracle recipe (make -C oracle <target>)."""
+    _run(["make", "-C", os.path.join(ROOT, "oracle"), target, "REF=" + reference_dir()])
+
+
 def build_oracle(verbose: bool = False) -> None:
     """Compile the CPU oracle (and the reference build when its sources are present)."""
     oracle = os.path.join(ROOT, "oracle")
     out = _run(["make", "-C", oracle, "all"])
-    ref = os.environ.get("OOC_REFERENCE", "/root/reference")
-    if os.path.isdir(os.path.join(ref, "src", "svo_builder")):
-        out += _run(["make", "-C", oracle, "ref", "REF=" + ref])
+    if reference_present():
+        out += _run(["make", "-C", oracle, "ref", "REF=" + reference_dir()])
     if verbose:
         sys.stdout.write(out)
 

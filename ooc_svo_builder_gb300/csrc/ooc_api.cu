@@ -129,10 +129,10 @@ struct ooc_ctx {
   bool timing = false;
   float phase_ms[kPhases] = {0, 0, 0, 0, 0, 0};
   unsigned long long launches = 0;
-  DevBuf d_tris, d_items, d_hist, d_axis, d_bits, d_scan, d_scanpart, d_keys, d_size, d_dsize, d_start, d_dstart,
+  DevBuf d_tris, d_hist, d_axis, d_bits, d_scan, d_scanpart, d_keys, d_size, d_dsize, d_start, d_dstart,
       d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo, d_itemmask,
       d_firstchild, d_itembox;
-  PinBuf h_nodes, h_data, h_misc, h_recs, h_tables1, h_tables2;
+  PinBuf h_misc, h_recs, h_tables1, h_tables2;
   // double-buffered outputs of pipelined sub-batches
   DevBuf d_out_nodes[2], d_out_data[2];
   PinBuf h_root[2];
@@ -1338,13 +1338,13 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   if (c->own_stream) cudaStreamSynchronize(c->own_stream);
   if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   if (c->h2d_stream) cudaStreamSynchronize(c->h2d_stream);
-  DevBuf* bufs[] = {&c->d_tris, &c->d_items, &c->d_hist, &c->d_axis, &c->d_bits, &c->d_scan, &c->d_scanpart,
+  DevBuf* bufs[] = {&c->d_tris, &c->d_hist, &c->d_axis, &c->d_bits, &c->d_scan, &c->d_scanpart,
                     &c->d_keys, &c->d_size, &c->d_dsize, &c->d_start, &c->d_dstart, &c->d_cache, &c->d_winners,
                     &c->d_taskoff, &c->d_taskpart, &c->d_counter, &c->d_nodes, &c->d_data, &c->d_recs,
                     &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
-  PinBuf* pins[] = {&c->h_nodes, &c->h_data, &c->h_misc, &c->h_recs, &c->h_tables1, &c->h_tables2};
+  PinBuf* pins[] = {&c->h_misc, &c->h_recs, &c->h_tables1, &c->h_tables2};
   for (PinBuf* b : pins)
     if (b->p) cudaFreeHost(b->p);
   for (int i = 0; i < 2; i++) {

@@ -112,8 +112,8 @@ void launch_part_count(const float* tris, int stride, uint64_t n_tris, const flo
 void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
                       int pa_bits, uint64_t n_parts, uint32_t* cursor, uint32_t* items, cudaStream_t st);
 
-void launch_vox_small(const VoxJob& j, int pass, cudaStream_t st);
-void launch_vox_large(const VoxJob& j, int pass, cudaStream_t st, int num_sms);
+void launch_vox_small_occupancy(const VoxJob& j, cudaStream_t st);
+void launch_vox_large_occupancy(const VoxJob& j, cudaStream_t st, int num_sms);
 
 // src holds n entries of (index, `words` u64 values); dst[index*words + q] = value q.
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st);

@@ -558,10 +558,6 @@ __device__ __forceinline__ void vox_small_win_item(const VoxJob& j, uint64_t i) 
   }
 }
 
-__global__ void k_vox_small_win(VoxJob j) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < j.n_items) vox_small_win_item(j, i);
-}
 
 // Lines 32*L*k .. 32*L*(k+1)-1 of large item i, L = lines_per_lane (lane, lane+32, ...).
 template <int PASS>
@@ -1272,24 +1268,19 @@ void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const floa
                                                          (uint32_t)n_parts, cursor, items, use_smem);
 }
 
-void launch_vox_small(const VoxJob& j, int pass, cudaStream_t st) {
+// One-stripe occupancy pass with the job as a kernel parameter (the
+// allocation-free entry point uses these two).
+void launch_vox_small_occupancy(const VoxJob& j, cudaStream_t st) {
   if (j.n_items == 0) return;
-  if (pass == 0) {
-    KScope k("vox_small_occupancy", st);
-    k_vox_small_occ<<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
-  } else {
-    KScope k("vox_small_winner", st);
-    k_vox_small_win<<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
-  }
+  KScope k("vox_small_occupancy", st);
+  k_vox_small_occ<<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
 }
 
-void launch_vox_large(const VoxJob& j, int pass, cudaStream_t st, int num_sms) {
+void launch_vox_large_occupancy(const VoxJob& j, cudaStream_t st, int num_sms) {
   if (j.n_items == 0) return;
   cudaMemsetAsync(j.task_counter, 0, sizeof(unsigned long long), st);
-  const unsigned grid = (unsigned)num_sms * 8;
-  KScope k(pass == 0 ? "vox_large_occupancy" : "vox_large_winner", st);
-  if (pass == 0) k_vox_large<0><<<grid, 256, 0, st>>>(j);
-  else k_vox_large<1><<<grid, 256, 0, st>>>(j);
+  KScope k("vox_large_occupancy", st);
+  k_vox_large<0><<<(unsigned)num_sms * 8, 256, 0, st>>>(j);
 }
 
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st) {

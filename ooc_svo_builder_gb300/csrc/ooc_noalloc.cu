@@ -112,9 +112,9 @@ extern "C" int ooc_voxelize_occupancy_noalloc(const ooc_build_params* params, co
       cudaMemsetAsync(j.task_off + n_tris, 0, 8, st) != cudaSuccess) {
     out = OOC_ERR_DEVICE;
   } else {
-    launch_vox_small(j, 0, st);
+    launch_vox_small_occupancy(j, st);
     scan_u64_exclusive(j.task_off, n_tris + 1, partials, st);
-    launch_vox_large(j, 0, st, sms);
+    launch_vox_large_occupancy(j, st, sms);
     if (cudaGetLastError() != cudaSuccess) out = OOC_ERR_DEVICE;
   }
   g_hooks = saved;

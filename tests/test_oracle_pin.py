@@ -63,15 +63,11 @@ def test_oracle_matches_reference_build(tmp_path, seed, N, limit, payload, extra
 def test_reference_optimisation_levels_agree(tmp_path):
     """The reference has undefined behaviour in its uint_fast32_t& casts; -O0 and the
     recipe's -O3 -fno-strict-aliasing must give the same octree."""
-    src = "/root/reference/src/svo_builder"
-    if not (os.path.isdir(src) and _reference_available(True)):
+    from ooc_svo_builder_gb300 import build as recipe
+    if not (recipe.reference_present() and _reference_available(True)):
         pytest.skip("reference sources not present")
-    exe = str(tmp_path / "ref_O0")
-    inc = ["-I", os.path.join(ROOT, "oracle", "glm_shim"), "-I", "/root/reference/src/libs/libtri/include",
-           "-I", "/root/reference/src/libs/libmorton/include"]
-    srcs = [os.path.join(src, f) for f in ("main.cpp", "OctreeBuilder.cpp", "partitioner.cpp", "voxelizer.cpp")]
-    subprocess.run(["g++", "-std=c++11", "-O0", "-ffp-contract=off", "-w", "-DBINARY_VOXELIZATION", *inc, *srcs,
-                    "-o", exe], check=True)
+    recipe.build_reference("ref-O0")
+    exe = os.path.join(ROOT, "oracle", "_ref", "svo_builder_binary_O0")
     tris = tri.random_tris(800, 301, False, lo=-0.1, hi=1.1, max_edge=0.2)
     a = _run_ref(tmp_path, tris, 256, 2)
     base = str(tmp_path / "m")
