@@ -131,7 +131,8 @@ struct ooc_ctx {
   unsigned long long launches = 0;
   DevBuf d_tris, d_hist, d_axis, d_bits, d_scan, d_scanpart, d_keys, d_size, d_dsize, d_start, d_dstart,
       d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo, d_itemmask,
-      d_firstchild, d_itembox;
+      d_firstchild, d_itembox, d_leaf, d_touch;
+  bool leaf_zero = true;  // d_leaf and d_touch hold only zeros (no sub-batch left them dirty)
   PinBuf h_misc, h_recs, h_tables1, h_tables2;
   // double-buffered outputs of pipelined sub-batches
   DevBuf d_out_nodes[2], d_out_data[2];
@@ -539,16 +540,19 @@ struct Placed {  // a stripe after the level counts
   uint64_t out_node_off = 0, out_data_off = 0;  // host mode: offsets in the batch output buffers
 };
 
-int pyramid_levels(int Ds, Level* lv, uint64_t& words, uint64_t& blocks) {
+// Levels 0..Ds of a stripe appended to the buffers: the words of levels
+// 0..Ds-1 to `words`, the leaf level's to `leaf_words`, every level's blocks to `blocks`.
+int pyramid_levels(int Ds, Level* lv, uint64_t& words, uint64_t& leaf_words, uint64_t& blocks) {
   for (int l = 0; l <= Ds; l++) {
     const uint64_t nbits = 1ull << (3 * l);
     uint64_t nw = (nbits + 31) / 32;
     nw = (nw + 7) / 8 * 8;
-    lv[l].off_w = words;
+    uint64_t& acc = l == Ds ? leaf_words : words;
+    lv[l].off_w = acc;
     lv[l].off_b = blocks;
     lv[l].nwords = nw;
     lv[l].nblocks = nw / 8;
-    words += nw;
+    acc += nw;
     blocks += nw / 8;
   }
   return Ds;
@@ -667,21 +671,32 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   // ---- geometry of every stripe ----
   std::vector<Pyramid> pyr(n);
   std::vector<VoxJob> vj(n);
-  std::vector<uint64_t> item_beg(n + 1, 0);
-  uint64_t words = 0, blocks = 0, items = 0;
+  std::vector<uint64_t> item_beg(n + 1, 0), touch_beg(n, 0);
+  uint64_t words = 0, leaf_words = 0, blocks = 0, tbytes = 0, items = 0;
   int max_depth = 0;
   for (uint32_t s = 0; s < n; s++) {
     const StripeRef& r = sb[s];
     const MeshWork& m = meshes[r.mesh];
     std::memset(&pyr[s], 0, sizeof(Pyramid));
     pyr[s].depth = m.pl.Ds;
-    pyramid_levels(m.pl.Ds, pyr[s].lv, words, blocks);
+    pyramid_levels(m.pl.Ds, pyr[s].lv, words, leaf_words, blocks);
+    touch_beg[s] = tbytes;
+    tbytes += touch_bytes(pyr[s].lv[m.pl.Ds]);
     max_depth = std::max(max_depth, m.pl.Ds);
     item_beg[s] = items;
     items += r.n_items;
   }
   item_beg[n] = items;
   uint32_t* bits = ensure<uint32_t>(c->d_bits, words * 4);
+  // the leaf levels and their block marks are all zero between sub-batches
+  if (leaf_words * 4 > c->d_leaf.cap || tbytes > c->d_touch.cap) c->leaf_zero = false;
+  uint32_t* leaf = ensure<uint32_t>(c->d_leaf, leaf_words * 4);
+  uint8_t* touch = ensure<uint8_t>(c->d_touch, tbytes);
+  if (!c->leaf_zero) {
+    ck(cudaMemsetAsync(leaf, 0, c->d_leaf.cap, st), "memset leaf levels");
+    ck(cudaMemsetAsync(touch, 0, c->d_touch.cap, st), "memset leaf marks");
+    c->leaf_zero = true;
+  }
   uint32_t* scan = ensure<uint32_t>(c->d_scan, (blocks + 1) * 4);
   uint32_t* scanpart = ensure<uint32_t>(c->d_scanpart, scan_partials_needed(blocks + 1) * 4);
   uint64_t* task_off = ensure<uint64_t>(c->d_taskoff, (items + 1) * 8);
@@ -693,11 +708,17 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   uint32_t* flag = d_root + (uint64_t)n * 16;
 
   constexpr int kTopPyramidLevel = 5;  // levels 0..5 have at most 512 blocks: one CTA per stripe
+  // Stripes of 512^3 voxels and more mark their leaf blocks; smaller leaf
+  // levels are read and zeroed whole (their marks would cost the
+  // voxelization more than they save).
+  constexpr int kMarkDepth = 9;
   for (uint32_t s = 0; s < n; s++) {
     const StripeRef& r = sb[s];
     const MeshWork& m = meshes[r.mesh];
     Pyramid& P = pyr[s];
     P.bits = bits;
+    P.leaf = leaf;
+    P.touch = P.depth >= kMarkDepth ? touch + touch_beg[s] : nullptr;
     P.scan = scan;
     VoxJob& j = vj[s];
     std::memset(&j, 0, sizeof(j));
@@ -720,7 +741,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     j.unit_div = m.pl.unit_div;
     j.small_vol = c->tuning.small_vol;
     j.lines_per_lane = c->tuning.lines_per_lane;
-    j.leafbits = bits + P.lv[P.depth].off_w;
+    j.leafbits = leaf + P.lv[P.depth].off_w;
+    j.leaftouch = P.touch;
     j.task_off = task_off + item_beg[s];
     j.task_counter = counter;
     j.item_mask = m.pl.binary ? nullptr : item_mask + item_beg[s];
@@ -748,10 +770,10 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const uint64_t* d_beg = reinterpret_cast<const uint64_t*>(t1 + o_beg);
 
   uint32_t* lvl = ensure_pinned<uint32_t>(c->h_misc, ((uint64_t)n * 16 + 64) * 4);  // level bases, then root info
+  c->leaf_zero = false;  // until the clean at the end of the sub-batch is queued
   run_launches(c, st, 0, [&] {
     {
       PhaseScope ph(c, PH_VOX, st);
-      ck(cudaMemsetAsync(bits, 0, words * 4, st), "memset bits");
       ck(cudaMemsetAsync(task_off + items, 0, 8, st), "memset task_off");
       ck(cudaMemsetAsync(flag, 0, 4, st), "memset flag");
       launch_b_vox_small(d_vj, dp1(o_cpi), n, cp_items[n], 0, n == 1 ? &vj[0] : nullptr, st);
@@ -942,6 +964,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const Light cp_leaves = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
     return (live(s) && pyr[s].depth >= 1) ? pl[s].n_leaf : 0;  // a depth-0 root is the leaf
   });
+  const Light cp_clean = light_prefix(c, n, [&](uint32_t s) -> uint64_t { return touch_bytes(pyr[s].lv[pyr[s].depth]) / 16; });
   std::vector<Light> cp_bu(max_depth + 1), cp_td(max_depth + 1);
   for (int r = 1; r <= max_depth; r++)
     cp_bu[r] = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
@@ -961,6 +984,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const size_t o_cpay = up2.add(cp_pay.data(), (n + 1) * 8);
   const size_t o_clp = up2.add(cp_leafpay.beg.data(), (n + 1) * 8);
   const size_t o_cl = up2.add(cp_leaves.beg.data(), (n + 1) * 8);
+  const size_t o_cln = up2.add(cp_clean.beg.data(), (n + 1) * 8);
   std::vector<size_t> o_bu(cp_bu.size(), 0), o_td(cp_td.size(), 0);
   for (size_t r = 1; r < cp_bu.size(); r++) o_bu[r] = up2.add(cp_bu[r].beg.data(), (n + 1) * 8);
   for (size_t l = 0; l < cp_td.size(); l++) o_td[l] = up2.add(cp_td[l].beg.data(), (n + 1) * 8);
@@ -997,8 +1021,11 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       launch_b_top_down_leaves(d_pyr2, d_ej, dp2(o_cl), n, cp_leaves.beg[n], cp_leaves.ept, sp1, se1, st);
       launch_b_root_info(d_pyr2, d_ej, n, d_root, st);
       ck(cudaMemcpyAsync(hr, d_root, ((uint64_t)n * 16 + 1) * 4, cudaMemcpyDeviceToHost, st), "root info");
+      // the last reader of the leaf levels is done: zero them for the next sub-batch
+      launch_b_clean_leaves(d_pyr2, dp2(o_cln), n, cp_clean.beg[n], cp_clean.ept, sp1, st);
     }
   });
+  c->leaf_zero = true;
   ck(cudaEventRecord(c->ev_compute[slot], st), "event");
   if (os.mode == OUT_HOST) {
     // the records travel to the host on the copy stream while the next sub-batch computes
@@ -1181,7 +1208,7 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, co
       if (cnt == 0) continue;  // main.cpp:330: partitions without triangles are skipped
       Level tmp[kMaxLevels];
       uint64_t w = 0, b = 0;
-      pyramid_levels(m.pl.Ds, tmp, w, b);
+      pyramid_levels(m.pl.Ds, tmp, w, w, b);
       if (!sb.empty() && budget_words + w > budget) flush();
       sb.push_back(StripeRef{mi, s, part, ibeg, cnt});
       budget_words += w;
@@ -1341,7 +1368,7 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   DevBuf* bufs[] = {&c->d_tris, &c->d_hist, &c->d_axis, &c->d_bits, &c->d_scan, &c->d_scanpart,
                     &c->d_keys, &c->d_size, &c->d_dsize, &c->d_start, &c->d_dstart, &c->d_cache, &c->d_winners,
                     &c->d_taskoff, &c->d_taskpart, &c->d_counter, &c->d_nodes, &c->d_data, &c->d_recs,
-                    &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox};
+                    &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox, &c->d_leaf, &c->d_touch};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   PinBuf* pins[] = {&c->h_misc, &c->h_recs, &c->h_tables1, &c->h_tables2};

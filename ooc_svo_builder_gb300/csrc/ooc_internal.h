@@ -17,7 +17,7 @@ constexpr int kMaxLevels = kMaxStripeDepth + 1;
 // words are padded to whole 256-bit blocks (8 words) and each block has a
 // popcount entry in the concatenated scan array.
 struct Level {
-  uint64_t off_w;    // first word of this level in the bits buffer
+  uint64_t off_w;    // first word of this level in its buffer (`leaf` for the leaf level, `bits` above it)
   uint64_t off_b;    // first block entry of this level in the scan buffer
   uint64_t nwords;   // padded word count (multiple of 8)
   uint64_t nblocks;  // nwords / 8
@@ -25,12 +25,23 @@ struct Level {
   uint64_t n;        // set bits (nodes) at this level, filled after the scan
 };
 
+// The leaf level lives in its own buffer, which is all zero between builds:
+// the voxelization marks every 256-bit leaf block it sets a bit in (`touch`,
+// one byte per block, written with plain stores), the passes over the leaf
+// level read only marked blocks, and the last kernel of a sub-batch zeroes the
+// marked blocks and the marks.  The levels above the leaf are written in full
+// by the pyramid passes.
 struct Pyramid {
   int depth;  // Ds: levels 0..Ds, level Ds = voxels of the stripe
   Level lv[kMaxLevels];
-  uint32_t* bits;  // all levels' words
-  uint32_t* scan;  // exclusive prefix popcount per 256-bit block, all levels (+1 total)
+  uint32_t* bits;   // words of levels 0..Ds-1
+  uint32_t* leaf;   // words of level Ds
+  uint8_t* touch;   // byte b non-zero: leaf block b may have a set bit (NULL: every block is read)
+  uint32_t* scan;   // exclusive prefix popcount per 256-bit block, all levels (+1 total)
 };
+
+// Mark bytes of a stripe's leaf level, padded to 16 bytes.
+__host__ __device__ inline uint64_t touch_bytes(const Level& leaf) { return (leaf.nblocks + 15) / 16 * 16; }
 
 // Inputs of the voxelization kernels for one stripe.
 struct VoxJob {
@@ -45,6 +56,7 @@ struct VoxJob {
   uint32_t small_vol;       // items with at most this many candidates (<= 64) run one per thread
   uint32_t lines_per_lane;  // lines of a large item each lane of a warp task walks (task = 32 x this)
   uint32_t* leafbits;       // level-Ds words
+  uint8_t* leaftouch;       // byte per 256-bit block of leafbits, set when a bit of the block is (may be NULL)
   // pass B (payload winners)
   const uint32_t* leafscan; // scan entries of level Ds (exclusive, minus its base)
   uint32_t leafscan_base;
@@ -135,6 +147,9 @@ void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, 
 void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cudaStream_t st);
 void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, uint32_t* keys,
                       const Pyramid* single, cudaStream_t st);
+// Zero the marked leaf blocks of every stripe and the marks: one thread per 16 mark bytes.
+void launch_b_clean_leaves(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept,
+                           const Pyramid* single, cudaStream_t st);
 // out[s * (kMaxLevels + 1) + l] = global node index of level l's first node, l = 0..depth+1.
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, cudaStream_t st);
 void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,

@@ -307,6 +307,15 @@ __device__ __forceinline__ uint32_t in_block_rank(const uint32_t* __restrict__ b
   return r;
 }
 
+// Sets `acc` in leaf word w and marks the word's 256-bit block, so every
+// block with a set bit is marked.  The mark is a plain byte store: threads
+// that mark the same block store the same value, and nothing reads the marks
+// before the launch ends.
+__device__ __forceinline__ void set_leaf(const VoxJob& j, uint32_t w, uint32_t acc) {
+  atomicOr(&j.leafbits[w], acc);
+  if (j.leaftouch) j.leaftouch[w >> 3] = 1;
+}
+
 // Rank of bit `b` among the set bits of the leaf level.
 __device__ __forceinline__ uint32_t leaf_rank(const VoxJob& j, uint32_t b) {
   const uint32_t blk = b >> 8;
@@ -350,14 +359,14 @@ __device__ __forceinline__ uint64_t vox_column(const VoxJob& j, const TriSetup& 
     const uint32_t m = mxy | mz;
     const uint32_t w = m >> 5;
     if (w != cur_w) {
-      if (acc) atomicOr(&j.leafbits[cur_w], acc);
+      if (acc) set_leaf(j, cur_w, acc);
       cur_w = w;
       acc = 0;
     }
     acc |= 1u << (m & 31);
     if (z - z0 < 64) col |= 1ull << (z - z0);
   }
-  if (acc) atomicOr(&j.leafbits[cur_w], acc);
+  if (acc) set_leaf(j, cur_w, acc);
   return col;
 }
 
@@ -423,7 +432,7 @@ __device__ __forceinline__ void vox_line(const VoxJob& j, const TriSetup& s, uin
     if (PASS == 0) {
       const uint32_t wd = m >> 5;
       if (wd != cur_w) {
-        if (acc) atomicOr(&j.leafbits[cur_w], acc);
+        if (acc) set_leaf(j, cur_w, acc);
         cur_w = wd;
         acc = 0;
       }
@@ -498,7 +507,7 @@ __device__ __forceinline__ void vox_line(const VoxJob& j, const TriSetup& s, uin
       for (int w = start - 1; w >= w0 && side(w) == 0; w--)
         if (rest()) emit(w);
   }
-  if (PASS == 0 && acc) atomicOr(&j.leafbits[cur_w], acc);
+  if (PASS == 0 && acc) set_leaf(j, cur_w, acc);
 }
 
 // Pass 0, one thread per item: items with at most small_vol (<= 64) candidates
@@ -619,43 +628,57 @@ __device__ __forceinline__ uint32_t nonzero_bytes(uint32_t w) {
   return ((t >> 7) & 1u) | ((t >> 14) & 2u) | ((t >> 21) & 4u) | ((t >> 28) & 8u);
 }
 
+// First word of level l (the leaf level has its own buffer).
+__device__ __forceinline__ uint32_t* level_words(const Pyramid& p, int l) {
+  return (l == p.depth ? p.leaf : p.bits) + p.lv[l].off_w;
+}
+
+// Whether leaf block b may hold a set bit: unmarked blocks are all zero.
+__device__ __forceinline__ bool leaf_marked(const Pyramid& p, uint64_t b) { return !p.touch || p.touch[b] != 0; }
+
 __device__ __forceinline__ void pyramid_block(const Pyramid& p, int l, uint64_t b) {
   const Level& L = p.lv[l];
-  const uint4* q = reinterpret_cast<const uint4*>(p.bits + L.off_w + 8 * b);
-  const uint4 q0 = q[0], q1 = q[1];
-  const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
   uint32_t c = 0, pw = 0;
+  if (l != p.depth || leaf_marked(p, b)) {
+    const uint4* q = reinterpret_cast<const uint4*>(level_words(p, l) + 8 * b);
+    const uint4 q0 = q[0], q1 = q[1];
+    const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
 #pragma unroll
-  for (int k = 0; k < 8; k++) {
-    c += __popc(w[k]);
-    pw |= nonzero_bytes(w[k]) << (4 * k);
+    for (int k = 0; k < 8; k++) {
+      c += __popc(w[k]);
+      pw |= nonzero_bytes(w[k]) << (4 * k);
+    }
   }
   p.scan[L.off_b + b] = c;
-  if (l > 0) p.bits[p.lv[l - 1].off_w + b] = pw;
+  if (l > 0) level_words(p, l - 1)[b] = pw;
 }
 
-// Global node index of bit `b` of a level: the concatenated scan already
+// Global node index of bit `b` of level l: the concatenated scan already
 // counts every node of the shallower levels.
-__device__ __forceinline__ uint64_t node_index(const uint32_t* __restrict__ bits, const uint32_t* __restrict__ scan,
-                                               const Level& L, uint64_t b) {
+__device__ __forceinline__ uint64_t node_index(const Pyramid& p, int l, uint64_t b) {
   const uint64_t blk = b >> 8;
-  return (uint64_t)scan[L.off_b + blk] + in_block_rank(bits + L.off_w + blk * 8, b);
+  return (uint64_t)p.scan[p.lv[l].off_b + blk] + in_block_rank(level_words(p, l) + blk * 8, b);
 }
 
-__device__ __forceinline__ uint32_t child_mask(const uint32_t* __restrict__ bits, const Level& C, uint32_t k) {
-  return (bits[C.off_w + (k >> 2)] >> ((k & 3) * 8)) & 0xffu;
+__device__ __forceinline__ uint32_t child_mask(const Pyramid& p, int l, uint32_t k) {
+  return (level_words(p, l)[k >> 2] >> ((k & 3) * 8)) & 0xffu;
 }
 
 // Keys of all levels in one launch, one thread per 256-bit block (blocks are
-// 8 aligned words and never straddle two levels).
+// 8 aligned words and never straddle two levels); unmarked leaf blocks are skipped.
 __device__ __forceinline__ void compact_block(const Pyramid& p, uint64_t b, uint32_t* __restrict__ keys) {
-  const uint4* q = reinterpret_cast<const uint4*>(p.bits + 8 * b);
+  int l = p.depth;  // most blocks are leaf blocks, most of those unmarked
+  if (b < p.lv[l].off_b) {
+    l = 0;
+    while (p.lv[l + 1].off_b <= b) l++;
+  }
+  const uint64_t lb = b - p.lv[l].off_b;
+  if (l == p.depth && !leaf_marked(p, lb)) return;
+  const uint4* q = reinterpret_cast<const uint4*>(level_words(p, l) + 8 * lb);
   const uint4 q0 = q[0], q1 = q[1];
   if (!(q0.x | q0.y | q0.z | q0.w | q1.x | q1.y | q1.z | q1.w)) return;
   const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
-  int l = 0;
-  while (l < p.depth && p.lv[l + 1].off_b <= b) l++;
-  const uint64_t wl0 = (b - p.lv[l].off_b) * 8;
+  const uint64_t wl0 = lb * 8;
   uint64_t r = p.scan[b];
 #pragma unroll
   for (int k = 0; k < 8; k++) {
@@ -664,6 +687,34 @@ __device__ __forceinline__ void compact_block(const Pyramid& p, uint64_t b, uint
       const int bit = __ffs(word) - 1;
       keys[r++] = (uint32_t)(((wl0 + k) << 5) | (uint64_t)bit);
       word &= word - 1;
+    }
+  }
+}
+
+// Mark bytes 16i .. 16i+15 of a stripe: zero their marked leaf blocks, then
+// the marks.  A stripe without marks has its 16 leaf blocks zeroed outright.
+__device__ __forceinline__ void clean_touch16(const Pyramid& p, uint64_t i) {
+  if (i * 16 >= touch_bytes(p.lv[p.depth])) return;
+  if (!p.touch) {  // T threads zero the level's 2 x nblocks <= 32 T uint4, coalesced
+    const uint64_t T = touch_bytes(p.lv[p.depth]) / 16, n4 = p.lv[p.depth].nwords / 4;
+    uint4* leaf = reinterpret_cast<uint4*>(level_words(p, p.depth));
+    for (uint64_t q = i; q < n4; q += T) leaf[q] = make_uint4(0u, 0u, 0u, 0u);
+    return;
+  }
+  uint4* t4 = reinterpret_cast<uint4*>(p.touch) + i;
+  const uint4 t = *t4;
+  if (!(t.x | t.y | t.z | t.w)) return;
+  const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+  *t4 = z;
+  uint4* leaf = reinterpret_cast<uint4*>(level_words(p, p.depth));
+  const uint32_t tw[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const uint32_t nz = nonzero_bytes(tw[q]);  // bit k: mark byte k of this word is set
+    for (uint32_t m = nz; m; m &= m - 1) {
+      const uint64_t blk = i * 16 + (uint64_t)(4 * q + __ffs(m) - 1);
+      leaf[2 * blk] = z;
+      leaf[2 * blk + 1] = z;
     }
   }
 }
@@ -803,12 +854,11 @@ __device__ __forceinline__ void average_children(const EmitJob& e, uint32_t mask
 // Subtree node / data counts, first-child index and (-levels) averages of node i of level l.
 __device__ __forceinline__ void bottom_up_node(const Pyramid& p, const EmitJob& e, int l, uint64_t i) {
   const Level& L = p.lv[l];
-  const Level& C = p.lv[l + 1];
   const uint64_t gi = L.koff + i;
   const uint32_t k = e.keys[gi];
-  const uint32_t mask = child_mask(p.bits, C, k);
+  const uint32_t mask = child_mask(p, l + 1, k);
   const int nch = __popc(mask);
-  const uint64_t c0 = node_index(p.bits, p.scan, C, (uint64_t)k << 3);
+  const uint64_t c0 = node_index(p, l + 1, (uint64_t)k << 3);
   const bool child_leaf = (l + 1 == p.depth);
   uint32_t sz, dsz;
   if (child_leaf) {
@@ -869,7 +919,7 @@ __device__ __forceinline__ void top_down_node(const Pyramid& p, const EmitJob& e
   const Level& L = p.lv[l];
   const uint64_t gi = L.koff + i;
   const uint32_t k = e.keys[gi];
-  const uint32_t mask = child_mask(p.bits, p.lv[l + 1], k);
+  const uint32_t mask = child_mask(p, l + 1, k);
   const int nch = __popc(mask);
   const uint64_t st = e.start[gi];
   uint64_t run_d = e.dstart[gi];
@@ -881,7 +931,7 @@ __device__ __forceinline__ void top_down_node(const Pyramid& p, const EmitJob& e
     const uint64_t c = c0 + (uint64_t)j;
     const uint32_t kc = e.keys[c];
     if (!child_leaf) {
-      const uint32_t mc = child_mask(p.bits, p.lv[l + 2], kc);
+      const uint32_t mc = child_mask(p, l + 2, kc);
       const uint64_t szc = e.size[c], dszc = e.dsize[c];
       e.start[c] = run_s;
       e.dstart[c] = run_d;
@@ -916,17 +966,17 @@ __device__ __forceinline__ void top_down_child(const Pyramid& p, const EmitJob& 
   const uint64_t c = C.koff + i;
   const uint32_t kc = e.keys[c];
   const uint32_t pk = kc >> 3;
-  const uint64_t pidx = node_index(p.bits, p.scan, p.lv[l], pk);
+  const uint64_t pidx = node_index(p, l, pk);
   const uint64_t f = e.first_child[pidx];
   const uint64_t rank = c - f;
-  const uint32_t pmask = child_mask(p.bits, C, pk);
+  const uint32_t pmask = child_mask(p, l + 1, pk);
   uint64_t run_s = e.start[pidx], run_d = e.dstart[pidx];
   const uint64_t cb = run_s + (uint64_t)e.size[pidx] - 1 - (uint64_t)__popc(pmask);
   for (uint64_t q = f; q < c; q++) {
     run_s += (uint64_t)e.size[q] - 1;
     run_d += e.dsize[q];
   }
-  const uint32_t mc = child_mask(p.bits, p.lv[l + 2], kc);
+  const uint32_t mc = child_mask(p, l + 2, kc);
   const uint64_t szc = e.size[c], dszc = e.dsize[c];
   e.start[c] = run_s;
   e.dstart[c] = run_d;
@@ -939,13 +989,12 @@ __device__ __forceinline__ void top_down_child(const Pyramid& p, const EmitJob& 
 // where its child group and data run start.
 __device__ __forceinline__ void top_down_leaf(const Pyramid& p, const EmitJob& e, uint64_t i) {
   const Level& L = p.lv[p.depth];
-  const Level& P = p.lv[p.depth - 1];
   const uint64_t gi = L.koff + i;
   const uint32_t k = e.keys[gi];
   const uint32_t pk = k >> 3;
-  const uint64_t pidx = node_index(p.bits, p.scan, P, pk);
+  const uint64_t pidx = node_index(p, p.depth - 1, pk);
   const uint64_t rank = gi - e.first_child[pidx];
-  const uint32_t pmask = child_mask(p.bits, L, pk);
+  const uint32_t pmask = child_mask(p, p.depth, pk);
   const uint64_t pcb = e.start[pidx] + (uint64_t)e.size[pidx] - 1 - (uint64_t)__popc(pmask);
   if (e.binary) {
     store_node_record(e, pcb + rank, 1, 0, ~0ull);
@@ -978,7 +1027,7 @@ __device__ void root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base
       leaf_value(e, 0, 0, c);
     }
   }
-  out[0] = p.depth >= 1 ? child_mask(p.bits, p.lv[1], 0) : 0u;
+  out[0] = p.depth >= 1 ? child_mask(p, 1, 0) : 0u;
   for (int q = 0; q < 6; q++) out[1 + q] = __float_as_uint(c[q]);
   if (p.depth >= 1) {
     if (e.levels) store_data_record(e, data_base + e.dsize[r0] - 1, 0, c);
@@ -1120,7 +1169,28 @@ __global__ void kb_pyramid_top(const Pyramid* __restrict__ pyrs, int l_hi) {
   __syncthreads();
   for (int l = l_hi < sp.depth ? l_hi : sp.depth; l >= 0; l--) {
     for (uint64_t b = threadIdx.x; b < sp.lv[l].nblocks; b += blockDim.x) pyramid_block(sp, l, b);
+    // the padding words of level l-1 (levels 0..2 are padded to a whole block)
+    if (l > 0)
+      for (uint64_t w = sp.lv[l].nblocks + threadIdx.x; w < sp.lv[l - 1].nwords; w += blockDim.x)
+        level_words(sp, l - 1)[w] = 0u;
     __syncthreads();
+  }
+}
+
+// Zero the marked leaf blocks and the marks of every stripe.
+template <bool SINGLE>
+__global__ void __launch_bounds__(kChunk) kb_clean_leaves(const Pyramid* __restrict__ pyrs,
+                                                          const uint64_t* __restrict__ cta_beg, uint32_t n, uint32_t ept,
+                                                          Pyramid p0) {
+  if constexpr (SINGLE) {
+    for (uint32_t k = 0; k < ept; k++) clean_touch16(p0, ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x);
+  } else {
+    __shared__ Pyramid sp;
+    uint64_t cta;
+    const uint32_t s = cta_stripe(cta_beg, n, cta);
+    stage(sp, pyrs[s]);
+    __syncthreads();
+    for (uint32_t k = 0; k < ept; k++) clean_touch16(sp, (cta * ept + k) * kChunk + threadIdx.x);
   }
 }
 
@@ -1349,6 +1419,17 @@ void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, 
   if (single) p0 = *single;
   if (single) kb_compact<true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys, ept, p0);
   else kb_compact<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys, ept, p0);
+}
+
+void launch_b_clean_leaves(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept,
+                           const Pyramid* single, cudaStream_t st) {
+  if (ctas == 0) return;
+  KScope k("clean_leaves", st);
+  Pyramid p0;
+  std::memset(&p0, 0, sizeof(p0));
+  if (single) p0 = *single;
+  if (single) kb_clean_leaves<true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, ept, p0);
+  else kb_clean_leaves<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, ept, p0);
 }
 
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, cudaStream_t st) {
