@@ -131,7 +131,7 @@ struct ooc_ctx {
   unsigned long long launches = 0;
   DevBuf d_tris, d_hist, d_axis, d_bits, d_scan, d_scanpart, d_keys, d_size, d_dsize, d_start, d_dstart,
       d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo, d_itemmask,
-      d_firstchild, d_itembox, d_leaf, d_touch;
+      d_firstchild, d_itembox, d_leaf, d_touch, d_local;
   bool leaf_zero = true;  // d_leaf and d_touch hold only zeros (no sub-batch left them dirty)
   PinBuf h_misc, h_recs, h_tables1, h_tables2;
   // double-buffered outputs of pipelined sub-batches
@@ -540,20 +540,27 @@ struct Placed {  // a stripe after the level counts
   uint64_t out_node_off = 0, out_data_off = 0;  // host mode: offsets in the batch output buffers
 };
 
+// Stripes of 512^3 voxels and more mark their leaf blocks; smaller leaf
+// levels are read and zeroed whole (their marks would cost the voxelization
+// more than they save).
+constexpr int kMarkDepth = 9;
+
 // Levels 0..Ds of a stripe appended to the buffers: the words of levels
-// 0..Ds-1 to `words`, the leaf level's to `leaf_words`, every level's blocks to `blocks`.
-int pyramid_levels(int Ds, Level* lv, uint64_t& words, uint64_t& leaf_words, uint64_t& blocks) {
+// 0..Ds-1 to `words`, the leaf level's to `leaf_words`, every level's scan
+// entries to `entries` (one per group of kLeafGroup blocks for a marked leaf level).
+int pyramid_levels(int Ds, Level* lv, uint64_t& words, uint64_t& leaf_words, uint64_t& entries, bool marked) {
   for (int l = 0; l <= Ds; l++) {
     const uint64_t nbits = 1ull << (3 * l);
     uint64_t nw = (nbits + 31) / 32;
     nw = (nw + 7) / 8 * 8;
     uint64_t& acc = l == Ds ? leaf_words : words;
     lv[l].off_w = acc;
-    lv[l].off_b = blocks;
+    lv[l].off_b = entries;
     lv[l].nwords = nw;
     lv[l].nblocks = nw / 8;
+    lv[l].nscan = (l == Ds && marked) ? (lv[l].nblocks + kLeafGroup - 1) / kLeafGroup : lv[l].nblocks;
     acc += nw;
-    blocks += nw / 8;
+    entries += lv[l].nscan;
   }
   return Ds;
 }
@@ -671,17 +678,19 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   // ---- geometry of every stripe ----
   std::vector<Pyramid> pyr(n);
   std::vector<VoxJob> vj(n);
-  std::vector<uint64_t> item_beg(n + 1, 0), touch_beg(n, 0);
-  uint64_t words = 0, leaf_words = 0, blocks = 0, tbytes = 0, items = 0;
+  std::vector<uint64_t> item_beg(n + 1, 0), touch_beg(n, 0), local_beg(n, 0);
+  uint64_t words = 0, leaf_words = 0, blocks = 0, tbytes = 0, nlocal = 0, items = 0;
   int max_depth = 0;
   for (uint32_t s = 0; s < n; s++) {
     const StripeRef& r = sb[s];
     const MeshWork& m = meshes[r.mesh];
     std::memset(&pyr[s], 0, sizeof(Pyramid));
     pyr[s].depth = m.pl.Ds;
-    pyramid_levels(m.pl.Ds, pyr[s].lv, words, leaf_words, blocks);
+    pyramid_levels(m.pl.Ds, pyr[s].lv, words, leaf_words, blocks, m.pl.Ds >= kMarkDepth);
     touch_beg[s] = tbytes;
     tbytes += touch_bytes(pyr[s].lv[m.pl.Ds]);
+    local_beg[s] = nlocal;
+    if (m.pl.Ds >= kMarkDepth) nlocal += pyr[s].lv[m.pl.Ds].nblocks;
     max_depth = std::max(max_depth, m.pl.Ds);
     item_beg[s] = items;
     items += r.n_items;
@@ -692,6 +701,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   if (leaf_words * 4 > c->d_leaf.cap || tbytes > c->d_touch.cap) c->leaf_zero = false;
   uint32_t* leaf = ensure<uint32_t>(c->d_leaf, leaf_words * 4);
   uint8_t* touch = ensure<uint8_t>(c->d_touch, tbytes);
+  uint16_t* local = ensure<uint16_t>(c->d_local, nlocal * 2);
   if (!c->leaf_zero) {
     ck(cudaMemsetAsync(leaf, 0, c->d_leaf.cap, st), "memset leaf levels");
     ck(cudaMemsetAsync(touch, 0, c->d_touch.cap, st), "memset leaf marks");
@@ -708,10 +718,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   uint32_t* flag = d_root + (uint64_t)n * 16;
 
   constexpr int kTopPyramidLevel = 5;  // levels 0..5 have at most 512 blocks: one CTA per stripe
-  // Stripes of 512^3 voxels and more mark their leaf blocks; smaller leaf
-  // levels are read and zeroed whole (their marks would cost the
-  // voxelization more than they save).
-  constexpr int kMarkDepth = 9;
   for (uint32_t s = 0; s < n; s++) {
     const StripeRef& r = sb[s];
     const MeshWork& m = meshes[r.mesh];
@@ -719,6 +725,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     P.bits = bits;
     P.leaf = leaf;
     P.touch = P.depth >= kMarkDepth ? touch + touch_beg[s] : nullptr;
+    P.local = P.depth >= kMarkDepth ? local + local_beg[s] : nullptr;
     P.scan = scan;
     VoxJob& j = vj[s];
     std::memset(&j, 0, sizeof(j));
@@ -753,7 +760,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   for (int r = 0; r <= max_depth - kTopPyramidLevel - 1; r++)
     cp_pyr.push_back(light_prefix(c, n, [&](uint32_t s) -> uint64_t {
       const int l = pyr[s].depth - r;
-      return l > kTopPyramidLevel ? pyr[s].lv[l].nblocks : 0;
+      return l > kTopPyramidLevel ? pyr[s].lv[l].nscan : 0;
     }));
 
   Uploader up1;
@@ -943,6 +950,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       e.winners = winners + P.lv[P.depth].koff;
       vj[s].winners = winners + P.lv[P.depth].koff;
       vj[s].leafscan = scan + P.lv[P.depth].off_b;
+      vj[s].leaflocal = P.local;
       vj[s].leafscan_base = (uint32_t)P.lv[P.depth].koff;
     }
     if (q.empty) continue;
@@ -952,7 +960,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   }
   auto live = [&](uint32_t s) { return !pl[s].empty; };
   const Light cp_compact = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
-    return pyr[s].lv[pyr[s].depth].off_b + pyr[s].lv[pyr[s].depth].nblocks - pyr[s].lv[0].off_b;
+    const uint64_t upper = pyr[s].lv[pyr[s].depth].off_b - pyr[s].lv[0].off_b;  // compact_elems
+    return (upper + 31) / 32 * 32 + (pyr[s].lv[pyr[s].depth].nscan + 31) / 32 * 32;
   });
   const std::vector<uint64_t> cp_pay = cta_prefix(n, kChunk, [&](uint32_t s) -> uint64_t {
     return meshes[sb[s].mesh].pl.binary ? 0 : sb[s].n_items;
@@ -1208,7 +1217,7 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, co
       if (cnt == 0) continue;  // main.cpp:330: partitions without triangles are skipped
       Level tmp[kMaxLevels];
       uint64_t w = 0, b = 0;
-      pyramid_levels(m.pl.Ds, tmp, w, w, b);
+      pyramid_levels(m.pl.Ds, tmp, w, w, b, false);
       if (!sb.empty() && budget_words + w > budget) flush();
       sb.push_back(StripeRef{mi, s, part, ibeg, cnt});
       budget_words += w;
@@ -1368,7 +1377,7 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   DevBuf* bufs[] = {&c->d_tris, &c->d_hist, &c->d_axis, &c->d_bits, &c->d_scan, &c->d_scanpart,
                     &c->d_keys, &c->d_size, &c->d_dsize, &c->d_start, &c->d_dstart, &c->d_cache, &c->d_winners,
                     &c->d_taskoff, &c->d_taskpart, &c->d_counter, &c->d_nodes, &c->d_data, &c->d_recs,
-                    &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox, &c->d_leaf, &c->d_touch};
+                    &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox, &c->d_leaf, &c->d_touch, &c->d_local};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   PinBuf* pins[] = {&c->h_misc, &c->h_recs, &c->h_tables1, &c->h_tables2};

@@ -21,6 +21,7 @@ struct Level {
   uint64_t off_b;    // first block entry of this level in the scan buffer
   uint64_t nwords;   // padded word count (multiple of 8)
   uint64_t nblocks;  // nwords / 8
+  uint64_t nscan;    // scan entries: nblocks, or one per group of 16 blocks for a marked leaf level
   uint64_t koff;     // first node of this level in the per-node arrays
   uint64_t n;        // set bits (nodes) at this level, filled after the scan
 };
@@ -31,14 +32,21 @@ struct Level {
 // level read only marked blocks, and the last kernel of a sub-batch zeroes the
 // marked blocks and the marks.  The levels above the leaf are written in full
 // by the pyramid passes.
+//
+// A marked leaf level has one scan entry per group of kLeafGroup blocks (the
+// group's node count) and, for each marked block, the count of the group's
+// nodes before it (`local`), so the scan never visits unmarked blocks.
 struct Pyramid {
   int depth;  // Ds: levels 0..Ds, level Ds = voxels of the stripe
   Level lv[kMaxLevels];
   uint32_t* bits;   // words of levels 0..Ds-1
   uint32_t* leaf;   // words of level Ds
   uint8_t* touch;   // byte b non-zero: leaf block b may have a set bit (NULL: every block is read)
+  uint16_t* local;  // marked leaf level: nodes of block b's group before block b (written for marked blocks)
   uint32_t* scan;   // exclusive prefix popcount per 256-bit block, all levels (+1 total)
 };
+
+constexpr uint64_t kLeafGroup = 16;  // leaf blocks per scan entry of a marked leaf level
 
 // Mark bytes of a stripe's leaf level, padded to 16 bytes.
 __host__ __device__ inline uint64_t touch_bytes(const Level& leaf) { return (leaf.nblocks + 15) / 16 * 16; }
@@ -59,6 +67,7 @@ struct VoxJob {
   uint8_t* leaftouch;       // byte per 256-bit block of leafbits, set when a bit of the block is (may be NULL)
   // pass B (payload winners)
   const uint32_t* leafscan; // scan entries of level Ds (exclusive, minus its base)
+  const uint16_t* leaflocal;// marked leaf level: Pyramid::local (leafscan then has one entry per group)
   uint32_t leafscan_base;
   uint32_t* winners;        // per leaf: min triangle index
   uint64_t* task_off;       // per item: exclusive prefix of warp tasks (n_items + 1)

@@ -319,7 +319,8 @@ __device__ __forceinline__ void set_leaf(const VoxJob& j, uint32_t w, uint32_t a
 // Rank of bit `b` among the set bits of the leaf level.
 __device__ __forceinline__ uint32_t leaf_rank(const VoxJob& j, uint32_t b) {
   const uint32_t blk = b >> 8;
-  return j.leafscan[blk] - j.leafscan_base + in_block_rank(j.leafbits + (uint64_t)blk * 8, b);
+  const uint32_t base = j.leaflocal ? j.leafscan[blk / kLeafGroup] + j.leaflocal[blk] : j.leafscan[blk];
+  return base - j.leafscan_base + in_block_rank(j.leafbits + (uint64_t)blk * 8, b);
 }
 
 // One z column of a small item: sets its voxels' bits and returns the column's
@@ -633,53 +634,91 @@ __device__ __forceinline__ uint32_t* level_words(const Pyramid& p, int l) {
   return (l == p.depth ? p.leaf : p.bits) + p.lv[l].off_w;
 }
 
-// Whether leaf block b may hold a set bit: unmarked blocks are all zero.
-__device__ __forceinline__ bool leaf_marked(const Pyramid& p, uint64_t b) { return !p.touch || p.touch[b] != 0; }
-
+// Block b of level l (not a marked leaf level): its popcount and parent word.
 __device__ __forceinline__ void pyramid_block(const Pyramid& p, int l, uint64_t b) {
   const Level& L = p.lv[l];
+  const uint4* q = reinterpret_cast<const uint4*>(level_words(p, l) + 8 * b);
+  const uint4 q0 = q[0], q1 = q[1];
+  const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
   uint32_t c = 0, pw = 0;
-  if (l != p.depth || leaf_marked(p, b)) {
-    const uint4* q = reinterpret_cast<const uint4*>(level_words(p, l) + 8 * b);
-    const uint4 q0 = q[0], q1 = q[1];
-    const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      c += __popc(w[k]);
-      pw |= nonzero_bytes(w[k]) << (4 * k);
-    }
+  for (int k = 0; k < 8; k++) {
+    c += __popc(w[k]);
+    pw |= nonzero_bytes(w[k]) << (4 * k);
   }
   p.scan[L.off_b + b] = c;
   if (l > 0) level_words(p, l - 1)[b] = pw;
 }
 
-// Global node index of bit `b` of level l: the concatenated scan already
-// counts every node of the shallower levels.
+// Global node index of the first node of block blk of level l: the
+// concatenated scan already counts every node of the shallower levels.
+__device__ __forceinline__ uint64_t block_base(const Pyramid& p, int l, uint64_t blk) {
+  if (l == p.depth && p.touch) return (uint64_t)p.scan[p.lv[l].off_b + blk / kLeafGroup] + p.local[blk];
+  return p.scan[p.lv[l].off_b + blk];
+}
+
+// Global node index of bit `b` of level l.
 __device__ __forceinline__ uint64_t node_index(const Pyramid& p, int l, uint64_t b) {
   const uint64_t blk = b >> 8;
-  return (uint64_t)p.scan[p.lv[l].off_b + blk] + in_block_rank(level_words(p, l) + blk * 8, b);
+  return block_base(p, l, blk) + in_block_rank(level_words(p, l) + blk * 8, b);
+}
+
+// A marked leaf level, group q of kLeafGroup blocks: the parent words, the
+// group's node count (its scan entry) and each marked block's offset in it.
+__device__ __forceinline__ void leaf_group(const Pyramid& p, uint64_t q) {
+  static_assert(kLeafGroup == 16, "one uint4 of marks per group");
+  const Level& L = p.lv[p.depth];
+  const uint4 m4 = reinterpret_cast<const uint4*>(p.touch)[q];
+  uint4* parent = reinterpret_cast<uint4*>(level_words(p, p.depth - 1) + q * kLeafGroup);
+  if (!(m4.x | m4.y | m4.z | m4.w)) {
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    parent[0] = z;
+    parent[1] = z;
+    parent[2] = z;
+    parent[3] = z;
+    p.scan[L.off_b + q] = 0u;
+    return;
+  }
+  const uint32_t mw[4] = {m4.x, m4.y, m4.z, m4.w};
+  uint32_t pw[16];
+  uint32_t total = 0;
+#pragma unroll
+  for (int k = 0; k < 16; k++) {
+    pw[k] = 0u;
+    if ((mw[k >> 2] >> (8 * (k & 3))) & 0xffu) {
+      const uint64_t b = q * kLeafGroup + (uint64_t)k;
+      const uint4* w4 = reinterpret_cast<const uint4*>(level_words(p, p.depth) + 8 * b);
+      const uint4 q0 = w4[0], q1 = w4[1];
+      const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+      uint32_t c = 0;
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        c += __popc(w[i]);
+        pw[k] |= nonzero_bytes(w[i]) << (4 * i);
+      }
+      p.local[b] = (uint16_t)total;
+      total += c;
+    }
+  }
+  parent[0] = make_uint4(pw[0], pw[1], pw[2], pw[3]);
+  parent[1] = make_uint4(pw[4], pw[5], pw[6], pw[7]);
+  parent[2] = make_uint4(pw[8], pw[9], pw[10], pw[11]);
+  parent[3] = make_uint4(pw[12], pw[13], pw[14], pw[15]);
+  p.scan[L.off_b + q] = total;
 }
 
 __device__ __forceinline__ uint32_t child_mask(const Pyramid& p, int l, uint32_t k) {
   return (level_words(p, l)[k >> 2] >> ((k & 3) * 8)) & 0xffu;
 }
 
-// Keys of all levels in one launch, one thread per 256-bit block (blocks are
-// 8 aligned words and never straddle two levels); unmarked leaf blocks are skipped.
-__device__ __forceinline__ void compact_block(const Pyramid& p, uint64_t b, uint32_t* __restrict__ keys) {
-  int l = p.depth;  // most blocks are leaf blocks, most of those unmarked
-  if (b < p.lv[l].off_b) {
-    l = 0;
-    while (p.lv[l + 1].off_b <= b) l++;
-  }
-  const uint64_t lb = b - p.lv[l].off_b;
-  if (l == p.depth && !leaf_marked(p, lb)) return;
-  const uint4* q = reinterpret_cast<const uint4*>(level_words(p, l) + 8 * lb);
+// Keys of block lb of level l, from node index r on.
+__device__ __forceinline__ void block_keys(const uint32_t* __restrict__ words, uint64_t lb, uint64_t r,
+                                           uint32_t* __restrict__ keys) {
+  const uint4* q = reinterpret_cast<const uint4*>(words + 8 * lb);
   const uint4 q0 = q[0], q1 = q[1];
   if (!(q0.x | q0.y | q0.z | q0.w | q1.x | q1.y | q1.z | q1.w)) return;
   const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
   const uint64_t wl0 = lb * 8;
-  uint64_t r = p.scan[b];
 #pragma unroll
   for (int k = 0; k < 8; k++) {
     uint32_t word = w[k];
@@ -687,6 +726,69 @@ __device__ __forceinline__ void compact_block(const Pyramid& p, uint64_t b, uint
       const int bit = __ffs(word) - 1;
       keys[r++] = (uint32_t)(((wl0 + k) << 5) | (uint64_t)bit);
       word &= word - 1;
+    }
+  }
+}
+
+// Keys of all levels in one launch.  The elements of a stripe are the blocks
+// of levels 0..depth-1 (blocks are 8 aligned words and never straddle two
+// levels), padded to a multiple of 32, then the leaf level's scan entries,
+// padded likewise, so every warp works on one region.  An unmarked leaf level
+// has one element per block.  In a marked leaf level each lane takes a group
+// of kLeafGroup blocks; the warp gathers the marked blocks of its 32 groups and
+// hands them out one per lane.
+__device__ __forceinline__ uint64_t compact_elems(const Pyramid& p) {
+  const uint64_t upper = p.lv[p.depth].off_b - p.lv[0].off_b;
+  return (upper + 31) / 32 * 32 + (p.lv[p.depth].nscan + 31) / 32 * 32;
+}
+
+__device__ __forceinline__ void compact_elem(const Pyramid& p, uint64_t e, uint32_t* __restrict__ keys) {
+  const Level& L = p.lv[p.depth];
+  const uint64_t first = p.lv[0].off_b, upper = L.off_b - first, up32 = (upper + 31) / 32 * 32;
+  if (e >= compact_elems(p)) return;  // whole warps
+  if (e < up32) {
+    if (e >= upper) return;
+    int l = 0;
+    while (p.lv[l + 1].off_b <= first + e) l++;
+    block_keys(level_words(p, l), first + e - p.lv[l].off_b, p.scan[first + e], keys);
+    return;
+  }
+  const uint64_t q = e - up32;
+  if (!p.touch) {
+    if (q < L.nblocks) block_keys(level_words(p, p.depth), q, p.scan[L.off_b + q], keys);
+    return;
+  }
+  // marked leaf level: all 32 lanes of the warp are here
+  const int lane = threadIdx.x & 31;
+  uint32_t marked = 0;  // bit k: block k of group q is marked
+  if (q < L.nscan) {
+    const uint4 m4 = reinterpret_cast<const uint4*>(p.touch)[q];
+    marked = nonzero_bytes(m4.x) | (nonzero_bytes(m4.y) << 4) | (nonzero_bytes(m4.z) << 8) | (nonzero_bytes(m4.w) << 12);
+  }
+  const uint32_t cnt = __popc(marked);
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const uint32_t total = __shfl_sync(FULL, incl, 31);
+  const uint64_t q0 = q - (uint64_t)lane;
+  for (uint32_t round = 0; round < total; round += 32) {
+    const uint32_t j = round + (uint32_t)lane;  // this lane's marked block, in warp order
+    uint32_t o = 0;                             // its owner lane: the first with incl > j
+#pragma unroll
+    for (uint32_t st = 16; st; st >>= 1) {
+      const uint32_t t = __shfl_sync(FULL, incl, (int)(o + st - 1));
+      if (t <= j) o += st;
+    }
+    uint32_t m = __shfl_sync(FULL, marked, (int)o);
+    const uint32_t before = __shfl_sync(FULL, incl - cnt, (int)o);
+    if (j < total) {
+      for (uint32_t k = j - before; k; k--) m &= m - 1;
+      const uint64_t qo = q0 + o;
+      const uint64_t blk = qo * kLeafGroup + (uint64_t)(__ffs(m) - 1);
+      block_keys(level_words(p, p.depth), blk, (uint64_t)p.scan[L.off_b + qo] + p.local[blk], keys);
     }
   }
 }
@@ -1138,6 +1240,12 @@ __global__ void __launch_bounds__(256, 4) kb_vox_large(const VoxJob* __restrict_
   }
 }
 
+// Element e of level l: a block, or a group of blocks of a marked leaf level.
+__device__ __forceinline__ void pyramid_elem(const Pyramid& p, int l, uint64_t e) {
+  if (l == p.depth && p.touch) leaf_group(p, e);
+  else pyramid_block(p, l, e);
+}
+
 // Level depth - r of every stripe that has CTAs in this launch.
 template <bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_pyramid(const Pyramid* __restrict__ pyrs,
@@ -1147,7 +1255,7 @@ __global__ void __launch_bounds__(kChunk) kb_pyramid(const Pyramid* __restrict__
     const int l = p0.depth - r;
     for (uint32_t k = 0; k < ept; k++) {
       const uint64_t b = ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x;
-      if (b < p0.lv[l].nblocks) pyramid_block(p0, l, b);
+      if (b < p0.lv[l].nscan) pyramid_elem(p0, l, b);
     }
   } else {
     __shared__ Pyramid sp;
@@ -1158,7 +1266,7 @@ __global__ void __launch_bounds__(kChunk) kb_pyramid(const Pyramid* __restrict__
     const int l = sp.depth - r;
     for (uint32_t k = 0; k < ept; k++) {
       const uint64_t b = (cta * ept + k) * kChunk + threadIdx.x;
-      if (b < sp.lv[l].nblocks) pyramid_block(sp, l, b);
+      if (b < sp.lv[l].nscan) pyramid_elem(sp, l, b);
     }
   }
 }
@@ -1194,11 +1302,6 @@ __global__ void __launch_bounds__(kChunk) kb_clean_leaves(const Pyramid* __restr
   }
 }
 
-__device__ __forceinline__ void compact_stripe_block(const Pyramid& p, uint64_t b, uint32_t* __restrict__ keys) {
-  const uint64_t first = p.lv[0].off_b, end = p.lv[p.depth].off_b + p.lv[p.depth].nblocks;
-  if (first + b < end) compact_block(p, first + b, keys);
-}
-
 // Every block of every level of the stripe.
 template <bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__ pyrs,
@@ -1206,14 +1309,14 @@ __global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__
                                                      uint32_t* __restrict__ keys, uint32_t ept, Pyramid p0) {
   if constexpr (SINGLE) {
     for (uint32_t k = 0; k < ept; k++)
-      compact_stripe_block(p0, ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x, keys);
+      compact_elem(p0, ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x, keys);
   } else {
     __shared__ Pyramid sp;
     uint64_t cta;
     const uint32_t s = cta_stripe(cta_beg, n, cta);
     stage(sp, pyrs[s]);
     __syncthreads();
-    for (uint32_t k = 0; k < ept; k++) compact_stripe_block(sp, (cta * ept + k) * kChunk + threadIdx.x, keys);
+    for (uint32_t k = 0; k < ept; k++) compact_elem(sp, (cta * ept + k) * kChunk + threadIdx.x, keys);
   }
 }
 
@@ -1223,7 +1326,7 @@ __global__ void kb_level_bases(const Pyramid* __restrict__ pyrs, uint32_t n_stri
   const Pyramid& p = pyrs[s];
   uint32_t* o = out + (uint64_t)s * (kMaxLevels + 1);
   for (int l = 0; l <= p.depth; l++) o[l] = p.scan[p.lv[l].off_b];
-  o[p.depth + 1] = p.scan[p.lv[p.depth].off_b + p.lv[p.depth].nblocks];
+  o[p.depth + 1] = p.scan[p.lv[p.depth].off_b + p.lv[p.depth].nscan];
 }
 
 // Kinds of per-node launches that take (Pyramid, EmitJob) pairs.

@@ -61,6 +61,22 @@ def test_failing_allocation_aborts_batch_and_context_recovers(builder):
     assert len(builder.build_batch_device(meshes, params)) == 6
 
 
+def test_failure_after_voxelization_leaves_no_bits_behind(builder):
+    """A batch whose allocation fails after its voxelization (512^3 stripes, whose leaf levels
+    are kept zero between builds) must not leak set bits into the next build."""
+    meshes = [tri.icosphere_tris(4, seed=5 + i, payload=True) for i in range(2)]
+    params = [make_params(512, 2048, geometry_only=False) for _ in range(2)]
+    arr, keep = builder._mesh_array(meshes, params)
+    infos = (ooc.BuildInfo * 2)()
+    cb = ooc.ALLOC(lambda user, mesh, nb, db, stream, pn, pd: 1)
+    rc = builder.lib.ooc_build_batch_device(builder.h, arr, 2, ctypes.cast(cb, ctypes.c_void_p), None, None, infos)
+    assert rc == 2  # OOC_ERR_OOM
+    t = tri.icosphere_tris(3, seed=9, payload=True)  # a different, smaller surface in the same stripe
+    got = builder.build(t, make_params(512, 2048, geometry_only=False))
+    nodes, data, _ = pyoracle.build(t, 512, 2048)
+    assert not octree.diff(got.tree, octree.Octree(512, nodes, data))
+
+
 def test_ready_callback_error_aborts(builder):
     meshes = [tri.random_tris(300, 20 + i, False, max_edge=0.1) for i in range(3)]
     params = [make_params(64, 2048) for _ in range(3)]

@@ -185,3 +185,40 @@ def test_soup_64_partitions(builder):
     got, want, info = run_both(builder, t, 1024, limit=16)
     assert info["n_partitions"] == 64
     assert_same(got, want, info)
+
+
+# Stripes of 512^3 voxels and more keep their leaf level zero between builds, mark the
+# blocks the voxelization writes and scan the leaf level by groups of blocks; these cases
+# put that path against the oracle.
+@pytest.mark.parametrize("N,sub,payload,levels", [(512, 4, False, False), (1024, 4, False, False),
+                                                  (512, 4, True, True), (1024, 5, True, False)])
+def test_marked_leaf_levels(builder, N, sub, payload, levels):
+    t = tri.icosphere_tris(sub, payload=payload)
+    assert_same(*run_both(builder, t, N, levels=levels))
+
+
+def test_marked_soup_payload(builder):
+    t = tri.soup_tris(100_000, 1024, seed=41, sigma=1.0, n_spheres=20, payload=True)
+    assert_same(*run_both(builder, t, 1024))
+
+
+def test_marked_eight_stripes(builder):
+    """Gridsize 2048 at -l 2048: eight partitions of 1024^3, one sub-batch."""
+    t = tri.icosphere_tris(3, radius=0.2)
+    got, want, info = run_both(builder, t, 2048)
+    assert info["n_partitions"] == 8
+    assert_same(got, want, info)
+
+
+def test_marked_and_unmarked_in_one_batch(builder):
+    meshes = [tri.soup_tris(20_000, 1024, seed=43, sigma=1.0, n_spheres=5, payload=True),
+              tri.icosphere_tris(3, seed=2),
+              tri.icosphere_tris(4, seed=3, payload=True),
+              tri.random_tris(2000, 44, False, max_edge=0.1)]
+    sizes = [1024, 64, 512, 256]
+    params = [make_params(N, 2048, geometry_only=t.shape[1] == 9) for t, N in zip(meshes, sizes)]
+    got = builder.build_batch(meshes, params)
+    for t, N, g in zip(meshes, sizes, got):
+        nodes, data, _ = pyoracle.build(t, N, 2048)
+        d = octree.diff(g.tree, octree.Octree(N, nodes, data))
+        assert not d, "\n".join(d)
