@@ -249,8 +249,8 @@ void ring_take(ooc_ctx* c, D2HRing& r, uint64_t a, uint64_t b, F&& out) {
 // shapes skip instantiation.  The captured region neither allocates nor
 // synchronises; phase and kernel timing launch directly.
 template <typename F>
-void run_launches(ooc_ctx* c, cudaStream_t st, int which, F&& launches) {
-  if (!c->tuning.graphs || c->timing || g_hooks.begin) {
+void run_launches(ooc_ctx* c, cudaStream_t st, int which, F&& launches, bool direct = false) {
+  if (direct || !c->tuning.graphs || c->timing || g_hooks.begin) {
     launches();
     return;
   }
@@ -507,6 +507,9 @@ struct MeshWork {
   uint64_t n_items = 0;
   int64_t last_stripe = -1;  // last stripe with items (-1: none)
   cudaEvent_t uploaded = nullptr;  // the triangles are on the device once this has completed (null: already)
+  // a one-partition mesh uploaded in pieces: (end item, event after its copy), so the
+  // voxelization of each piece starts as soon as it is on the device
+  std::vector<std::pair<uint64_t, cudaEvent_t>> pieces;
   uint64_t index = 0;        // in the batch
   // caller-owned device destination (output to device destinations)
   void* dst_nodes = nullptr;
@@ -523,7 +526,7 @@ struct MeshWork {
       : prm(o.prm), pl(o.pl), d_tris(o.d_tris), n_tris(o.n_tris), part_off(std::move(o.part_off)), items(o.items),
         out(o.out), top(o.top), next_stripe(o.next_stripe), dry(o.dry), layout(o.layout),
         layout_next(o.layout_next), filled(o.filled), n_items(o.n_items), last_stripe(o.last_stripe),
-        uploaded(o.uploaded),
+        uploaded(o.uploaded), pieces(std::move(o.pieces)),
         index(o.index), dst_nodes(o.dst_nodes), dst_data(o.dst_data), dst_ready(o.dst_ready),
         total_nodes(o.total_nodes), total_data(o.total_data), carried_nodes(o.carried_nodes),
         carried_data(o.carried_data) {}
@@ -675,6 +678,9 @@ struct Pending {
 void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, const std::vector<StripeRef>& sb,
                    const OutSpec& os, Pending& out_pending, int slot) {
   const uint32_t n = (uint32_t)sb.size();
+  // a lone stripe of a mesh uploaded in pieces voxelizes each piece on arrival
+  const std::vector<std::pair<uint64_t, cudaEvent_t>>* pieces =
+      (n == 1 && !meshes[sb[0].mesh].pieces.empty()) ? &meshes[sb[0].mesh].pieces : nullptr;
   // ---- geometry of every stripe ----
   std::vector<Pyramid> pyr(n);
   std::vector<VoxJob> vj(n);
@@ -783,7 +789,23 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       PhaseScope ph(c, PH_VOX, st);
       ck(cudaMemsetAsync(task_off + items, 0, 8, st), "memset task_off");
       ck(cudaMemsetAsync(flag, 0, 4, st), "memset flag");
-      launch_b_vox_small(d_vj, dp1(o_cpi), n, cp_items[n], 0, n == 1 ? &vj[0] : nullptr, st);
+      if (pieces) {
+        // each piece of the triangles as soon as its copy is done
+        uint64_t beg = 0;
+        for (const auto& pc : *pieces) {
+          ck(cudaStreamWaitEvent(st, pc.second, 0), "wait piece");
+          VoxJob jc = vj[0];
+          jc.ibeg += beg;
+          jc.n_items = pc.first - beg;
+          jc.task_off += beg;
+          if (jc.item_mask) jc.item_mask += beg;
+          if (jc.item_box) jc.item_box += beg;
+          launch_b_vox_small(nullptr, nullptr, 1, (jc.n_items + kChunk - 1) / kChunk, 0, &jc, st);
+          beg = pc.first;
+        }
+      } else {
+        launch_b_vox_small(d_vj, dp1(o_cpi), n, cp_items[n], 0, n == 1 ? &vj[0] : nullptr, st);
+      }
       scan_u64_exclusive(task_off, items + 1, taskpart, st);
       launch_b_vox_large(d_vj, d_beg, n, task_off, items, counter, 0, st, c->num_sms, (int)c->tuning.large_block,
                          (int)c->tuning.large_ctas_per_sm);
@@ -799,7 +821,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       launch_b_level_bases(d_pyr, n, d_root, st);
       ck(cudaMemcpyAsync(lvl, d_root, (uint64_t)n * (kMaxLevels + 1) * 4, cudaMemcpyDeviceToHost, st), "levels");
     }
-  });
+  }, pieces != nullptr);  // waits on the upload stream are not captured
   ck(cudaStreamSynchronize(st), "level counts");
 
   // ---- counts, placement in the files ----
@@ -1199,7 +1221,10 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, co
   // launch sub-batch k, then finish k-1 while k computes
   auto flush = [&]() {
     // uploads arrive in mesh order: the sub-batch's last mesh being there covers the others
-    if (meshes[sb.back().mesh].uploaded) ck(cudaStreamWaitEvent(st, meshes[sb.back().mesh].uploaded, 0), "wait upload");
+    // (a lone stripe of a mesh uploaded in pieces waits for each piece instead)
+    const MeshWork& last = meshes[sb.back().mesh];
+    if (last.uploaded && !(sb.size() == 1 && !last.pieces.empty()))
+      ck(cudaStreamWaitEvent(st, last.uploaded, 0), "wait upload");
     run_sub_batch(c, st, meshes, sb, os, pend[k & 1], k & 1);
     if (os.mode == OUT_CTX) finish_sub_batch(c, meshes, pend[k & 1], os);
     else finish_sub_batch(c, meshes, pend[(k + 1) & 1], os);
@@ -1482,24 +1507,45 @@ struct BatchInput {
   static uint64_t bytes(const ooc_mesh& m) { return m.n_tris * (m.params.geometry_only ? 9 : 21) * 4; }
   // Queue the uploads on the context's upload stream, with an event after
   // every group of about 16 MB, so each sub-batch waits only for its meshes.
+  // A one-partition mesh of more than two groups goes up in pieces of about
+  // 16 MB, each with its event, and its voxelization follows piece by piece.
   void upload(ooc_ctx* c, const ooc_mesh* in, cudaStream_t st) {
     ck(cudaEventRecord(c->ev_compute[0], st), "event");  // the device buffer is free once earlier work on st is done
     ck(cudaStreamWaitEvent(c->h2d_stream, c->ev_compute[0], 0), "wait");
     PhaseScope ph(c, PH_COPY, c->h2d_stream);
+    constexpr uint64_t kGroup = 16ull << 20;
     size_t used = 0, group = 0;
     uint64_t acc = 0;
+    auto event = [&]() {
+      if (used == c->up_events.size()) {
+        cudaEvent_t e;
+        ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        c->up_events.push_back(e);
+      }
+      cudaEvent_t e = c->up_events[used++];
+      ck(cudaEventRecord(e, c->h2d_stream), "event");
+      return e;
+    };
     for (size_t i = 0; i < meshes.size(); i++) {
-      if (bytes(in[i]))
-        ck(cudaMemcpyAsync(d_all + off[i], in[i].tris, bytes(in[i]), cudaMemcpyHostToDevice, c->h2d_stream), "H2D");
-      acc += bytes(in[i]);
-      if (acc >= (16ull << 20) || i + 1 == meshes.size()) {
-        if (used == c->up_events.size()) {
-          cudaEvent_t e;
-          ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
-          c->up_events.push_back(e);
+      const uint64_t nb = bytes(in[i]);
+      MeshWork& m = meshes[i];
+      m.pieces.clear();
+      if (m.pl.P == 1 && nb > 2 * kGroup) {
+        const uint64_t rec = nb / in[i].n_tris, per = kGroup / rec;  // triangles per piece
+        for (uint64_t t0 = 0; t0 < in[i].n_tris; t0 += per) {
+          const uint64_t t1 = std::min<uint64_t>(in[i].n_tris, t0 + per);
+          ck(cudaMemcpyAsync(d_all + off[i] + t0 * rec, reinterpret_cast<const char*>(in[i].tris) + t0 * rec,
+                             (t1 - t0) * rec, cudaMemcpyHostToDevice, c->h2d_stream), "H2D");
+          m.pieces.emplace_back(t1, event());
         }
-        cudaEvent_t e = c->up_events[used++];
-        ck(cudaEventRecord(e, c->h2d_stream), "event");
+        for (; group <= i; group++) meshes[group].uploaded = m.pieces.back().second;
+        acc = 0;
+        continue;
+      }
+      if (nb) ck(cudaMemcpyAsync(d_all + off[i], in[i].tris, nb, cudaMemcpyHostToDevice, c->h2d_stream), "H2D");
+      acc += nb;
+      if (acc >= kGroup || i + 1 == meshes.size()) {
+        const cudaEvent_t e = event();
         for (; group <= i; group++) meshes[group].uploaded = e;
         acc = 0;
       }

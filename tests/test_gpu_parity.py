@@ -222,3 +222,12 @@ def test_marked_and_unmarked_in_one_batch(builder):
         nodes, data, _ = pyoracle.build(t, N, 2048)
         d = octree.diff(g.tree, octree.Octree(N, nodes, data))
         assert not d, "\n".join(d)
+
+
+@pytest.mark.parametrize("payload,N,T", [(True, 128, 450_000), (False, 512, 1_000_000)])
+def test_upload_in_pieces(builder, payload, N, T):
+    """Host meshes of more than 32 MB in one partition go up in 16 MB pieces, each
+    voxelized as soon as it is on the device."""
+    t = tri.soup_tris(T, N, seed=45, sigma=0.5 if N == 512 else 1.0, n_spheres=30, payload=payload)
+    assert t.nbytes > 32 << 20
+    assert_same(*run_both(builder, t, N))
