@@ -201,6 +201,18 @@ def algorithmic_bytes(kernel: str, n_tris: int, info: dict, S: int, payload: boo
     return 0.0
 
 
+def small_candidates(tris: np.ndarray, gridsize: int, small_vol: int = 64) -> int:
+    """Candidate voxels of the triangles the one-thread-per-triangle pass voxelizes: the sum of
+    their clamped grid-box volumes (voxelizer.cpp:199-204, boxes of at most `small_vol` voxels).
+    Meshes in the unit cube, so unit_div = gridsize."""
+    v = tris[:, :9].reshape(-1, 3, 3).astype(np.float32)
+    g = np.float32(gridsize)
+    lo = np.clip((v.min(axis=1) * g).astype(np.int64), 0, gridsize - 1)
+    hi = np.clip((v.max(axis=1) * g).astype(np.int64), 0, gridsize - 1)
+    vol = np.prod(hi - lo + 1, axis=1)
+    return int(vol[vol <= small_vol].sum())
+
+
 def run_ours(args, world, rank, local):
     import torch
     import ooc_svo_builder_gb300 as ooc
@@ -321,6 +333,16 @@ def run_ours(args, world, rank, local):
                 "traffic_source": traffic_src,
                 "peak_source": peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
                 "per_launch_ms": per_launch_ms, "algorithmic_bytes_per_launch": alg_per_launch}
+    # The voxelization is issue-bound, not HBM-bound: its own roofline is the FP32 rate without
+    # FMA (152 SMs x 128 lanes x the measured SM clock) against the 47 flops of the full
+    # Schwarz-Seidel test per candidate voxel (voxelizer.cpp:266-287).
+    if dominant == "vox_small_occupancy" and dom_n and clocks.get("sm_mhz"):
+        flops = 47.0 * small_candidates(tris, w["gridsize"]) / max(1, launches_per_build)
+        fp32_peak = 152 * 128 * clocks["sm_mhz"] * 1e6 / 1e12
+        fp32_achieved = flops / (per_launch_ms / 1e3) / 1e12
+        roofline["fp32"] = {"bound": "fp32 issue (no FMA)", "achieved": fp32_achieved, "peak": fp32_peak,
+                            "unit": "TFLOP/s", "frac": fp32_achieved / fp32_peak,
+                            "flops_per_launch": flops, "peak_source": "152 SMs x 128 FP32 lanes x measured SM clock"}
 
     line = {
         "metric": "Mtri/s", "value": value, "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,

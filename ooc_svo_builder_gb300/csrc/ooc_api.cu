@@ -769,6 +769,12 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       return l > kTopPyramidLevel ? pyr[s].lv[l].nscan : 0;
     }));
 
+  // keys of every level, launched as soon as the level counts are back (its prefix needs no count)
+  const Light cp_compact = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
+    const uint64_t upper = pyr[s].lv[pyr[s].depth].off_b - pyr[s].lv[0].off_b;  // compact_elems
+    return (upper + 31) / 32 * 32 + (pyr[s].lv[pyr[s].depth].nscan + 31) / 32 * 32;
+  });
+
   Uploader up1;
   const size_t o_vj = up1.add(vj.data(), n * sizeof(VoxJob));
   const size_t o_pyr = up1.add(pyr.data(), n * sizeof(Pyramid));
@@ -776,6 +782,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const size_t o_cpi = up1.add(cp_items.data(), (n + 1) * 8);
   std::vector<size_t> o_cpp(cp_pyr.size());
   for (size_t r = 0; r < cp_pyr.size(); r++) o_cpp[r] = up1.add(cp_pyr[r].beg.data(), (n + 1) * 8);
+  const size_t o_cc = up1.add(cp_compact.beg.data(), (n + 1) * 8);
   unsigned char* t1 = up1.run(c, c->d_tables1, c->h_tables1, st);
   auto dp1 = [&](size_t off) { return reinterpret_cast<const uint64_t*>(t1 + off); };
   const VoxJob* d_vj = reinterpret_cast<const VoxJob*>(t1 + o_vj);
@@ -848,6 +855,12 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   }
   // node indices are 32-bit within a sub-batch (the block scan is u32)
   if (summed != total_nodes) fail(OOC_ERR_LIMIT, "more than 2^32 nodes in one sub-batch; lower the batch budget");
+  // the keys need only the phase-A tables: the GPU compacts while the host lays out the rest
+  uint32_t* keys = ensure<uint32_t>(c->d_keys, total_nodes * 4);
+  {
+    PhaseScope ph(c, PH_PYR, st);
+    launch_b_compact(d_pyr, dp1(o_cc), n, cp_compact.beg[n], cp_compact.ept, keys, n == 1 ? &pyr[0] : nullptr, st);
+  }
   // the grouping above the stripes, run ahead on placeholders: where every stripe's records start
   for (uint32_t s = 0; s < n; s++) {
     MeshWork& m = meshes[sb[s].mesh];
@@ -873,7 +886,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     any_levels = any_levels || m.pl.levels;
     any_payload = any_payload || !m.pl.binary;
   }
-  uint32_t* keys = ensure<uint32_t>(c->d_keys, total_nodes * 4);
   uint32_t* size = ensure<uint32_t>(c->d_size, total_nodes * 4);
   uint32_t* dsize = ensure<uint32_t>(c->d_dsize, total_nodes * 4);
   uint32_t* first_child = ensure<uint32_t>(c->d_firstchild, total_nodes * 4);
@@ -981,10 +993,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     e.l_small = ls;
   }
   auto live = [&](uint32_t s) { return !pl[s].empty; };
-  const Light cp_compact = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
-    const uint64_t upper = pyr[s].lv[pyr[s].depth].off_b - pyr[s].lv[0].off_b;  // compact_elems
-    return (upper + 31) / 32 * 32 + (pyr[s].lv[pyr[s].depth].nscan + 31) / 32 * 32;
-  });
   const std::vector<uint64_t> cp_pay = cta_prefix(n, kChunk, [&](uint32_t s) -> uint64_t {
     return meshes[sb[s].mesh].pl.binary ? 0 : sb[s].n_items;
   });
@@ -1011,7 +1019,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const size_t o_vj2 = up2.add(vj.data(), n * sizeof(VoxJob));
   const size_t o_pyr2 = up2.add(pyr.data(), n * sizeof(Pyramid));
   const size_t o_ej = up2.add(ej.data(), n * sizeof(EmitJob));
-  const size_t o_cc = up2.add(cp_compact.beg.data(), (n + 1) * 8);
   const size_t o_cpay = up2.add(cp_pay.data(), (n + 1) * 8);
   const size_t o_clp = up2.add(cp_leafpay.beg.data(), (n + 1) * 8);
   const size_t o_cl = up2.add(cp_leaves.beg.data(), (n + 1) * 8);
@@ -1029,10 +1036,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
 
   uint32_t* hr = ensure_pinned<uint32_t>(c->h_root[slot], ((uint64_t)n * 16 + 1) * 4);
   run_launches(c, st, 1, [&] {
-    {
-      PhaseScope ph(c, PH_PYR, st);
-      launch_b_compact(d_pyr2, dp2(o_cc), n, cp_compact.beg[n], cp_compact.ept, keys, n == 1 ? &pyr[0] : nullptr, st);
-    }
     if (any_payload) {
       PhaseScope ph(c, PH_VOX, st);
       ck(cudaMemsetAsync(winners, 0xff, total_nodes * 4, st), "memset winners");

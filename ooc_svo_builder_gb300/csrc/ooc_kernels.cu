@@ -605,6 +605,7 @@ template <int PASS>
 __global__ void __launch_bounds__(256, 4) k_vox_large(VoxJob j) {
   const int lane = threadIdx.x & 31;
   const uint64_t total = j.task_off[j.n_items];
+  if (total == 0) return;
   for (;;) {
     unsigned long long task = 0;
     if (lane == 0) task = atomicAdd(j.task_counter, 1ull);
@@ -1219,6 +1220,7 @@ __global__ void __launch_bounds__(256, 4) kb_vox_large(const VoxJob* __restrict_
                                                     uint64_t total_items, unsigned long long* counter) {
   const int lane = threadIdx.x & 31;
   const uint64_t total = task_off[total_items];
+  if (total == 0) return;  // no large items in this launch: no counter traffic
   for (;;) {
     unsigned long long task = 0;
     if (lane == 0) task = atomicAdd(counter, 1ull);
