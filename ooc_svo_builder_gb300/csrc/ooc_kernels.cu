@@ -1088,6 +1088,44 @@ __device__ __forceinline__ void top_down_child(const Pyramid& p, const EmitJob& 
   if (e.levels) store_data_record(e, di, 0, e.cache + c * 6);
 }
 
+// Two children of level l+1 at once, i0 < i1 (either may be past the level's
+// end): every load of both is issued before the first store, so the two
+// chains of dependent loads overlap.
+__device__ __forceinline__ void top_down_children(const Pyramid& p, const EmitJob& e, int l, uint64_t i0, uint64_t i1) {
+  const Level& C = p.lv[l + 1];
+  if (i0 >= C.n) return;
+  const bool v1 = i1 < C.n;
+  const uint64_t c0 = C.koff + i0, c1 = C.koff + (v1 ? i1 : i0);
+  const uint32_t kc0 = e.keys[c0], kc1 = e.keys[c1];
+  const uint64_t p0 = node_index(p, l, kc0 >> 3), p1 = node_index(p, l, kc1 >> 3);
+  const uint64_t f0 = e.first_child[p0], f1 = e.first_child[p1];
+  const uint32_t pm0 = child_mask(p, l + 1, kc0 >> 3), pm1 = child_mask(p, l + 1, kc1 >> 3);
+  uint64_t rs0 = e.start[p0], rd0 = e.dstart[p0], rs1 = e.start[p1], rd1 = e.dstart[p1];
+  const uint64_t cb0 = rs0 + (uint64_t)e.size[p0] - 1 - (uint64_t)__popc(pm0);
+  const uint64_t cb1 = rs1 + (uint64_t)e.size[p1] - 1 - (uint64_t)__popc(pm1);
+  const uint32_t mc0 = child_mask(p, l + 2, kc0), mc1 = child_mask(p, l + 2, kc1);
+  const uint64_t sz0 = e.size[c0], dsz0 = e.dsize[c0], sz1 = e.size[c1], dsz1 = e.dsize[c1];
+  for (uint64_t q = f0; q < c0; q++) {
+    rs0 += (uint64_t)e.size[q] - 1;
+    rd0 += e.dsize[q];
+  }
+  for (uint64_t q = f1; q < c1; q++) {
+    rs1 += (uint64_t)e.size[q] - 1;
+    rd1 += e.dsize[q];
+  }
+  e.start[c0] = rs0;
+  e.dstart[c0] = rd0;
+  const uint64_t di0 = rd0 + dsz0 - 1;
+  store_node_record(e, cb0 + (c0 - f0), e.levels ? di0 : 0, rs0 + sz0 - 1 - (uint64_t)__popc(mc0), child_offsets(mc0));
+  if (e.levels) store_data_record(e, di0, 0, e.cache + c0 * 6);
+  if (!v1) return;
+  e.start[c1] = rs1;
+  e.dstart[c1] = rd1;
+  const uint64_t di1 = rd1 + dsz1 - 1;
+  store_node_record(e, cb1 + (c1 - f1), e.levels ? di1 : 0, rs1 + sz1 - 1 - (uint64_t)__popc(mc1), child_offsets(mc1));
+  if (e.levels) store_data_record(e, di1, 0, e.cache + c1 * 6);
+}
+
 // Leaf records, one thread per leaf: the parent (level depth-1) already knows
 // where its child group and data run start.
 __device__ __forceinline__ void top_down_leaf(const Pyramid& p, const EmitJob& e, uint64_t i) {
@@ -1353,7 +1391,14 @@ __global__ void __launch_bounds__(kChunk) kb_nodes(const Pyramid* __restrict__ p
                                                    const uint64_t* __restrict__ cta_beg, uint32_t n, int arg, uint32_t ept,
                                                    Pyramid p0, EmitJob e0) {
   if constexpr (SINGLE) {
-    for (uint32_t k = 0; k < ept; k++) node_op<OP>(p0, e0, arg, ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x);
+    if constexpr (OP == OP_TOP_DOWN) {
+      for (uint32_t k = 0; k < ept; k += 2) {
+        const uint64_t i = ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x;
+        top_down_children(p0, e0, arg, i, k + 1 < ept ? i + kChunk : ~0ull);
+      }
+    } else {
+      for (uint32_t k = 0; k < ept; k++) node_op<OP>(p0, e0, arg, ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x);
+    }
   } else {
     __shared__ Pyramid sp;
     __shared__ EmitJob se;
@@ -1362,7 +1407,14 @@ __global__ void __launch_bounds__(kChunk) kb_nodes(const Pyramid* __restrict__ p
     stage(sp, pyrs[s]);
     stage(se, emits[s]);
     __syncthreads();
-    for (uint32_t k = 0; k < ept; k++) node_op<OP>(sp, se, arg, (cta * ept + k) * kChunk + threadIdx.x);
+    if constexpr (OP == OP_TOP_DOWN) {
+      for (uint32_t k = 0; k < ept; k += 2) {
+        const uint64_t i = (cta * ept + k) * kChunk + threadIdx.x;
+        top_down_children(sp, se, arg, i, k + 1 < ept ? i + kChunk : ~0ull);
+      }
+    } else {
+      for (uint32_t k = 0; k < ept; k++) node_op<OP>(sp, se, arg, (cta * ept + k) * kChunk + threadIdx.x);
+    }
   }
 }
 
