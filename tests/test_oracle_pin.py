@@ -75,3 +75,36 @@ def test_reference_optimisation_levels_agree(tmp_path):
                    check=True)
     b = octree.read_octree(base + "256_8")
     assert not octree.diff(a, b)
+
+
+@pytest.mark.parametrize("payload", [False, True])
+def test_reference_partition_invariance_inside_the_grid(tmp_path, payload):
+    """For triangles inside the grid the reference gives the same octree with one partition
+    (-l 2048) and with eight (-l 2): its partition box filter (partitioner.cpp:54-61) keeps
+    every triangle a partition's voxel test can set a voxel for."""
+    if not _reference_available(not payload):
+        pytest.skip("reference build not present (make -C oracle ref needs the reference sources)")
+    tris = tri.random_tris(1500, 208, payload, lo=0.02, hi=0.98, max_edge=0.2)
+    (tmp_path / "one").mkdir()
+    (tmp_path / "eight").mkdir()
+    d = octree.diff(_run_ref(tmp_path / "one", tris, 256, 2048), _run_ref(tmp_path / "eight", tris, 256, 2))
+    assert not d, "\n".join(d)
+
+
+def test_reference_outside_triangles_depend_on_partitions():
+    """Triangles just outside the grid are where the partition count shows.  With one
+    partition their clamped box (voxelizer.cpp:199-204) puts candidates on the grid's outer
+    layer, and the Schwarz-Seidel test, which has no bounding-box axis of its own, passes some
+    of them.  With eight partitions the box filter drops those triangles first.  Every voxel
+    that only one partition count sets lies on the grid's faces.  The oracle follows the
+    reference in both, which test_oracle_matches_reference_build pins; the GPU follows the
+    oracle."""
+    t = tri.random_tris(1500, 208, True, lo=-0.1, hi=1.1, max_edge=0.2)
+    _, d1, _ = pyoracle.build(t, 256, 2048)
+    _, d8, i8 = pyoracle.build(t, 256, 2)
+    assert i8["n_partitions"] == 8
+    one, eight = set(d1["morton"][1:].tolist()), set(d8["morton"][1:].tolist())
+    assert eight <= one and one != eight
+    for m in one - eight:
+        xyz = [sum(((m >> (3 * i + a)) & 1) << i for i in range(21)) for a in range(3)]
+        assert min(xyz) == 0 or max(xyz) == 255, xyz
