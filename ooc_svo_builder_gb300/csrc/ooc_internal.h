@@ -146,9 +146,10 @@ void launch_b_vox_small(const VoxJob* jobs, const uint64_t* cta_beg, uint32_t n,
                         const VoxJob* single, cudaStream_t st);
 // Large items of every stripe; task_off is the batch-wide exclusive scan (total_items + 1 entries),
 // item_beg[s] the first batch item of stripe s (ascending).
+// `lines_per_lane` is every job's (it sizes each warp's shared list of lines).
 void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n_stripes, const uint64_t* task_off,
                         uint64_t total_items, unsigned long long* counter, int pass, cudaStream_t st, int num_sms,
-                        int block, int ctas_per_sm);
+                        int block, int ctas_per_sm, uint32_t lines_per_lane);
 // Level depth - r of each stripe.
 void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, int r,
                       const Pyramid* single, cudaStream_t st);

@@ -414,9 +414,7 @@ __device__ __forceinline__ void vox_line(const VoxJob& j, const TriSetup& s, uin
     py = W == 1 ? fw : (W == 0 ? fa : fb);
     pz = W == 2 ? fw : fb;
   };
-  corner(w0);
-  // the projection test that does not depend on the walk coordinate
-  if (!(W == 2 ? pass_xy(s, px, py) : (W == 0 ? pass_yz(s, py, pz) : pass_zx(s, pz, px)))) return;
+  corner(w0);  // the caller has passed the projection test that does not depend on the walk coordinate
   // the two that do (with the plane test they complete the voxel test)
   auto rest = [&]() {
     return W == 2 ? (pass_yz(s, py, pz) && pass_zx(s, pz, px))
@@ -570,8 +568,19 @@ __device__ __forceinline__ void vox_small_win_item(const VoxJob& j, uint64_t i) 
 
 
 // Lines 32*L*k .. 32*L*(k+1)-1 of large item i, L = lines_per_lane (lane, lane+32, ...).
+// The projection test that does not depend on the walk coordinate, for line (ca, cb).
+__device__ __forceinline__ bool line_passes(const VoxJob& j, const TriSetup& s, int W, int ca, int cb) {
+  const float fa = __fmul_rn((float)ca, j.u), fb = __fmul_rn((float)cb, j.u);
+  return W == 2 ? pass_xy(s, fa, fb) : (W == 0 ? pass_yz(s, fa, fb) : pass_zx(s, fb, fa));
+}
+
+// Lines of a task, first tested by every lane against the projection that does not
+// depend on the walk coordinate; the lines that pass are packed into the warp's list
+// (`lines_smem`, 32 x lines_per_lane entries) and then walked one per lane, so lanes
+// do not idle beside lines outside the triangle.
 template <int PASS>
-__device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint64_t k, int lane) {
+__device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint64_t k, int lane,
+                                               uint32_t* __restrict__ lines_smem) {
   if (PASS == 1 && !j.winners) return;  // binary-mode stripe in a mixed batch: no winner pass
   const uint64_t t = item_triangle(j, i);
   const TriVerts tv = load_verts(j.tris, t, j.stride);
@@ -582,7 +591,6 @@ __device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint
   const uint32_t ea = (uint32_t)(W == 0 ? hi[1] - lo[1] + 1 : hi[0] - lo[0] + 1);  // first axis across the walk
   const uint32_t lines = (uint32_t)item_lines(W, lo, hi);
   const uint32_t c0 = (uint32_t)k * 32u * j.lines_per_lane + (uint32_t)lane;
-  if (c0 >= lines) return;
   TriSetup s;
   tri_setup(tv, j.u, s);
   const int top = max(hi[0], max(hi[1], hi[2]));
@@ -592,18 +600,33 @@ __device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint
   const int wlo = W == 0 ? lo[0] : (W == 1 ? lo[1] : lo[2]);
   const int whi = W == 0 ? hi[0] : (W == 1 ? hi[1] : hi[2]);
   const int alo = W == 0 ? lo[1] : lo[0], blo = W == 2 ? lo[1] : lo[2];
+  // all 32 lanes: test, then pack the passing lines as (ca - alo) | (cb - blo) << 16
+  const uint32_t lt = (1u << lane) - 1u;
+  uint32_t n = 0;
 #pragma unroll 1
   for (uint32_t q = 0; q < j.lines_per_lane; q++) {
     const uint32_t c = c0 + 32u * q;
-    if (c >= lines) break;
-    vox_line<PASS>(j, s, (uint32_t)t, W, alo + (int)(c % ea), blo + (int)(c / ea), wlo, whi, mono, dir, inv_dir);
+    const uint32_t ra = c % ea, rb = c / ea;
+    const bool ok = c < lines && line_passes(j, s, W, alo + (int)ra, blo + (int)rb);
+    const uint32_t vote = __ballot_sync(FULL, ok);
+    if (ok) lines_smem[n + __popc(vote & lt)] = ra | (rb << 16);
+    n += __popc(vote);
   }
+  __syncwarp();
+#pragma unroll 1
+  for (uint32_t q = (uint32_t)lane; q < n; q += 32u) {
+    const uint32_t r = lines_smem[q];
+    vox_line<PASS>(j, s, (uint32_t)t, W, alo + (int)(r & 0xffffu), blo + (int)(r >> 16), wlo, whi, mono, dir, inv_dir);
+  }
+  __syncwarp();  // the list is free for the warp's next task
 }
 
 // Persistent warps pull 32-column tasks of large items from a global counter.
 template <int PASS>
 __global__ void __launch_bounds__(256, 4) k_vox_large(VoxJob j) {
+  extern __shared__ uint32_t lines_smem[];  // 32 x lines_per_lane per warp
   const int lane = threadIdx.x & 31;
+  uint32_t* wl = lines_smem + (threadIdx.x >> 5) * 32u * j.lines_per_lane;
   const uint64_t total = j.task_off[j.n_items];
   if (total == 0) return;
   for (;;) {
@@ -617,7 +640,7 @@ __global__ void __launch_bounds__(256, 4) k_vox_large(VoxJob j) {
       if (j.task_off[mid] <= task) lo_i = mid;
       else hi_i = mid;
     }
-    vox_large_task<PASS>(j, lo_i, task - j.task_off[lo_i], lane);
+    vox_large_task<PASS>(j, lo_i, task - j.task_off[lo_i], lane, wl);
   }
 }
 
@@ -1255,8 +1278,11 @@ __global__ void __launch_bounds__(kChunk, 4) kb_vox_small(const VoxJob* __restri
 template <int PASS>
 __global__ void __launch_bounds__(256, 4) kb_vox_large(const VoxJob* __restrict__ jobs, const uint64_t* __restrict__ item_beg,
                                                     uint32_t n_stripes, const uint64_t* __restrict__ task_off,
-                                                    uint64_t total_items, unsigned long long* counter) {
+                                                    uint64_t total_items, unsigned long long* counter,
+                                                    uint32_t lines_per_lane) {
+  extern __shared__ uint32_t lines_smem[];  // 32 x lines_per_lane per warp (every job has this lines_per_lane)
   const int lane = threadIdx.x & 31;
+  uint32_t* wl = lines_smem + (threadIdx.x >> 5) * 32u * lines_per_lane;
   const uint64_t total = task_off[total_items];
   if (total == 0) return;  // no large items in this launch: no counter traffic
   for (;;) {
@@ -1276,7 +1302,7 @@ __global__ void __launch_bounds__(256, 4) kb_vox_large(const VoxJob* __restrict_
       if (item_beg[mid] <= lo_i) s0 = mid;
       else s1 = mid;
     }
-    vox_large_task<PASS>(jobs[s0], lo_i - item_beg[s0], task - task_off[lo_i], lane);
+    vox_large_task<PASS>(jobs[s0], lo_i - item_beg[s0], task - task_off[lo_i], lane, wl);
   }
 }
 
@@ -1507,7 +1533,7 @@ void launch_vox_large_occupancy(const VoxJob& j, cudaStream_t st, int num_sms) {
   if (j.n_items == 0) return;
   cudaMemsetAsync(j.task_counter, 0, sizeof(unsigned long long), st);
   KScope k("vox_large_occupancy", st);
-  k_vox_large<0><<<(unsigned)num_sms * 8, 256, 0, st>>>(j);
+  k_vox_large<0><<<(unsigned)num_sms * 8, 256, 256 * j.lines_per_lane * 4, st>>>(j);
 }
 
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st) {
@@ -1541,13 +1567,20 @@ void launch_b_vox_small(const VoxJob* jobs, const uint64_t* cta_beg, uint32_t n,
 
 void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n_stripes, const uint64_t* task_off,
                         uint64_t total_items, unsigned long long* counter, int pass, cudaStream_t st, int num_sms,
-                        int block, int ctas_per_sm) {
+                        int block, int ctas_per_sm, uint32_t lines_per_lane) {
   if (total_items == 0) return;
   cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
   const unsigned grid = (unsigned)num_sms * (unsigned)ctas_per_sm;
+  const size_t smem = (size_t)block * lines_per_lane * 4;  // each warp's list of passing lines
+  if (smem > (48u << 10)) {  // beyond the default dynamic limit (at most 256 x 64 x 4 = 64 KiB)
+    cudaFuncSetAttribute(kb_vox_large<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(kb_vox_large<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }
   KScope k(pass == 0 ? "vox_large_occupancy" : "vox_large_winner", st);
-  if (pass == 0) kb_vox_large<0><<<grid, block, 0, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter);
-  else kb_vox_large<1><<<grid, block, 0, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter);
+  if (pass == 0)
+    kb_vox_large<0><<<grid, block, smem, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter, lines_per_lane);
+  else
+    kb_vox_large<1><<<grid, block, smem, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter, lines_per_lane);
 }
 
 void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, int r,
