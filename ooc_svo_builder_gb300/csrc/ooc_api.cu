@@ -131,7 +131,8 @@ struct ooc_ctx {
   unsigned long long launches = 0;
   DevBuf d_tris, d_hist, d_axis, d_bits, d_scan, d_scanpart, d_keys, d_size, d_dsize, d_start, d_dstart,
       d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo, d_itemmask,
-      d_firstchild, d_itembox, d_leaf, d_touch, d_local;
+      d_firstchild, d_itembox, d_leaf, d_touch, d_local, d_taskmap;
+  uint64_t max_tasks = 0;  // most large-item warp tasks a sub-batch has had (sizes the task map)
   bool leaf_zero = true;  // d_leaf and d_touch hold only zeros (no sub-batch left them dirty)
   PinBuf h_misc, h_recs, h_tables1, h_tables2;
   // double-buffered outputs of pipelined sub-batches
@@ -790,6 +791,16 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const uint64_t* d_beg = reinterpret_cast<const uint64_t*>(t1 + o_beg);
 
   uint32_t* lvl = ensure_pinned<uint32_t>(c->h_misc, ((uint64_t)n * 16 + 64) * 4);  // level bases, then root info
+  // Warp task -> item map, sized by the items and the most tasks a sub-batch has had.
+  // Built once the context has seen a sub-batch with many tasks: with few, the large
+  // items' search of the task offsets costs less than the map's launch.
+  constexpr uint64_t kMapMinTasks = 4096;
+  uint64_t* task_map = nullptr;
+  uint64_t map_cap = 0;
+  if (c->max_tasks >= kMapMinTasks) {
+    task_map = ensure<uint64_t>(c->d_taskmap, std::max<uint64_t>(items, c->max_tasks) * 8);
+    map_cap = c->d_taskmap.cap / 8;
+  }
   c->leaf_zero = false;  // until the clean at the end of the sub-batch is queued
   run_launches(c, st, 0, [&] {
     {
@@ -814,8 +825,9 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
         launch_b_vox_small(d_vj, dp1(o_cpi), n, cp_items[n], 0, n == 1 ? &vj[0] : nullptr, st);
       }
       scan_u64_exclusive(task_off, items + 1, taskpart, st);
+      if (map_cap) launch_b_task_map(dp1(o_cpi), n, cp_items[n], d_beg, task_off, items, task_map, map_cap, st);
       launch_b_vox_large(d_vj, d_beg, n, task_off, items, counter, 0, st, c->num_sms, (int)c->tuning.large_block,
-                         (int)c->tuning.large_ctas_per_sm, c->tuning.lines_per_lane);
+                         (int)c->tuning.large_ctas_per_sm, c->tuning.lines_per_lane, task_map, map_cap);
     }
     {
       PhaseScope ph(c, PH_PYR, st);
@@ -825,11 +837,15 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
                          st);
       launch_b_pyramid_top(d_pyr, n, kTopPyramidLevel, st);
       scan_u32_exclusive(scan, blocks + 1, scanpart, st);
-      launch_b_level_bases(d_pyr, n, d_root, st);
-      ck(cudaMemcpyAsync(lvl, d_root, (uint64_t)n * (kMaxLevels + 1) * 4, cudaMemcpyDeviceToHost, st), "levels");
+      launch_b_level_bases(d_pyr, n, d_root, task_off + items, reinterpret_cast<uint64_t*>(d_root + (uint64_t)n * 16 + 8),
+                           st);
+      ck(cudaMemcpyAsync(lvl, d_root, ((uint64_t)n * 16 + 10) * 4, cudaMemcpyDeviceToHost, st), "levels");
     }
   }, pieces != nullptr);  // waits on the upload stream are not captured
   ck(cudaStreamSynchronize(st), "level counts");
+  uint64_t tasks_seen;
+  std::memcpy(&tasks_seen, lvl + (uint64_t)n * 16 + 8, 8);
+  c->max_tasks = std::max(c->max_tasks, tasks_seen);
 
   // ---- counts, placement in the files ----
   std::vector<Placed> pl(n);
@@ -1041,7 +1057,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       ck(cudaMemsetAsync(winners, 0xff, total_nodes * 4, st), "memset winners");
       launch_b_vox_small(d_vj2, dp2(o_cpay), n, cp_pay[n], 1, n == 1 ? &vj[0] : nullptr, st);
       launch_b_vox_large(d_vj2, d_beg, n, task_off, items, counter, 1, st, c->num_sms, (int)c->tuning.large_block,
-                         (int)c->tuning.large_ctas_per_sm, c->tuning.lines_per_lane);
+                         (int)c->tuning.large_ctas_per_sm, c->tuning.lines_per_lane, task_map, map_cap);
       launch_b_leaf_payload(d_pyr2, d_ej, dp2(o_clp), n, cp_leafpay.beg[n], cp_leafpay.ept, sp1, se1, st);
     }
     {
@@ -1405,7 +1421,7 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   DevBuf* bufs[] = {&c->d_tris, &c->d_hist, &c->d_axis, &c->d_bits, &c->d_scan, &c->d_scanpart,
                     &c->d_keys, &c->d_size, &c->d_dsize, &c->d_start, &c->d_dstart, &c->d_cache, &c->d_winners,
                     &c->d_taskoff, &c->d_taskpart, &c->d_counter, &c->d_nodes, &c->d_data, &c->d_recs,
-                    &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox, &c->d_leaf, &c->d_touch, &c->d_local};
+                    &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox, &c->d_leaf, &c->d_touch, &c->d_local, &c->d_taskmap};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   PinBuf* pins[] = {&c->h_misc, &c->h_recs, &c->h_tables1, &c->h_tables2};

@@ -146,10 +146,15 @@ void launch_b_vox_small(const VoxJob* jobs, const uint64_t* cta_beg, uint32_t n,
                         const VoxJob* single, cudaStream_t st);
 // Large items of every stripe; task_off is the batch-wide exclusive scan (total_items + 1 entries),
 // item_beg[s] the first batch item of stripe s (ascending).
-// `lines_per_lane` is every job's (it sizes each warp's shared list of lines).
+// map[t] = item | stripe << 32 for every warp task t, if they all fit in `cap` entries
+// (CTAs as for launch_b_vox_small: `cta_beg` over the stripes' items).
+void launch_b_task_map(const uint64_t* cta_beg, uint32_t n, uint64_t ctas, const uint64_t* item_beg,
+                       const uint64_t* task_off, uint64_t total_items, uint64_t* map, uint64_t cap, cudaStream_t st);
+// `lines_per_lane` is every job's (it sizes each warp's shared list of lines); tasks find
+// their item in `map` when the tasks fit in `cap`, else by searching task_off.
 void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n_stripes, const uint64_t* task_off,
                         uint64_t total_items, unsigned long long* counter, int pass, cudaStream_t st, int num_sms,
-                        int block, int ctas_per_sm, uint32_t lines_per_lane);
+                        int block, int ctas_per_sm, uint32_t lines_per_lane, const uint64_t* map, uint64_t cap);
 // Level depth - r of each stripe.
 void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, int r,
                       const Pyramid* single, cudaStream_t st);
@@ -161,7 +166,9 @@ void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, 
 void launch_b_clean_leaves(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept,
                            const Pyramid* single, cudaStream_t st);
 // out[s * (kMaxLevels + 1) + l] = global node index of level l's first node, l = 0..depth+1.
-void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, cudaStream_t st);
+// Also *tasks_out = *tasks (the large-item task count travels back with the level counts).
+void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, const uint64_t* tasks,
+                          uint64_t* tasks_out, cudaStream_t st);
 void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
                            uint64_t ctas, uint32_t ept, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 // Level depth - r of each stripe.

@@ -1275,11 +1275,26 @@ __global__ void __launch_bounds__(kChunk, 4) kb_vox_small(const VoxJob* __restri
   }
 }
 
+// The item and stripe of every warp task: map[t] = item | stripe << 32, one thread
+// per item writing its tasks' entries.  Written only when all tasks fit in `cap`.
+__global__ void __launch_bounds__(kChunk) kb_task_map(const uint64_t* __restrict__ cta_beg, uint32_t n,
+                                                      const uint64_t* __restrict__ item_beg,
+                                                      const uint64_t* __restrict__ task_off, uint64_t total_items,
+                                                      uint64_t* __restrict__ map, uint64_t cap) {
+  uint64_t cta;
+  const uint32_t s = cta_stripe(cta_beg, n, cta);
+  if (task_off[total_items] > cap) return;
+  const uint64_t i = item_beg[s] + cta * kChunk + threadIdx.x;
+  if (i >= item_beg[s + 1]) return;
+  for (uint64_t t = task_off[i], e = task_off[i + 1]; t < e; t++) map[t] = i | ((uint64_t)s << 32);
+}
+
 template <int PASS>
 __global__ void __launch_bounds__(256, 4) kb_vox_large(const VoxJob* __restrict__ jobs, const uint64_t* __restrict__ item_beg,
                                                     uint32_t n_stripes, const uint64_t* __restrict__ task_off,
                                                     uint64_t total_items, unsigned long long* counter,
-                                                    uint32_t lines_per_lane) {
+                                                    uint32_t lines_per_lane, const uint64_t* __restrict__ map,
+                                                    uint64_t cap) {
   extern __shared__ uint32_t lines_smem[];  // 32 x lines_per_lane per warp (every job has this lines_per_lane)
   const int lane = threadIdx.x & 31;
   uint32_t* wl = lines_smem + (threadIdx.x >> 5) * 32u * lines_per_lane;
@@ -1290,17 +1305,25 @@ __global__ void __launch_bounds__(256, 4) kb_vox_large(const VoxJob* __restrict_
     if (lane == 0) task = atomicAdd(counter, 1ull);
     task = __shfl_sync(FULL, task, 0);
     if (task >= total) break;
-    uint64_t lo_i = 0, hi_i = total_items;  // task_off[lo_i] <= task < task_off[hi_i]
-    while (hi_i - lo_i > 1) {
-      const uint64_t mid = (lo_i + hi_i) >> 1;
-      if (task_off[mid] <= task) lo_i = mid;
-      else hi_i = mid;
-    }
-    uint32_t s0 = 0, s1 = n_stripes;  // item_beg[s0] <= lo_i < item_beg[s1]
-    while (s1 - s0 > 1) {
-      const uint32_t mid = (s0 + s1) >> 1;
-      if (item_beg[mid] <= lo_i) s0 = mid;
-      else s1 = mid;
+    uint64_t lo_i = 0;
+    uint32_t s0 = 0;
+    if (total <= cap) {  // one load instead of two searches of dependent loads
+      const uint64_t v = map[task];
+      lo_i = (uint32_t)v;
+      s0 = (uint32_t)(v >> 32);
+    } else {
+      uint64_t hi_i = total_items;  // task_off[lo_i] <= task < task_off[hi_i]
+      while (hi_i - lo_i > 1) {
+        const uint64_t mid = (lo_i + hi_i) >> 1;
+        if (task_off[mid] <= task) lo_i = mid;
+        else hi_i = mid;
+      }
+      uint32_t s1 = n_stripes;  // item_beg[s0] <= lo_i < item_beg[s1]
+      while (s1 - s0 > 1) {
+        const uint32_t mid = (s0 + s1) >> 1;
+        if (item_beg[mid] <= lo_i) s0 = mid;
+        else s1 = mid;
+      }
     }
     vox_large_task<PASS>(jobs[s0], lo_i - item_beg[s0], task - task_off[lo_i], lane, wl);
   }
@@ -1386,8 +1409,10 @@ __global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__
   }
 }
 
-__global__ void kb_level_bases(const Pyramid* __restrict__ pyrs, uint32_t n_stripes, uint32_t* __restrict__ out) {
+__global__ void kb_level_bases(const Pyramid* __restrict__ pyrs, uint32_t n_stripes, uint32_t* __restrict__ out,
+                               const uint64_t* __restrict__ tasks, uint64_t* __restrict__ tasks_out) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) *tasks_out = *tasks;
   if (s >= n_stripes) return;
   const Pyramid& p = pyrs[s];
   uint32_t* o = out + (uint64_t)s * (kMaxLevels + 1);
@@ -1565,9 +1590,16 @@ void launch_b_vox_small(const VoxJob* jobs, const uint64_t* cta_beg, uint32_t n,
   }
 }
 
+void launch_b_task_map(const uint64_t* cta_beg, uint32_t n, uint64_t ctas, const uint64_t* item_beg,
+                       const uint64_t* task_off, uint64_t total_items, uint64_t* map, uint64_t cap, cudaStream_t st) {
+  if (ctas == 0) return;
+  KScope k("task_map", st);
+  kb_task_map<<<(unsigned)ctas, kChunk, 0, st>>>(cta_beg, n, item_beg, task_off, total_items, map, cap);
+}
+
 void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n_stripes, const uint64_t* task_off,
                         uint64_t total_items, unsigned long long* counter, int pass, cudaStream_t st, int num_sms,
-                        int block, int ctas_per_sm, uint32_t lines_per_lane) {
+                        int block, int ctas_per_sm, uint32_t lines_per_lane, const uint64_t* map, uint64_t cap) {
   if (total_items == 0) return;
   cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
   const unsigned grid = (unsigned)num_sms * (unsigned)ctas_per_sm;
@@ -1578,9 +1610,11 @@ void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n
   }
   KScope k(pass == 0 ? "vox_large_occupancy" : "vox_large_winner", st);
   if (pass == 0)
-    kb_vox_large<0><<<grid, block, smem, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter, lines_per_lane);
+    kb_vox_large<0><<<grid, block, smem, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter, lines_per_lane,
+                                               map, cap);
   else
-    kb_vox_large<1><<<grid, block, smem, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter, lines_per_lane);
+    kb_vox_large<1><<<grid, block, smem, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter, lines_per_lane,
+                                               map, cap);
 }
 
 void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, int r,
@@ -1622,10 +1656,11 @@ void launch_b_clean_leaves(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_
   else kb_clean_leaves<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, ept, p0);
 }
 
-void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, cudaStream_t st) {
+void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, const uint64_t* tasks,
+                          uint64_t* tasks_out, cudaStream_t st) {
   if (n_stripes == 0) return;
   KScope k("level_bases", st);
-  kb_level_bases<<<grid_for(n_stripes, 128), 128, 0, st>>>(pyrs, n_stripes, out);
+  kb_level_bases<<<grid_for(n_stripes, 128), 128, 0, st>>>(pyrs, n_stripes, out, tasks, tasks_out);
 }
 
 namespace {
