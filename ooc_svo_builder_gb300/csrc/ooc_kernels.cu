@@ -602,9 +602,11 @@ __device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint
   const int alo = W == 0 ? lo[1] : lo[0], blo = W == 2 ? lo[1] : lo[2];
   // all 32 lanes: test, then pack the passing lines as (ca - alo) | (cb - blo) << 16
   const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t first = (uint32_t)k * 32u * j.lines_per_lane;  // the task's first line (same for all lanes)
+  const uint32_t rounds = min(j.lines_per_lane, (lines - first + 31u) / 32u);
   uint32_t n = 0;
 #pragma unroll 1
-  for (uint32_t q = 0; q < j.lines_per_lane; q++) {
+  for (uint32_t q = 0; q < rounds; q++) {
     const uint32_t c = c0 + 32u * q;
     const uint32_t ra = c % ea, rb = c / ea;
     const bool ok = c < lines && line_passes(j, s, W, alo + (int)ra, blo + (int)rb);
