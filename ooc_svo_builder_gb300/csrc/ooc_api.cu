@@ -549,15 +549,17 @@ struct Placed {  // a stripe after the level counts
 // more than they save).
 constexpr int kMarkDepth = 9;
 
-// Levels 0..Ds of a stripe appended to the buffers: the words of levels
-// 0..Ds-1 to `words`, the leaf level's to `leaf_words`, every level's scan
-// entries to `entries` (one per group of kLeafGroup blocks for a marked leaf level).
+// Levels 0..Ds of a stripe appended to the buffers: the words of the levels
+// kept zero between builds (the leaf level, and with marks the level above it)
+// to `leaf_words`, the others to `words`, every level's scan entries to
+// `entries` (one per group of kLeafGroup blocks for a marked leaf level).
 int pyramid_levels(int Ds, Level* lv, uint64_t& words, uint64_t& leaf_words, uint64_t& entries, bool marked) {
+  const int zl = marked ? Ds - 1 : Ds;
   for (int l = 0; l <= Ds; l++) {
     const uint64_t nbits = 1ull << (3 * l);
     uint64_t nw = (nbits + 31) / 32;
     nw = (nw + 7) / 8 * 8;
-    uint64_t& acc = l == Ds ? leaf_words : words;
+    uint64_t& acc = l >= zl ? leaf_words : words;
     lv[l].off_w = acc;
     lv[l].off_b = entries;
     lv[l].nwords = nw;
@@ -732,6 +734,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     P.bits = bits;
     P.leaf = leaf;
     P.touch = P.depth >= kMarkDepth ? touch + touch_beg[s] : nullptr;
+    P.zl = P.depth >= kMarkDepth ? P.depth - 1 : P.depth;
     P.local = P.depth >= kMarkDepth ? local + local_beg[s] : nullptr;
     P.scan = scan;
     VoxJob& j = vj[s];

@@ -26,7 +26,8 @@ struct Level {
   uint64_t n;        // set bits (nodes) at this level, filled after the scan
 };
 
-// The leaf level lives in its own buffer, which is all zero between builds:
+// The leaf level (with a marked leaf level, also the level above it) lives in
+// its own buffer, which is all zero between builds:
 // the voxelization marks every 256-bit leaf block it sets a bit in (`touch`,
 // one byte per block, written with plain stores), the passes over the leaf
 // level read only marked blocks, and the last kernel of a sub-batch zeroes the
@@ -38,9 +39,10 @@ struct Level {
 // nodes before it (`local`), so the scan never visits unmarked blocks.
 struct Pyramid {
   int depth;  // Ds: levels 0..Ds, level Ds = voxels of the stripe
+  int zl;     // levels zl..Ds live in `leaf` (Ds, or Ds-1 when the leaf level is marked)
   Level lv[kMaxLevels];
-  uint32_t* bits;   // words of levels 0..Ds-1
-  uint32_t* leaf;   // words of level Ds
+  uint32_t* bits;   // words of levels 0..zl-1
+  uint32_t* leaf;   // words of levels zl..Ds, zero between builds outside marked groups
   uint8_t* touch;   // byte b non-zero: leaf block b may have a set bit (NULL: every block is read)
   uint16_t* local;  // marked leaf level: nodes of block b's group before block b (written for marked blocks)
   uint32_t* scan;   // exclusive prefix popcount per 256-bit block, all levels (+1 total)

@@ -655,14 +655,25 @@ __device__ __forceinline__ uint32_t nonzero_bytes(uint32_t w) {
   return ((t >> 7) & 1u) | ((t >> 14) & 2u) | ((t >> 21) & 4u) | ((t >> 28) & 8u);
 }
 
-// First word of level l (the leaf level has its own buffer).
+// First word of level l (levels zl.. live in the buffer kept zero between builds).
 __device__ __forceinline__ uint32_t* level_words(const Pyramid& p, int l) {
-  return (l == p.depth ? p.leaf : p.bits) + p.lv[l].off_w;
+  return (l >= p.zl ? p.leaf : p.bits) + p.lv[l].off_w;
+}
+
+// Whether the leaf blocks under block b of level depth-1 (leaf blocks 8b..8b+7,
+// one word of that block each) are all unmarked, so the block is zero.
+__device__ __forceinline__ bool parent_block_empty(const Pyramid& p, uint64_t b) {
+  return reinterpret_cast<const uint64_t*>(p.touch)[b] == 0ull;
 }
 
 // Block b of level l (not a marked leaf level): its popcount and parent word.
 __device__ __forceinline__ void pyramid_block(const Pyramid& p, int l, uint64_t b) {
   const Level& L = p.lv[l];
+  if (p.touch && l == p.depth - 1 && parent_block_empty(p, b)) {
+    p.scan[L.off_b + b] = 0u;
+    if (l > 0) level_words(p, l - 1)[b] = 0u;
+    return;
+  }
   const uint4* q = reinterpret_cast<const uint4*>(level_words(p, l) + 8 * b);
   const uint4 q0 = q[0], q1 = q[1];
   const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
@@ -696,12 +707,7 @@ __device__ __forceinline__ void leaf_group(const Pyramid& p, uint64_t q) {
   const Level& L = p.lv[p.depth];
   const uint4 m4 = reinterpret_cast<const uint4*>(p.touch)[q];
   uint4* parent = reinterpret_cast<uint4*>(level_words(p, p.depth - 1) + q * kLeafGroup);
-  if (!(m4.x | m4.y | m4.z | m4.w)) {
-    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
-    parent[0] = z;
-    parent[1] = z;
-    parent[2] = z;
-    parent[3] = z;
+  if (!(m4.x | m4.y | m4.z | m4.w)) {  // the parent words stay zero
     p.scan[L.off_b + q] = 0u;
     return;
   }
@@ -776,7 +782,9 @@ __device__ __forceinline__ void compact_elem(const Pyramid& p, uint64_t e, uint3
     if (e >= upper) return;
     int l = 0;
     while (p.lv[l + 1].off_b <= first + e) l++;
-    block_keys(level_words(p, l), first + e - p.lv[l].off_b, p.scan[first + e], keys);
+    const uint64_t lb = first + e - p.lv[l].off_b;
+    if (p.touch && l == p.depth - 1 && parent_block_empty(p, lb)) return;
+    block_keys(level_words(p, l), lb, p.scan[first + e], keys);
     return;
   }
   const uint64_t q = e - up32;
@@ -819,8 +827,9 @@ __device__ __forceinline__ void compact_elem(const Pyramid& p, uint64_t e, uint3
   }
 }
 
-// Mark bytes 16i .. 16i+15 of a stripe: zero their marked leaf blocks, then
-// the marks.  A stripe without marks has its 16 leaf blocks zeroed outright.
+// Mark bytes 16i .. 16i+15 of a stripe: zero their marked leaf blocks, the
+// group's 16 parent words, then the marks.  A stripe without marks has its 16
+// leaf blocks zeroed outright.
 __device__ __forceinline__ void clean_touch16(const Pyramid& p, uint64_t i) {
   if (i * 16 >= touch_bytes(p.lv[p.depth])) return;
   if (!p.touch) {  // T threads zero the level's 2 x nblocks <= 32 T uint4, coalesced
@@ -834,6 +843,11 @@ __device__ __forceinline__ void clean_touch16(const Pyramid& p, uint64_t i) {
   if (!(t.x | t.y | t.z | t.w)) return;
   const uint4 z = make_uint4(0u, 0u, 0u, 0u);
   *t4 = z;
+  uint4* parent = reinterpret_cast<uint4*>(level_words(p, p.depth - 1) + i * 16);  // the group's 16 parent words
+  parent[0] = z;
+  parent[1] = z;
+  parent[2] = z;
+  parent[3] = z;
   uint4* leaf = reinterpret_cast<uint4*>(level_words(p, p.depth));
   const uint32_t tw[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
