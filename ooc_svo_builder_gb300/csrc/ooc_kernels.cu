@@ -780,8 +780,11 @@ __device__ __forceinline__ void compact_elem(const Pyramid& p, uint64_t e, uint3
   if (e >= compact_elems(p)) return;  // whole warps
   if (e < up32) {
     if (e >= upper) return;
-    int l = 0;
-    while (p.lv[l + 1].off_b <= first + e) l++;
+    int l = p.depth - 1;  // most upper blocks are on the level above the leaves
+    if (first + e < p.lv[l].off_b) {
+      l = 0;
+      while (p.lv[l + 1].off_b <= first + e) l++;
+    }
     const uint64_t lb = first + e - p.lv[l].off_b;
     if (p.touch && l == p.depth - 1 && parent_block_empty(p, lb)) return;
     block_keys(level_words(p, l), lb, p.scan[first + e], keys);
