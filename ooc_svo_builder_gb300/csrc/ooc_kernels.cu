@@ -329,7 +329,9 @@ __device__ __forceinline__ uint32_t leaf_rank(const VoxJob& j, uint32_t b) {
 // is the same rounded product the per-voxel expression would form, and the
 // one addition that joins the halves is commutative, so every test is bit for
 // bit the reference's (voxelizer.cpp:266-287).
-__device__ __forceinline__ uint64_t vox_column(const VoxJob& j, const TriSetup& s, int x, int y, int z0, int z1) {
+// `mxy` holds the Morton bits of (x, y) and `mz0` those of z0, stripe-local.
+__device__ __forceinline__ uint64_t vox_column(const VoxJob& j, const TriSetup& s, int x, int y, int z0, int z1,
+                                               uint32_t mxy, uint32_t mz0) {
   const float px = __fmul_rn((float)x, j.u);
   const float py = __fmul_rn((float)y, j.u);
   if (!pass_xy(s, px, py)) return 0;
@@ -340,9 +342,8 @@ __device__ __forceinline__ uint64_t vox_column(const VoxJob& j, const TriSetup& 
     yz_col[k] = __fmul_rn(s.yz[k][0], py);  // dot2(yz, (py, pz)) = yz0*py + yz1*pz
     zx_col[k] = __fmul_rn(s.zx[k][1], px);  // dot2(zx, (pz, px)) = zx0*pz + zx1*px
   }
-  const uint32_t mxy = spread3_10((uint32_t)(x - j.sa[0])) | (spread3_10((uint32_t)(y - j.sa[1])) << 1);
   constexpr uint32_t ZBITS = 0x24924924u;  // Morton bit positions of z (2, 5, ..., 29)
-  uint32_t mz = spread3_10((uint32_t)(z0 - j.sa[2])) << 2;
+  uint32_t mz = mz0;
   uint32_t cur_w = 0xffffffffu, acc = 0;
   uint64_t col = 0;
   for (int z = z0; z <= z1; z++, mz = ((mz | ~ZBITS) + 4u) & ZBITS) {
@@ -523,12 +524,20 @@ __device__ __forceinline__ void vox_small_occ_item(const VoxJob& j, uint64_t i) 
     if (bx * by * bz <= j.small_vol) {
       TriSetup s;
       tri_setup(tv, j.u, s);
+      // Morton bits of the box's coordinates, stepped by the carry trick: setting every
+      // bit outside an axis' positions makes +1 carry across them
+      constexpr uint32_t XBITS = 0x09249249u, YBITS = 0x12492492u;
+      const uint32_t mz0 = spread3_10((uint32_t)(lo[2] - j.sa[2])) << 2;
+      const uint32_t my0 = spread3_10((uint32_t)(lo[1] - j.sa[1])) << 1;
+      uint32_t mx = spread3_10((uint32_t)(lo[0] - j.sa[0]));
       uint32_t shift = 0;
-      for (int x = lo[0]; x <= hi[0]; x++)
-        for (int y = lo[1]; y <= hi[1]; y++) {
-          mask |= vox_column(j, s, x, y, lo[2], hi[2]) << shift;
+      for (int x = lo[0]; x <= hi[0]; x++, mx = ((mx | ~XBITS) + 1u) & XBITS) {
+        uint32_t my = my0;
+        for (int y = lo[1]; y <= hi[1]; y++, my = ((my | ~YBITS) + 2u) & YBITS) {
+          mask |= vox_column(j, s, x, y, lo[2], hi[2], mx | my, mz0) << shift;
           shift += (uint32_t)bz;
         }
+      }
       if (j.item_mask && mask) {
         // stripe-local box origin (10 bits per axis) and extents - 1 (6 bits each)
         j.item_box[i] = (uint64_t)(lo[0] - j.sa[0]) | ((uint64_t)(lo[1] - j.sa[1]) << 10) |
@@ -556,11 +565,14 @@ __device__ __forceinline__ void vox_small_win_item(const VoxJob& j, uint64_t i) 
   const uint64_t box = j.item_box[i];
   const uint32_t lx = (uint32_t)box & 1023u, ly = (uint32_t)(box >> 10) & 1023u, lz = (uint32_t)(box >> 20) & 1023u;
   const uint32_t by = (uint32_t)(box >> 36 & 63u) + 1u, bz = (uint32_t)(box >> 42 & 63u) + 1u;
+  // q / d for q < 64, d <= 64 as (q * ceil(2^16 / d)) >> 16: the error of the rounded-up
+  // reciprocal adds less than q / 2^16 < 1/d, which never carries past the next integer
+  const uint32_t rz = (65535u + bz) / bz, ry = (65535u + by) / by;
   while (mask) {
     const uint32_t q = (uint32_t)(__ffsll((long long)mask) - 1);
     mask &= mask - 1;
-    const uint32_t col = q / bz, z = q - col * bz;
-    const uint32_t x = col / by, y = col - x * by;
+    const uint32_t col = (q * rz) >> 16, z = q - col * bz;
+    const uint32_t x = (col * ry) >> 16, y = col - x * by;
     const uint32_t m = morton_local(lx + x, ly + y, lz + z);
     atomicMin(&j.winners[leaf_rank(j, m)], t);
   }
