@@ -809,7 +809,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     {
       PhaseScope ph(c, PH_VOX, st);
       ck(cudaMemsetAsync(task_off + items, 0, 8, st), "memset task_off");
-      ck(cudaMemsetAsync(flag, 0, 4, st), "memset flag");
       if (pieces) {
         // each piece of the triangles as soon as its copy is done
         uint64_t beg = 0;
@@ -834,14 +833,13 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     }
     {
       PhaseScope ph(c, PH_PYR, st);
-      ck(cudaMemsetAsync(scan + blocks, 0, 4, st), "memset scan");
       for (size_t r = 0; r < cp_pyr.size(); r++)
         launch_b_pyramid(d_pyr, dp1(o_cpp[r]), n, cp_pyr[r].beg[n], cp_pyr[r].ept, (int)r, n == 1 ? &pyr[0] : nullptr,
                          st);
-      launch_b_pyramid_top(d_pyr, n, kTopPyramidLevel, st);
+      launch_b_pyramid_top(d_pyr, n, kTopPyramidLevel, scan + blocks, st);
       scan_u32_exclusive(scan, blocks + 1, scanpart, st);
       launch_b_level_bases(d_pyr, n, d_root, task_off + items, reinterpret_cast<uint64_t*>(d_root + (uint64_t)n * 16 + 8),
-                           st);
+                           flag, st);
       ck(cudaMemcpyAsync(lvl, d_root, ((uint64_t)n * 16 + 10) * 4, cudaMemcpyDeviceToHost, st), "levels");
     }
   }, pieces != nullptr);  // waits on the upload stream are not captured

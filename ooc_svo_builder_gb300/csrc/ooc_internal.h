@@ -161,16 +161,18 @@ void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n
 void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, int r,
                       const Pyramid* single, cudaStream_t st);
 // One CTA per stripe: levels min(l_hi, depth) .. 0.
-void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cudaStream_t st);
+// Also zeroes *scan_end, the block scan's total entry, before the scan.
+void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, uint32_t* scan_end, cudaStream_t st);
 void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, uint32_t* keys,
                       const Pyramid* single, cudaStream_t st);
 // Zero the marked leaf blocks of every stripe and the marks: one thread per 16 mark bytes.
 void launch_b_clean_leaves(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept,
                            const Pyramid* single, cudaStream_t st);
 // out[s * (kMaxLevels + 1) + l] = global node index of level l's first node, l = 0..depth+1.
-// Also *tasks_out = *tasks (the large-item task count travels back with the level counts).
+// Also *tasks_out = *tasks (the large-item task count travels back with the level counts)
+// and *flag = 0 (the layout check flag the record kernels may set).
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, const uint64_t* tasks,
-                          uint64_t* tasks_out, cudaStream_t st);
+                          uint64_t* tasks_out, uint32_t* flag, cudaStream_t st);
 void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
                            uint64_t ctas, uint32_t ept, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 // Level depth - r of each stripe.

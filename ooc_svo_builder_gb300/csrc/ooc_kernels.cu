@@ -100,7 +100,8 @@ __global__ void __launch_bounds__(1024) k_scan_partials(T* partials, uint64_t np
   }
 }
 
-// Each thread scans SCAN_ITEMS consecutive elements staged through shared memory.
+// Each thread scans SCAN_ITEMS consecutive elements staged through shared memory
+// (`partials` NULL: a single tile, nothing before it).
 template <typename T>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(T* data, uint64_t n, const T* __restrict__ partials) {
   __shared__ T tile[SCAN_TILE + SCAN_TILE / 32];
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(T* data, uint64_t n,
     sum += v[q];
   }
   T total;
-  T run = block_exclusive(sum, total) + partials[blockIdx.x];
+  T run = block_exclusive(sum, total) + (partials ? partials[blockIdx.x] : T(0));
 #pragma unroll
   for (int q = 0; q < SCAN_ITEMS; q++) {
     const uint32_t li = threadIdx.x * SCAN_ITEMS + q;
@@ -141,6 +142,11 @@ template <typename T>
 void scan_exclusive(T* data, uint64_t n, T* partials, cudaStream_t st) {
   if (n == 0) return;
   const unsigned nb = (unsigned)((n + SCAN_TILE - 1) / SCAN_TILE);
+  if (nb == 1) {  // one tile: one launch
+    KScope k("scan_down", st);
+    k_scan_down<T><<<1, SCAN_THREADS, 0, st>>>(data, n, nullptr);
+    return;
+  }
   {
     KScope k("scan_reduce", st);
     k_scan_reduce<T><<<nb, SCAN_THREADS, 0, st>>>(data, n, partials);
@@ -1391,7 +1397,8 @@ __global__ void __launch_bounds__(kChunk) kb_pyramid(const Pyramid* __restrict__
   }
 }
 
-__global__ void kb_pyramid_top(const Pyramid* __restrict__ pyrs, int l_hi) {
+__global__ void kb_pyramid_top(const Pyramid* __restrict__ pyrs, int l_hi, uint32_t* __restrict__ scan_end) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *scan_end = 0u;  // the scan's total entry
   __shared__ Pyramid sp;
   stage(sp, pyrs[blockIdx.x]);
   __syncthreads();
@@ -1441,9 +1448,13 @@ __global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__
 }
 
 __global__ void kb_level_bases(const Pyramid* __restrict__ pyrs, uint32_t n_stripes, uint32_t* __restrict__ out,
-                               const uint64_t* __restrict__ tasks, uint64_t* __restrict__ tasks_out) {
+                               const uint64_t* __restrict__ tasks, uint64_t* __restrict__ tasks_out,
+                               uint32_t* __restrict__ flag) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s == 0) *tasks_out = *tasks;
+  if (s == 0) {
+    *tasks_out = *tasks;
+    *flag = 0u;  // the layout check flag of the sub-batch's record kernels
+  }
   if (s >= n_stripes) return;
   const Pyramid& p = pyrs[s];
   uint32_t* o = out + (uint64_t)s * (kMaxLevels + 1);
@@ -1659,10 +1670,10 @@ void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, 
   else kb_pyramid<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, r, ept, p0);
 }
 
-void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, cudaStream_t st) {
+void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, uint32_t* scan_end, cudaStream_t st) {
   if (n_stripes == 0) return;
   KScope k("pyramid_top", st);
-  kb_pyramid_top<<<n_stripes, 512, 0, st>>>(pyrs, l_hi);
+  kb_pyramid_top<<<n_stripes, 512, 0, st>>>(pyrs, l_hi, scan_end);
 }
 
 void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept,
@@ -1688,10 +1699,10 @@ void launch_b_clean_leaves(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_
 }
 
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, const uint64_t* tasks,
-                          uint64_t* tasks_out, cudaStream_t st) {
+                          uint64_t* tasks_out, uint32_t* flag, cudaStream_t st) {
   if (n_stripes == 0) return;
   KScope k("level_bases", st);
-  kb_level_bases<<<grid_for(n_stripes, 128), 128, 0, st>>>(pyrs, n_stripes, out, tasks, tasks_out);
+  kb_level_bases<<<grid_for(n_stripes, 128), 128, 0, st>>>(pyrs, n_stripes, out, tasks, tasks_out, flag);
 }
 
 namespace {
