@@ -1057,8 +1057,9 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       PhaseScope ph(c, PH_VOX, st);
       ck(cudaMemsetAsync(winners, 0xff, total_nodes * 4, st), "memset winners");
       launch_b_vox_small(d_vj2, dp2(o_cpay), n, cp_pay[n], 1, n == 1 ? &vj[0] : nullptr, st);
-      launch_b_vox_large(d_vj2, d_beg, n, task_off, items, counter, 1, st, c->num_sms, (int)c->tuning.large_block,
-                         (int)c->tuning.large_ctas_per_sm, c->tuning.lines_per_lane, task_map, map_cap);
+      if (tasks_seen)  // the count came back with the level counts
+        launch_b_vox_large(d_vj2, d_beg, n, task_off, items, counter, 1, st, c->num_sms, (int)c->tuning.large_block,
+                           (int)c->tuning.large_ctas_per_sm, c->tuning.lines_per_lane, task_map, map_cap);
       launch_b_leaf_payload(d_pyr2, d_ej, dp2(o_clp), n, cp_leafpay.beg[n], cp_leafpay.ept, sp1, se1, st);
     }
     {
