@@ -906,8 +906,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   uint32_t* size = ensure<uint32_t>(c->d_size, total_nodes * 4);
   uint32_t* dsize = ensure<uint32_t>(c->d_dsize, total_nodes * 4);
   uint32_t* first_child = ensure<uint32_t>(c->d_firstchild, total_nodes * 4);
-  uint64_t* start = ensure<uint64_t>(c->d_start, total_nodes * 8);
-  uint64_t* dstart = ensure<uint64_t>(c->d_dstart, total_nodes * 8);
+  uint32_t* start = ensure<uint32_t>(c->d_start, total_nodes * 4);  // stripe-relative: a stripe spans < 2^32
+  uint32_t* dstart = ensure<uint32_t>(c->d_dstart, total_nodes * 4);
   float* cache = any_levels ? ensure<float>(c->d_cache, total_nodes * 24) : nullptr;
   uint32_t* winners = any_payload ? ensure<uint32_t>(c->d_winners, total_nodes * 4) : nullptr;
   uint64_t out_nodes = 0, out_data = 0;

@@ -91,8 +91,8 @@ struct EmitJob {
   const uint32_t* keys;     // per node: local key (Morton prefix within its level)
   uint32_t* size;           // per node: nodes in its subtree
   uint32_t* dsize;          // per node: data records in its subtree
-  uint64_t* start;          // per node: global index of the first node written inside its subtree
-  uint64_t* dstart;         // per node: global index of its subtree's first data record
+  uint32_t* start;          // per node: first node written inside its subtree, minus node_base
+  uint32_t* dstart;         // per node: its subtree's first data record, minus data_base
   float* cache;             // per node: 6 floats (colour, normal); only with -levels
   uint32_t* first_child;    // per internal node: global index of its first child
   int leaf_inline;          // payload leaves computed while their records are written (no -levels)

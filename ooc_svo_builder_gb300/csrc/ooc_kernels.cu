@@ -1084,8 +1084,8 @@ __device__ __forceinline__ void top_down_node(const Pyramid& p, const EmitJob& e
   const uint32_t k = e.keys[gi];
   const uint32_t mask = child_mask(p, l + 1, k);
   const int nch = __popc(mask);
-  const uint64_t st = e.start[gi];
-  uint64_t run_d = e.dstart[gi];
+  const uint64_t st = e.node_base + e.start[gi];
+  uint64_t run_d = e.data_base + e.dstart[gi];
   uint64_t run_s = st;
   const uint64_t cb = st + (uint64_t)e.size[gi] - 1 - (uint64_t)nch;
   const uint64_t c0 = e.first_child[gi];
@@ -1096,8 +1096,8 @@ __device__ __forceinline__ void top_down_node(const Pyramid& p, const EmitJob& e
     if (!child_leaf) {
       const uint32_t mc = child_mask(p, l + 2, kc);
       const uint64_t szc = e.size[c], dszc = e.dsize[c];
-      e.start[c] = run_s;
-      e.dstart[c] = run_d;
+      e.start[c] = (uint32_t)(run_s - e.node_base);
+      e.dstart[c] = (uint32_t)(run_d - e.data_base);
       const uint64_t di = run_d + dszc - 1;
       store_node_record(e, cb + j, e.levels ? di : 0, run_s + szc - 1 - (uint64_t)__popc(mc), child_offsets(mc));
       if (e.levels) store_data_record(e, di, 0, e.cache + c * 6);
@@ -1133,7 +1133,7 @@ __device__ __forceinline__ void top_down_child(const Pyramid& p, const EmitJob& 
   const uint64_t f = e.first_child[pidx];
   const uint64_t rank = c - f;
   const uint32_t pmask = child_mask(p, l + 1, pk);
-  uint64_t run_s = e.start[pidx], run_d = e.dstart[pidx];
+  uint64_t run_s = e.node_base + e.start[pidx], run_d = e.data_base + e.dstart[pidx];
   const uint64_t cb = run_s + (uint64_t)e.size[pidx] - 1 - (uint64_t)__popc(pmask);
   for (uint64_t q = f; q < c; q++) {
     run_s += (uint64_t)e.size[q] - 1;
@@ -1141,8 +1141,8 @@ __device__ __forceinline__ void top_down_child(const Pyramid& p, const EmitJob& 
   }
   const uint32_t mc = child_mask(p, l + 2, kc);
   const uint64_t szc = e.size[c], dszc = e.dsize[c];
-  e.start[c] = run_s;
-  e.dstart[c] = run_d;
+  e.start[c] = (uint32_t)(run_s - e.node_base);
+  e.dstart[c] = (uint32_t)(run_d - e.data_base);
   const uint64_t di = run_d + dszc - 1;
   store_node_record(e, cb + rank, e.levels ? di : 0, run_s + szc - 1 - (uint64_t)__popc(mc), child_offsets(mc));
   if (e.levels) store_data_record(e, di, 0, e.cache + c * 6);
@@ -1160,7 +1160,8 @@ __device__ __forceinline__ void top_down_children(const Pyramid& p, const EmitJo
   const uint64_t p0 = node_index(p, l, kc0 >> 3), p1 = node_index(p, l, kc1 >> 3);
   const uint64_t f0 = e.first_child[p0], f1 = e.first_child[p1];
   const uint32_t pm0 = child_mask(p, l + 1, kc0 >> 3), pm1 = child_mask(p, l + 1, kc1 >> 3);
-  uint64_t rs0 = e.start[p0], rd0 = e.dstart[p0], rs1 = e.start[p1], rd1 = e.dstart[p1];
+  uint64_t rs0 = e.node_base + e.start[p0], rd0 = e.data_base + e.dstart[p0];
+  uint64_t rs1 = e.node_base + e.start[p1], rd1 = e.data_base + e.dstart[p1];
   const uint64_t cb0 = rs0 + (uint64_t)e.size[p0] - 1 - (uint64_t)__popc(pm0);
   const uint64_t cb1 = rs1 + (uint64_t)e.size[p1] - 1 - (uint64_t)__popc(pm1);
   const uint32_t mc0 = child_mask(p, l + 2, kc0), mc1 = child_mask(p, l + 2, kc1);
@@ -1173,14 +1174,14 @@ __device__ __forceinline__ void top_down_children(const Pyramid& p, const EmitJo
     rs1 += (uint64_t)e.size[q] - 1;
     rd1 += e.dsize[q];
   }
-  e.start[c0] = rs0;
-  e.dstart[c0] = rd0;
+  e.start[c0] = (uint32_t)(rs0 - e.node_base);
+  e.dstart[c0] = (uint32_t)(rd0 - e.data_base);
   const uint64_t di0 = rd0 + dsz0 - 1;
   store_node_record(e, cb0 + (c0 - f0), e.levels ? di0 : 0, rs0 + sz0 - 1 - (uint64_t)__popc(mc0), child_offsets(mc0));
   if (e.levels) store_data_record(e, di0, 0, e.cache + c0 * 6);
   if (!v1) return;
-  e.start[c1] = rs1;
-  e.dstart[c1] = rd1;
+  e.start[c1] = (uint32_t)(rs1 - e.node_base);
+  e.dstart[c1] = (uint32_t)(rd1 - e.data_base);
   const uint64_t di1 = rd1 + dsz1 - 1;
   store_node_record(e, cb1 + (c1 - f1), e.levels ? di1 : 0, rs1 + sz1 - 1 - (uint64_t)__popc(mc1), child_offsets(mc1));
   if (e.levels) store_data_record(e, di1, 0, e.cache + c1 * 6);
@@ -1196,12 +1197,12 @@ __device__ __forceinline__ void top_down_leaf(const Pyramid& p, const EmitJob& e
   const uint64_t pidx = node_index(p, p.depth - 1, pk);
   const uint64_t rank = gi - e.first_child[pidx];
   const uint32_t pmask = child_mask(p, p.depth, pk);
-  const uint64_t pcb = e.start[pidx] + (uint64_t)e.size[pidx] - 1 - (uint64_t)__popc(pmask);
+  const uint64_t pcb = e.node_base + e.start[pidx] + (uint64_t)e.size[pidx] - 1 - (uint64_t)__popc(pmask);
   if (e.binary) {
     store_node_record(e, pcb + rank, 1, 0, ~0ull);
     return;
   }
-  const uint64_t di = e.dstart[pidx] + rank;
+  const uint64_t di = e.data_base + e.dstart[pidx] + rank;
   store_node_record(e, pcb + rank, di, 0, ~0ull);
   float v[6];
   if (e.leaf_inline) {
@@ -1534,8 +1535,8 @@ __global__ void kb_top_down_top(const Pyramid* __restrict__ pyrs, const EmitJob*
   __syncthreads();
   if (sp.depth < 1 || sp.lv[sp.depth].n == 0) return;
   if (threadIdx.x == 0) {
-    se.start[sp.lv[0].koff] = se.node_base;
-    se.dstart[sp.lv[0].koff] = se.data_base;
+    se.start[sp.lv[0].koff] = 0u;  // the stripe root starts at the stripe's bases
+    se.dstart[sp.lv[0].koff] = 0u;
   }
   __syncthreads();
   const int last = se.l_small < sp.depth - 2 ? se.l_small : sp.depth - 2;
