@@ -140,6 +140,7 @@ struct ooc_ctx {
   PinBuf h_root[2];
   D2HRing ring[2][2];  // [slot][OOC_STREAM_NODES / OOC_STREAM_DATA]
   cudaEvent_t ev_compute[2] = {nullptr, nullptr};
+  cudaEvent_t ev_data[2] = {nullptr, nullptr};  // host output: a sub-batch's data file is final
   cudaStream_t copy_stream = nullptr;
   cudaStream_t h2d_stream = nullptr;     // batch uploads, overlapping the sub-batches that do not need them yet
   std::vector<cudaEvent_t> up_events;    // recorded on h2d_stream as groups of meshes arrive
@@ -1013,10 +1014,17 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const std::vector<uint64_t> cp_pay = cta_prefix(n, kChunk, [&](uint32_t s) -> uint64_t {
     return meshes[sb[s].mesh].pl.binary ? 0 : sb[s].n_items;
   });
+  // leaf payloads: into the cache with -levels, else straight into the data file
+  // (a depth-0 stripe's one voxel is written with its root)
   const Light cp_leafpay = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
     const Plan& mp = meshes[sb[s].mesh].pl;
-    return (live(s) && mp.levels && !mp.binary) ? pl[s].n_leaf : 0;
+    if (!live(s) || mp.binary) return 0;
+    return (mp.levels || pyr[s].depth >= 1) ? pl[s].n_leaf : 0;
   });
+  // host output: without -levels the data file is final after the leaf payload pass,
+  // so its copy back starts there, beside the node layout
+  bool early_data = os.mode == OUT_HOST;
+  for (uint32_t s = 0; s < n; s++) early_data = early_data && !meshes[sb[s].mesh].pl.levels;
   const Light cp_leaves = light_prefix(c, n, [&](uint32_t s) -> uint64_t {
     return (live(s) && pyr[s].depth >= 1) ? pl[s].n_leaf : 0;  // a depth-0 root is the leaf
   });
@@ -1052,8 +1060,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const EmitJob* se1 = n == 1 ? &ej[0] : nullptr;
 
   uint32_t* hr = ensure_pinned<uint32_t>(c->h_root[slot], ((uint64_t)n * 16 + 1) * 4);
-  run_launches(c, st, 1, [&] {
-    if (any_payload) {
+  if (any_payload) run_launches(c, st, 1, [&] {
+    {
       PhaseScope ph(c, PH_VOX, st);
       ck(cudaMemsetAsync(winners, 0xff, total_nodes * 4, st), "memset winners");
       launch_b_vox_small(d_vj2, dp2(o_cpay), n, cp_pay[n], 1, n == 1 ? &vj[0] : nullptr, st);
@@ -1062,6 +1070,11 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
                            (int)c->tuning.large_ctas_per_sm, c->tuning.lines_per_lane, task_map, map_cap);
       launch_b_leaf_payload(d_pyr2, d_ej, dp2(o_clp), n, cp_leafpay.beg[n], cp_leafpay.ept, sp1, se1, st);
     }
+  });
+  // recorded between the two launch sequences: an event recorded inside a captured
+  // graph cannot be waited on from another stream
+  if (early_data) ck(cudaEventRecord(c->ev_data[slot], st), "event");
+  run_launches(c, st, 2, [&] {
     {
       PhaseScope ph(c, PH_TREE, st);
       for (size_t r = 1; r < cp_bu.size(); r++)
@@ -1081,9 +1094,13 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   ck(cudaEventRecord(c->ev_compute[slot], st), "event");
   if (os.mode == OUT_HOST) {
     // the records travel to the host on the copy stream while the next sub-batch computes
+    if (early_data) {
+      ck(cudaStreamWaitEvent(c->copy_stream, c->ev_data[slot], 0), "wait");
+      ring_start(c, c->ring[slot][OOC_STREAM_DATA], c->d_out_data[slot].p, out_data * 32);
+    }
     ck(cudaStreamWaitEvent(c->copy_stream, c->ev_compute[slot], 0), "wait");
     ring_start(c, c->ring[slot][OOC_STREAM_NODES], c->d_out_nodes[slot].p, out_nodes * 24);
-    ring_start(c, c->ring[slot][OOC_STREAM_DATA], c->d_out_data[slot].p, out_data * 32);
+    if (!early_data) ring_start(c, c->ring[slot][OOC_STREAM_DATA], c->d_out_data[slot].p, out_data * 32);
   }
   out_pending.active = true;
   out_pending.slot = slot;
@@ -1406,7 +1423,9 @@ int ooc_ctx_create(int32_t device, ooc_ctx** out) {
       cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->h2d_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_compute[0], cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_compute[1], cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&c->ev_compute[1], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_data[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_data[1], cudaEventDisableTiming) != cudaSuccess) {
     delete c;
     return OOC_ERR_DEVICE;
   }
@@ -1439,6 +1458,7 @@ void ooc_ctx_destroy(ooc_ctx* c) {
     }
     if (c->h_root[i].p) cudaFreeHost(c->h_root[i].p);
     if (c->ev_compute[i]) cudaEventDestroy(c->ev_compute[i]);
+    if (c->ev_data[i]) cudaEventDestroy(c->ev_data[i]);
   }
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->h2d_stream) cudaStreamDestroy(c->h2d_stream);

@@ -95,7 +95,7 @@ struct EmitJob {
   uint32_t* dstart;         // per node: its subtree's first data record, minus data_base
   float* cache;             // per node: 6 floats (colour, normal); only with -levels
   uint32_t* first_child;    // per internal node: global index of its first child
-  int leaf_inline;          // payload leaves computed while their records are written (no -levels)
+  int leaf_inline;          // payload without -levels: the leaf payload pass writes the leaves' data records
   const uint32_t* winners;
   uint64_t* node_win;       // node window (3 u64 per record)
   uint64_t node_win_base;   // global node index of node_win[0]

@@ -962,14 +962,23 @@ __device__ bool leaf_value(const EmitJob& e, uint64_t li, uint32_t key, float ou
   return true;
 }
 
-// Leaf payloads into the per-node cache (needed before the -levels averages).
+__device__ __forceinline__ void store_data_record(const EmitJob& e, uint64_t idx, uint64_t morton, const float* v);
+
+// Leaf payloads: with -levels into the per-node cache (the averages need them);
+// without, straight into the data file, where leaf i of the stripe is data record
+// data_base + i (its data records are its leaves in key order), so the data file
+// is final before the node records are laid out.
 __device__ __forceinline__ void leaf_payload(const Pyramid& p, const EmitJob& e, uint64_t i) {
   const Level& L = p.lv[p.depth];
+  const uint32_t k = e.keys[L.koff + i];
   float v[6];
-  if (leaf_value(e, i, e.keys[L.koff + i], v)) {
+  if (!leaf_value(e, i, k, v)) return;
+  if (e.levels) {
     float* out = e.cache + (L.koff + i) * 6;
 #pragma unroll
     for (int q = 0; q < 6; q++) out[q] = v[q];
+  } else {
+    store_data_record(e, e.data_base + i, e.stripe_base + k, v);
   }
 }
 
@@ -1107,14 +1116,12 @@ __device__ __forceinline__ void top_down_node(const Pyramid& p, const EmitJob& e
       store_node_record(e, cb + j, 1, 0, ~0ull);
     } else {
       store_node_record(e, cb + j, run_d, 0, ~0ull);
-      float v[6];
-      if (e.leaf_inline) {
-        if (!leaf_value(e, c - p.lv[p.depth].koff, kc, v)) return;
-      } else {
+      if (!e.leaf_inline) {  // (without -levels the leaf payload pass wrote the data record)
+        float v[6];
 #pragma unroll
         for (int q = 0; q < 6; q++) v[q] = e.cache[c * 6 + q];
+        store_data_record(e, run_d, e.stripe_base + kc, v);
       }
-      store_data_record(e, run_d, e.stripe_base + kc, v);
       run_d += 1;
     }
   }
@@ -1204,13 +1211,10 @@ __device__ __forceinline__ void top_down_leaf(const Pyramid& p, const EmitJob& e
   }
   const uint64_t di = e.data_base + e.dstart[pidx] + rank;
   store_node_record(e, pcb + rank, di, 0, ~0ull);
+  if (e.leaf_inline) return;  // the leaf payload pass wrote the data record
   float v[6];
-  if (e.leaf_inline) {
-    if (!leaf_value(e, i, k, v)) return;
-  } else {
 #pragma unroll
-    for (int q = 0; q < 6; q++) v[q] = e.cache[gi * 6 + q];
-  }
+  for (int q = 0; q < 6; q++) v[q] = e.cache[gi * 6 + q];
   store_data_record(e, di, e.stripe_base + k, v);
 }
 
