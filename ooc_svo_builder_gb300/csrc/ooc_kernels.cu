@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const T* __restric
   if (threadIdx.x == 0) partials[blockIdx.x] = total;
 }
 
+// Also partials[np] = the grand total.
 template <typename T>
 __global__ void __launch_bounds__(1024) k_scan_partials(T* partials, uint64_t np) {
   T carry = 0;
@@ -98,12 +99,15 @@ __global__ void __launch_bounds__(1024) k_scan_partials(T* partials, uint64_t np
     if (i < np) partials[i] = ex + carry;
     carry += total;
   }
+  if (threadIdx.x == 0) partials[np] = carry;
 }
 
 // Each thread scans SCAN_ITEMS consecutive elements staged through shared memory
 // (`partials` NULL: a single tile, nothing before it).
 template <typename T>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(T* data, uint64_t n, const T* __restrict__ partials) {
+  // the elements are counts: a zero total means all zero, which is already their scan
+  if (partials && partials[gridDim.x] == T(0)) return;
   __shared__ T tile[SCAN_TILE + SCAN_TILE / 32];
   const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
 #pragma unroll
@@ -1099,20 +1103,38 @@ __device__ __forceinline__ void top_down_node(const Pyramid& p, const EmitJob& e
   const uint64_t cb = st + (uint64_t)e.size[gi] - 1 - (uint64_t)nch;
   const uint64_t c0 = e.first_child[gi];
   const bool child_leaf = (l + 1 == p.depth);
+  if (!child_leaf) {
+    // every child's loads first (they are independent), then the running sums and stores
+    uint32_t kc[8], szc[8], dszc[8], mc[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (j < nch) {
+        kc[j] = e.keys[c0 + j];
+        szc[j] = e.size[c0 + j];
+        dszc[j] = e.dsize[c0 + j];
+      }
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (j < nch) mc[j] = child_mask(p, l + 2, kc[j]);
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (j < nch) {
+        const uint64_t c = c0 + (uint64_t)j;
+        e.start[c] = (uint32_t)(run_s - e.node_base);
+        e.dstart[c] = (uint32_t)(run_d - e.data_base);
+        const uint64_t di = run_d + dszc[j] - 1;
+        store_node_record(e, cb + j, e.levels ? di : 0, run_s + szc[j] - 1 - (uint64_t)__popc(mc[j]),
+                          child_offsets(mc[j]));
+        if (e.levels) store_data_record(e, di, 0, e.cache + c * 6);
+        run_s += szc[j] - 1;
+        run_d += dszc[j];
+      }
+    return;
+  }
   for (int j = 0; j < nch; j++) {
     const uint64_t c = c0 + (uint64_t)j;
     const uint32_t kc = e.keys[c];
-    if (!child_leaf) {
-      const uint32_t mc = child_mask(p, l + 2, kc);
-      const uint64_t szc = e.size[c], dszc = e.dsize[c];
-      e.start[c] = (uint32_t)(run_s - e.node_base);
-      e.dstart[c] = (uint32_t)(run_d - e.data_base);
-      const uint64_t di = run_d + dszc - 1;
-      store_node_record(e, cb + j, e.levels ? di : 0, run_s + szc - 1 - (uint64_t)__popc(mc), child_offsets(mc));
-      if (e.levels) store_data_record(e, di, 0, e.cache + c * 6);
-      run_s += szc - 1;
-      run_d += dszc;
-    } else if (e.binary) {
+    if (e.binary) {
       store_node_record(e, cb + j, 1, 0, ~0ull);
     } else {
       store_node_record(e, cb + j, run_d, 0, ~0ull);
