@@ -208,11 +208,6 @@ __device__ __forceinline__ float plane_xy(const TriSetup& s, float px, float py)
   return __fadd_rn(__fmul_rn(s.n[0], px), __fmul_rn(s.n[1], py));
 }
 
-// The whole per-voxel test of voxelizer.cpp:266-287 at one voxel corner.
-__device__ __forceinline__ bool pass_voxel(const TriSetup& s, float px, float py, float pz) {
-  return pass_xy(s, px, py) && pass_z(s, plane_xy(s, px, py), px, py, pz);
-}
-
 // The projection tests that do not depend on x (YZ) and on y (ZX).
 __device__ __forceinline__ bool pass_yz(const TriSetup& s, float py, float pz) {
 #pragma unroll

@@ -1149,37 +1149,12 @@ __device__ __forceinline__ void top_down_node(const Pyramid& p, const EmitJob& e
   }
 }
 
-// The same for one child: node i of level l+1 (an internal node) finds its
-// parent's run starts and adds its earlier siblings' subtree sizes (siblings
-// are consecutive in the key order), so the launch reads and writes the
-// child level contiguously.
-__device__ __forceinline__ void top_down_child(const Pyramid& p, const EmitJob& e, int l, uint64_t i) {
-  const Level& C = p.lv[l + 1];
-  const uint64_t c = C.koff + i;
-  const uint32_t kc = e.keys[c];
-  const uint32_t pk = kc >> 3;
-  const uint64_t pidx = node_index(p, l, pk);
-  const uint64_t f = e.first_child[pidx];
-  const uint64_t rank = c - f;
-  const uint32_t pmask = child_mask(p, l + 1, pk);
-  uint64_t run_s = e.node_base + e.start[pidx], run_d = e.data_base + e.dstart[pidx];
-  const uint64_t cb = run_s + (uint64_t)e.size[pidx] - 1 - (uint64_t)__popc(pmask);
-  for (uint64_t q = f; q < c; q++) {
-    run_s += (uint64_t)e.size[q] - 1;
-    run_d += e.dsize[q];
-  }
-  const uint32_t mc = child_mask(p, l + 2, kc);
-  const uint64_t szc = e.size[c], dszc = e.dsize[c];
-  e.start[c] = (uint32_t)(run_s - e.node_base);
-  e.dstart[c] = (uint32_t)(run_d - e.data_base);
-  const uint64_t di = run_d + dszc - 1;
-  store_node_record(e, cb + rank, e.levels ? di : 0, run_s + szc - 1 - (uint64_t)__popc(mc), child_offsets(mc));
-  if (e.levels) store_data_record(e, di, 0, e.cache + c * 6);
-}
-
-// Two children of level l+1 at once, i0 < i1 (either may be past the level's
-// end): every load of both is issued before the first store, so the two
-// chains of dependent loads overlap.
+// Children of level l+1, one thread per child, two at once (i0 < i1; either may
+// be past the level's end).  A child finds its parent's run starts and adds its
+// earlier siblings' subtree sizes (siblings are consecutive in the key order), so
+// the launch reads and writes the child level contiguously.  Every load of both
+// children is issued before the first store, so their chains of dependent loads
+// overlap.
 __device__ __forceinline__ void top_down_children(const Pyramid& p, const EmitJob& e, int l, uint64_t i0, uint64_t i1) {
   const Level& C = p.lv[l + 1];
   if (i0 >= C.n) return;
@@ -1500,7 +1475,7 @@ __device__ __forceinline__ void node_op(const Pyramid& p, const EmitJob& e, int 
     const int l = p.depth - arg;  // arg = distance from the leaf level
     if (i < p.lv[l].n) bottom_up_node(p, e, l, i);
   } else if (OP == OP_TOP_DOWN) {
-    if (i < p.lv[arg + 1].n) top_down_child(p, e, arg, i);  // arg = absolute parent level
+    top_down_children(p, e, arg, i, ~0ull);  // arg = absolute parent level
   } else {
     if (i < p.lv[p.depth].n) top_down_leaf(p, e, i);
   }
