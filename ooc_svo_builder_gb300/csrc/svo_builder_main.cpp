@@ -20,7 +20,9 @@ const char* kVersion = "1.6.4";
 std::string filename;
 uint64_t gridsize = 1024;      // main.cpp:30
 uint64_t memory_limit = 2048;  // main.cpp:31
+float sparseness_limit = 0.10f;  // main.cpp:32; printed by -v, no effect on the output
 int color = OOC_COLOR_MODEL;
+const char* color_name = "Color from model (fallback to fixed color if model has no color)";
 bool generate_levels = false;
 bool verbose = false;
 
@@ -55,7 +57,11 @@ void print_invalid() {
 
 bool is_pow2(unsigned int x) { return x != 0 && !(x & (x - 1)); }
 
-// parseProgramParameters (main.cpp:100-196)
+// parseProgramParameters (main.cpp:100-196).  Values are parsed with atoi into
+// the reference's unsigned types, so "-l -5" passes the ">= 1" check as a huge
+// limit (one partition) exactly as it does there.  One deliberate difference: a
+// flag that takes a value but ends the command line reads past argv there and
+// crashes; here it is an invalid argument.
 void parse(int argc, char** argv) {
   std::cout << "Reading program parameters ..." << std::endl;
   if (argc < 3) {
@@ -74,7 +80,7 @@ void parse(int argc, char** argv) {
       }
       i++;
     } else if (a == "-s" && has_next) {
-      gridsize = (uint64_t)std::atoi(argv[i + 1]);
+      gridsize = (uint64_t)(int64_t)std::atoi(argv[i + 1]);
       if (!is_pow2((unsigned int)gridsize)) {
         std::cout << "Requested gridsize is not a power of 2" << std::endl;
         print_invalid();
@@ -82,17 +88,16 @@ void parse(int argc, char** argv) {
       }
       i++;
     } else if (a == "-l" && has_next) {
-      const long v = std::atoi(argv[i + 1]);
-      if (v <= 1) {
+      memory_limit = (uint64_t)(int64_t)std::atoi(argv[i + 1]);
+      if (memory_limit <= 1) {
         std::cout << "Requested memory limit is nonsensical. Use a value >= 1" << std::endl;
         print_invalid();
         std::exit(0);
       }
-      memory_limit = (uint64_t)v;
       i++;
     } else if (a == "-d" && has_next) {
-      const int percent = std::atoi(argv[i + 1]);
-      if (percent / 100.0f < 0) {
+      sparseness_limit = std::atoi(argv[i + 1]) / 100.0f;
+      if (sparseness_limit < 0) {
         std::cout << "Requested data memory limit is nonsensical. Use a value > 0" << std::endl;
         print_invalid();
         std::exit(0);
@@ -108,11 +113,20 @@ void parse(int argc, char** argv) {
       (void)c;
       std::cout << "You asked to generate colors, but we're only doing binary voxelisation." << std::endl;
 #else
-      if (c == "model") color = OOC_COLOR_MODEL;
-      else if (c == "linear") color = OOC_COLOR_LINEAR;
-      else if (c == "normal") color = OOC_COLOR_NORMAL;
-      else if (c == "fixed") color = OOC_COLOR_FIXED;
-      else std::cout << "Unrecognized color switch: " << c << ", so reverting to colors from model." << std::endl;
+      if (c == "model") {
+        color = OOC_COLOR_MODEL;
+      } else if (c == "linear") {
+        color = OOC_COLOR_LINEAR;
+        color_name = "Linear";
+      } else if (c == "normal") {
+        color = OOC_COLOR_NORMAL;
+        color_name = "Normal";
+      } else if (c == "fixed") {
+        color = OOC_COLOR_FIXED;
+        color_name = "Fixed";
+      } else {
+        std::cout << "Unrecognized color switch: " << c << ", so reverting to colors from model." << std::endl;
+      }
 #endif
       i++;
     } else if (a == "-h") {
@@ -127,33 +141,77 @@ void parse(int argc, char** argv) {
     std::cout << "  filename: " << filename << std::endl;
     std::cout << "  gridsize: " << gridsize << std::endl;
     std::cout << "  memory limit: " << memory_limit << std::endl;
+    std::cout << "  sparseness optimization limit: " << sparseness_limit << " resulting in "
+              << sparseness_limit * (float)memory_limit << " memory limit." << std::endl;
+    std::cout << "  color type: " << color_name << std::endl;
     std::cout << "  generate levels: " << generate_levels << std::endl;
+    std::cout << "  verbosity: " << verbose << std::endl;
   }
 }
 
-// readTriHeader's checks (main.cpp:244-267)
+bool file_exists(const std::string& name) {
+  std::FILE* f = std::fopen(name.c_str(), "r");
+  if (!f) return false;
+  std::fclose(f);
+  return true;
+}
+
+// readTriHeader (main.cpp:244-267) over parseTriHeader (tri_tools.h:75-115):
+// the same token loop and the same messages, each followed by exit status 0.
+// The loop keeps the last keyword when a read fails at the end of the file, so a
+// header without END reports a trailing unknown keyword twice, as there.
 void check_tri(const std::string& fn) {
   std::cout << "Parsing tri header " << fn << " ..." << std::endl;
-  std::ifstream f(fn.c_str());
+  std::ifstream f(fn.c_str(), std::ios::in);
   if (!f) {
     std::cout << "  Error: file " << fn << " does not exist." << std::endl;
     std::exit(0);
   }
-  std::string tok;
-  int geo = 0;
+  const std::string base = fn.substr(0, fn.find_last_of("."));
+  std::string word;
+  f >> word;
+  if (word != "#tri") {
+    std::cout << "  Error: first line reads [" << word << "] instead of [#tri]" << std::endl;
+    std::exit(0);
+  }
+  int version = 0, geo = 0;
+  uint64_t n_triangles = 0;
+  float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
+  f >> version;
   bool seen_end = false;
-  while (f >> tok) {
-    if (tok == "geo_only") f >> geo;
-    if (tok == "END") {
+  while (f.good() && !seen_end) {
+    f >> word;
+    if (word == "END") {
       seen_end = true;
-      break;
+    } else if (word == "ntriangles") {
+      f >> n_triangles;
+    } else if (word == "geo_only") {
+      f >> geo;
+    } else if (word == "bbox") {
+      f >> bmin[0] >> bmin[1] >> bmin[2] >> bmax[0] >> bmax[1] >> bmax[2];
+    } else {
+      std::cout << "  unrecognized keyword [" << word << "], skipping" << std::endl;
+      char c;
+      do {
+        c = (char)f.get();
+      } while (f.good() && c != '\n');
     }
   }
-  const std::string base = fn.substr(0, fn.find_last_of("."));
-  std::ifstream d((base + ".tridata").c_str());
-  if (!seen_end || !d) {
+  if (!seen_end) {
+    std::cout << "  error reading header" << std::endl;
+    std::exit(0);
+  }
+  if (!file_exists(base + ".tri") || !file_exists(base + ".tridata")) {
     std::cout << "Not all required .tri or .tridata files exist. Please regenerate using tri_convert." << std::endl;
     std::exit(0);
+  }
+  if (verbose) {
+    std::cout << "  base_filename: " << base << std::endl;
+    std::cout << "  tri version: " << version << std::endl;
+    std::cout << "  geometry only: " << geo << std::endl;
+    std::cout << "  n_triangles: " << n_triangles << std::endl;
+    std::cout << "  bbox min: " << bmin[0] << " " << bmin[1] << " " << bmin[2] << std::endl;
+    std::cout << "  bbox max: " << bmax[0] << " " << bmax[1] << " " << bmax[2] << std::endl;
   }
 #ifdef OOC_CLI_BINARY
   if (!geo) {
@@ -172,6 +230,21 @@ void check_tri(const std::string& fn) {
 #endif
 }
 
+// estimate_partitions' report (partitioner.cpp:12-28); the count is the library's.
+// Dividing the in-core size by 8 once per factor of 8 partitions floors to the
+// same value as dividing it by the partition count.
+uint64_t report_partitions() {
+  std::cout << "Estimating best partition count ..." << std::endl;
+  const uint64_t required = gridsize * gridsize * gridsize / 1024 / 1024;
+  std::cout << "  to do this in-core I would need " << required << " Mb of system memory" << std::endl;
+  const uint64_t P = ooc_estimate_partitions(gridsize, memory_limit);
+  if (P == 1)
+    std::cout << "  memory limit of " << memory_limit << " Mb allows that" << std::endl;
+  else
+    std::cout << "  going to do it in " << P << " partitions of " << required / P << " Mb each." << std::endl;
+  return P;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -179,7 +252,7 @@ int main(int argc, char** argv) {
   print_info();
   parse(argc, argv);
   check_tri(filename);
-  const uint64_t P = ooc_estimate_partitions(gridsize, memory_limit);
+  const uint64_t P = report_partitions();
   std::cout << "Partitioning data into " << P << " partitions ... ";
   std::cout.flush();
 
