@@ -1404,6 +1404,12 @@ int guarded(ooc_ctx* c, F&& f) {
 
 }  // namespace
 
+namespace ooc {
+void set_ctx_error(ooc_ctx* c, const std::string& msg) {
+  if (c) c->err = msg;
+}
+}  // namespace ooc
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

@@ -14,6 +14,7 @@
 #include <thread>
 #include <vector>
 
+#include "ooc_internal.h"
 #include "ooc_svo_gpu.h"
 
 namespace {
@@ -193,7 +194,10 @@ extern "C" int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_bui
   if (!ctx || !tri_path || !params_in) return OOC_ERR_INVALID;
   TriHeader h;
   std::string err;
-  if (!parse_tri_header(tri_path, h, err)) return OOC_ERR_IO;
+  if (!parse_tri_header(tri_path, h, err)) {
+    ooc::set_ctx_error(ctx, err);
+    return OOC_ERR_IO;
+  }
   ooc_build_params prm = *params_in;
   prm.geometry_only = h.geo_only ? 1 : 0;
   for (int a = 0; a < 3; a++) {
@@ -203,9 +207,13 @@ extern "C" int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_bui
   const int stride = prm.geometry_only ? 9 : 21;
   const size_t bytes = (size_t)h.n_triangles * stride * sizeof(float);
   void* tris = nullptr;
-  if (bytes && cudaMalloc(&tris, bytes) != cudaSuccess) return OOC_ERR_OOM;
+  if (bytes && cudaMalloc(&tris, bytes) != cudaSuccess) {
+    ooc::set_ctx_error(ctx, "cannot allocate " + std::to_string(bytes) + " bytes of device memory for the triangles");
+    return OOC_ERR_OOM;
+  }
   if (bytes && !read_to_device(h.base + ".tridata", bytes, tris, err)) {
     cudaFree(tris);
+    ooc::set_ctx_error(ctx, err);
     return OOC_ERR_IO;
   }
   const uint64_t P = ooc_estimate_partitions(prm.gridsize, prm.memory_limit_mb);
@@ -218,12 +226,16 @@ extern "C" int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_bui
   std::memset(&local, 0, sizeof(local));
   if (!fn || !fd) {
     rc = OOC_ERR_IO;
+    ooc::set_ctx_error(ctx, "cannot create " + base + (fn ? ".octreedata" : ".octreenodes"));
   } else {
     FileWriter wn(fn), wd(fd);
     FileWriter* w[2] = {&wn, &wd};
     rc = ooc_build_from_device(ctx, &prm, static_cast<const float*>(tris), h.n_triangles, writer_sink, w, &local);
     const bool ok_n = wn.finish(), ok_d = wd.finish();
-    if (rc == OOC_OK && !(ok_n && ok_d)) rc = OOC_ERR_IO;
+    if (rc == OOC_OK && !(ok_n && ok_d)) {
+      rc = OOC_ERR_IO;
+      ooc::set_ctx_error(ctx, "cannot write " + base + (ok_n ? ".octreedata" : ".octreenodes"));
+    }
   }
   if (fn) std::fclose(fn);
   if (fd) std::fclose(fd);
@@ -237,7 +249,10 @@ extern "C" int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_bui
   out << "n_data " << local.n_data << std::endl;
   out << "END" << std::endl;
   out.close();
-  if (!out) return OOC_ERR_IO;
+  if (!out) {
+    ooc::set_ctx_error(ctx, "cannot write " + base + ".octree");
+    return OOC_ERR_IO;
+  }
   if (out_base && out_base_len) {
     std::strncpy(out_base, base.c_str(), (size_t)out_base_len - 1);
     out_base[out_base_len - 1] = 0;

@@ -5,6 +5,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
+struct ooc_ctx;
+
 namespace ooc {
 
 // Maximum stripe: 8^10 = 2^30 voxels, a 1024^3 Morton-aligned cube whose
@@ -114,6 +118,9 @@ struct EmitJob {
 // when cta_beg[s] <= b < cta_beg[s+1] and handles that stripe's elements
 // kChunk * (b - cta_beg[s]) onward.
 constexpr uint32_t kChunk = 256;
+
+// The message ooc_last_error returns for `c` (for failures found outside ooc_api.cu).
+void set_ctx_error(ooc_ctx* c, const std::string& msg);
 
 // ---- launches (ooc_kernels.cu); all asynchronous on `st` ----
 extern unsigned long long g_launches;  // kernel launches since the last reset (host counter)

@@ -103,3 +103,20 @@ def test_invalid_parameters(builder, field, value):
         builder.build(t, p)
     assert e.value.code == 1  # OOC_ERR_INVALID
     still_builds(builder)
+
+
+def test_file_errors_name_the_file(builder, tmp_path):
+    """ooc_build_files: a missing header and a .tridata shorter than its header's triangle
+    count fail with OOC_ERR_IO and a message naming the file; no device work is left behind."""
+    p = make_params(64, 2048, geometry_only=False)
+    with pytest.raises(ooc.OocError) as e:
+        builder.build_files(str(tmp_path / "absent.tri"), p)
+    assert e.value.code == 4 and "absent.tri does not exist" in str(e.value)
+    base = str(tmp_path / "short")
+    tri.write_tri(base, tri.random_tris(100, 3, True))
+    with open(base + ".tridata", "r+b") as f:
+        f.truncate(84 * 60)
+    with pytest.raises(ooc.OocError) as e:
+        builder.build_files(base + ".tri", p)
+    assert e.value.code == 4 and "short read of " + base + ".tridata" in str(e.value)
+    still_builds(builder)
