@@ -146,3 +146,23 @@ def diff(a: Octree, b: Octree, max_report: int = 5) -> list:
 
 def equal(a: Octree, b: Octree) -> bool:
     return not diff(a, b, max_report=1)
+
+
+CANONICAL_NAN = np.uint32(0x7FC00000)
+
+
+def digest(tree: Octree) -> dict:
+    """SHA-256 of the node and data files, with every NaN in the data records' colour and
+    normal replaced by one quiet-NaN pattern first, so two trees have the same digest
+    exactly when `diff` finds them equal (up to hash collisions)."""
+    import hashlib
+
+    data = tree.data.copy()
+    for field in ("color", "normal"):
+        f = data[field]
+        bits = f.view(np.uint32)
+        bits[np.isnan(f)] = CANONICAL_NAN
+    return {"gridlength": int(tree.gridlength), "n_nodes": int(tree.nodes.shape[0]),
+            "n_data": int(tree.data.shape[0]),
+            "nodes_sha256": hashlib.sha256(np.ascontiguousarray(tree.nodes).tobytes()).hexdigest(),
+            "data_sha256": hashlib.sha256(data.tobytes()).hexdigest()}

@@ -1,12 +1,16 @@
-"""Full-size configurations, through properties that need no oracle run: the octree check
-(structure, leaf count = filled voxels, depth) and the batched path against the plain one."""
+"""Full-size configurations.  Configurations 1 and 2 against the oracle run on the same mesh
+and against the reference's recorded digests; configuration 3 (too large for a CPU run)
+through properties: the octree check (structure, leaf count = filled voxels, depth) and the
+batched path against the plain one."""
 import hashlib
 
 import numpy as np
 import pytest
 
+import golden_cases
 import ooc_svo_builder_gb300 as ooc
-from ooc_svo_builder_gb300 import make_params, tri
+import pyoracle
+from ooc_svo_builder_gb300 import make_params, octree, tri
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -45,3 +49,19 @@ def test_configuration_2_full_size_batch_equals_plain(builder):
     info = builder.build_device(d.data_ptr(), t.shape[0], p)
     c = device_check(builder, info, 1024, False)
     assert c["errors"] == [] and c["n_leaves"] == info["n_filled"] == plain.info["n_filled"]
+
+
+@pytest.mark.parametrize("name", sorted(golden_cases.FULLSIZE))
+def test_full_size_matches_oracle_and_reference(builder, name):
+    """Configurations 1 and 2 at full size through ooc_build: equal to the oracle on the same
+    mesh (bit for bit, NaNs aside), and to the reference's recorded digest when this host's
+    generator gives the recorded mesh."""
+    w, want = golden_cases.FULLSIZE[name], golden_cases.fullsize_reference()[name]
+    t = w["make"]()
+    got = builder.build(t, make_params(w["gridsize"], w["limit"], geometry_only=not w["payload"], color=w["color"]))
+    nodes, data, info = pyoracle.build(t, w["gridsize"], w["limit"], color=w["color"])
+    d = octree.diff(got.tree, octree.Octree(w["gridsize"], nodes, data))
+    assert not d, "\n".join(d)
+    assert got.info["n_filled"] == info["n_filled"]
+    if golden_cases.input_sha256(t) == want["input_sha256"]:
+        assert octree.digest(got.tree) == want["digest"]
