@@ -5,7 +5,9 @@ sources by ``make -C oracle ref`` (output oracle/_ref/) on the full-size meshes 
 tests/golden_cases.py FULLSIZE, and stores per configuration: the SHA-256 of the input
 triangles, the octree digest (``octree.digest``: node and data files, NaNs made
 canonical), the header text and the filled-voxel count, in fullsize_reference.json.
-The CPU oracle is run on the same mesh and must give the same digest.  Regenerate with
+It does the same, per mesh, for the first meshes of the seeded streams of
+configurations 4 and 5 (golden_cases STREAMS) into stream_samples_reference.json.
+The CPU oracle is run on the same meshes and must give the same digests.  Regenerate with
 ``python tests/golden/make_fullsize_golden.py`` (needs the reference build).
 """
 from __future__ import annotations
@@ -17,6 +19,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 for p in (ROOT, os.path.dirname(HERE), os.path.join(ROOT, "oracle")):
@@ -27,37 +31,84 @@ import pyoracle  # noqa: E402
 from ooc_svo_builder_gb300 import octree, tri  # noqa: E402
 
 
+def run_reference(t, gridsize, limit, payload, color):
+    """The reference build on one mesh: (octree, header text, filled voxels, partitions, command)."""
+    with tempfile.TemporaryDirectory() as d:
+        base = os.path.join(d, "mesh")
+        tri.write_tri(base, t)
+        exe = pyoracle.ref_binary(not payload)
+        cmd = [exe, "-f", base + ".tri", "-s", str(gridsize), "-l", str(limit)]
+        if payload:
+            cmd += ["-c", color]
+        stdout = subprocess.run(cmd, cwd=d, stdout=subprocess.PIPE, text=True, check=True).stdout
+        filled = int([ln for ln in stdout.splitlines() if ln.startswith("Total amount of voxels")][0].split()[-1])
+        P = int([ln for ln in stdout.splitlines() if ln.startswith("Partitioning data into")][0].split()[3])
+        obase = base + "%d_%d" % (gridsize, P)
+        tree = octree.read_octree(obase)
+        with open(obase + ".octree") as f:
+            header = f.read()
+    command = " ".join([os.path.basename(exe)] + cmd[1:]).replace(base, "mesh")
+    return tree, header, filled, P, command
+
+
+def reference_undefined(gridsize, mortons):
+    """Why the reference's output is undefined for a build with these set voxels, or None.
+
+    finalizeTree (OctreeBuilder.cpp:35-37) pads with empty voxels only while the next
+    Morton code is below N^3 - 1.  When the last set voxel is N^3 - 2, the last voxel is
+    never added, the top groups are never completed and the root is read from an empty
+    buffer; with N = 1 and no set voxel the same read happens."""
+    last = int(mortons.max()) if mortons.size else None
+    if gridsize ** 3 >= 2 and last == gridsize ** 3 - 2:
+        return "the last set voxel is N^3-2: finalizeTree leaves the tree unfinished (OctreeBuilder.cpp:35-37)"
+    if gridsize == 1 and last is None:
+        return "N = 1 with no set voxel: finalizeTree reads the root from an empty buffer (OctreeBuilder.cpp:35-41)"
+    return None
+
+
+def checked_digest(name, t, gridsize, limit, payload, color):
+    """Digest of the reference's output, which the oracle must reproduce; where the reference's
+    output is undefined (see reference_undefined), the reason and the oracle's digest."""
+    tree, header, filled, P, command = run_reference(t, gridsize, limit, payload, color)
+    nodes, data, info = pyoracle.build(t, gridsize, limit, color=color)
+    mine_tree = octree.Octree(gridsize, nodes, data)
+    dig, mine = octree.digest(tree), octree.digest(mine_tree)
+    assert info["n_filled"] == filled, name
+    row = {"command": command, "input_sha256": golden_cases.input_sha256(t), "n_triangles": int(t.shape[0]),
+           "n_partitions": P, "n_filled": filled}
+    if mine != dig:
+        mortons = data["morton"][1:] if payload else octree.leaves(mine_tree)[0]
+        why = reference_undefined(gridsize, np.asarray(mortons, dtype=np.uint64))
+        assert why, "%s: the oracle differs from the reference" % name
+        row.update({"reference_undefined": why, "oracle_digest": mine})
+    else:
+        nan = int(sum(int(np.isnan(tree.data[f]).sum()) for f in ("color", "normal")))
+        row.update({"header": header, "digest": dig, "nan_data_fields": nan})
+    return row
+
+
 def main() -> None:
     out = {}
     for name, w in golden_cases.FULLSIZE.items():
-        t = w["make"]()
-        with tempfile.TemporaryDirectory() as d:
-            base = os.path.join(d, "mesh")
-            tri.write_tri(base, t)
-            exe = pyoracle.ref_binary(not w["payload"])
-            cmd = [exe, "-f", base + ".tri", "-s", str(w["gridsize"]), "-l", str(w["limit"])]
-            if w["payload"]:
-                cmd += ["-c", w["color"]]
-            t0 = time.time()
-            stdout = subprocess.run(cmd, cwd=d, stdout=subprocess.PIPE, text=True, check=True).stdout
-            sec = time.time() - t0
-            filled = int([ln for ln in stdout.splitlines() if ln.startswith("Total amount of voxels")][0].split()[-1])
-            P = int([ln for ln in stdout.splitlines() if ln.startswith("Partitioning data into")][0].split()[3])
-            obase = base + "%d_%d" % (w["gridsize"], P)
-            tree = octree.read_octree(obase)
-            with open(obase + ".octree") as f:
-                header = f.read()
-        nodes, data, info = pyoracle.build(t, w["gridsize"], w["limit"], color=w["color"])
-        dig = octree.digest(tree)
-        assert octree.digest(octree.Octree(w["gridsize"], nodes, data)) == dig, name
-        assert info["n_filled"] == filled, name
-        out[name] = {"command": " ".join([os.path.basename(exe)] + cmd[1:]).replace(base, "mesh"),
-                     "input_sha256": golden_cases.input_sha256(t), "n_triangles": int(t.shape[0]),
-                     "n_partitions": P, "n_filled": filled, "header": header, "digest": dig,
-                     "nan_data_fields": int(sum(int(octree.np.isnan(tree.data[f]).sum()) for f in ("color", "normal")))}
-        print("%s: reference %.1f s, %d nodes, %d data records" % (name, sec, dig["n_nodes"], dig["n_data"]))
+        t0 = time.time()
+        out[name] = checked_digest(name, w["make"](), w["gridsize"], w["limit"], w["payload"], w["color"])
+        print("%s: %.1f s" % (name, time.time() - t0))
     with open(os.path.join(HERE, "fullsize_reference.json"), "w") as f:
         json.dump(out, f, indent=1)
+        f.write("\n")
+    streams = {}
+    for name in golden_cases.STREAMS:
+        t0 = time.time()
+        rows = []
+        for i, (t, N, payload) in enumerate(golden_cases.stream_sample(name)):
+            r = checked_digest("%s[%d]" % (name, i), t, N, golden_cases.STREAM_LIMIT_MB, payload, "model")
+            r["gridsize"], r["payload"] = N, payload
+            r.pop("header", None)
+            rows.append(r)
+        streams[name] = rows
+        print("%s: %d meshes, %.1f s" % (name, len(rows), time.time() - t0))
+    with open(os.path.join(HERE, "stream_samples_reference.json"), "w") as f:
+        json.dump(streams, f, indent=1)
         f.write("\n")
 
 

@@ -44,3 +44,23 @@ def fullsize_reference():
 def input_sha256(tris) -> str:
     import hashlib
     return hashlib.sha256(np.ascontiguousarray(tris).tobytes()).hexdigest()
+
+
+# The first meshes of the seeded mesh streams of configurations 4 (batched builds) and 5
+# (served requests); their reference digests are in golden/stream_samples_reference.json.
+STREAMS = {
+    "batch4096": dict(seed=4, n=64, gridsizes=(64, 128, 256, 512)),
+    "serve": dict(seed=5, n=16, gridsizes=(128, 256, 512, 1024, 2048)),
+}
+STREAM_LIMIT_MB = 2048
+
+
+def stream_sample(name):
+    """[(triangles, gridsize, payload)] of the first meshes of stream `name`."""
+    s = STREAMS[name]
+    return tri.batch_meshes(s["n"], seed=s["seed"], gridsizes=s["gridsizes"])
+
+
+def stream_samples_reference():
+    with open(os.path.join(GOLDEN, "stream_samples_reference.json")) as f:
+        return json.load(f)

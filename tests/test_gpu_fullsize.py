@@ -65,3 +65,21 @@ def test_full_size_matches_oracle_and_reference(builder, name):
     assert got.info["n_filled"] == info["n_filled"]
     if golden_cases.input_sha256(t) == want["input_sha256"]:
         assert octree.digest(got.tree) == want["digest"]
+
+
+@pytest.mark.parametrize("name", sorted(golden_cases.STREAMS))
+def test_stream_samples_in_one_batch_match_reference(builder, name):
+    """The first meshes of the configuration-4 and -5 streams, built in one ooc_build_batch
+    call: each equals the reference's recorded digest (the oracle's where the reference's
+    output is undefined), or the oracle on the same mesh when this host's generator gives
+    other meshes."""
+    sample = golden_cases.stream_sample(name)
+    rows = golden_cases.stream_samples_reference()[name]
+    params = [make_params(N, golden_cases.STREAM_LIMIT_MB, geometry_only=not payload) for _, N, payload in sample]
+    got = builder.build_batch([t for t, _, _ in sample], params)
+    for i, ((t, N, payload), want) in enumerate(zip(sample, rows)):
+        if golden_cases.input_sha256(t) == want["input_sha256"]:
+            assert octree.digest(got[i].tree) == want.get("digest", want.get("oracle_digest")), i
+        else:
+            nodes, data, _ = pyoracle.build(t, N, golden_cases.STREAM_LIMIT_MB)
+            assert not octree.diff(got[i].tree, octree.Octree(N, nodes, data)), i

@@ -122,3 +122,27 @@ def test_oracle_matches_reference_at_full_size(name):
     assert octree.digest(octree.Octree(w["gridsize"], nodes, data)) == want["digest"]
     assert info["n_filled"] == want["n_filled"] and info["n_partitions"] == want["n_partitions"]
     assert octree.header_text(w["gridsize"], nodes.shape[0], data.shape[0]) == want["header"]
+
+
+@pytest.mark.parametrize("name", sorted(golden_cases.STREAMS))
+def test_oracle_matches_reference_on_stream_samples(name):
+    """The first meshes of the configuration-4 and -5 streams: the oracle gives the reference's
+    digest.  Where the reference's output is undefined (its finalizeTree leaves the tree
+    unfinished when the last set voxel is N^3-2), the recorded digest is the oracle's own,
+    and the condition is checked to hold."""
+    checked = 0
+    for (t, N, payload), want in zip(golden_cases.stream_sample(name), golden_cases.stream_samples_reference()[name]):
+        if golden_cases.input_sha256(t) != want["input_sha256"]:
+            continue
+        nodes, data, info = pyoracle.build(t, N, golden_cases.STREAM_LIMIT_MB)
+        tree = octree.Octree(N, nodes, data)
+        assert info["n_filled"] == want["n_filled"] and info["n_partitions"] == want["n_partitions"]
+        if "reference_undefined" in want:
+            mortons = data["morton"][1:] if payload else octree.leaves(tree)[0]
+            assert int(mortons.max()) == N ** 3 - 2
+            assert octree.digest(tree) == want["oracle_digest"]
+        else:
+            assert octree.digest(tree) == want["digest"]
+        checked += 1
+    if not checked:
+        pytest.skip("the mesh generator gives other bytes on this host")
