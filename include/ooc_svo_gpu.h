@@ -302,7 +302,9 @@ int ooc_server_submit(ooc_server* server, const ooc_mesh* mesh, uint64_t* id);
 int ooc_server_poll(ooc_server* server, int32_t timeout_ms, ooc_result* out);
 /* Copy a polled result's files into host memory (either location). */
 int ooc_server_read(ooc_server* server, uint64_t id, void* nodes_host, void* data_host);
-/* Free a polled result's buffers. */
+/* Free a polled result's buffers.  A device-resident result is freed stream-
+ * ordered on a stream of the server's own, so work the caller queued on the
+ * result must have completed before this call. */
 int ooc_server_release(ooc_server* server, uint64_t id);
 /* Drop the requests not yet started, let running batches finish, then stop
  * the engines and free everything (results not yet released included). */
