@@ -31,7 +31,7 @@ import pyoracle  # noqa: E402
 from ooc_svo_builder_gb300 import octree, tri  # noqa: E402
 
 
-def run_reference(t, gridsize, limit, payload, color):
+def run_reference(t, gridsize, limit, payload, color, levels=False):
     """The reference build on one mesh: (octree, header text, filled voxels, partitions, command)."""
     with tempfile.TemporaryDirectory() as d:
         base = os.path.join(d, "mesh")
@@ -40,6 +40,8 @@ def run_reference(t, gridsize, limit, payload, color):
         cmd = [exe, "-f", base + ".tri", "-s", str(gridsize), "-l", str(limit)]
         if payload:
             cmd += ["-c", color]
+        if levels:
+            cmd.append("-levels")
         stdout = subprocess.run(cmd, cwd=d, stdout=subprocess.PIPE, text=True, check=True).stdout
         filled = int([ln for ln in stdout.splitlines() if ln.startswith("Total amount of voxels")][0].split()[-1])
         P = int([ln for ln in stdout.splitlines() if ln.startswith("Partitioning data into")][0].split()[3])
@@ -66,11 +68,11 @@ def reference_undefined(gridsize, mortons):
     return None
 
 
-def checked_digest(name, t, gridsize, limit, payload, color):
+def checked_digest(name, t, gridsize, limit, payload, color, levels=False):
     """Digest of the reference's output, which the oracle must reproduce; where the reference's
     output is undefined (see reference_undefined), the reason and the oracle's digest."""
-    tree, header, filled, P, command = run_reference(t, gridsize, limit, payload, color)
-    nodes, data, info = pyoracle.build(t, gridsize, limit, color=color)
+    tree, header, filled, P, command = run_reference(t, gridsize, limit, payload, color, levels)
+    nodes, data, info = pyoracle.build(t, gridsize, limit, color=color, levels=levels)
     mine_tree = octree.Octree(gridsize, nodes, data)
     dig, mine = octree.digest(tree), octree.digest(mine_tree)
     assert info["n_filled"] == filled, name
@@ -91,7 +93,8 @@ def main() -> None:
     out = {}
     for name, w in golden_cases.FULLSIZE.items():
         t0 = time.time()
-        out[name] = checked_digest(name, w["make"](), w["gridsize"], w["limit"], w["payload"], w["color"])
+        out[name] = checked_digest(name, w["make"](), w["gridsize"], w["limit"], w["payload"], w["color"],
+                                   w.get("levels", False))
         print("%s: %.1f s" % (name, time.time() - t0))
     with open(os.path.join(HERE, "fullsize_reference.json"), "w") as f:
         json.dump(out, f, indent=1)

@@ -33,6 +33,9 @@ FULLSIZE = {
     # svo_builder -s 1024 -l 2048 -c model on a 1024x1024-vertex heightfield (2,093,058 triangles)
     "heightfield1024": dict(gridsize=1024, limit=2048, payload=True, color="model",
                             make=lambda: tri.heightfield_tris(1024, seed=2, payload=True)),
+    # the same with -levels: averaged payloads on every inner node
+    "heightfield1024_levels": dict(gridsize=1024, limit=2048, payload=True, color="model", levels=True,
+                                   make=lambda: tri.heightfield_tris(1024, seed=2, payload=True)),
 }
 
 

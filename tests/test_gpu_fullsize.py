@@ -53,13 +53,15 @@ def test_configuration_2_full_size_batch_equals_plain(builder):
 
 @pytest.mark.parametrize("name", sorted(golden_cases.FULLSIZE))
 def test_full_size_matches_oracle_and_reference(builder, name):
-    """Configurations 1 and 2 at full size through ooc_build: equal to the oracle on the same
+    """Configurations 1 and 2 (also with -levels) at full size through ooc_build: equal to the oracle on the same
     mesh (bit for bit, NaNs aside), and to the reference's recorded digest when this host's
     generator gives the recorded mesh."""
     w, want = golden_cases.FULLSIZE[name], golden_cases.fullsize_reference()[name]
     t = w["make"]()
-    got = builder.build(t, make_params(w["gridsize"], w["limit"], geometry_only=not w["payload"], color=w["color"]))
-    nodes, data, info = pyoracle.build(t, w["gridsize"], w["limit"], color=w["color"])
+    levels = w.get("levels", False)
+    got = builder.build(t, make_params(w["gridsize"], w["limit"], geometry_only=not w["payload"], color=w["color"],
+                                       levels=levels))
+    nodes, data, info = pyoracle.build(t, w["gridsize"], w["limit"], color=w["color"], levels=levels)
     d = octree.diff(got.tree, octree.Octree(w["gridsize"], nodes, data))
     assert not d, "\n".join(d)
     assert got.info["n_filled"] == info["n_filled"]

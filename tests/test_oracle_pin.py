@@ -112,13 +112,14 @@ def test_reference_outside_triangles_depend_on_partitions():
 
 @pytest.mark.parametrize("name", sorted(golden_cases.FULLSIZE))
 def test_oracle_matches_reference_at_full_size(name):
-    """Configurations 1 and 2 at full size: the oracle's octree has the digest the reference
-    build gave on the same mesh (recorded by tests/golden/make_fullsize_golden.py)."""
+    """Configurations 1 and 2 (also with -levels) at full size: the oracle's octree has the
+    digest the reference build gave on the same mesh (recorded by
+    tests/golden/make_fullsize_golden.py)."""
     w, want = golden_cases.FULLSIZE[name], golden_cases.fullsize_reference()[name]
     t = w["make"]()
     if golden_cases.input_sha256(t) != want["input_sha256"]:
         pytest.skip("the mesh generator gives other bytes on this host")
-    nodes, data, info = pyoracle.build(t, w["gridsize"], w["limit"], color=w["color"])
+    nodes, data, info = pyoracle.build(t, w["gridsize"], w["limit"], color=w["color"], levels=w.get("levels", False))
     assert octree.digest(octree.Octree(w["gridsize"], nodes, data)) == want["digest"]
     assert info["n_filled"] == want["n_filled"] and info["n_partitions"] == want["n_partitions"]
     assert octree.header_text(w["gridsize"], nodes.shape[0], data.shape[0]) == want["header"]
