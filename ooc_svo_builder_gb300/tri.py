@@ -64,34 +64,43 @@ def write_tri(base: str, tris: np.ndarray, bbox_min=(0.0, 0.0, 0.0), bbox_max=(1
 
 
 def read_tri_header(path: str) -> TriHeader:
-    """Parse a .tri header like parseTriHeader (tri_tools.h:75-115)."""
+    """Parse a .tri header like parseTriHeader (tri_tools.h:75-115): whitespace-separated
+    words after ``#tri <version>``; ``ntriangles``, ``geo_only`` and ``bbox`` take their
+    values, ``END`` ends the header, and any other word skips the rest of its line."""
     with open(path) as f:
-        toks = f.read().split()
-    if not toks or toks[0] != "#tri":
-        raise ValueError("first token is not #tri")
-    version = int(toks[1])
-    i = 2
-    n = 0
-    geo = 0
-    bmin = (0.0, 0.0, 0.0)
-    bmax = (0.0, 0.0, 0.0)
-    done = False
-    while i < len(toks):
-        t = toks[i]
-        i += 1
+        text = f.read()
+    pos = 0
+
+    def word():
+        nonlocal pos
+        while pos < len(text) and text[pos].isspace():
+            pos += 1
+        start = pos
+        while pos < len(text) and not text[pos].isspace():
+            pos += 1
+        return text[start:pos] if pos > start else None
+
+    if word() != "#tri":
+        raise ValueError("first word is not #tri")
+    version = int(word())
+    n, geo = 0, 0
+    bmin = bmax = (0.0, 0.0, 0.0)
+    while True:
+        t = word()
+        if t is None:
+            raise ValueError("error reading header")
         if t == "END":
-            done = True
             break
         if t == "ntriangles":
-            n = int(toks[i]); i += 1
+            n = int(word())
         elif t == "geo_only":
-            geo = int(toks[i]); i += 1
+            geo = int(word())
         elif t == "bbox":
-            vals = [float(np.float32(x)) for x in toks[i:i + 6]]
-            i += 6
+            vals = [float(np.float32(word())) for _ in range(6)]
             bmin, bmax = tuple(vals[:3]), tuple(vals[3:])
-    if not done:
-        raise ValueError("error reading header")
+        else:
+            nl = text.find("\n", pos)
+            pos = len(text) if nl < 0 else nl + 1
     return TriHeader(version, n, geo, bmin, bmax, path[: path.rfind(".")])
 
 
