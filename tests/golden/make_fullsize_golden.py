@@ -53,21 +53,6 @@ def run_reference(t, gridsize, limit, payload, color, levels=False):
     return tree, header, filled, P, command
 
 
-def reference_undefined(gridsize, mortons):
-    """Why the reference's output is undefined for a build with these set voxels, or None.
-
-    finalizeTree (OctreeBuilder.cpp:35-37) pads with empty voxels only while the next
-    Morton code is below N^3 - 1.  When the last set voxel is N^3 - 2, the last voxel is
-    never added, the top groups are never completed and the root is read from an empty
-    buffer; with N = 1 and no set voxel the same read happens."""
-    last = int(mortons.max()) if mortons.size else None
-    if gridsize ** 3 >= 2 and last == gridsize ** 3 - 2:
-        return "the last set voxel is N^3-2: finalizeTree leaves the tree unfinished (OctreeBuilder.cpp:35-37)"
-    if gridsize == 1 and last is None:
-        return "N = 1 with no set voxel: finalizeTree reads the root from an empty buffer (OctreeBuilder.cpp:35-41)"
-    return None
-
-
 def checked_digest(name, t, gridsize, limit, payload, color, levels=False):
     """Digest of the reference's output, which the oracle must reproduce; where the reference's
     output is undefined (see reference_undefined), the reason and the oracle's digest."""
@@ -79,8 +64,7 @@ def checked_digest(name, t, gridsize, limit, payload, color, levels=False):
     row = {"command": command, "input_sha256": golden_cases.input_sha256(t), "n_triangles": int(t.shape[0]),
            "n_partitions": P, "n_filled": filled}
     if mine != dig:
-        mortons = data["morton"][1:] if payload else octree.leaves(mine_tree)[0]
-        why = reference_undefined(gridsize, np.asarray(mortons, dtype=np.uint64))
+        why = golden_cases.reference_undefined(gridsize, golden_cases.set_voxels(mine_tree, payload))
         assert why, "%s: the oracle differs from the reference" % name
         row.update({"reference_undefined": why, "oracle_digest": mine})
     else:
