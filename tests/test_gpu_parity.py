@@ -7,7 +7,6 @@ x86-64, AArch64 and the GPU even for the reference itself).
 import numpy as np
 import pytest
 
-import golden_cases
 import pyoracle
 from ooc_svo_builder_gb300 import make_params, octree, tri
 
@@ -233,15 +232,3 @@ def test_upload_in_pieces(builder, payload, N, T):
     assert t.nbytes > 32 << 20
     assert_same(*run_both(builder, t, N))
 
-
-@pytest.mark.parametrize("i", range(golden_cases.N_SEEDED))
-def test_seeded_cases_match_oracle(builder, i):
-    """The seeded mix the oracle is pinned on against the reference build: inside, outside
-    and lattice-aligned inputs, sub-voxel triangles, soups and spheres, gridsize 1 to 256,
-    1 to 64 partitions, every colour mode, with and without -levels."""
-    t, N, limit, payload, color, levels, kind = golden_cases.seeded_case(i)
-    got = builder.build(t, make_params(N, limit, geometry_only=not payload, color=color, levels=levels))
-    nodes, data, info = pyoracle.build(t, N, limit, color=color, levels=levels)
-    d = octree.diff(got.tree, octree.Octree(N, nodes, data))
-    assert not d, kind + "\n" + "\n".join(d)
-    assert got.info["n_filled"] == info["n_filled"]
