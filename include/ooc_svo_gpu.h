@@ -341,7 +341,11 @@ int ooc_check_octree_device(const void* nodes, uint64_t n_nodes, const void* dat
 
 /* File front end used by the svo_builder CLIs: reads <base>.tri/.tridata and
  * writes <base><gridsize>_<npartitions>.octree/.octreenodes/.octreedata
- * (main.cpp:296-398).  `out_base` receives the output base name (may be NULL). */
+ * (main.cpp:296-398).  `out_base` receives the output base name (may be NULL).
+ * The header's geo_only and bbox override those fields of `params`.  A header
+ * that does not parse, a .tridata shorter than its triangle count, or an
+ * output file that cannot be written returns OOC_ERR_IO, and ooc_last_error
+ * names the file. */
 int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_build_params* params, char* out_base,
                     uint64_t out_base_len, ooc_build_info* info);
 
