@@ -214,6 +214,25 @@ int ooc_phase_times(const ooc_ctx* ctx, float* ms, int32_t n);
 /* Launch count of this library's kernels in the last build of `ctx`. */
 uint64_t ooc_kernel_launches(const ooc_ctx* ctx);
 
+/* Per-partition counts of the last build of `ctx` (its first mesh), for the
+ * progress lines of the reference's driver: for partitions first ..
+ * first + n - 1, the triangles binned to it (TripInfo::part_tricounts,
+ * partitioner.cpp:80-98 and :101-149; with one partition every triangle) and
+ * the voxels it filled ("found N new voxels", main.cpp:346-348).  Either
+ * array may be NULL; entries past the last partition are left alone.
+ * Returns the build's partition count (0 before the first build, or after a
+ * failed one). */
+uint64_t ooc_partition_counts(const ooc_ctx* ctx, uint64_t first, uint64_t n, uint64_t* triangles,
+                              uint64_t* filled);
+
+/* Host wall-clock milliseconds of the file work of the last ooc_build_files
+ * call of `ctx`: [0] reading the .tri header and the .tridata into device
+ * memory, [1] writing the octree files after the build (waiting for the
+ * writer threads, and the header).  They stand in for the reference's
+ * IO IN / IO OUT timers (main.cpp:219-241).  `n` entries are written (at
+ * most 2). */
+int ooc_file_times(const ooc_ctx* ctx, float* ms, int32_t n);
+
 /* Per-kernel CUDA-event timing of later builds on `ctx`: `kernel` names one
  * kernel (e.g. "vox_small_occupancy"), "*" selects all, NULL or "" turns it
  * off.  Each timed launch is bracketed by two events on the build stream. */
@@ -256,9 +275,13 @@ int ooc_voxelize_occupancy_noalloc(const ooc_build_params* params, const float* 
                                    uint32_t* occupancy_device, uint64_t occupancy_words, void* stream);
 
 /* ---- Serving loop (no counterpart in the reference) ----
- * Requests (meshes) are admitted by their computed HBM footprint -- triangles,
- * the occupancy pyramids of their stripes, and per-node arrays plus output
- * for an estimate of their nodes -- against `memory_budget`, and run in
+ * Requests (meshes) are admitted by their computed HBM footprint against
+ * `memory_budget`: their triangles, the occupancy pyramids of their stripes,
+ * and per-node arrays plus output records for an upper bound on their nodes
+ * (a tree whose L leaves are at depth D has at most min(8^l, L) nodes at level
+ * l, and L is at most the summed grid boxes of the triangles, clamped to the
+ * grid).  A request whose footprint exceeds the whole budget is refused at
+ * submission (OOC_ERR_LIMIT).  Requests run in
  * continuously formed batches: each of `engines` contexts (own streams and
  * scratch) takes, whenever it is free, every queued request that fits (at
  * most max_batch) and builds them in one batch call (ooc_build_batch, or
@@ -278,6 +301,13 @@ typedef struct {
   uint32_t max_batch;      /* requests per batch, >= 1 (1: every request alone)     */
   int32_t result_location; /* OOC_RESULT_HOST or OOC_RESULT_DEVICE                  */
   uint64_t memory_budget;  /* bytes of HBM the requests in flight may hold          */
+  /* Fault injection for tests, 0 in normal use: the first batch of two or more
+   * requests fails when it reaches its mesh number `fail_batch_at_mesh`
+   * (1-based): the result sink refuses that mesh's bytes (host results) or its
+   * allocation fails as if out of memory (device results).  The batch's
+   * requests not yet complete then run again alone, as after any failed batch. */
+  uint32_t fail_batch_at_mesh;
+  uint32_t reserved;
 } ooc_server_config;
 
 typedef struct {
@@ -296,7 +326,9 @@ typedef struct {
 } ooc_result;
 
 int ooc_server_create(const ooc_server_config* cfg, ooc_server** out);
-/* Queue one mesh; its triangles (host memory) must stay valid until its result is polled. */
+/* Queue one mesh; its triangles (host memory) must stay valid until its result
+ * is polled.  OOC_ERR_INVALID for parameters ooc_build would refuse,
+ * OOC_ERR_LIMIT when the request's footprint exceeds memory_budget. */
 int ooc_server_submit(ooc_server* server, const ooc_mesh* mesh, uint64_t* id);
 /* Next completed request (OOC_OK), or OOC_ERR_TIMEOUT after `timeout_ms`. */
 int ooc_server_poll(ooc_server* server, int32_t timeout_ms, ooc_result* out);

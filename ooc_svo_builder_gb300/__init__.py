@@ -35,7 +35,8 @@ EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_
            "ooc_voxelize_occupancy_noalloc", "ooc_build_batch", "ooc_server_create", "ooc_server_submit",
            "ooc_server_poll", "ooc_server_release", "ooc_server_destroy", "ooc_build_batch_device",
            "ooc_arena_alloc", "ooc_set_batch_budget", "ooc_batch_budget", "ooc_server_read", "ooc_get_tuning",
-           "ooc_set_tuning", "ooc_autotune", "ooc_check_octree_device", "ooc_build_from_device")
+           "ooc_set_tuning", "ooc_autotune", "ooc_check_octree_device", "ooc_build_from_device",
+           "ooc_partition_counts", "ooc_file_times")
 CHECK_BITS = {1: "child group order", 2: "reference count", 4: "depth", 8: "data index", 16: "payload Morton code"}
 
 
@@ -65,7 +66,8 @@ RESULT_HOST, RESULT_DEVICE = 0, 1
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("engines", ctypes.c_int32), ("max_batch", ctypes.c_uint32),
-                ("result_location", ctypes.c_int32), ("memory_budget", ctypes.c_uint64)]
+                ("result_location", ctypes.c_int32), ("memory_budget", ctypes.c_uint64),
+                ("fail_batch_at_mesh", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class Result(ctypes.Structure):
@@ -152,6 +154,11 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_phase_times.restype = ctypes.c_int
     lib.ooc_kernel_launches.argtypes = [ctypes.c_void_p]
     lib.ooc_kernel_launches.restype = ctypes.c_uint64
+    lib.ooc_partition_counts.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, P(ctypes.c_uint64),
+                                         P(ctypes.c_uint64)]
+    lib.ooc_partition_counts.restype = ctypes.c_uint64
+    lib.ooc_file_times.argtypes = [ctypes.c_void_p, P(ctypes.c_float), ctypes.c_int32]
+    lib.ooc_file_times.restype = ctypes.c_int
     lib.ooc_build_files.argtypes = [ctypes.c_void_p, ctypes.c_char_p, P(BuildParams), ctypes.c_char_p,
                                     ctypes.c_uint64, P(BuildInfo)]
     lib.ooc_build_files.restype = ctypes.c_int
@@ -304,6 +311,14 @@ class Builder:
 
     def kernel_launches(self) -> int:
         return int(self.lib.ooc_kernel_launches(self.h))
+
+    def partition_counts(self):
+        """(triangles per partition, filled voxels per partition) of the last build's first mesh."""
+        n = int(self.lib.ooc_partition_counts(self.h, 0, 0, None, None))
+        tris = (ctypes.c_uint64 * max(n, 1))()
+        filled = (ctypes.c_uint64 * max(n, 1))()
+        self.lib.ooc_partition_counts(self.h, 0, n, tris, filled)
+        return [int(v) for v in tris[:n]], [int(v) for v in filled[:n]]
 
     def set_kernel_timing(self, kernel):
         """Time `kernel` ("*" = all, None = off) with CUDA events in later builds."""
@@ -492,10 +507,12 @@ class Server:
     """The serving loop: submit meshes, poll completed octrees (see ooc_server_* in the C ABI)."""
 
     def __init__(self, device: int = 0, engines: int = 2, max_batch: int = 256, memory_budget: int = 120 << 30,
-                 resident: bool = False):
-        """`resident`: results stay in device memory (read with poll(copy=True) or ooc_server_read)."""
+                 resident: bool = False, fail_batch_at_mesh: int = 0):
+        """`resident`: results stay in device memory (read with poll(copy=True) or ooc_server_read).
+        `fail_batch_at_mesh`: fault injection for tests (ooc_server_config)."""
         self.lib = load_library()
-        cfg = ServerConfig(device, engines, max_batch, RESULT_DEVICE if resident else RESULT_HOST, memory_budget)
+        cfg = ServerConfig(device, engines, max_batch, RESULT_DEVICE if resident else RESULT_HOST, memory_budget,
+                           fail_batch_at_mesh, 0)
         h = ctypes.c_void_p()
         rc = self.lib.ooc_server_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc != OOC_OK:

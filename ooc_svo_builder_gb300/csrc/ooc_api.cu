@@ -18,6 +18,7 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -129,6 +130,7 @@ struct ooc_ctx {
   bool timing = false;
   float phase_ms[kPhases] = {0, 0, 0, 0, 0, 0};
   unsigned long long launches = 0;
+  ooc::LaunchState lstate;  // this context's launch count and timing hooks, installed per API call
   DevBuf d_tris, d_hist, d_axis, d_bits, d_scan, d_scanpart, d_keys, d_size, d_dsize, d_start, d_dstart,
       d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo, d_itemmask,
       d_firstchild, d_itembox, d_leaf, d_touch, d_local, d_taskmap;
@@ -162,6 +164,9 @@ struct ooc_ctx {
   std::vector<std::string> knames;
   std::vector<float> kms;
   std::vector<uint64_t> kcount;
+  // the last build's first mesh: triangles binned to each partition, voxels it filled
+  std::vector<uint64_t> part_tris, part_filled;
+  float file_ms[2] = {0, 0};  // ooc_build_files: input read and upload, output written (host ms)
 };
 
 namespace {
@@ -228,13 +233,21 @@ void ring_start(ooc_ctx* c, D2HRing& r, const void* src, uint64_t len) {
   while (r.issued < r.n_chunks && r.issued < (uint64_t)kRingK) ring_issue(c, r);
 }
 
-// Hand bytes [a, b) to `out` in order; calls over one sub-batch cover its bytes in increasing order.
+// Hand bytes [a, b) to `out` in order; calls over one sub-batch cover its bytes in
+// increasing order.  With `block` false it stops at the first chunk whose copy has
+// not landed yet.  Returns how far it got (b when done).
 template <typename F>
-void ring_take(ooc_ctx* c, D2HRing& r, uint64_t a, uint64_t b, F&& out) {
+uint64_t ring_take(ooc_ctx* c, D2HRing& r, uint64_t a, uint64_t b, bool block, F&& out) {
   while (a < b) {
     const uint64_t j = a / kRingChunk;
     if (j >= r.issued || j < r.released) fail(OOC_ERR_DEVICE, "internal copy-back order");
-    ck(cudaEventSynchronize(r.ev[j % kRingK]), "D2H");
+    if (block) {
+      ck(cudaEventSynchronize(r.ev[j % kRingK]), "D2H");
+    } else {
+      const cudaError_t e = cudaEventQuery(r.ev[j % kRingK]);
+      if (e == cudaErrorNotReady) return a;
+      ck(e, "D2H");
+    }
     const uint64_t end = std::min(b, (j + 1) * kRingChunk);
     out(static_cast<const char*>(r.buf.p) + (j % kRingK) * kRingChunk + (a - j * kRingChunk), end - a);
     a = end;
@@ -243,6 +256,7 @@ void ring_take(ooc_ctx* c, D2HRing& r, uint64_t a, uint64_t b, F&& out) {
       if (r.issued < r.n_chunks) ring_issue(c, r);
     }
   }
+  return a;
 }
 
 // Run `launches` on `st`, directly or captured into a CUDA graph and replayed.
@@ -252,7 +266,7 @@ void ring_take(ooc_ctx* c, D2HRing& r, uint64_t a, uint64_t b, F&& out) {
 // synchronises; phase and kernel timing launch directly.
 template <typename F>
 void run_launches(ooc_ctx* c, cudaStream_t st, int which, F&& launches, bool direct = false) {
-  if (direct || !c->tuning.graphs || c->timing || g_hooks.begin) {
+  if (direct || !c->tuning.graphs || c->timing || c->lstate.hooks.begin) {
     launches();
     return;
   }
@@ -506,6 +520,7 @@ struct MeshWork {
   TopBuilder layout;         // the same grouping run ahead on placeholders: file positions only
   uint64_t layout_next = 0;
   uint64_t filled = 0;
+  std::vector<uint64_t> part_filled;  // voxels filled in each partition
   uint64_t n_items = 0;
   int64_t last_stripe = -1;  // last stripe with items (-1: none)
   cudaEvent_t uploaded = nullptr;  // the triangles are on the device once this has completed (null: already)
@@ -520,14 +535,15 @@ struct MeshWork {
   uint64_t total_nodes = 0, total_data = 0;
   uint64_t carried_nodes = 0, carried_data = 0;  // records parked in the carry buffers
   MeshWork(const Plan& p, Emitter* o)
-      : pl(p), out(o), top(p.Ls, p.levels != 0, o), layout(p.Ls, p.levels != 0, nullptr) {
+      : pl(p), out(o), top(p.Ls, p.levels != 0, o), layout(p.Ls, p.levels != 0, nullptr), part_filled(p.P, 0) {
     dry.dry = true;
   }
   MeshWork(const MeshWork&) = delete;
   MeshWork(MeshWork&& o) noexcept
       : prm(o.prm), pl(o.pl), d_tris(o.d_tris), n_tris(o.n_tris), part_off(std::move(o.part_off)), items(o.items),
         out(o.out), top(o.top), next_stripe(o.next_stripe), dry(o.dry), layout(o.layout),
-        layout_next(o.layout_next), filled(o.filled), n_items(o.n_items), last_stripe(o.last_stripe),
+        layout_next(o.layout_next), filled(o.filled), part_filled(std::move(o.part_filled)), n_items(o.n_items),
+        last_stripe(o.last_stripe),
         uploaded(o.uploaded), pieces(std::move(o.pieces)),
         index(o.index), dst_nodes(o.dst_nodes), dst_data(o.dst_data), dst_ready(o.dst_ready),
         total_nodes(o.total_nodes), total_data(o.total_data), carried_nodes(o.carried_nodes),
@@ -677,10 +693,31 @@ struct Pending {
   std::vector<StripeRef> sb;
   std::vector<Placed> pl;
   std::vector<int> depth;
+  // how far the hand-over has got (finish_sub_batch resumes from here)
+  bool checked = false;  // the sub-batch's kernels are done and its layout flag is clear
+  uint32_t at = 0;       // stripe being handed over
+  int stage = 0;         // 0 not started, 1 node bytes, 2 data bytes
+  uint64_t cur = 0;      // next byte of the current range
 };
 
+// Waits for the level counts on `st`.  Meanwhile `idle` (if set) hands the previous
+// sub-batch's landed copy-back chunks to the sink, so the copy stream keeps moving;
+// it returns false once there is nothing left for it to do.
+void wait_level_counts(cudaStream_t st, const std::function<bool()>& idle) {
+  if (idle) {
+    for (;;) {
+      const cudaError_t e = cudaStreamQuery(st);
+      if (e == cudaSuccess) return;
+      if (e != cudaErrorNotReady) ck(e, "level counts");
+      if (!idle()) break;
+      std::this_thread::yield();
+    }
+  }
+  ck(cudaStreamSynchronize(st), "level counts");
+}
+
 void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, const std::vector<StripeRef>& sb,
-                   const OutSpec& os, Pending& out_pending, int slot) {
+                   const OutSpec& os, Pending& out_pending, int slot, const std::function<bool()>& idle = nullptr) {
   const uint32_t n = (uint32_t)sb.size();
   // a lone stripe of a mesh uploaded in pieces voxelizes each piece on arrival
   const std::vector<std::pair<uint64_t, cudaEvent_t>>* pieces =
@@ -844,7 +881,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       ck(cudaMemcpyAsync(lvl, d_root, ((uint64_t)n * 16 + 10) * 4, cudaMemcpyDeviceToHost, st), "levels");
     }
   }, pieces != nullptr);  // waits on the upload stream are not captured
-  ck(cudaStreamSynchronize(st), "level counts");
+  wait_level_counts(st, idle);
   uint64_t tasks_seen;
   std::memcpy(&tasks_seen, lvl + (uint64_t)n * 16 + 8, 8);
   c->max_tasks = std::max(c->max_tasks, tasks_seen);
@@ -1104,40 +1141,72 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   }
   out_pending.active = true;
   out_pending.slot = slot;
+  out_pending.checked = false;
+  out_pending.at = 0;
+  out_pending.stage = 0;
+  out_pending.cur = 0;
   out_pending.sb = sb;
   out_pending.pl = pl;
   out_pending.depth.resize(n);
   for (uint32_t s = 0; s < n; s++) out_pending.depth[s] = pyr[s].depth;
 }
 
-// Wait for a sub-batch's records and hand its stripes to their meshes, in file order.
-void finish_sub_batch(ooc_ctx* c, std::vector<MeshWork>& meshes, Pending& pd, const OutSpec& os) {
-  if (!pd.active) return;
-  pd.active = false;
+// Hand a sub-batch's stripes to their meshes, in file order.  With `block` it
+// waits for every record; without, it stops (returning false) where the next
+// record has not reached the host yet, and a later call resumes there.  Returns
+// true once the whole sub-batch is handed over.
+bool finish_sub_batch(ooc_ctx* c, std::vector<MeshWork>& meshes, Pending& pd, const OutSpec& os, bool block = true) {
+  if (!pd.active) return true;
   const int slot = pd.slot;
   const uint32_t n = (uint32_t)pd.sb.size();
-  ck(cudaEventSynchronize(c->ev_compute[slot]), "sub-batch");
-  ck(cudaGetLastError(), "sub-batch kernels");
-  const uint32_t* hr = static_cast<const uint32_t*>(c->h_root[slot].p);
-  if (hr[(uint64_t)n * 16] != 0)
-    fail(OOC_ERR_DEVICE, "internal layout check failed (flag " + std::to_string(hr[(uint64_t)n * 16]) + ")");
-  for (uint32_t s = 0; s < n; s++) {
-    MeshWork& m = meshes[pd.sb[s].mesh];
-    for (; m.next_stripe < pd.sb[s].stripe; m.next_stripe++) m.top.push(m.top.top, TNode());
-    m.next_stripe++;
-    const Placed& q = pd.pl[s];
-    if (q.node_base != m.top.node_pos || q.data_base != m.top.data_pos)
-      fail(OOC_ERR_DEVICE, "internal placement mismatch");
-    if (q.empty) {
-      m.top.push(m.top.top, TNode());
-      continue;
+  if (!pd.checked) {
+    if (block) {
+      ck(cudaEventSynchronize(c->ev_compute[slot]), "sub-batch");
+    } else {
+      const cudaError_t e = cudaEventQuery(c->ev_compute[slot]);
+      if (e == cudaErrorNotReady) return false;
+      ck(e, "sub-batch");
     }
-    m.filled += q.n_leaf;
+    ck(cudaGetLastError(), "sub-batch kernels");
+    const uint32_t* hr = static_cast<const uint32_t*>(c->h_root[slot].p);
+    if (hr[(uint64_t)n * 16] != 0)
+      fail(OOC_ERR_DEVICE, "internal layout check failed (flag " + std::to_string(hr[(uint64_t)n * 16]) + ")");
+    pd.checked = true;
+    pd.at = 0;
+    pd.stage = 0;
+  }
+  const uint32_t* hr = static_cast<const uint32_t*>(c->h_root[slot].p);
+  for (; pd.at < n; pd.at++, pd.stage = 0) {
+    const uint32_t s = pd.at;
+    MeshWork& m = meshes[pd.sb[s].mesh];
+    const Placed& q = pd.pl[s];
+    if (pd.stage == 0) {
+      for (; m.next_stripe < pd.sb[s].stripe; m.next_stripe++) m.top.push(m.top.top, TNode());
+      m.next_stripe++;
+      if (q.node_base != m.top.node_pos || q.data_base != m.top.data_pos)
+        fail(OOC_ERR_DEVICE, "internal placement mismatch");
+      if (q.empty) {
+        m.top.push(m.top.top, TNode());
+        continue;
+      }
+      m.filled += q.n_leaf;
+      m.part_filled[pd.sb[s].part] += q.n_leaf;
+      pd.stage = 1;
+      pd.cur = q.out_node_off * 24;
+    }
     if (os.mode == OUT_HOST) {
-      ring_take(c, c->ring[slot][OOC_STREAM_NODES], q.out_node_off * 24, (q.out_node_off + q.node_span) * 24,
-                [&](const void* p, uint64_t n) { m.out->span(OOC_STREAM_NODES, p, n); });
-      ring_take(c, c->ring[slot][OOC_STREAM_DATA], q.out_data_off * 32, (q.out_data_off + q.data_span) * 32,
-                [&](const void* p, uint64_t n) { m.out->span(OOC_STREAM_DATA, p, n); });
+      if (pd.stage == 1) {
+        const uint64_t end = (q.out_node_off + q.node_span) * 24;
+        pd.cur = ring_take(c, c->ring[slot][OOC_STREAM_NODES], pd.cur, end, block,
+                           [&](const void* p, uint64_t nb) { m.out->span(OOC_STREAM_NODES, p, nb); });
+        if (pd.cur < end) return false;
+        pd.stage = 2;
+        pd.cur = q.out_data_off * 32;
+      }
+      const uint64_t end = (q.out_data_off + q.data_span) * 32;
+      pd.cur = ring_take(c, c->ring[slot][OOC_STREAM_DATA], pd.cur, end, block,
+                         [&](const void* p, uint64_t nb) { m.out->span(OOC_STREAM_DATA, p, nb); });
+      if (pd.cur < end) return false;
     }
     m.top.node_pos += q.node_span;
     m.top.data_pos += q.data_span;
@@ -1159,6 +1228,8 @@ void finish_sub_batch(ooc_ctx* c, std::vector<MeshWork>& meshes, Pending& pd, co
     }
     m.top.push(m.top.top, r);
   }
+  pd.active = false;
+  return true;
 }
 
 // Binning of a P > 1 mesh into per-partition item lists (K1).
@@ -1263,7 +1334,13 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, co
     const MeshWork& last = meshes[sb.back().mesh];
     if (last.uploaded && !(sb.size() == 1 && !last.pieces.empty()))
       ck(cudaStreamWaitEvent(st, last.uploaded, 0), "wait upload");
-    run_sub_batch(c, st, meshes, sb, os, pend[k & 1], k & 1);
+    // host output: while this sub-batch's level counts are pending, the previous
+    // one's landed records go to the sink, so its copy back keeps the link busy
+    Pending& prev = pend[(k + 1) & 1];
+    std::function<bool()> pump;
+    if (os.mode == OUT_HOST && prev.active)
+      pump = [&]() { return !finish_sub_batch(c, meshes, prev, os, false); };
+    run_sub_batch(c, st, meshes, sb, os, pend[k & 1], k & 1, pump);
     if (os.mode == OUT_CTX) finish_sub_batch(c, meshes, pend[k & 1], os);
     else finish_sub_batch(c, meshes, pend[(k + 1) & 1], os);
     complete();
@@ -1291,6 +1368,12 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, co
   finish_sub_batch(c, meshes, pend[(k + 1) & 1], os);
   complete();
   if (n_done != meshes.size()) fail(OOC_ERR_DEVICE, "internal: mesh left unfinished");
+  // per-partition counts of the first mesh (the progress lines of the drop-in CLIs)
+  const MeshWork& m0 = meshes[0];
+  c->part_tris.assign(m0.pl.P, 0);
+  for (uint64_t p = 0; p < m0.pl.P; p++)
+    c->part_tris[p] = m0.pl.P > 1 ? (uint64_t)m0.part_off[p + 1] - m0.part_off[p] : m0.n_tris;
+  c->part_filled = m0.part_filled;
 }
 
 void fill_info(const MeshWork& m, ooc_build_info* info) {
@@ -1364,6 +1447,8 @@ void kernel_end(void* user, const char* name, cudaStream_t st) {
 
 void begin_build(ooc_ctx* c) {
   ck(cudaSetDevice(c->device), "cudaSetDevice");
+  c->part_tris.clear();
+  c->part_filled.clear();
   // a build that failed part-way may have left copies queued into the staging buffers
   ck(cudaStreamSynchronize(c->copy_stream), "cudaStreamSynchronize");
   ck(cudaStreamSynchronize(c->h2d_stream), "cudaStreamSynchronize");
@@ -1372,26 +1457,28 @@ void begin_build(ooc_ctx* c) {
   c->kmarks.clear();
   c->ev_used = 0;
   c->res_valid = false;
-  g_launches = 0;
+  c->lstate.launches = 0;
   if (c->kfilter.empty()) {
-    g_hooks = KernelHooks();
+    c->lstate.hooks = KernelHooks();
   } else {
-    g_hooks.user = c;
-    g_hooks.begin = kernel_begin;
-    g_hooks.end = kernel_end;
+    c->lstate.hooks.user = c;
+    c->lstate.hooks.begin = kernel_begin;
+    c->lstate.hooks.end = kernel_end;
   }
 }
 
+// Runs one API call on `c`: its launches report to c's own launch state.
 template <typename F>
 int guarded(ooc_ctx* c, F&& f) {
   if (!c) return OOC_ERR_INVALID;
+  LaunchScope scope(&c->lstate);
   try {
     f();
-    c->launches = g_launches;
+    c->launches = c->lstate.launches;
     return OOC_OK;
   } catch (const OocError& e) {
     c->err = e.msg;
-    c->launches = g_launches;
+    c->launches = c->lstate.launches;
     return e.code;
   } catch (const std::bad_alloc&) {
     c->err = "host allocation failed";
@@ -1407,6 +1494,11 @@ int guarded(ooc_ctx* c, F&& f) {
 namespace ooc {
 void set_ctx_error(ooc_ctx* c, const std::string& msg) {
   if (c) c->err = msg;
+}
+void set_ctx_file_times(ooc_ctx* c, float read_ms, float write_ms) {
+  if (!c) return;
+  c->file_ms[0] = read_ms;
+  c->file_ms[1] = write_ms;
 }
 }  // namespace ooc
 
@@ -1908,6 +2000,22 @@ int ooc_phase_times(const ooc_ctx* c, float* ms, int32_t n) {
 }
 
 uint64_t ooc_kernel_launches(const ooc_ctx* c) { return c ? c->launches : 0; }
+
+uint64_t ooc_partition_counts(const ooc_ctx* c, uint64_t first, uint64_t n, uint64_t* triangles, uint64_t* filled) {
+  if (!c) return 0;
+  const uint64_t P = c->part_tris.size();
+  for (uint64_t i = 0; i < n && first + i < P; i++) {
+    if (triangles) triangles[i] = c->part_tris[first + i];
+    if (filled) filled[i] = c->part_filled[first + i];
+  }
+  return P;
+}
+
+int ooc_file_times(const ooc_ctx* c, float* ms, int32_t n) {
+  if (!c || !ms || n < 0) return OOC_ERR_INVALID;
+  for (int i = 0; i < n && i < 2; i++) ms[i] = c->file_ms[i];
+  return OOC_OK;
+}
 
 int ooc_set_kernel_timing(ooc_ctx* c, const char* kernel) {
   if (!c) return OOC_ERR_INVALID;

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
@@ -192,6 +193,12 @@ int writer_sink(void* user, int32_t kind, const void* bytes, uint64_t n) {
 extern "C" int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_build_params* params_in, char* out_base,
                                uint64_t out_base_len, ooc_build_info* info) {
   if (!ctx || !tri_path || !params_in) return OOC_ERR_INVALID;
+  using clock = std::chrono::steady_clock;
+  auto ms_since = [](clock::time_point t) {
+    return (float)std::chrono::duration<double, std::milli>(clock::now() - t).count();
+  };
+  const clock::time_point t_read = clock::now();
+  ooc::set_ctx_file_times(ctx, 0.0f, 0.0f);
   TriHeader h;
   std::string err;
   if (!parse_tri_header(tri_path, h, err)) {
@@ -216,12 +223,14 @@ extern "C" int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_bui
     ooc::set_ctx_error(ctx, err);
     return OOC_ERR_IO;
   }
+  const float read_ms = ms_since(t_read);
   const uint64_t P = ooc_estimate_partitions(prm.gridsize, prm.memory_limit_mb);
   // <base><gridsize>_<npartitions> (partitioner.cpp:90, 141; main.cpp:325)
   const std::string base = h.base + std::to_string(prm.gridsize) + "_" + std::to_string(P);
   FILE* fn = std::fopen((base + ".octreenodes").c_str(), "wb");
   FILE* fd = std::fopen((base + ".octreedata").c_str(), "wb");
   int rc = OOC_OK;
+  clock::time_point t_write = clock::now();
   ooc_build_info local;
   std::memset(&local, 0, sizeof(local));
   if (!fn || !fd) {
@@ -231,6 +240,7 @@ extern "C" int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_bui
     FileWriter wn(fn), wd(fd);
     FileWriter* w[2] = {&wn, &wd};
     rc = ooc_build_from_device(ctx, &prm, static_cast<const float*>(tris), h.n_triangles, writer_sink, w, &local);
+    t_write = clock::now();
     const bool ok_n = wn.finish(), ok_d = wd.finish();
     if (rc == OOC_OK && !(ok_n && ok_d)) {
       rc = OOC_ERR_IO;
@@ -253,6 +263,7 @@ extern "C" int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_bui
     ooc::set_ctx_error(ctx, "cannot write " + base + ".octree");
     return OOC_ERR_IO;
   }
+  ooc::set_ctx_file_times(ctx, read_ms, ms_since(t_write));
   if (out_base && out_base_len) {
     std::strncpy(out_base, base.c_str(), (size_t)out_base_len - 1);
     out_base[out_base_len - 1] = 0;

@@ -121,9 +121,10 @@ constexpr uint32_t kChunk = 256;
 
 // The message ooc_last_error returns for `c` (for failures found outside ooc_api.cu).
 void set_ctx_error(ooc_ctx* c, const std::string& msg);
+// ooc_file_times' values for `c` (set by ooc_build_files).
+void set_ctx_file_times(ooc_ctx* c, float read_ms, float write_ms);
 
 // ---- launches (ooc_kernels.cu); all asynchronous on `st` ----
-extern unsigned long long g_launches;  // kernel launches since the last reset (host counter)
 
 // Optional callbacks around every kernel launch (per-kernel CUDA-event timing).
 struct KernelHooks {
@@ -131,7 +132,26 @@ struct KernelHooks {
   void (*begin)(void* user, const char* kernel, cudaStream_t st) = nullptr;
   void (*end)(void* user, const char* kernel, cudaStream_t st) = nullptr;
 };
-extern KernelHooks g_hooks;
+
+// Launch accounting of one build: its kernel count and its timing callbacks.
+// Every launch wrapper reports to the state installed on the calling host
+// thread (none installed: nothing is counted or timed).  A context owns one
+// and installs it with LaunchScope for the length of each API call, so builds
+// of different contexts on different threads never share a counter or hooks,
+// and a call made from inside another call's callback restores the outer
+// call's state when it returns.
+struct LaunchState {
+  unsigned long long launches = 0;
+  KernelHooks hooks;
+};
+LaunchState* current_launch_state();
+struct LaunchScope {
+  LaunchState* prev;
+  explicit LaunchScope(LaunchState* s);
+  ~LaunchScope();
+  LaunchScope(const LaunchScope&) = delete;
+  LaunchScope& operator=(const LaunchScope&) = delete;
+};
 
 void scan_u32_exclusive(uint32_t* data, uint64_t n, uint32_t* partials, cudaStream_t st);
 void scan_u64_exclusive(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st);
@@ -142,8 +162,11 @@ void launch_part_count(const float* tris, int stride, uint64_t n_tris, const flo
 void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
                       int pa_bits, uint64_t n_parts, uint32_t* cursor, uint32_t* items, cudaStream_t st);
 
-void launch_vox_small_occupancy(const VoxJob& j, cudaStream_t st);
-void launch_vox_large_occupancy(const VoxJob& j, cudaStream_t st, int num_sms);
+// One-stripe occupancy pass with the job as a kernel parameter (the allocation-free
+// entry point's launches); each returns the status of its own launch calls.
+cudaError_t launch_vox_small_occupancy(const VoxJob& j, cudaStream_t st);
+cudaError_t launch_vox_large_occupancy(const VoxJob& j, cudaStream_t st, int num_sms);
+cudaError_t scan_u64_exclusive_checked(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st);
 
 // src holds n entries of (index, `words` u64 values); dst[index*words + q] = value q.
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st);

@@ -12,22 +12,30 @@
 
 namespace ooc {
 
-unsigned long long g_launches = 0;
-KernelHooks g_hooks;
+namespace {
+thread_local LaunchState* t_launch = nullptr;  // the state of the call running on this thread
+}  // namespace
+
+LaunchState* current_launch_state() { return t_launch; }
+LaunchScope::LaunchScope(LaunchState* s) : prev(t_launch) { t_launch = s; }
+LaunchScope::~LaunchScope() { t_launch = prev; }
 
 namespace {
 constexpr unsigned FULL = 0xffffffffu;
 
-// Counts one launch and brackets it with the timing hooks when they are set.
+// Counts one launch and brackets it with the timing hooks of the calling
+// thread's launch state, when one is installed.
 struct KScope {
   const char* name;
   cudaStream_t st;
-  KScope(const char* n, cudaStream_t s) : name(n), st(s) {
-    g_launches++;
-    if (g_hooks.begin) g_hooks.begin(g_hooks.user, name, st);
+  LaunchState* ls;
+  KScope(const char* n, cudaStream_t s) : name(n), st(s), ls(t_launch) {
+    if (!ls) return;
+    ls->launches++;
+    if (ls->hooks.begin) ls->hooks.begin(ls->hooks.user, name, st);
   }
   ~KScope() {
-    if (g_hooks.end) g_hooks.end(g_hooks.user, name, st);
+    if (ls && ls->hooks.end) ls->hooks.end(ls->hooks.user, name, st);
   }
 };
 constexpr int SCAN_THREADS = 256;
@@ -1591,18 +1599,59 @@ void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const floa
 }
 
 // One-stripe occupancy pass with the job as a kernel parameter (the
-// allocation-free entry point uses these two).
-void launch_vox_small_occupancy(const VoxJob& j, cudaStream_t st) {
-  if (j.n_items == 0) return;
+// allocation-free entry point uses these).  Launched with cudaLaunchKernel so
+// that each returns the status of its own launch.
+cudaError_t launch_vox_small_occupancy(const VoxJob& j, cudaStream_t st) {
+  if (j.n_items == 0) return cudaSuccess;
   KScope k("vox_small_occupancy", st);
-  k_vox_small_occ<<<grid_for(j.n_items, 256), 256, 0, st>>>(j);
+  VoxJob arg = j;
+  void* args[] = {&arg};
+  return cudaLaunchKernel(reinterpret_cast<const void*>(&k_vox_small_occ), dim3(grid_for(j.n_items, 256)), dim3(256),
+                          args, 0, st);
 }
 
-void launch_vox_large_occupancy(const VoxJob& j, cudaStream_t st, int num_sms) {
-  if (j.n_items == 0) return;
-  cudaMemsetAsync(j.task_counter, 0, sizeof(unsigned long long), st);
+cudaError_t launch_vox_large_occupancy(const VoxJob& j, cudaStream_t st, int num_sms) {
+  if (j.n_items == 0) return cudaSuccess;
+  const cudaError_t e = cudaMemsetAsync(j.task_counter, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
   KScope k("vox_large_occupancy", st);
-  k_vox_large<0><<<(unsigned)num_sms * 8, 256, 256 * j.lines_per_lane * 4, st>>>(j);
+  VoxJob arg = j;
+  void* args[] = {&arg};
+  return cudaLaunchKernel(reinterpret_cast<const void*>(&k_vox_large<0>), dim3((unsigned)num_sms * 8), dim3(256), args,
+                          (size_t)256 * j.lines_per_lane * 4, st);
+}
+
+// scan_exclusive<uint64_t> with the status of every launch returned.
+cudaError_t scan_u64_exclusive_checked(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const unsigned nb = (unsigned)((n + SCAN_TILE - 1) / SCAN_TILE);
+  const uint64_t* none = nullptr;
+  if (nb == 1) {
+    KScope k("scan_down", st);
+    void* args[] = {&data, &n, &none};
+    return cudaLaunchKernel(reinterpret_cast<const void*>(&k_scan_down<uint64_t>), dim3(1), dim3(SCAN_THREADS), args,
+                            0, st);
+  }
+  cudaError_t e;
+  {
+    KScope k("scan_reduce", st);
+    void* args[] = {&data, &n, &partials};
+    e = cudaLaunchKernel(reinterpret_cast<const void*>(&k_scan_reduce<uint64_t>), dim3(nb), dim3(SCAN_THREADS), args,
+                         0, st);
+  }
+  if (e != cudaSuccess) return e;
+  {
+    KScope k("scan_partials", st);
+    uint64_t np = nb;
+    void* args[] = {&partials, &np};
+    e = cudaLaunchKernel(reinterpret_cast<const void*>(&k_scan_partials<uint64_t>), dim3(1), dim3(1024), args, 0, st);
+  }
+  if (e != cudaSuccess) return e;
+  KScope k("scan_down", st);
+  const uint64_t* cp = partials;
+  void* args[] = {&data, &n, &cp};
+  return cudaLaunchKernel(reinterpret_cast<const void*>(&k_scan_down<uint64_t>), dim3(nb), dim3(SCAN_THREADS), args, 0,
+                          st);
 }
 
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st) {

@@ -77,9 +77,10 @@ extern "C" int ooc_voxelize_occupancy_noalloc(const ooc_build_params* params, co
   if (rc != OOC_OK) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
 
-  // The kernels report to the library's timing hooks; this call has no context to report to.
-  const KernelHooks saved = g_hooks;
-  g_hooks = KernelHooks();
+  // This call has no context: its launches report to a launch state of its own
+  // with no timing hooks, installed on this thread for the call only.
+  LaunchState own;
+  LaunchScope scope(&own);
 
   const float u = (params->bbox_max[0] - params->bbox_min[0]) / (float)N;  // main.cpp:311
   VoxJob j;
@@ -107,16 +108,11 @@ extern "C" int ooc_voxelize_occupancy_noalloc(const ooc_build_params* params, co
 
   // What must start at zero: the output bits and the end of the task-offset
   // scan (the other scratch entries are fully written before they are read).
-  int out = OOC_OK;
-  if (cudaMemsetAsync(occupancy_device, 0, words * 4, st) != cudaSuccess ||
-      cudaMemsetAsync(j.task_off + n_tris, 0, 8, st) != cudaSuccess) {
-    out = OOC_ERR_DEVICE;
-  } else {
-    launch_vox_small_occupancy(j, st);
-    scan_u64_exclusive(j.task_off, n_tris + 1, partials, st);
-    launch_vox_large_occupancy(j, st, sms);
-    if (cudaGetLastError() != cudaSuccess) out = OOC_ERR_DEVICE;
-  }
-  g_hooks = saved;
-  return out;
+  // Every step's own status is checked; the first failure ends the call.
+  if (cudaMemsetAsync(occupancy_device, 0, words * 4, st) != cudaSuccess) return OOC_ERR_DEVICE;
+  if (cudaMemsetAsync(j.task_off + n_tris, 0, 8, st) != cudaSuccess) return OOC_ERR_DEVICE;
+  if (launch_vox_small_occupancy(j, st) != cudaSuccess) return OOC_ERR_DEVICE;
+  if (scan_u64_exclusive_checked(j.task_off, n_tris + 1, partials, st) != cudaSuccess) return OOC_ERR_DEVICE;
+  if (launch_vox_large_occupancy(j, st, sms) != cudaSuccess) return OOC_ERR_DEVICE;
+  return OOC_OK;
 }

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -81,9 +82,15 @@ bool valid(const ooc_mesh& m) {
 }
 
 // HBM a request may hold while it is in flight: its triangles, the occupancy
-// pyramids of its stripes, and per-node arrays plus output records for an
-// estimate of its nodes (about twice the surface area in voxels, times 1.5
-// for the inner levels).
+// pyramids of its stripes, and per-node arrays plus output records for an upper
+// bound on its nodes.  The leaves are at most the grid voxels inside the
+// triangles' grid boxes (voxelizer.cpp:189-204 tests no voxel outside them),
+// and a tree with L leaves at depth D has at most min(8^l, L) nodes at level l.
+// A node costs at most kNodeBytes: its 24-byte record and 32-byte data record,
+// its key, subtree sizes and starts, first child and winner (7 x 4 bytes) and
+// its -levels cache (24 bytes), with room for the batch's job tables.
+constexpr uint64_t kNodeBytes = 120;
+
 uint64_t footprint(const ooc_mesh& m) {
   const ooc_build_params& p = m.params;
   const uint64_t N = p.gridsize;
@@ -99,18 +106,27 @@ uint64_t footprint(const ooc_mesh& m) {
   for (int l = 0; l <= Ds; l++) words += (((1ull << (3 * l)) + 31) / 32 + 7) / 8 * 8;
   const uint64_t stripes = (N * N * N) >> (3 * Ds);
   bytes += words * 4 * stripes;
-  const float u = (p.bbox_max[0] - p.bbox_min[0]) / (float)N;
-  double area = 0.0;
-  for (uint64_t t = 0; t < m.n_tris; t++) {
+  // grid boxes as voxelizer.cpp:189-204 forms them: truncated, clamped to the grid
+  const float unit_div = 1.0f / ((p.bbox_max[0] - p.bbox_min[0]) / (float)N);
+  const double cells = (double)N * (double)N * (double)N;
+  double leaves = 0.0;
+  for (uint64_t t = 0; t < m.n_tris && leaves < cells; t++) {
     const float* v = m.tris + t * stride;
-    const double ax = v[3] - v[0], ay = v[4] - v[1], az = v[5] - v[2];
-    const double bx = v[6] - v[0], by = v[7] - v[1], bz = v[8] - v[2];
-    const double cx = ay * bz - az * by, cy = az * bx - ax * bz, cz = ax * by - ay * bx;
-    area += 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+    double vol = 1.0;
+    for (int a = 0; a < 3; a++) {
+      const float lo = std::min(v[a], std::min(v[3 + a], v[6 + a])) * unit_div;
+      const float hi = std::max(v[a], std::max(v[3 + a], v[6 + a])) * unit_div;
+      // NaN or out-of-range coordinates count as the whole axis
+      const double l = (lo >= 0.0f) ? std::min((double)lo, (double)N - 1) : 0.0;
+      const double h = (hi < (float)N) ? std::max((double)hi, 0.0) : (double)N - 1;
+      vol *= (h >= l) ? std::floor(h) - std::floor(l) + 1.0 : (double)N;
+    }
+    leaves += vol;
   }
-  const double voxels = std::min<double>(2.0 * area / (double)u / (double)u + 2.0 * (double)m.n_tris,
-                                         (double)N * (double)N * (double)N);
-  bytes += (uint64_t)(voxels * 1.5 * 120.0);
+  leaves = std::min(leaves, cells);
+  double nodes = 0.0;
+  for (int l = 0; l <= D; l++) nodes += std::min(std::ldexp(1.0, 3 * l), leaves);
+  bytes += (uint64_t)std::min(nodes * (double)kNodeBytes, 1.8e19);
   return bytes;
 }
 
@@ -128,12 +144,15 @@ struct ooc_server {
   std::unordered_map<uint64_t, Request*> held;  // polled, not yet released
   uint64_t next_id = 1;
   uint64_t in_flight = 0;  // admitted footprints, plus device results not yet released
+  std::atomic<bool> injected{false};  // the fault injection of cfg.fail_batch_at_mesh has fired
   bool stop = false;
   Clock::time_point t0 = Clock::now();
 
   double now_us() const { return std::chrono::duration<double, std::micro>(Clock::now() - t0).count(); }
 
-  bool fits(const Request* r) const { return in_flight == 0 || in_flight + r->footprint <= cfg.memory_budget; }
+  // every queued footprint is within the budget (ooc_server_submit), so a request
+  // always fits once nothing else holds memory
+  bool fits(const Request* r) const { return in_flight + r->footprint <= cfg.memory_budget; }
 
   // A request is complete (and can be polled, then released by the caller)
   // as soon as its mesh is; the engine does not touch it afterwards.
@@ -154,7 +173,14 @@ struct ooc_server {
     std::vector<ooc_build_info> infos;
     std::vector<char>* published;  // by index into the engine's batch
     std::vector<size_t> index;
+    bool inject = false;  // fault injection armed for this call
   };
+
+  // ooc_server_config::fail_batch_at_mesh: whether this batch's mesh `mesh` is the one to fail
+  static bool injected_failure(Call& call, uint64_t mesh) {
+    if (!call.inject || mesh + 1 != call.s->cfg.fail_batch_at_mesh) return false;
+    return !call.s->injected.exchange(true);  // once per server
+  }
 
   static void mark(Call& call, uint64_t mesh) {
     Request* r = call.reqs[mesh];
@@ -170,6 +196,7 @@ struct ooc_server {
       mark(call, mesh);
       return 0;
     }
+    if (injected_failure(call, mesh)) return 1;
     Bytes& dst = kind == OOC_STREAM_NODES ? r->nodes : r->data;
     return dst.append(bytes, n) ? 0 : 1;
   }
@@ -179,6 +206,7 @@ struct ooc_server {
     Call& call = *static_cast<Call*>(user);
     Request* r = call.reqs[mesh];
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (injected_failure(call, mesh)) return 1;
     if (cudaMallocAsync(&r->d_nodes, nodes_bytes, st) != cudaSuccess) return 1;
     if (cudaMallocAsync(&r->d_data, data_bytes, st) != cudaSuccess) return 1;
     r->d_nodes_bytes = nodes_bytes;
@@ -203,6 +231,7 @@ struct ooc_server {
   int run(ooc_ctx* ctx, const std::vector<Request*>& batch, const std::vector<size_t>& index,
           std::vector<char>& published) {
     Call call{this, {}, std::vector<ooc_build_info>(index.size()), &published, index};
+    call.inject = cfg.fail_batch_at_mesh != 0 && !injected.load() && index.size() > 1;
     std::vector<ooc_mesh> meshes(index.size());
     for (size_t i = 0; i < index.size(); i++) {
       Request* r = batch[index[i]];
@@ -327,6 +356,10 @@ int ooc_server_submit(ooc_server* s, const ooc_mesh* mesh, uint64_t* id) {
   if (!r) return OOC_ERR_OOM;
   r->mesh = *mesh;
   r->footprint = footprint(*mesh);
+  if (r->footprint > s->cfg.memory_budget) {
+    delete r;
+    return OOC_ERR_LIMIT;
+  }
   r->t_submit = t;
   {
     std::lock_guard<std::mutex> lk(s->mu);

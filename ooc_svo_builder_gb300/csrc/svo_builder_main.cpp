@@ -10,6 +10,7 @@
 #include <fstream>
 #include <iostream>
 #include <string>
+#include <vector>
 
 #include "ooc_svo_gpu.h"
 
@@ -25,6 +26,12 @@ int color = OOC_COLOR_MODEL;
 const char* color_name = "Color from model (fallback to fixed color if model has no color)";
 bool generate_levels = false;
 bool verbose = false;
+
+// the .tri header (check_tri)
+std::string base;  // the file name without its extension
+int version = 0;
+uint64_t n_triangles = 0;
+float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
 
 void print_info() {
   std::cout << "--------------------------------------------------------------------" << std::endl;
@@ -167,16 +174,14 @@ void check_tri(const std::string& fn) {
     std::cout << "  Error: file " << fn << " does not exist." << std::endl;
     std::exit(0);
   }
-  const std::string base = fn.substr(0, fn.find_last_of("."));
+  base = fn.substr(0, fn.find_last_of("."));
   std::string word;
   f >> word;
   if (word != "#tri") {
     std::cout << "  Error: first line reads [" << word << "] instead of [#tri]" << std::endl;
     std::exit(0);
   }
-  int version = 0, geo = 0;
-  uint64_t n_triangles = 0;
-  float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
+  int geo = 0;
   f >> version;
   bool seen_end = false;
   while (f.good() && !seen_end) {
@@ -245,6 +250,39 @@ uint64_t report_partitions() {
   return P;
 }
 
+// createBuffers' verbose report of the partition boxes (partitioner.cpp:43-77):
+// Morton range, grid box and world box of every partition, with the world box
+// as the reference forms it, grid coordinate times the unit length in float.
+void report_partition_boxes(uint64_t P, float unitlength) {
+  const uint64_t part = gridsize * gridsize * gridsize / P;
+  auto decode = [](uint64_t m, unsigned int v[3]) {
+    for (int a = 0; a < 3; a++) {
+      unsigned int c = 0;
+      for (int b = 0; b < 21; b++) c |= (unsigned int)((m >> (3 * b + a)) & 1u) << b;
+      v[a] = c;
+    }
+  };
+  for (uint64_t i = 0; i < P; i++) {
+    unsigned int lo[3], hi[3];
+    decode(part * i, lo);
+    decode(part * (i + 1) - 1, hi);
+    float wlo[3], whi[3];
+    for (int a = 0; a < 3; a++) {
+      wlo[a] = lo[a] * unitlength;
+      whi[a] = (hi[a] + 1) * unitlength;
+    }
+    std::cout << "Partitioning partition #" << i + 1 << " / " << P << " id: " << i << " ..." << std::endl;
+    std::cout << "  morton from " << part * i << " to " << part * (i + 1) << std::endl;
+    std::cout << "  grid coordinates from (" << lo[0] << "," << lo[1] << "," << lo[2] << ") to (" << hi[0] << ","
+              << hi[1] << "," << hi[2] << ")" << std::endl;
+    std::cout << "  worldspace coordinates from (" << wlo[0] << "," << wlo[1] << "," << wlo[2] << ") to (" << whi[0]
+              << "," << whi[1] << "," << whi[2] << ")" << std::endl;
+  }
+}
+
+// The reference's timers count whole milliseconds (timer.h:59).
+double whole_ms(double ms) { return (double)(long long)ms; }
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -275,28 +313,80 @@ int main(int argc, char** argv) {
   ooc_build_info info = {};
   char out_base[4096];
   const int rc = ooc_build_files(ctx, filename.c_str(), &prm, out_base, sizeof(out_base), &info);
+  if (verbose && P > 1) report_partition_boxes(P, (bmax[0] - bmin[0]) / (float)gridsize);
   std::cout << "done." << std::endl;
   if (rc != OOC_OK) {
     std::cout << "Build failed (" << rc << "): " << ooc_last_error(ctx) << std::endl;
     ooc_ctx_destroy(ctx);
     return 0;
   }
-  std::cout << "Voxelized and built " << info.n_stripes << " stripe(s) on the GPU" << std::endl;
+  // per-partition progress (main.cpp:329-355); the partitions were built together,
+  // so their lines come after the build, in partition order
+  std::vector<uint64_t> tris(P, 0), filled(P, 0);
+  ooc_partition_counts(ctx, 0, P, tris.data(), filled.data());
+  const std::string trip_base = base + std::to_string(gridsize) + "_" + std::to_string(P);
+  if (verbose) {  // readTripHeader's TripInfo::print (main.cpp:271-279, trip_tools.h:28-40)
+    std::cout << "  base_filename: " << trip_base << std::endl;
+    std::cout << "  trip version: " << version << std::endl;
+#ifdef OOC_CLI_BINARY
+    std::cout << "  geometry only: 1" << std::endl;
+#else
+    std::cout << "  geometry only: 0" << std::endl;
+#endif
+    std::cout << "  gridsize: " << gridsize << std::endl;
+    std::cout << "  bbox min: " << bmin[0] << " " << bmin[1] << " " << bmin[2] << std::endl;
+    std::cout << "  bbox max: " << bmax[0] << " " << bmax[1] << " " << bmax[2] << std::endl;
+    std::cout << "  n_triangles: " << n_triangles << std::endl;
+    std::cout << "  n_partitions: " << P << std::endl;
+    for (uint64_t i = 0; i < P; i++) std::cout << "  partition " << i << " - tri_count: " << tris[i] << std::endl;
+  }
+  for (uint64_t i = 0; i < P; i++) {
+    if (tris[i] == 0) continue;  // main.cpp:330
+    std::cout << "Voxelizing partition " << i << " ..." << std::endl;
+    if (verbose) {
+      std::cout << "  reading " << tris[i] << " triangles from " << trip_base << "_" << i << ".tripdata" << std::endl;
+      std::cout << "  found " << filled[i] << " new voxels." << std::endl;
+    }
+    std::cout << "Building SVO for partition " << i << " ..." << std::endl;
+  }
   std::cout << "done" << std::endl;
   std::cout << "Total amount of voxels: " << info.n_filled << std::endl;
-  float ms[6] = {0, 0, 0, 0, 0, 0};
+  float ms[6] = {0, 0, 0, 0, 0, 0}, fms[2] = {0, 0};
   ooc_phase_times(ctx, ms, 6);
+  ooc_file_times(ctx, fms, 2);
   ooc_ctx_destroy(ctx);
   const double main_ms =
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-  std::cout << "Total MAIN time      : " << main_ms << " ms." << std::endl;
-  std::cout << "GPU PHASES (device time)" << std::endl;
-  std::cout << "  partitioning        : " << ms[0] << " ms." << std::endl;
-  std::cout << "  voxelizing          : " << ms[1] << " ms." << std::endl;
-  std::cout << "  occupancy pyramid   : " << ms[2] << " ms." << std::endl;
-  std::cout << "  octree layout       : " << ms[3] << " ms." << std::endl;
-  std::cout << "  host<->device copies: " << ms[4] << " ms." << std::endl;
-  std::cout << "  whole build         : " << ms[5] << " ms." << std::endl;
-  std::cout << "Output: " << out_base << ".octree" << std::endl;
+  // printTimerInfo (main.cpp:219-241), filled from the GPU phases and the file times
+  const double part_in = whole_ms(fms[0]), part_algo = whole_ms(ms[0]), part_total = whole_ms(fms[0] + ms[0]);
+  const double vox_algo = whole_ms(ms[1] + ms[2]), vox_total = vox_algo;
+  const double svo_out = whole_ms(fms[1]), svo_algo = whole_ms(ms[3]), svo_total = whole_ms(fms[1] + ms[3] + ms[4]);
+  std::cout << "Total MAIN time      : " << whole_ms(main_ms) << " ms." << std::endl;
+  std::cout << "PARTITIONING" << std::endl;
+  std::cout << "  Total time\t\t: " << part_total << " ms." << std::endl;
+  std::cout << "  IO IN time\t\t: " << part_in << " ms." << std::endl;
+  std::cout << "  algorithm time\t: " << part_algo << " ms." << std::endl;
+  std::cout << "  IO OUT time\t\t: " << 0.0 << " ms." << std::endl;
+  std::cout << "  misc time\t\t: " << part_total - part_in - part_algo << " s." << std::endl;
+  std::cout << "VOXELIZING" << std::endl;
+  std::cout << "  Total time\t\t: " << vox_total << " ms." << std::endl;
+  std::cout << "  IO IN time\t\t: " << 0.0 << " ms." << std::endl;
+  std::cout << "  algorithm time\t: " << vox_algo << " ms." << std::endl;
+  std::cout << "  misc time\t\t: " << vox_total - vox_algo << " s." << std::endl;
+  std::cout << "SVO BUILDING" << std::endl;
+  std::cout << "  Total time\t\t: " << svo_total << " ms." << std::endl;
+  std::cout << "  IO OUT time\t\t: " << svo_out << " ms." << std::endl;
+  std::cout << "  algorithm time\t: " << svo_algo << " ms." << std::endl;
+  std::cout << "  misc time\t\t: " << svo_total - svo_out - svo_algo << " s." << std::endl;
+  if (std::getenv("OOC_GPU_PHASES")) {  // device-time detail, off unless asked for
+    std::cout << "GPU PHASES (device time)" << std::endl;
+    std::cout << "  partitioning        : " << ms[0] << " ms." << std::endl;
+    std::cout << "  voxelizing          : " << ms[1] << " ms." << std::endl;
+    std::cout << "  occupancy pyramid   : " << ms[2] << " ms." << std::endl;
+    std::cout << "  octree layout       : " << ms[3] << " ms." << std::endl;
+    std::cout << "  host<->device copies: " << ms[4] << " ms." << std::endl;
+    std::cout << "  whole build         : " << ms[5] << " ms." << std::endl;
+    std::cout << "Output: " << out_base << ".octree" << std::endl;
+  }
   return 0;
 }

@@ -166,3 +166,60 @@ def digest(tree: Octree) -> dict:
             "n_data": int(tree.data.shape[0]),
             "nodes_sha256": hashlib.sha256(np.ascontiguousarray(tree.nodes).tobytes()).hexdigest(),
             "data_sha256": hashlib.sha256(data.tobytes()).hexdigest()}
+
+
+class StreamDigest:
+    """`digest` of an octree whose node and data files arrive in pieces, in file order
+    (a build's sink, or files read in chunks), without holding them: the same hashes
+    as ``digest(tree)`` of the whole files."""
+
+    def __init__(self, gridlength: int):
+        import hashlib
+        self.gridlength = int(gridlength)
+        self._h = {0: hashlib.sha256(), 1: hashlib.sha256()}
+        self._n = {0: 0, 1: 0}
+        self._tail = b""  # bytes of a data record split between two pieces
+        self.nan_fields = 0
+
+    def update(self, kind: int, piece) -> None:
+        """Append `piece` (bytes-like) to the node file (kind 0) or the data file (kind 1)."""
+        if kind == 0:
+            self._h[0].update(piece)
+            self._n[0] += len(piece)
+            return
+        b = self._tail + bytes(piece)
+        whole = len(b) // DATA_DTYPE.itemsize * DATA_DTYPE.itemsize
+        self._tail = b[whole:]
+        if whole:
+            data = np.frombuffer(b[:whole], dtype=DATA_DTYPE).copy()
+            for field in ("color", "normal"):
+                f = data[field]
+                m = np.isnan(f)
+                self.nan_fields += int(m.sum())
+                f.view(np.uint32)[m] = CANONICAL_NAN
+            self._h[1].update(data.tobytes())
+            self._n[1] += whole
+
+    def result(self) -> dict:
+        if self._tail or self._n[0] % NODE_DTYPE.itemsize:
+            raise ValueError("octree files end inside a record")
+        return {"gridlength": self.gridlength, "n_nodes": self._n[0] // NODE_DTYPE.itemsize,
+                "n_data": self._n[1] // DATA_DTYPE.itemsize, "nodes_sha256": self._h[0].hexdigest(),
+                "data_sha256": self._h[1].hexdigest()}
+
+
+def file_digest(base: str, chunk: int = 64 << 20) -> dict:
+    """`digest` of the octree files at `base`, read in chunks (for files too large to load)."""
+    h = parse_header(base + ".octree")
+    d = StreamDigest(h["gridlength"])
+    for kind, ext in ((0, ".octreenodes"), (1, ".octreedata")):
+        with open(base + ext, "rb") as f:
+            while True:
+                b = f.read(chunk)
+                if not b:
+                    break
+                d.update(kind, b)
+    out = d.result()
+    if out["n_nodes"] != h["n_nodes"] or out["n_data"] != h["n_data"]:
+        raise ValueError("octree files disagree with the header")
+    return out

@@ -14,6 +14,10 @@ from __future__ import annotations
 
 import os
 
+import re
+
+import numpy as np
+
 from ooc_svo_builder_gb300 import tri
 
 # (executable, arguments); paths are relative to the folder make_inputs() fills
@@ -49,6 +53,20 @@ CASES = [
 ]
 
 
+# Complete runs: every stdout line from the parameter parse to the timer block must
+# match the reference's, timing values aside (full_run_lines).  Binary runs with -v
+# use meshes sparse enough that no partition overflows the -d side-array: that
+# verbose-only message (voxelizer.cpp:177-184) is not reproduced.
+FULL_RUNS = [
+    ("svo_builder_binary", ["-f", "soup.tri", "-s", "256", "-l", "2"]),
+    ("svo_builder_binary", ["-f", "spheres.tri", "-s", "256", "-l", "2", "-v"]),
+    ("svo_builder_binary", ["-f", "spheres.tri", "-s", "64"]),
+    ("svo_builder", ["-f", "paysoup.tri", "-s", "256", "-l", "2", "-c", "linear", "-levels"]),
+    ("svo_builder", ["-f", "pay.tri", "-s", "64", "-levels", "-v"]),
+    ("svo_builder_binary", ["-f", "unknown.tri", "-v", "-s", "256", "-l", "2"]),
+]
+
+
 def case_id(exe: str, args) -> str:
     return " ".join([exe, *args])
 
@@ -69,6 +87,16 @@ def make_inputs(folder: str) -> None:
     with open(os.path.join(folder, "unknown.tri"), "w") as f:
         f.write("#tri 1\nntriangles 0\nauthor someone else\ngeo_only 1\nbbox 0 0 0 2 2 2\nEND\n")
     open(os.path.join(folder, "unknown.tridata"), "w").close()
+    # complete runs: a soup over 8 partitions, two small spheres in two octants (six
+    # partitions without triangles), a payload soup
+    tri.write_tri(os.path.join(folder, "soup"), tri.soup_tris(3000, 64, seed=5, sigma=1.0, n_spheres=3))
+    a = tri.icosphere_tris(2, radius=0.04, jitter=0.0, seed=1)
+    b = a.copy()
+    a[:, :9] -= np.float32(0.25)
+    b[:, [0, 3, 6]] += np.float32(0.3)
+    tri.write_tri(os.path.join(folder, "spheres"), np.concatenate([a, b]))
+    tri.write_tri(os.path.join(folder, "paysoup"), tri.soup_tris(2000, 64, seed=6, sigma=1.0, n_spheres=3,
+                                                                 payload=True))
 
 
 def diagnostics(stdout: str):
@@ -86,3 +114,13 @@ def diagnostics(stdout: str):
             break
         out.append(ln)
     return out
+
+
+_TIME = re.compile(r"(time[\t ]*: )-?[0-9][0-9.e+-]*( m?s\.)$")
+
+
+def full_run_lines(stdout: str):
+    """A complete run's lines from the parameter parse on, with every timer value
+    (main.cpp:219-241) replaced by <t>."""
+    lines = stdout.splitlines()
+    return [_TIME.sub(r"\1<t>\2", ln) for ln in lines[lines.index("Reading program parameters ..."):]]

@@ -9,6 +9,11 @@ It does the same, per mesh, for the first meshes of the seeded streams of
 configurations 4 and 5 (golden_cases STREAMS) into stream_samples_reference.json.
 The CPU oracle is run on the same meshes and must give the same digests.  Regenerate with
 ``python tests/golden/make_fullsize_golden.py`` (needs the reference build).
+
+``--large`` runs the reference once on configuration 3 (golden_cases FULLSIZE_LARGE: the
+seeded 20M-triangle soup, ``svo_builder_binary -s 4096 -l 2048``, 64 partitions).  Its node
+file is about 16 GB, so it is hashed from disk in chunks instead of loaded, and the oracle is
+not run beside it (it would take as long again); the row goes into the same JSON file.
 """
 from __future__ import annotations
 
@@ -53,6 +58,49 @@ def run_reference(t, gridsize, limit, payload, color, levels=False):
     return tree, header, filled, P, command
 
 
+def file_digest(obase: str) -> tuple:
+    """(octree.digest of the files at obase, header text, NaN data fields), reading the node
+    and data files in 64 MiB chunks."""
+    with open(obase + ".octree") as f:
+        header = f.read()
+    d = octree.StreamDigest(octree.parse_header(obase + ".octree")["gridlength"])
+    for kind, ext in ((0, ".octreenodes"), (1, ".octreedata")):
+        with open(obase + ext, "rb") as f:
+            while True:
+                b = f.read(64 << 20)
+                if not b:
+                    break
+                d.update(kind, b)
+    return d.result(), header, d.nan_fields
+
+
+def large_digest(t, gridsize, limit, payload, color, workdir):
+    """The reference build on a mesh too large to load its octree: the row of
+    fullsize_reference.json, digests computed from the files in chunks."""
+    os.makedirs(workdir, exist_ok=True)
+    base = os.path.join(workdir, "mesh")
+    tri.write_tri(base, t)
+    exe = pyoracle.ref_binary(not payload)
+    cmd = [exe, "-f", base + ".tri", "-s", str(gridsize), "-l", str(limit)]
+    if payload:
+        cmd += ["-c", color]
+    t0 = time.time()
+    stdout = subprocess.run(cmd, cwd=workdir, stdout=subprocess.PIPE, text=True, check=True).stdout
+    secs = time.time() - t0
+    filled = int([ln for ln in stdout.splitlines() if ln.startswith("Total amount of voxels")][0].split()[-1])
+    P = int([ln for ln in stdout.splitlines() if ln.startswith("Partitioning data into")][0].split()[3])
+    obase = base + "%d_%d" % (gridsize, P)
+    dig, header, nan = file_digest(obase)
+    for ext in (".octree", ".octreenodes", ".octreedata", ".tri", ".tridata"):
+        path = (obase if ext.startswith(".octree") else base) + ext
+        if os.path.exists(path):
+            os.remove(path)
+    command = " ".join([os.path.basename(exe)] + cmd[1:]).replace(base, "mesh")
+    return {"command": command, "input_sha256": golden_cases.input_sha256(t), "n_triangles": int(t.shape[0]),
+            "n_partitions": P, "n_filled": filled, "header": header, "digest": dig, "nan_data_fields": nan,
+            "reference_seconds": round(secs, 1), "oracle_checked": False}
+
+
 def checked_digest(name, t, gridsize, limit, payload, color, levels=False):
     """Digest of the reference's output, which the oracle must reproduce; where the reference's
     output is undefined (see reference_undefined), the reason and the oracle's digest."""
@@ -73,8 +121,26 @@ def checked_digest(name, t, gridsize, limit, payload, color, levels=False):
     return row
 
 
+def main_large(workdir: str) -> None:
+    path = os.path.join(HERE, "fullsize_reference.json")
+    for name, w in golden_cases.FULLSIZE_LARGE.items():
+        t0 = time.time()
+        row = large_digest(w["make"](), w["gridsize"], w["limit"], w["payload"], w["color"], workdir)
+        with open(path) as f:
+            out = json.load(f)
+        out[name] = row
+        with open(path, "w") as f:
+            json.dump(out, f, indent=1)
+            f.write("\n")
+        print("%s: %.1f s" % (name, time.time() - t0))
+
+
 def main() -> None:
-    out = {}
+    if "--large" in sys.argv:
+        main_large(sys.argv[sys.argv.index("--large") + 1] if len(sys.argv) > sys.argv.index("--large") + 1
+                   else tempfile.mkdtemp())
+        return
+    out = {k: v for k, v in golden_cases.fullsize_reference().items() if k in golden_cases.FULLSIZE_LARGE}
     for name, w in golden_cases.FULLSIZE.items():
         t0 = time.time()
         out[name] = checked_digest(name, w["make"](), w["gridsize"], w["limit"], w["payload"], w["color"],

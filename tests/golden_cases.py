@@ -39,6 +39,14 @@ FULLSIZE = {
 }
 
 
+# Configuration 3, recorded by make_fullsize_golden.py --large: svo_builder_binary -s 4096
+# -l 2048 (64 partitions) on the seeded 20M-triangle soup; the node file is about 16 GB.
+FULLSIZE_LARGE = {
+    "soup4096": dict(gridsize=4096, limit=2048, payload=False, color="model",
+                     make=lambda: tri.soup_tris(20_000_000, 4096, seed=3, sigma=1.0)),
+}
+
+
 def fullsize_reference():
     with open(os.path.join(GOLDEN, "fullsize_reference.json")) as f:
         return json.load(f)

@@ -49,3 +49,20 @@ def test_recorded_answers_are_the_reference_build(inputs, exe, args):
         pytest.skip("reference build not present (make -C oracle ref needs the reference sources)")
     r = run(inputs, exe, args, ref)
     assert cli_cases.diagnostics(r.stdout) == EXPECTED[cli_cases.case_id(exe, args)]["lines"]
+
+
+FULL = json.load(open(os.path.join(os.path.dirname(GOLDEN), "cli_full_runs.json")))
+
+
+def test_every_complete_run_has_a_recorded_answer():
+    assert sorted(FULL) == sorted(cli_cases.case_id(e, a) for e, a in cli_cases.FULL_RUNS)
+
+
+@pytest.mark.parametrize("exe,args", cli_cases.FULL_RUNS, ids=[cli_cases.case_id(e, a) for e, a in cli_cases.FULL_RUNS])
+def test_recorded_complete_runs_are_the_reference_build(inputs, exe, args):
+    """Where the reference build is present, the recorded complete runs are still its output."""
+    ref = os.path.dirname(pyoracle.ref_binary(True))
+    if not os.path.exists(os.path.join(ref, exe)):
+        pytest.skip("reference build not present (make -C oracle ref needs the reference sources)")
+    r = run(inputs, exe, args, ref)
+    assert cli_cases.full_run_lines(r.stdout) == FULL[cli_cases.case_id(exe, args)]["lines"]

@@ -104,3 +104,27 @@ def test_diff_and_digest_see_any_change_but_not_nan_bits():
     data5["normal"][1, 2] = np.nextafter(data5["normal"][1, 2], np.float32(2))
     e = octree.Octree(32, nodes, data5)
     assert octree.diff(tree, e) and octree.digest(tree) != octree.digest(e)
+
+
+def test_stream_digest_equals_whole_digest(tmp_path):
+    """octree.StreamDigest over pieces cut anywhere (inside records too) and file_digest
+    over chunked reads give octree.digest of the whole tree, NaNs made canonical."""
+    rng = np.random.default_rng(7)
+    nodes = np.frombuffer(rng.integers(0, 255, 1001 * 24, dtype=np.uint8).tobytes(), octree.NODE_DTYPE)
+    data = np.zeros(777, octree.DATA_DTYPE)
+    data["morton"] = rng.integers(0, 1 << 40, 777)
+    data["color"] = rng.random((777, 3))
+    data["color"][5, 1] = np.nan
+    data["normal"][9, 2] = np.float32(np.nan)
+    tree = octree.Octree(64, nodes, data)
+    want = octree.digest(tree)
+    d = octree.StreamDigest(64)
+    nb, db = nodes.tobytes(), data.tobytes()
+    for i in range(0, len(nb), 1000):
+        d.update(0, nb[i:i + 1000])
+    for i in range(0, len(db), 999):
+        d.update(1, db[i:i + 999])
+    assert d.result() == want and d.nan_fields == 2
+    base = str(tmp_path / "t")
+    octree.write_octree(base, tree)
+    assert octree.file_digest(base, chunk=4096) == want

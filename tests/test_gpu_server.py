@@ -1,5 +1,7 @@
 """Serving loop: requests submitted together run in shared batches, and each
-result is byte-identical to the same mesh built alone with ooc_build."""
+result equals the oracle on that request's mesh and flags (and so the same mesh
+built alone with ooc_build), also when a batch fails part-way and its unfinished
+requests run again alone."""
 import threading
 import time
 
@@ -7,9 +9,45 @@ import numpy as np
 import pytest
 
 import ooc_svo_builder_gb300 as ooc
+import pyoracle
 from ooc_svo_builder_gb300 import make_params, octree, tri
 
 pytestmark = pytest.mark.gpu
+
+COLOR_NAMES = {v: k for k, v in ooc.COLOR_MODES.items()}
+
+
+def oracle_tree(t, p):
+    """The oracle's octree for one request."""
+    nodes, data, _ = pyoracle.build(t, int(p.gridsize), int(p.memory_limit_mb), color=COLOR_NAMES[p.color_mode],
+                                    levels=bool(p.generate_levels))
+    return octree.Octree(int(p.gridsize), nodes, data)
+
+
+def serve_all(reqs, feed_delay=0.0, **server_kw):
+    """Submit every request (from a second thread when feed_delay > 0) and poll until all
+    are back: (ids, {id: polled result})."""
+    with ooc.Server(0, **server_kw) as srv:
+        ids = [None] * len(reqs)
+
+        def feed():
+            for i, (t, p) in enumerate(reqs):
+                ids[i] = srv.submit(t, p)
+                if feed_delay:
+                    time.sleep(feed_delay)
+
+        th = threading.Thread(target=feed)
+        th.start()
+        if not feed_delay:
+            th.join()
+        got = {}
+        deadline = time.time() + 180
+        while len(got) < len(reqs) and time.time() < deadline:
+            r = srv.poll(1000)
+            if r is not None:
+                got[r["id"]] = r
+        th.join()
+    return ids, got
 
 
 def request_mix(seed=9, count=40):
@@ -31,53 +69,78 @@ def request_mix(seed=9, count=40):
     return out
 
 
-@pytest.mark.parametrize("resident", [False, True], ids=["host", "device"])
-def test_results_alone_equal_results_in_the_mix(builder, resident):
+@pytest.fixture(scope="module")
+def mix40():
     reqs = request_mix()
-    alone = [builder.build(t, p).tree for t, p in reqs]
-    with ooc.Server(0, engines=2, max_batch=16, memory_budget=8 << 30, resident=resident) as srv:
-        ids = [srv.submit(t, p) for t, p in reqs]
-        got = {}
-        deadline = time.time() + 120
-        while len(got) < len(ids) and time.time() < deadline:
-            r = srv.poll(1000)
-            if r is not None:
-                got[r["id"]] = r
+    return reqs, [oracle_tree(t, p) for t, p in reqs]
+
+
+@pytest.fixture(scope="module")
+def mix30():
+    reqs = request_mix(seed=11, count=30)
+    return reqs, [oracle_tree(t, p) for t, p in reqs]
+
+
+@pytest.mark.parametrize("resident", [False, True], ids=["host", "device"])
+def test_results_in_the_mix_equal_oracle(builder, mix40, resident):
+    reqs, want = mix40
+    ids, got = serve_all(reqs, engines=2, max_batch=16, memory_budget=8 << 30, resident=resident)
     assert len(got) == len(ids)
     assert max(r["batch_size"] for r in got.values()) > 1, "no request shared a batch"
-    for rid, want in zip(ids, alone):
+    for k, (rid, w) in enumerate(zip(ids, want)):
         r = got[rid]
         assert r["status"] == 0
         assert r["location"] == (1 if resident else 0)
-        d = octree.diff(r["tree"], want)
-        assert not d, "\n".join(d)
+        d = octree.diff(r["tree"], w)
+        assert not d, "request %d: %s" % (k, "\n".join(d))
         assert r["t_submit_us"] <= r["t_start_us"] <= r["t_done_us"]
+    # and the same mesh built alone through ooc_build
+    for k in range(0, len(reqs), 7):
+        assert not octree.diff(builder.build(*reqs[k]).tree, want[k])
 
 
 @pytest.mark.parametrize("resident", [False, True], ids=["host", "device"])
-def test_arrivals_while_busy_join_later_batches(builder, resident):
+def test_arrivals_while_busy_join_later_batches(mix30, resident):
     # a submitting thread keeps adding requests while the engines are running
-    reqs = request_mix(seed=11, count=30)
-    alone = [builder.build(t, p).tree for t, p in reqs]
-    with ooc.Server(0, engines=2, max_batch=8, memory_budget=8 << 30, resident=resident) as srv:
-        ids = [None] * len(reqs)
+    reqs, want = mix30
+    ids, got = serve_all(reqs, feed_delay=0.002, engines=2, max_batch=8, memory_budget=8 << 30, resident=resident)
+    for k, (rid, w) in enumerate(zip(ids, want)):
+        assert got[rid]["status"] == 0
+        assert not octree.diff(got[rid]["tree"], w), k
 
-        def feed():
-            for i, (t, p) in enumerate(reqs):
-                ids[i] = srv.submit(t, p)
-                time.sleep(0.002)
 
-        th = threading.Thread(target=feed)
-        th.start()
-        got = {}
-        deadline = time.time() + 120
-        while len(got) < len(reqs) and time.time() < deadline:
+@pytest.mark.parametrize("resident", [False, True], ids=["host", "device"])
+def test_failed_batch_reruns_its_unfinished_requests_alone(mix40, resident):
+    """The first shared batch fails at its third mesh (fault injection on the host: the
+    result sink refuses it, or its allocation fails as if out of memory).  The batch's
+    first two requests are complete already; every other one runs again alone.  All
+    results still equal the oracle."""
+    reqs, want = mix40
+    ids, got = serve_all(reqs, engines=1, max_batch=16, memory_budget=8 << 30, resident=resident,
+                         fail_batch_at_mesh=3)
+    assert len(got) == len(ids)
+    sizes = [got[rid]["batch_size"] for rid in ids]
+    assert max(sizes) > 1 and sizes.count(1) >= 1, sizes
+    for k, (rid, w) in enumerate(zip(ids, want)):
+        assert got[rid]["status"] == 0, k
+        assert not octree.diff(got[rid]["tree"], w), k
+
+
+def test_request_larger_than_budget_is_refused():
+    """Admission by computed footprint: a request whose triangles and occupancy pyramids
+    alone exceed the budget is refused at submission; smaller ones still run."""
+    t = tri.icosphere_tris(3)
+    with ooc.Server(0, engines=1, max_batch=4, memory_budget=64 << 20) as srv:
+        with pytest.raises(ooc.OocError) as e:
+            srv.submit(t, make_params(1024))  # a 1024^3 stripe's pyramid is ~146 MB
+        assert e.value.code == 6  # OOC_ERR_LIMIT
+        rid = srv.submit(t, make_params(64))
+        r = None
+        deadline = time.time() + 60
+        while r is None and time.time() < deadline:
             r = srv.poll(1000)
-            if r is not None:
-                got[r["id"]] = r
-        th.join()
-    for rid, want in zip(ids, alone):
-        assert not octree.diff(got[rid]["tree"], want)
+    assert r is not None and r["id"] == rid and r["status"] == 0
+    assert not octree.diff(r["tree"], oracle_tree(t, make_params(64)))
 
 
 def test_submit_rejects_invalid_request():

@@ -30,7 +30,8 @@ def test_server_calls_reject_null():
 def test_result_struct_layout():
     # ooc_result: id, status, reserved, nodes, nodes_bytes, data, data_bytes, info (6 x u64), 3 doubles, batch_size
     assert ctypes.sizeof(ooc.Result) == 8 + 4 + 4 + 8 * 4 + 48 + 24 + 8
-    assert ctypes.sizeof(ooc.ServerConfig) == 24
+    # ooc_server_config: device, engines, max_batch, result_location, memory_budget, fail_batch_at_mesh, reserved
+    assert ctypes.sizeof(ooc.ServerConfig) == 32
 
 
 def test_tuning_calls_reject_null():
