@@ -78,8 +78,28 @@ def measured_peaks() -> dict:
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "of measured (MEASURED_PEAKS.json hbm_gbs)"}
+    return {"hbm_gbs": 6800.0, "source": "of fallback (MEASURED_PEAKS.json absent: 6.8 TB/s, one earlier GB300 copy)"}
+
+
+def workload_config(name: str, world: int) -> dict:
+    """The `config` of a workload's bench line; both arms print the same one."""
+    w = WORKLOADS[name]
+    N = w["gridsize"]
+    T = {"heightfield1024": 2 * (HEIGHTFIELD_N - 1) ** 2, "icosphere256": 20 * 4 ** 5, "soup4096": 20_000_000,
+         "soup1024": 4_000_000, "soup2048": 1_000_000}[name]
+    # estimate_partitions (partitioner.cpp:12-28) and stripes of at most 1024^3 voxels
+    need, P = N ** 3 // (1 << 20), 1
+    while need > w["limit"]:
+        need //= 8
+        P *= 8
+    stripes = max(1, N ** 3 // min(N ** 3, 1 << 30))
+    tri_bytes = T * (84 if w["payload"] else 36)
+    return {"workload": w["desc"], "name": name, "gridsize": N, "memory_limit_mb": w["limit"], "n_triangles": T,
+            "mode": "payload" if w["payload"] else "binary", "partitions": P, "stripes": stripes,
+            "l2": "inputs larger than L2 (%.0f MB of triangles per step; L2 129 MB)" % (tri_bytes / 1e6)
+                  if tri_bytes > 129e6 else "inputs smaller than L2 (%.0f MB of triangles per step)" % (tri_bytes / 1e6),
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 class ClockSampler:
@@ -227,6 +247,7 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.Stream(device=local)
     b = ooc.Builder(local)
 
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     # warm-up (also sizes every device buffer)
     for _ in range(args.warmup):
         info = b.build_device(d_tris.data_ptr(), T, prm, stream.cuda_stream)
@@ -242,8 +263,16 @@ def run_ours(args, world, rank, local):
     b.set_kernel_timing(dominant)
 
     # ---- timed region: device-resident input ----
+    # The clock sampler watches a window of back-to-back builds around the timed ones: untimed
+    # builds for about a second before them and half a second after, so that its 200 ms samples
+    # see the GPU under this load even when the timed steps take only milliseconds.
     sampler = ClockSampler(local)
     sampler.start()
+    t_pre = time.perf_counter()
+    while time.perf_counter() - t_pre < args.clock_window * 2 / 3:
+        for _ in range(16):
+            b.build_device(d_tris.data_ptr(), T, prm, stream.cuda_stream)
+        torch.cuda.synchronize()
     barrier(world)
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -260,9 +289,16 @@ def run_ours(args, world, rank, local):
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier(world)
-    clocks = sampler.stop()
-    ms_total = max_over_ranks(ev0.elapsed_time(ev1), world)
+    t_post = time.perf_counter()
     b.set_kernel_timing(None)
+    while time.perf_counter() - t_post < args.clock_window / 3:
+        for _ in range(16):
+            b.build_device(d_tris.data_ptr(), T, prm, stream.cuda_stream)
+        torch.cuda.synchronize()
+    clocks = sampler.stop()
+    clocks["window"] = ("samples every 200 ms over %.1f s of back-to-back builds: untimed before the timed "
+                        "steps, the timed steps, untimed after" % args.clock_window)
+    ms_total = max_over_ranks(ev0.elapsed_time(ev1), world)
     ms_step = ms_total / args.steps
     value = world * T / (ms_step / 1e3) / 1e6
     nodes_per_s = world * info["n_nodes"] / (ms_step / 1e3)
@@ -331,28 +367,25 @@ def run_ours(args, world, rank, local):
     roofline = {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": traffic,
                 "traffic_source": traffic_src,
-                "peak_source": peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
+                "peak_source": peaks["source"],
                 "per_launch_ms": per_launch_ms, "algorithmic_bytes_per_launch": alg_per_launch}
     # The voxelization is issue-bound, not HBM-bound: its own roofline is the FP32 rate without
-    # FMA (152 SMs x 128 lanes x the measured SM clock) against the 47 flops of the full
+    # FMA (SMs x 128 lanes x the measured SM clock) against the 47 flops of the full
     # Schwarz-Seidel test per candidate voxel (voxelizer.cpp:266-287).
     if dominant == "vox_small_occupancy" and dom_n and clocks.get("sm_mhz"):
         flops = 47.0 * small_candidates(tris, w["gridsize"]) / max(1, launches_per_build)
-        fp32_peak = 152 * 128 * clocks["sm_mhz"] * 1e6 / 1e12
+        fp32_peak = sm_count * 128 * clocks["sm_mhz"] * 1e6 / 1e12
         fp32_achieved = flops / (per_launch_ms / 1e3) / 1e12
         roofline["fp32"] = {"bound": "fp32 issue (no FMA)", "achieved": fp32_achieved, "peak": fp32_peak,
                             "unit": "TFLOP/s", "frac": fp32_achieved / fp32_peak,
-                            "flops_per_launch": flops, "peak_source": "152 SMs x 128 FP32 lanes x measured SM clock"}
+                            "flops_per_launch": flops,
+                            "peak_source": "%d SMs (device attribute) x 128 FP32 lanes x measured SM clock" % sm_count}
 
     line = {
         "metric": "Mtri/s", "value": value, "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": w["desc"], "name": args.workload, "gridsize": w["gridsize"],
-                   "memory_limit_mb": w["limit"], "n_triangles": T, "mode": "payload" if payload else "binary",
-                   "partitions": info["n_partitions"], "stripes": info["n_stripes"],
-                   "l2": "inputs larger than L2 (%.0f MB of triangles per step; L2 129 MB)" % (h2d / 1e6),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(args.workload, world),
         "svo_nodes_per_s": nodes_per_s, "n_nodes": info["n_nodes"], "n_data": info["n_data"],
         "n_filled": info["n_filled"],
         "e2e": {"value": e2e_value, "unit": "Mtri/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -705,8 +738,7 @@ def run_reference(args, world, rank):
         "metric": "Mtri/s", "value": value, "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-        "config": {"workload": w["desc"], "name": args.workload, "gridsize": w["gridsize"],
-                   "memory_limit_mb": w["limit"], "n_triangles": T},
+        "config": workload_config(args.workload, world),
         "cpu_baseline": {"value": value, "unit": "Mtri/s", "cores": cores, "kind": "port",
                          "sample": "whole mesh per step on every core at once (%d processes x %d steps); "
                                    "per-core build %.0f ms" % (cores, args.steps, statistics.mean(secs) / args.steps * 1e3)},
@@ -729,6 +761,8 @@ def main():
     ap.add_argument("--engines", type=int, default=2, help="serve: engines of the served arm")
     ap.add_argument("--burst", type=int, default=4096, help="serve: requests of the capacity burst")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--clock-window", type=float, default=1.5,
+                    help="seconds of back-to-back builds the clock sampler watches around the timed steps")
     ap.add_argument("--no-files", action="store_true", help="skip the file-to-file measurement")
     ap.add_argument("--ref-cores", type=int, default=0, help="reference arm: host processes (default: all cores)")
     ap.add_argument("--traffic", type=float, default=None,

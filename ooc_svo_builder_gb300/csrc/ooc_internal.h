@@ -162,6 +162,17 @@ void launch_part_count(const float* tris, int stride, uint64_t n_tris, const flo
 void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
                       int pa_bits, uint64_t n_parts, uint32_t* cursor, uint32_t* items, cudaStream_t st);
 
+// Out-of-core binning of one chunk of the triangle stream for the partition group
+// [p0, p0 + gp) (gp <= kStreamMaxGroup): the chunk's records of each group partition q
+// are copied, in stream order, to out[base[q]...] (record indices), and base[q] moves
+// past them.  `mat` holds gp * stream_ctas(n) + 1 entries, `mat_partials`
+// scan_partials_needed of that.
+constexpr uint32_t kStreamMaxGroup = 4096;
+uint32_t stream_ctas(uint64_t n);
+void launch_stream_group_chunk(const float* tris, int stride, uint64_t n, const float* axis_lo, const float* axis_hi,
+                               int pa_bits, uint32_t p0, uint32_t gp, uint32_t* mat, uint32_t* mat_partials,
+                               uint64_t* base, float* out, cudaStream_t st);
+
 // One-stripe occupancy pass with the job as a kernel parameter (the allocation-free
 // entry point's launches); each returns the status of its own launch calls.
 cudaError_t launch_vox_small_occupancy(const VoxJob& j, cudaStream_t st);

@@ -289,6 +289,98 @@ __global__ void k_part_emit(const float* __restrict__ tris, int stride, uint64_t
         }
 }
 
+// ---------------------------------------------------------------------------
+// Out-of-core binning: the records of a group of consecutive partitions
+// [p0, p0 + gp), gathered from one chunk of the triangle stream into the
+// group's buffer, each partition's records contiguous and in stream order (the
+// order of the reference's per-partition .tripdata files, partitioner.cpp:
+// 101-149), so a smaller record index within a partition is an earlier
+// triangle.  CTAs of kStreamCta triangles; mat[q * n_cta + cta] is CTA cta's
+// count for group partition q, whose exclusive scan places every CTA's records.
+// ---------------------------------------------------------------------------
+constexpr int kStreamCta = 64;
+
+// Per-axis partition runs of triangle t, packed 7 bits per bound with bit 63 set,
+// or 0 when the triangle passes no partition's box test.
+__device__ __forceinline__ uint64_t stream_runs(const float* __restrict__ tris, int stride, uint64_t t,
+                                                const float* __restrict__ axis_lo, const float* __restrict__ axis_hi,
+                                                int PA) {
+  const WorldBox b = tri_world_box(tris, t, stride);
+  int x0, x1, y0, y1, z0, z1;
+  if (!(axis_run(b.lo[0], b.hi[0], axis_lo, axis_hi, PA, x0, x1) &&
+        axis_run(b.lo[1], b.hi[1], axis_lo + PA, axis_hi + PA, PA, y0, y1) &&
+        axis_run(b.lo[2], b.hi[2], axis_lo + 2 * PA, axis_hi + 2 * PA, PA, z0, z1)))
+    return 0ull;
+  return (uint64_t)x0 | ((uint64_t)x1 << 7) | ((uint64_t)y0 << 14) | ((uint64_t)y1 << 21) | ((uint64_t)z0 << 28) |
+         ((uint64_t)z1 << 35) | (1ull << 63);
+}
+
+__device__ __forceinline__ int run_bound(uint64_t r, int k) { return (int)((r >> (7 * k)) & 127u); }
+
+__global__ void __launch_bounds__(kStreamCta) k_stream_count(const float* __restrict__ tris, int stride, uint64_t n,
+                                                             const float* __restrict__ axis_lo,
+                                                             const float* __restrict__ axis_hi, int pa_bits,
+                                                             uint32_t p0, uint32_t gp, uint32_t* __restrict__ mat,
+                                                             uint32_t n_cta) {
+  extern __shared__ uint32_t cnt[];
+  for (uint32_t q = threadIdx.x; q < gp; q += kStreamCta) cnt[q] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) mat[(uint64_t)gp * n_cta] = 0;  // the scan's total entry
+  __syncthreads();
+  const uint64_t t = (uint64_t)blockIdx.x * kStreamCta + threadIdx.x;
+  if (t < n) {
+    const uint64_t r = stream_runs(tris, stride, t, axis_lo, axis_hi, 1 << pa_bits);
+    if (r)
+      for (int jx = run_bound(r, 0); jx <= run_bound(r, 1); jx++)
+        for (int jy = run_bound(r, 2); jy <= run_bound(r, 3); jy++)
+          for (int jz = run_bound(r, 4); jz <= run_bound(r, 5); jz++) {
+            const uint32_t q = morton_local(jx, jy, jz) - p0;
+            if (q < gp) atomicAdd(&cnt[q], 1u);
+          }
+  }
+  __syncthreads();
+  for (uint32_t q = threadIdx.x; q < gp; q += kStreamCta) mat[(uint64_t)q * n_cta + blockIdx.x] = cnt[q];
+}
+
+// Each record goes to base[q] + (its CTA's place among the chunk's records of q) +
+// (the CTA's earlier triangles that are in q).
+__global__ void __launch_bounds__(kStreamCta) k_stream_emit(const float* __restrict__ tris, int stride, uint64_t n,
+                                                            const float* __restrict__ axis_lo,
+                                                            const float* __restrict__ axis_hi, int pa_bits,
+                                                            uint32_t p0, uint32_t gp, const uint32_t* __restrict__ mat,
+                                                            uint32_t n_cta, const uint64_t* __restrict__ base,
+                                                            float* __restrict__ out) {
+  __shared__ uint64_t runs[kStreamCta];
+  const uint64_t t = (uint64_t)blockIdx.x * kStreamCta + threadIdx.x;
+  const uint64_t r = t < n ? stream_runs(tris, stride, t, axis_lo, axis_hi, 1 << pa_bits) : 0ull;
+  runs[threadIdx.x] = r;
+  __syncthreads();
+  if (!r) return;
+  const float* src = tris + t * (uint64_t)stride;
+  for (int jx = run_bound(r, 0); jx <= run_bound(r, 1); jx++)
+    for (int jy = run_bound(r, 2); jy <= run_bound(r, 3); jy++)
+      for (int jz = run_bound(r, 4); jz <= run_bound(r, 5); jz++) {
+        const uint32_t q = morton_local(jx, jy, jz) - p0;
+        if (q >= gp) continue;
+        uint32_t rank = 0;
+        for (uint32_t k = 0; k < threadIdx.x; k++) {
+          const uint64_t o = runs[k];
+          rank += (o >> 63) && run_bound(o, 0) <= jx && jx <= run_bound(o, 1) && run_bound(o, 2) <= jy &&
+                  jy <= run_bound(o, 3) && run_bound(o, 4) <= jz && jz <= run_bound(o, 5);
+        }
+        const uint64_t row = (uint64_t)q * n_cta;
+        const uint64_t dst = base[q] + (mat[row + blockIdx.x] - mat[row]) + rank;
+        float* d = out + dst * (uint64_t)stride;
+        for (int k = 0; k < stride; k++) d[k] = src[k];
+      }
+}
+
+// After a chunk: every group partition's next record moves past the chunk's records of it.
+__global__ void k_stream_advance(const uint32_t* __restrict__ mat, uint32_t n_cta, uint32_t gp,
+                                 uint64_t* __restrict__ base) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < gp) base[q] += mat[(uint64_t)(q + 1) * n_cta] - mat[(uint64_t)q * n_cta];
+}
+
 // ===========================================================================
 // Voxelization (voxelizer.cpp:168-306)
 //
@@ -1596,6 +1688,28 @@ void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const floa
   KScope k("part_emit", st);
   k_part_emit<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
                                                          (uint32_t)n_parts, cursor, items, use_smem);
+}
+
+uint32_t stream_ctas(uint64_t n) { return (uint32_t)((n + kStreamCta - 1) / kStreamCta); }
+
+void launch_stream_group_chunk(const float* tris, int stride, uint64_t n, const float* axis_lo, const float* axis_hi,
+                               int pa_bits, uint32_t p0, uint32_t gp, uint32_t* mat, uint32_t* mat_partials,
+                               uint64_t* base, float* out, cudaStream_t st) {
+  if (n == 0 || gp == 0) return;
+  const uint32_t n_cta = stream_ctas(n);
+  {
+    KScope k("stream_count", st);
+    k_stream_count<<<n_cta, kStreamCta, gp * sizeof(uint32_t), st>>>(tris, stride, n, axis_lo, axis_hi, pa_bits, p0,
+                                                                     gp, mat, n_cta);
+  }
+  scan_exclusive<uint32_t>(mat, (uint64_t)gp * n_cta + 1, mat_partials, st);
+  {
+    KScope k("stream_emit", st);
+    k_stream_emit<<<n_cta, kStreamCta, 0, st>>>(tris, stride, n, axis_lo, axis_hi, pa_bits, p0, gp, mat, n_cta, base,
+                                                out);
+  }
+  KScope k("stream_advance", st);
+  k_stream_advance<<<grid_for(gp, 256), 256, 0, st>>>(mat, n_cta, gp, base);
 }
 
 // One-stripe occupancy pass with the job as a kernel parameter (the

@@ -37,8 +37,11 @@ def test_two_contexts_on_two_threads():
         builders = (a, b)
         alone = []
         for k, (t, N, limit, kw) in enumerate(meshes):
-            got = builders[k].build(t, _params(t, N, limit, kw))
-            assert not octree.diff(got.tree, want[k])
+            # twice: a context's first build may launch fewer kernels (the large-triangle
+            # task map is built once the context has seen many tasks)
+            for _ in range(2):
+                got = builders[k].build(t, _params(t, N, limit, kw))
+                assert not octree.diff(got.tree, want[k])
             alone.append(builders[k].kernel_launches())
         assert alone[0] > 0 and alone[1] > 0
         timed_alone = set(b.kernel_times())
