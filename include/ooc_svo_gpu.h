@@ -225,6 +225,24 @@ uint64_t ooc_kernel_launches(const ooc_ctx* ctx);
 uint64_t ooc_partition_counts(const ooc_ctx* ctx, uint64_t first, uint64_t n, uint64_t* triangles,
                               uint64_t* filled);
 
+/* ---- Out-of-core builds (main.cpp:294-392: partitions streamed from disk) ----
+ * A one-mesh build (ooc_build, ooc_build_batch of one mesh, ooc_build_files)
+ * of more than one partition whose triangle records exceed the device
+ * triangle budget never holds the mesh in device memory.  A first pass over
+ * the triangles (host memory, or the .tridata file) counts each partition's
+ * records with the reference's box test (partitioner.cpp:101-149); the
+ * partitions are cut into consecutive groups whose records fit half the
+ * budget; before a group's partitions are voxelized, another pass gathers
+ * their records into device memory, each partition's in stream order, as the
+ * reference's .tripdata files hold them.  The output is the in-core build's,
+ * byte for byte.  One partition's records must fit half the budget
+ * (OOC_ERR_LIMIT otherwise).  `bytes` = 0 (the default) makes the budget half
+ * of the device memory free at the start of each build. */
+int ooc_set_stream_budget(ooc_ctx* ctx, uint64_t bytes);
+uint64_t ooc_stream_budget(const ooc_ctx* ctx);
+/* Passes over the triangles of the last build of `ctx` (0: not built out of core). */
+uint64_t ooc_stream_passes(const ooc_ctx* ctx);
+
 /* Host wall-clock milliseconds of the file work of the last ooc_build_files
  * call of `ctx`: [0] reading the .tri header and the .tridata into device
  * memory, [1] writing the octree files after the build (waiting for the
@@ -284,8 +302,10 @@ int ooc_voxelize_occupancy_noalloc(const ooc_build_params* params, const float* 
  * submission (OOC_ERR_LIMIT).  Requests run in
  * continuously formed batches: each of `engines` contexts (own streams and
  * scratch) takes, whenever it is free, every queued request that fits (at
- * most max_batch) and builds them in one batch call (ooc_build_batch, or
- * ooc_build_batch_device for results resident in device memory).  A request
+ * most max_batch) and builds them in one ooc_build_batch_device call, into
+ * device memory from the device's memory pool.  Host results are then copied
+ * into pinned blocks the server keeps for reuse, on a stream of its own, and
+ * their device memory is freed once the copy has landed.  A request
  * completes as soon as its mesh does, not when its batch does.  Each result is
  * byte-identical to ooc_build on that mesh alone.  Device-resident results
  * hold their HBM until released, and count against `memory_budget` until
@@ -303,9 +323,9 @@ typedef struct {
   uint64_t memory_budget;  /* bytes of HBM the requests in flight may hold          */
   /* Fault injection for tests, 0 in normal use: the first batch of two or more
    * requests fails when it reaches its mesh number `fail_batch_at_mesh`
-   * (1-based): the result sink refuses that mesh's bytes (host results) or its
-   * allocation fails as if out of memory (device results).  The batch's
-   * requests not yet complete then run again alone, as after any failed batch. */
+   * (1-based): that mesh's device allocation fails as if out of memory.  The
+   * batch's requests not yet complete then run again alone, as after any failed
+   * batch. */
   uint32_t fail_batch_at_mesh;
   uint32_t reserved;
 } ooc_server_config;

@@ -36,7 +36,8 @@ EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_
            "ooc_server_poll", "ooc_server_release", "ooc_server_destroy", "ooc_build_batch_device",
            "ooc_arena_alloc", "ooc_set_batch_budget", "ooc_batch_budget", "ooc_server_read", "ooc_get_tuning",
            "ooc_set_tuning", "ooc_autotune", "ooc_check_octree_device", "ooc_build_from_device",
-           "ooc_partition_counts", "ooc_file_times")
+           "ooc_partition_counts", "ooc_file_times", "ooc_set_stream_budget", "ooc_stream_budget",
+           "ooc_stream_passes")
 CHECK_BITS = {1: "child group order", 2: "reference count", 4: "depth", 8: "data index", 16: "payload Morton code"}
 
 
@@ -159,6 +160,12 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_partition_counts.restype = ctypes.c_uint64
     lib.ooc_file_times.argtypes = [ctypes.c_void_p, P(ctypes.c_float), ctypes.c_int32]
     lib.ooc_file_times.restype = ctypes.c_int
+    lib.ooc_set_stream_budget.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+    lib.ooc_set_stream_budget.restype = ctypes.c_int
+    lib.ooc_stream_budget.argtypes = [ctypes.c_void_p]
+    lib.ooc_stream_budget.restype = ctypes.c_uint64
+    lib.ooc_stream_passes.argtypes = [ctypes.c_void_p]
+    lib.ooc_stream_passes.restype = ctypes.c_uint64
     lib.ooc_build_files.argtypes = [ctypes.c_void_p, ctypes.c_char_p, P(BuildParams), ctypes.c_char_p,
                                     ctypes.c_uint64, P(BuildInfo)]
     lib.ooc_build_files.restype = ctypes.c_int
@@ -311,6 +318,19 @@ class Builder:
 
     def kernel_launches(self) -> int:
         return int(self.lib.ooc_kernel_launches(self.h))
+
+    def set_stream_budget(self, nbytes: int) -> None:
+        """Device bytes for the triangle records of an out-of-core build (0: half the free device memory)."""
+        self._check(self.lib.ooc_set_stream_budget(self.h, nbytes))
+
+    def stream_passes(self) -> int:
+        """Passes over the triangles of the last build (0: not built out of core)."""
+        return int(self.lib.ooc_stream_passes(self.h))
+
+    def file_times(self) -> dict:
+        arr = (ctypes.c_float * 2)()
+        self._check(self.lib.ooc_file_times(self.h, arr, 2))
+        return {"read": float(arr[0]), "write": float(arr[1])}
 
     def partition_counts(self):
         """(triangles per partition, filled voxels per partition) of the last build's first mesh."""

@@ -100,9 +100,15 @@ def build(verbose: bool = False, force: bool = False) -> str:
     return LIB
 
 
+# Where this build recipe looks for the reference's sources when OOC_REFERENCE is not set:
+# the read-only mount of the container the project is developed in.  The sources are only
+# compiled into oracle/_ref (test infrastructure); nothing else reads them.
+REFERENCE_MOUNT = "/root/reference"
+
+
 def reference_dir() -> str:
-    """Where the reference's sources are read from (OOC_REFERENCE, or the mount of this container)."""
-    return os.environ.get("OOC_REFERENCE", "/root/reference")
+    """Where the reference's sources are read from: OOC_REFERENCE, else REFERENCE_MOUNT."""
+    return os.environ.get("OOC_REFERENCE") or REFERENCE_MOUNT
 
 
 def reference_present() -> bool:

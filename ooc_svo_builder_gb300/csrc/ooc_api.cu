@@ -167,6 +167,12 @@ struct ooc_ctx {
   // the last build's first mesh: triangles binned to each partition, voxels it filled
   std::vector<uint64_t> part_tris, part_filled;
   float file_ms[2] = {0, 0};  // ooc_build_files: input read and upload, output written (host ms)
+  // out-of-core builds: device bytes for streamed triangle records (0: automatic), and their buffers
+  uint64_t stream_budget = 0;
+  DevBuf d_chunk[2], d_group[2], d_stream_mat, d_stream_part, d_stream_base, d_part_off;
+  PinBuf h_stage[2];
+  cudaEvent_t ev_stage[2] = {nullptr, nullptr};
+  uint64_t stream_passes = 0;  // passes over the source in the last build (0: not streamed)
 };
 
 namespace {
@@ -498,6 +504,22 @@ Plan make_plan(const ooc_build_params* p) {
   return pl;
 }
 
+// Triangles of an out-of-core build, read again from the start for every pass:
+// from host memory, or from a .tridata file (the reference streams each
+// partition from its .tripdata file the same way, main.cpp:329-345).
+struct StreamSource {
+  const char* host = nullptr;
+  std::string path;
+  uint64_t n_tris = 0, rec = 0;  // records and bytes per record
+  FILE* f = nullptr;
+  StreamSource() = default;
+  StreamSource(const StreamSource&) = delete;
+  StreamSource& operator=(const StreamSource&) = delete;
+  ~StreamSource() {
+    if (f) std::fclose(f);
+  }
+};
+
 // ---------------------------------------------------------------------------
 // The batch engine.  A batch is a list of meshes; every mesh is split into
 // stripes, and the stripes of all meshes run through one launch sequence (a
@@ -528,6 +550,16 @@ struct MeshWork {
   // voxelization of each piece starts as soon as it is on the device
   std::vector<std::pair<uint64_t, cudaEvent_t>> pieces;
   uint64_t index = 0;        // in the batch
+  // out-of-core: the triangles are read from `src` again for every group of partitions;
+  // the resident group's records (each partition's in stream order) are in d_tris
+  StreamSource* src = nullptr;
+  std::vector<std::pair<uint64_t, uint64_t>> groups;  // consecutive partitions [p0, p1)
+  size_t next_group = 0;
+  uint64_t group_end = 0;         // partitions below this are resident or done
+  uint64_t group_first_item = 0;  // part_off of the resident group's first partition
+  uint64_t resident = 0;          // records in d_tris
+  const float* d_axis = nullptr;  // the partitions' world slabs (stream_count)
+  const uint32_t* d_part_off = nullptr;
   // caller-owned device destination (output to device destinations)
   void* dst_nodes = nullptr;
   void* dst_data = nullptr;
@@ -545,7 +577,8 @@ struct MeshWork {
         layout_next(o.layout_next), filled(o.filled), part_filled(std::move(o.part_filled)), n_items(o.n_items),
         last_stripe(o.last_stripe),
         uploaded(o.uploaded), pieces(std::move(o.pieces)),
-        index(o.index), dst_nodes(o.dst_nodes), dst_data(o.dst_data), dst_ready(o.dst_ready),
+        index(o.index), src(o.src), groups(std::move(o.groups)), next_group(o.next_group), group_end(o.group_end),
+        group_first_item(o.group_first_item), resident(o.resident), d_axis(o.d_axis), d_part_off(o.d_part_off), dst_nodes(o.dst_nodes), dst_data(o.dst_data), dst_ready(o.dst_ready),
         total_nodes(o.total_nodes), total_data(o.total_data), carried_nodes(o.carried_nodes),
         carried_data(o.carried_data) {}
 };
@@ -882,6 +915,10 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     }
   }, pieces != nullptr);  // waits on the upload stream are not captured
   wait_level_counts(st, idle);
+  // the host lays out phase B next; the previous sub-batch's landed records keep moving meanwhile
+  auto pump = [&]() {
+    if (idle) idle();
+  };
   uint64_t tasks_seen;
   std::memcpy(&tasks_seen, lvl + (uint64_t)n * 16 + 8, 8);
   c->max_tasks = std::max(c->max_tasks, tasks_seen);
@@ -935,6 +972,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       tb.push(tb.top, ph);
     }
   }
+  pump();
   // ---- per-node arrays and output windows ----
   bool any_levels = false, any_payload = false;
   for (auto& m : meshes) {
@@ -1009,7 +1047,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     e.dstart = dstart;
     e.cache = m.pl.levels ? cache : nullptr;
     e.leaf_inline = (!m.pl.binary && !m.pl.levels) ? 1 : 0;
-    e.n_tris = m.n_tris;
+    e.n_tris = m.resident;
     e.flag = flag;
     e.node_base = q.node_base;
     e.data_base = q.data_base;
@@ -1047,6 +1085,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     while (ls + 1 <= P.depth - 1 && P.lv[ls + 1].n <= 256) ls++;
     e.l_small = ls;
   }
+  pump();
   auto live = [&](uint32_t s) { return !pl[s].empty; };
   const std::vector<uint64_t> cp_pay = cta_prefix(n, kChunk, [&](uint32_t s) -> uint64_t {
     return meshes[sb[s].mesh].pl.binary ? 0 : sb[s].n_items;
@@ -1077,6 +1116,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       const int last_top = std::min(ej[s].l_small, pyr[s].depth - 2);
       return (live(s) && l > last_top && l <= pyr[s].depth - 2) ? pyr[s].lv[l + 1].n : 0;  // one thread per child
     });
+  pump();
   Uploader up2;
   const size_t o_vj2 = up2.add(vj.data(), n * sizeof(VoxJob));
   const size_t o_pyr2 = up2.add(pyr.data(), n * sizeof(Pyramid));
@@ -1270,6 +1310,161 @@ void bin_mesh(ooc_ctx* c, cudaStream_t st, MeshWork& m, DevBuf& items_buf) {
   m.items = items;
 }
 
+// ---------------------------------------------------------------------------
+// Out-of-core builds.  A mesh whose triangle records do not fit the device
+// triangle budget is read in chunks: a first pass counts every partition's
+// records (K1's box test), the partitions are cut into consecutive groups
+// whose records fit half the budget, and before a group's stripes run, a pass
+// over the source gathers that group's records into one of two device buffers,
+// each partition's records contiguous and in stream order.  The sub-batches of
+// a group read them there; the other buffer holds the previous group until its
+// sub-batches are done (stream order on `st`).
+// ---------------------------------------------------------------------------
+constexpr uint64_t kStreamChunkBytes = 256ull << 20;  // one chunk of the source on the device
+constexpr uint64_t kStreamMatMax = 1ull << 24;        // count-matrix entries of one chunk
+
+uint64_t stream_budget(ooc_ctx* c) {
+  if (c->stream_budget) return c->stream_budget;
+  size_t free_b = 0, total_b = 0;
+  ck(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+  return free_b / 2;
+}
+
+// Whether a one-mesh build of `bytes` of triangle records over P partitions streams.
+bool wants_stream(ooc_ctx* c, uint64_t bytes, uint64_t P) { return P > 1 && bytes > stream_budget(c); }
+
+// One pass over the source, chunk by chunk: each chunk is copied into one of two
+// device buffers on `st` (a file through two pinned staging buffers) and handed
+// to use(device chunk, records).
+template <typename F>
+void stream_pass(ooc_ctx* c, cudaStream_t st, StreamSource& src, uint64_t chunk, F&& use) {
+  c->stream_passes++;
+  const uint64_t max_bytes = std::max<uint64_t>(1, std::min(chunk, src.n_tris)) * src.rec;
+  char* dev[2] = {ensure<char>(c->d_chunk[0], max_bytes), ensure<char>(c->d_chunk[1], max_bytes)};
+  char* pin[2] = {nullptr, nullptr};
+  if (!src.path.empty()) {
+    if (!src.f) src.f = std::fopen(src.path.c_str(), "rb");
+    if (!src.f) fail(OOC_ERR_IO, "cannot open " + src.path);
+    std::rewind(src.f);
+    for (int b = 0; b < 2; b++) {
+      pin[b] = ensure_pinned<char>(c->h_stage[b], max_bytes);
+      if (!c->ev_stage[b]) ck(cudaEventCreateWithFlags(&c->ev_stage[b], cudaEventDisableTiming), "cudaEventCreate");
+    }
+  }
+  uint64_t i = 0;
+  for (uint64_t t0 = 0; t0 < src.n_tris; t0 += chunk, i++) {
+    const uint64_t n = std::min(chunk, src.n_tris - t0);
+    const int b = (int)(i & 1);
+    if (src.f) {
+      ck(cudaEventSynchronize(c->ev_stage[b]), "staging");  // the buffer's last upload is done
+      if (std::fread(pin[b], (size_t)src.rec, (size_t)n, src.f) != n) fail(OOC_ERR_IO, "short read of " + src.path);
+      ck(cudaMemcpyAsync(dev[b], pin[b], n * src.rec, cudaMemcpyHostToDevice, st), "H2D");
+      ck(cudaEventRecord(c->ev_stage[b], st), "event");
+    } else {
+      ck(cudaMemcpyAsync(dev[b], src.host + t0 * src.rec, n * src.rec, cudaMemcpyHostToDevice, st), "H2D");
+    }
+    use(reinterpret_cast<const float*>(dev[b]), n);
+  }
+}
+
+// The partitions' world slabs along each axis (createBuffers, partitioner.cpp:56-61).
+float* upload_axis_boxes(ooc_ctx* c, cudaStream_t st, const Plan& pl) {
+  const int PA = 1 << pl.kP;
+  const uint64_t side = pl.N / PA;
+  std::vector<float> axis(6 * PA);
+  for (int a = 0; a < 3; a++)
+    for (int jj = 0; jj < PA; jj++) {
+      axis[a * PA + jj] = (float)(uint32_t)(jj * side) * pl.u;
+      axis[3 * PA + a * PA + jj] = (float)(uint32_t)((jj + 1) * side) * pl.u;
+    }
+  float* d_axis = ensure<float>(c->d_axis, axis.size() * 4);
+  ck(cudaMemcpyAsync(d_axis, axis.data(), axis.size() * 4, cudaMemcpyHostToDevice, st), "axis boxes");
+  ck(cudaStreamSynchronize(st), "axis boxes");  // `axis` is a local
+  return d_axis;
+}
+
+// First pass: records per partition (the reference's part_tricounts) and the groups.
+void stream_count(ooc_ctx* c, cudaStream_t st, MeshWork& m) {
+  const Plan& pl = m.pl;
+  PhaseScope ph(c, PH_BIN, st);
+  const int PA = 1 << pl.kP;
+  const float* d_axis = upload_axis_boxes(c, st, pl);
+  uint32_t* hist = ensure<uint32_t>(c->d_hist, pl.P * 4);
+  ck(cudaMemsetAsync(hist, 0, pl.P * 4, st), "memset hist");
+  const int stride = pl.binary ? 9 : 21;
+  stream_pass(c, st, *m.src, std::max<uint64_t>(1, kStreamChunkBytes / m.src->rec), [&](const float* d, uint64_t n) {
+    launch_part_count(d, stride, n, d_axis, d_axis + 3 * PA, pl.kP, pl.P, hist, st);
+  });
+  std::vector<uint32_t> h(pl.P);
+  ck(cudaMemcpyAsync(h.data(), hist, pl.P * 4, cudaMemcpyDeviceToHost, st), "hist");
+  ck(cudaStreamSynchronize(st), "counts");
+  m.part_off.assign(pl.P + 1, 0);
+  uint64_t acc = 0;
+  for (uint64_t i = 0; i < pl.P; i++) {
+    m.part_off[i] = (uint32_t)acc;
+    acc += h[i];
+    if (acc >= (1ull << 32)) fail(OOC_ERR_INVALID, "more than 2^32 (triangle, partition) pairs");
+  }
+  m.part_off[pl.P] = (uint32_t)acc;
+  m.n_items = acc;
+  uint32_t* d_off = ensure<uint32_t>(c->d_part_off, (pl.P + 1) * 4);
+  ck(cudaMemcpyAsync(d_off, m.part_off.data(), (pl.P + 1) * 4, cudaMemcpyHostToDevice, st), "partition offsets");
+  ck(cudaStreamSynchronize(st), "partition offsets");
+  m.d_part_off = d_off;
+  m.d_axis = d_axis;
+  // consecutive partitions whose records fit half the budget (the other half holds the previous group)
+  const uint64_t half = stream_budget(c) / 2;
+  m.groups.clear();
+  uint64_t p0 = 0, bytes = 0;
+  for (uint64_t p = 0; p < pl.P; p++) {
+    const uint64_t b = (uint64_t)h[p] * m.src->rec;
+    if (b > half)
+      fail(OOC_ERR_LIMIT, "partition " + std::to_string(p) + " holds " + std::to_string(b) +
+                              " bytes of triangles, more than half the device triangle budget");
+    if (p > p0 && (bytes + b > half || p - p0 == kStreamMaxGroup)) {
+      m.groups.push_back({p0, p});
+      p0 = p;
+      bytes = 0;
+    }
+    bytes += b;
+  }
+  m.groups.push_back({p0, pl.P});
+  m.next_group = 0;
+  m.group_end = 0;
+}
+
+// A later pass: the records of the group holding partition `part`, gathered into a device buffer.
+void stream_group(ooc_ctx* c, cudaStream_t st, MeshWork& m, uint64_t part) {
+  while (m.next_group < m.groups.size() && m.groups[m.next_group].second <= part) m.next_group++;
+  if (m.next_group == m.groups.size()) fail(OOC_ERR_DEVICE, "internal: partition outside every group");
+  const size_t g = m.next_group++;
+  const uint64_t p0 = m.groups[g].first, p1 = m.groups[g].second;
+  const uint32_t gp = (uint32_t)(p1 - p0);
+  const Plan& pl = m.pl;
+  PhaseScope ph(c, PH_BIN, st);
+  const int PA = 1 << pl.kP;
+  const int stride = pl.binary ? 9 : 21;
+  const float* d_axis = m.d_axis;
+  const uint64_t records = (uint64_t)m.part_off[p1] - m.part_off[p0];
+  float* out = ensure<float>(c->d_group[g & 1], std::max<uint64_t>(records, 1) * m.src->rec);
+  uint64_t* d_base = ensure<uint64_t>(c->d_stream_base, (uint64_t)gp * 8);
+  launch_stream_bases(m.d_part_off, (uint32_t)p0, gp, d_base, st);
+  const uint64_t chunk = std::max<uint64_t>(
+      kStreamCtaTris, std::min(kStreamChunkBytes / m.src->rec, kStreamMatMax / gp * kStreamCtaTris));
+  const uint64_t mat_n = (uint64_t)gp * stream_ctas(chunk) + 1;
+  uint32_t* mat = ensure<uint32_t>(c->d_stream_mat, mat_n * 4);
+  uint32_t* mat_part = ensure<uint32_t>(c->d_stream_part, scan_partials_needed(mat_n) * 4);
+  stream_pass(c, st, *m.src, chunk, [&](const float* d, uint64_t n) {
+    launch_stream_group_chunk(d, stride, n, d_axis, d_axis + 3 * PA, pl.kP, (uint32_t)p0, gp, mat, mat_part, d_base,
+                              out, st);
+  });
+  m.d_tris = out;
+  m.items = nullptr;
+  m.group_first_item = m.part_off[p0];
+  m.group_end = p1;
+  m.resident = records;
+}
+
 // Last records of a mesh whose stripes are all done: empty stripes after the
 // last one with items, then the root, written last (finalizeTree,
 // OctreeBuilder.cpp:34-55).
@@ -1287,7 +1482,10 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, co
   if (c->d_mesh_items.size() < meshes.size()) c->d_mesh_items.resize(meshes.size());
   for (size_t i = 0; i < meshes.size(); i++) {
     MeshWork& m = meshes[i];
-    if (m.pl.P > 1) {
+    if (!m.src) m.resident = m.n_tris;
+    if (m.pl.P > 1 && m.src) {
+      stream_count(c, st, m);
+    } else if (m.pl.P > 1) {
       if (m.uploaded) ck(cudaStreamWaitEvent(st, m.uploaded, 0), "wait upload");
       bin_mesh(c, st, m, c->d_mesh_items[i]);
     } else {
@@ -1352,9 +1550,14 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, co
     MeshWork& m = meshes[mi];
     for (uint64_t s = 0; s < m.pl.n_stripes; s++) {
       const uint64_t part = s / m.pl.stripes_per_part;
-      const uint64_t ibeg = m.pl.P > 1 ? m.part_off[part] : 0;
       const uint64_t cnt = items_of(m, s);
       if (cnt == 0) continue;  // main.cpp:330: partitions without triangles are skipped
+      if (m.src && part >= m.group_end) {
+        // out of core: the launched sub-batches read the previous group; gather the next
+        if (!sb.empty()) flush();
+        stream_group(c, st, m, part);
+      }
+      const uint64_t ibeg = m.pl.P > 1 ? m.part_off[part] - m.group_first_item : 0;
       Level tmp[kMaxLevels];
       uint64_t w = 0, b = 0;
       pyramid_levels(m.pl.Ds, tmp, w, w, b, false);
@@ -1447,6 +1650,7 @@ void kernel_end(void* user, const char* name, cudaStream_t st) {
 
 void begin_build(ooc_ctx* c) {
   ck(cudaSetDevice(c->device), "cudaSetDevice");
+  c->stream_passes = 0;
   c->part_tris.clear();
   c->part_filled.clear();
   // a build that failed part-way may have left copies queued into the staging buffers
@@ -1499,6 +1703,62 @@ void set_ctx_file_times(ooc_ctx* c, float read_ms, float write_ms) {
   if (!c) return;
   c->file_ms[0] = read_ms;
   c->file_ms[1] = write_ms;
+}
+}  // namespace ooc
+
+namespace {
+struct SingleSink {
+  ooc_sink_fn sink;
+  void* user;
+};
+int single_sink(void* user, uint64_t, int32_t kind, const void* bytes, uint64_t n) {
+  SingleSink* s = static_cast<SingleSink*>(user);
+  return kind == OOC_STREAM_END ? 0 : s->sink(s->user, kind, bytes, n);
+}
+}  // namespace
+
+namespace ooc {
+bool file_wants_stream(ooc_ctx* c, const ooc_build_params* prm, uint64_t n_tris) {
+  if (!c || !prm) return false;
+  try {
+    return wants_stream(c, n_tris * (prm->geometry_only ? 36 : 84),
+                        ooc_estimate_partitions(prm->gridsize, prm->memory_limit_mb));
+  } catch (...) {
+    return false;
+  }
+}
+
+int build_from_file_stream(ooc_ctx* c, const ooc_build_params* prm, const char* tridata, uint64_t n_tris,
+                           ooc_sink_fn sink, void* user, ooc_build_info* info) {
+  return guarded(c, [&] {
+    begin_build(c);
+    check_params(prm, n_tris);
+    if (!sink) fail(OOC_ERR_INVALID, "sink is NULL");
+    cudaStream_t st = c->own_stream;
+    SingleSink ss{sink, user};
+    Emitter out;
+    out.sink = single_sink;
+    out.user = &ss;
+    StreamSource src;
+    src.path = tridata;
+    src.n_tris = n_tris;
+    src.rec = prm->geometry_only ? 36 : 84;
+    std::vector<MeshWork> meshes;
+    meshes.emplace_back(make_plan(prm), &out);
+    meshes[0].prm = prm;
+    meshes[0].n_tris = n_tris;
+    meshes[0].src = &src;
+    {
+      PhaseScope all(c, PH_ALL, st);
+      OutSpec os;
+      os.mode = OUT_HOST;
+      build_meshes(c, st, meshes, os);
+    }
+    ck(cudaStreamSynchronize(st), "build");
+    ck(cudaGetLastError(), "build kernels");
+    fill_info(meshes[0], info);
+    finish_timing(c);
+  });
 }
 }  // namespace ooc
 
@@ -1585,16 +1845,6 @@ uint64_t ooc_estimate_partitions(uint64_t gridsize, uint64_t memory_limit_mb) {
   return n;
 }
 
-namespace {
-struct SingleSink {
-  ooc_sink_fn sink;
-  void* user;
-};
-int single_sink(void* user, uint64_t, int32_t kind, const void* bytes, uint64_t n) {
-  SingleSink* s = static_cast<SingleSink*>(user);
-  return kind == OOC_STREAM_END ? 0 : s->sink(s->user, kind, bytes, n);
-}
-}  // namespace
 
 int ooc_build(ooc_ctx* c, const ooc_build_params* prm, const float* tris_host, uint64_t n_tris, ooc_sink_fn sink,
               void* user, ooc_build_info* info) {
@@ -1623,6 +1873,7 @@ struct BatchInput {
   std::vector<Emitter> outs;
   std::vector<MeshWork> meshes;
   unsigned char* d_all = nullptr;
+  StreamSource src;  // a one-mesh call whose triangles exceed the device triangle budget
 
   BatchInput(ooc_ctx* c, const ooc_mesh* in, uint64_t n, bool device_records) : off(n + 1, 0), outs(n) {
     if (n && !in) fail(OOC_ERR_INVALID, "meshes are NULL");
@@ -1630,6 +1881,14 @@ struct BatchInput {
       check_params(&in[i].params, in[i].n_tris);
       if (in[i].n_tris && !in[i].tris) fail(OOC_ERR_INVALID, "triangles are NULL");
       off[i + 1] = off[i] + (bytes(in[i]) + 255) / 256 * 256;
+    }
+    const bool streamed = n == 1 && wants_stream(c, bytes(in[0]), ooc_estimate_partitions(
+                                                                       in[0].params.gridsize, in[0].params.memory_limit_mb));
+    if (streamed) {
+      src.host = static_cast<const char*>(static_cast<const void*>(in[0].tris));
+      src.n_tris = in[0].n_tris;
+      src.rec = in[0].params.geometry_only ? 36 : 84;
+      std::fill(off.begin(), off.end(), 0);
     }
     d_all = ensure<unsigned char>(c->d_tris, off[n]);
     meshes.reserve(n);
@@ -1641,6 +1900,10 @@ struct BatchInput {
       meshes.back().d_tris = reinterpret_cast<const float*>(d_all + off[i]);
       meshes.back().n_tris = in[i].n_tris;
       meshes.back().index = i;
+      if (streamed) {
+        meshes.back().src = &src;
+        meshes.back().d_tris = nullptr;
+      }
     }
   }
   static uint64_t bytes(const ooc_mesh& m) { return m.n_tris * (m.params.geometry_only ? 9 : 21) * 4; }
@@ -1669,6 +1932,7 @@ struct BatchInput {
       const uint64_t nb = bytes(in[i]);
       MeshWork& m = meshes[i];
       m.pieces.clear();
+      if (m.src) continue;  // out of core: read group by group during the build
       if (m.pl.P == 1 && nb > 2 * kGroup) {
         const uint64_t rec = nb / in[i].n_tris, per = kGroup / rec;  // triangles per piece
         for (uint64_t t0 = 0; t0 < in[i].n_tris; t0 += per) {
@@ -1965,6 +2229,7 @@ int ooc_build_from_device(ooc_ctx* c, const ooc_build_params* prm, const float* 
   });
 }
 
+
 int ooc_result_device(ooc_ctx* c, const void** nodes_device, const void** data_device) {
   if (!c) return OOC_ERR_INVALID;
   if (!c->res_valid) {
@@ -2010,6 +2275,16 @@ uint64_t ooc_partition_counts(const ooc_ctx* c, uint64_t first, uint64_t n, uint
   }
   return P;
 }
+
+int ooc_set_stream_budget(ooc_ctx* c, uint64_t bytes) {
+  if (!c) return OOC_ERR_INVALID;
+  c->stream_budget = bytes;
+  return OOC_OK;
+}
+
+uint64_t ooc_stream_budget(const ooc_ctx* c) { return c ? c->stream_budget : 0; }
+
+uint64_t ooc_stream_passes(const ooc_ctx* c) { return c ? c->stream_passes : 0; }
 
 int ooc_file_times(const ooc_ctx* c, float* ms, int32_t n) {
   if (!c || !ms || n < 0) return OOC_ERR_INVALID;

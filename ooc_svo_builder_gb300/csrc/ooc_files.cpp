@@ -213,12 +213,23 @@ extern "C" int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_bui
   }
   const int stride = prm.geometry_only ? 9 : 21;
   const size_t bytes = (size_t)h.n_triangles * stride * sizeof(float);
+  // out of core: the .tridata is read group of partitions by group, never whole
+  const bool streamed = ooc::file_wants_stream(ctx, &prm, h.n_triangles);
   void* tris = nullptr;
-  if (bytes && cudaMalloc(&tris, bytes) != cudaSuccess) {
+  if (streamed) {
+    FILE* probe = std::fopen((h.base + ".tridata").c_str(), "rb");
+    long size = -1;
+    if (probe && std::fseek(probe, 0, SEEK_END) == 0) size = std::ftell(probe);
+    if (probe) std::fclose(probe);
+    if (!probe || size < 0 || (uint64_t)size < bytes) {
+      ooc::set_ctx_error(ctx, probe ? "short read of " + h.base + ".tridata" : "cannot open " + h.base + ".tridata");
+      return OOC_ERR_IO;
+    }
+  } else if (bytes && cudaMalloc(&tris, bytes) != cudaSuccess) {
     ooc::set_ctx_error(ctx, "cannot allocate " + std::to_string(bytes) + " bytes of device memory for the triangles");
     return OOC_ERR_OOM;
   }
-  if (bytes && !read_to_device(h.base + ".tridata", bytes, tris, err)) {
+  if (!streamed && bytes && !read_to_device(h.base + ".tridata", bytes, tris, err)) {
     cudaFree(tris);
     ooc::set_ctx_error(ctx, err);
     return OOC_ERR_IO;
@@ -239,7 +250,10 @@ extern "C" int ooc_build_files(ooc_ctx* ctx, const char* tri_path, const ooc_bui
   } else {
     FileWriter wn(fn), wd(fd);
     FileWriter* w[2] = {&wn, &wd};
-    rc = ooc_build_from_device(ctx, &prm, static_cast<const float*>(tris), h.n_triangles, writer_sink, w, &local);
+    rc = streamed ? ooc::build_from_file_stream(ctx, &prm, (h.base + ".tridata").c_str(), h.n_triangles, writer_sink,
+                                                w, &local)
+                  : ooc_build_from_device(ctx, &prm, static_cast<const float*>(tris), h.n_triangles, writer_sink, w,
+                                          &local);
     t_write = clock::now();
     const bool ok_n = wn.finish(), ok_d = wd.finish();
     if (rc == OOC_OK && !(ok_n && ok_d)) {

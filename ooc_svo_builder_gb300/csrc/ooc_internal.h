@@ -7,7 +7,7 @@
 
 #include <string>
 
-struct ooc_ctx;
+#include "ooc_svo_gpu.h"
 
 namespace ooc {
 
@@ -121,6 +121,11 @@ constexpr uint32_t kChunk = 256;
 
 // The message ooc_last_error returns for `c` (for failures found outside ooc_api.cu).
 void set_ctx_error(ooc_ctx* c, const std::string& msg);
+// ooc_build_files' out-of-core path: whether a mesh of n_tris records streams, and the
+// build that reads them from the .tridata file partition group by partition group.
+bool file_wants_stream(ooc_ctx* c, const ooc_build_params* prm, uint64_t n_tris);
+int build_from_file_stream(ooc_ctx* c, const ooc_build_params* prm, const char* tridata, uint64_t n_tris,
+                           ooc_sink_fn sink, void* user, ooc_build_info* info);
 // ooc_file_times' values for `c` (set by ooc_build_files).
 void set_ctx_file_times(ooc_ctx* c, float read_ms, float write_ms);
 
@@ -168,7 +173,10 @@ void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const floa
 // past them.  `mat` holds gp * stream_ctas(n) + 1 entries, `mat_partials`
 // scan_partials_needed of that.
 constexpr uint32_t kStreamMaxGroup = 4096;
+constexpr uint64_t kStreamCtaTris = 64;  // triangles per CTA of the group binning
 uint32_t stream_ctas(uint64_t n);
+// base[q] = part_off[p0 + q] - part_off[p0] for q < gp: where each group partition's records start.
+void launch_stream_bases(const uint32_t* part_off, uint32_t p0, uint32_t gp, uint64_t* base, cudaStream_t st);
 void launch_stream_group_chunk(const float* tris, int stride, uint64_t n, const float* axis_lo, const float* axis_hi,
                                int pa_bits, uint32_t p0, uint32_t gp, uint32_t* mat, uint32_t* mat_partials,
                                uint64_t* base, float* out, cudaStream_t st);

@@ -298,7 +298,7 @@ __global__ void k_part_emit(const float* __restrict__ tris, int stride, uint64_t
 // triangle.  CTAs of kStreamCta triangles; mat[q * n_cta + cta] is CTA cta's
 // count for group partition q, whose exclusive scan places every CTA's records.
 // ---------------------------------------------------------------------------
-constexpr int kStreamCta = 64;
+constexpr int kStreamCta = (int)kStreamCtaTris;
 
 // Per-axis partition runs of triangle t, packed 7 bits per bound with bit 63 set,
 // or 0 when the triangle passes no partition's box test.
@@ -372,6 +372,12 @@ __global__ void __launch_bounds__(kStreamCta) k_stream_emit(const float* __restr
         float* d = out + dst * (uint64_t)stride;
         for (int k = 0; k < stride; k++) d[k] = src[k];
       }
+}
+
+__global__ void k_stream_bases(const uint32_t* __restrict__ part_off, uint32_t p0, uint32_t gp,
+                               uint64_t* __restrict__ base) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < gp) base[q] = (uint64_t)(part_off[p0 + q] - part_off[p0]);
 }
 
 // After a chunk: every group partition's next record moves past the chunk's records of it.
@@ -1691,6 +1697,12 @@ void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const floa
 }
 
 uint32_t stream_ctas(uint64_t n) { return (uint32_t)((n + kStreamCta - 1) / kStreamCta); }
+
+void launch_stream_bases(const uint32_t* part_off, uint32_t p0, uint32_t gp, uint64_t* base, cudaStream_t st) {
+  if (gp == 0) return;
+  KScope k("stream_bases", st);
+  k_stream_bases<<<grid_for(gp, 256), 256, 0, st>>>(part_off, p0, gp, base);
+}
 
 void launch_stream_group_chunk(const float* tris, int stride, uint64_t n, const float* axis_lo, const float* axis_hi,
                                int pa_bits, uint32_t p0, uint32_t gp, uint32_t* mat, uint32_t* mat_partials,

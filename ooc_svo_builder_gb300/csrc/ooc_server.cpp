@@ -6,10 +6,12 @@
 // max_batch) and builds them with one batch call; requests that arrive
 // meanwhile wait for the next free engine.  With two or more engines, one
 // batch's device work overlaps the next batch's.  A request completes as soon
-// as its own mesh does.  Results either come back to host memory (through the
-// library's copy-back ring) or stay resident in device memory, allocated
-// stream-ordered from the device's memory pool, until the caller releases
-// them.  Apart from that allocation the server uses only the public C ABI.
+// as its own mesh does.  Every batch is built into device memory, allocated
+// stream-ordered from the device's memory pool.  Resident results stay there
+// until the caller releases them; host results are copied into pinned blocks of
+// a pool the server keeps, on a stream of its own, and a delivery thread frees
+// their device memory and publishes them once the copy has landed.  Apart from
+// those allocations the server uses only the public C ABI.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -31,35 +33,53 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
-// Growable host buffer.  realloc of a large block remaps its pages instead of
-// copying them, so appending a result piece by piece costs one copy.
-struct Bytes {
-  char* p = nullptr;
-  size_t n = 0, cap = 0;
-  Bytes() = default;
-  Bytes(const Bytes&) = delete;
-  Bytes& operator=(const Bytes&) = delete;
-  ~Bytes() { std::free(p); }
-  bool append(const void* src, size_t k) {
-    if (n + k > cap) {
-      size_t nc = std::max<size_t>(std::max<size_t>(cap + cap / 2, n + k), 1 << 16);
-      char* q = static_cast<char*>(std::realloc(p, nc));
-      if (!q) return false;
-      p = q;
-      cap = nc;
-    }
-    std::memcpy(p + n, src, k);
-    n += k;
-    return true;
+// Pinned host blocks for host results, kept and reused across requests
+// (pinning memory costs far more than copying into it): power-of-two size
+// classes from 64 KiB.
+class PinnedPool {
+ public:
+  ~PinnedPool() {
+    for (auto& kv : free_)
+      for (void* p : kv.second) cudaFreeHost(p);
   }
-  void clear() { n = 0; }
+  void* get(size_t n, size_t& cap) {
+    cap = klass(n);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      auto it = free_.find(cap);
+      if (it != free_.end() && !it->second.empty()) {
+        void* p = it->second.back();
+        it->second.pop_back();
+        return p;
+      }
+    }
+    void* p = nullptr;
+    return cudaMallocHost(&p, cap) == cudaSuccess ? p : nullptr;
+  }
+  void put(void* p, size_t cap) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(mu_);
+    free_[cap].push_back(p);
+  }
+
+ private:
+  static size_t klass(size_t n) {
+    size_t c = 64 << 10;
+    while (c < n) c <<= 1;
+    return c;
+  }
+  std::mutex mu_;
+  std::unordered_map<size_t, std::vector<void*>> free_;
 };
 
 struct Request {
   uint64_t id = 0;
   ooc_mesh mesh;
   uint64_t footprint = 0;
-  Bytes nodes, data;                          // host results
+  void* h_nodes = nullptr;                    // host results (pinned pool blocks)
+  void* h_data = nullptr;
+  size_t h_nodes_cap = 0, h_data_cap = 0;
+  uint64_t h_nodes_bytes = 0, h_data_bytes = 0;
   void* d_nodes = nullptr;                    // device results
   void* d_data = nullptr;
   uint64_t d_nodes_bytes = 0, d_data_bytes = 0;
@@ -137,6 +157,14 @@ struct ooc_server {
   std::vector<ooc_ctx*> engines;
   std::vector<std::thread> threads;
   cudaStream_t release_stream = nullptr;  // device results are freed on it
+  cudaStream_t d2h_stream = nullptr;      // host results are copied back on it
+  PinnedPool pinned;
+  // host results whose copy back is queued, in order, with the event after it
+  std::deque<std::pair<Request*, cudaEvent_t>> deliveries;
+  std::vector<cudaEvent_t> spare_events;
+  std::condition_variable cv_deliver;
+  std::thread deliverer;
+  bool stop_delivery = false;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Request*> queue;
@@ -189,18 +217,6 @@ struct ooc_server {
     call.s->publish(r, OOC_OK);
   }
 
-  static int sink(void* user, uint64_t mesh, int32_t kind, const void* bytes, uint64_t n) {
-    Call& call = *static_cast<Call*>(user);
-    Request* r = call.reqs[mesh];
-    if (kind == OOC_STREAM_END) {
-      mark(call, mesh);
-      return 0;
-    }
-    if (injected_failure(call, mesh)) return 1;
-    Bytes& dst = kind == OOC_STREAM_NODES ? r->nodes : r->data;
-    return dst.append(bytes, n) ? 0 : 1;
-  }
-
   static int alloc(void* user, uint64_t mesh, uint64_t nodes_bytes, uint64_t data_bytes, void* stream, void** nodes,
                    void** data) {
     Call& call = *static_cast<Call*>(user);
@@ -217,8 +233,78 @@ struct ooc_server {
   }
 
   static int ready(void* user, uint64_t mesh) {
-    mark(*static_cast<Call*>(user), mesh);
+    Call& call = *static_cast<Call*>(user);
+    if (call.s->cfg.result_location == OOC_RESULT_DEVICE) {
+      mark(call, mesh);
+      return 0;
+    }
+    // host results: the mesh is complete in this batch (never rerun); it is published
+    // once its copy into pinned memory has landed
+    Request* r = call.reqs[mesh];
+    r->info = call.infos[mesh];
+    (*call.published)[call.index[mesh]] = 1;
+    call.s->deliver(r);
     return 0;
+  }
+
+  // Queue a host result's copy back into pinned pool blocks on d2h_stream.
+  void deliver(Request* r) {
+    r->h_nodes_bytes = r->d_nodes_bytes;
+    r->h_data_bytes = r->d_data_bytes;
+    bool ok = true;
+    if (r->h_nodes_bytes) ok = (r->h_nodes = pinned.get(r->h_nodes_bytes, r->h_nodes_cap)) != nullptr;
+    if (ok && r->h_data_bytes) ok = (r->h_data = pinned.get(r->h_data_bytes, r->h_data_cap)) != nullptr;
+    cudaEvent_t ev = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      if (!spare_events.empty()) {
+        ev = spare_events.back();
+        spare_events.pop_back();
+      }
+    }
+    if (ok && !ev) ok = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+    if (ok && r->h_nodes_bytes)
+      ok = cudaMemcpyAsync(r->h_nodes, r->d_nodes, r->h_nodes_bytes, cudaMemcpyDeviceToHost, d2h_stream) == cudaSuccess;
+    if (ok && r->h_data_bytes)
+      ok = cudaMemcpyAsync(r->h_data, r->d_data, r->h_data_bytes, cudaMemcpyDeviceToHost, d2h_stream) == cudaSuccess;
+    if (ok) ok = cudaEventRecord(ev, d2h_stream) == cudaSuccess;
+    if (!ok) {
+      if (ev) cudaEventDestroy(ev);
+      cudaStreamSynchronize(d2h_stream);  // nothing of this request stays queued
+      free_device(r);
+      r->d_nodes_bytes = r->d_data_bytes = 0;
+      publish(r, OOC_ERR_OOM);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      deliveries.push_back({r, ev});
+    }
+    cv_deliver.notify_one();
+  }
+
+  // Publishes host results in the order their copies were queued, once each has landed.
+  void delivery_loop() {
+    cudaSetDevice(cfg.device);
+    for (;;) {
+      std::pair<Request*, cudaEvent_t> d;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_deliver.wait(lk, [&] { return stop_delivery || !deliveries.empty(); });
+        if (deliveries.empty()) return;
+        d = deliveries.front();
+        deliveries.pop_front();
+      }
+      const bool ok = cudaEventSynchronize(d.second) == cudaSuccess;
+      Request* r = d.first;
+      free_device(r);
+      r->d_nodes_bytes = r->d_data_bytes = 0;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        spare_events.push_back(d.second);
+      }
+      publish(r, ok ? OOC_OK : OOC_ERR_DEVICE);
+    }
   }
 
   void free_device(Request* r) {
@@ -237,25 +323,18 @@ struct ooc_server {
       Request* r = batch[index[i]];
       call.reqs.push_back(r);
       meshes[i] = r->mesh;
-      r->nodes.clear();
-      r->data.clear();
     }
-    int rc;
-    if (cfg.result_location == OOC_RESULT_DEVICE) {
-      rc = ooc_build_batch_device(ctx, meshes.data(), meshes.size(), &ooc_server::alloc, &ooc_server::ready, &call,
-                                  call.infos.data());
-      if (rc != OOC_OK) {
-        // the failed call may have left writes queued into the destinations
-        cudaSetDevice(cfg.device);
-        cudaDeviceSynchronize();
-        for (size_t i = 0; i < index.size(); i++)
-          if (!published[index[i]]) {
-            free_device(call.reqs[i]);
-            call.reqs[i]->d_nodes_bytes = call.reqs[i]->d_data_bytes = 0;
-          }
-      }
-    } else {
-      rc = ooc_build_batch(ctx, meshes.data(), meshes.size(), &ooc_server::sink, &call, call.infos.data());
+    const int rc = ooc_build_batch_device(ctx, meshes.data(), meshes.size(), &ooc_server::alloc, &ooc_server::ready,
+                                          &call, call.infos.data());
+    if (rc != OOC_OK) {
+      // the failed call may have left writes queued into the destinations
+      cudaSetDevice(cfg.device);
+      cudaDeviceSynchronize();
+      for (size_t i = 0; i < index.size(); i++)
+        if (!published[index[i]]) {
+          free_device(call.reqs[i]);
+          call.reqs[i]->d_nodes_bytes = call.reqs[i]->d_data_bytes = 0;
+        }
     }
     return rc;
   }
@@ -332,18 +411,21 @@ int ooc_server_create(const ooc_server_config* cfg, ooc_server** out) {
     }
     s->engines.push_back(c);
   }
-  if (cfg->result_location == OOC_RESULT_DEVICE) {
+  {
     // keep freed result memory in the pool instead of returning it to the driver at every synchronisation
     cudaMemPool_t pool;
     uint64_t keep = ~0ull;
     if (cudaSetDevice(cfg->device) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, cfg->device) != cudaSuccess ||
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&s->release_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamCreateWithFlags(&s->release_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->d2h_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      if (s->release_stream) cudaStreamDestroy(s->release_stream);
       for (ooc_ctx* e : s->engines) ooc_ctx_destroy(e);
       delete s;
       return OOC_ERR_DEVICE;
     }
   }
+  if (cfg->result_location == OOC_RESULT_HOST) s->deliverer = std::thread([s] { s->delivery_loop(); });
   for (ooc_ctx* c : s->engines) s->threads.emplace_back([s, c] { s->engine_loop(c); });
   *out = s;
   return OOC_OK;
@@ -393,10 +475,10 @@ int ooc_server_poll(ooc_server* s, int32_t timeout_ms, ooc_result* out) {
     out->data = r->d_data;
     out->data_bytes = r->status == OOC_OK ? r->d_data_bytes : 0;
   } else {
-    out->nodes = r->nodes.p;
-    out->nodes_bytes = r->nodes.n;
-    out->data = r->data.p;
-    out->data_bytes = r->data.n;
+    out->nodes = r->h_nodes;
+    out->nodes_bytes = r->status == OOC_OK ? r->h_nodes_bytes : 0;
+    out->data = r->h_data;
+    out->data_bytes = r->status == OOC_OK ? r->h_data_bytes : 0;
   }
   out->info = r->info;
   out->t_submit_us = r->t_submit;
@@ -423,8 +505,8 @@ int ooc_server_read(ooc_server* s, uint64_t id, void* nodes_host, void* data_hos
     if (data_host && cudaMemcpy(data_host, r->d_data, r->d_data_bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
       return OOC_ERR_DEVICE;
   } else {
-    if (nodes_host) std::memcpy(nodes_host, r->nodes.p, r->nodes.n);
-    if (data_host) std::memcpy(data_host, r->data.p, r->data.n);
+    if (nodes_host && r->h_nodes_bytes) std::memcpy(nodes_host, r->h_nodes, r->h_nodes_bytes);
+    if (data_host && r->h_data_bytes) std::memcpy(data_host, r->h_data, r->h_data_bytes);
   }
   return OOC_OK;
 }
@@ -444,6 +526,8 @@ int ooc_server_release(ooc_server* s, uint64_t id) {
     cudaSetDevice(s->cfg.device);
     s->free_device(r);
   }
+  s->pinned.put(r->h_nodes, r->h_nodes_cap);
+  s->pinned.put(r->h_data, r->h_data_cap);
   delete r;
   s->cv_work.notify_all();
   return OOC_OK;
@@ -459,20 +543,28 @@ void ooc_server_destroy(ooc_server* s) {
   }
   s->cv_work.notify_all();
   for (std::thread& t : s->threads) t.join();
+  {  // the engines are done: deliver what they queued, then stop
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop_delivery = true;
+  }
+  s->cv_deliver.notify_all();
+  if (s->deliverer.joinable()) s->deliverer.join();
   for (ooc_ctx* c : s->engines) ooc_ctx_destroy(c);
-  if (s->release_stream) cudaSetDevice(s->cfg.device);
-  for (Request* r : s->done) {
+  cudaSetDevice(s->cfg.device);
+  auto drop = [s](Request* r) {
     s->free_device(r);
+    s->pinned.put(r->h_nodes, r->h_nodes_cap);
+    s->pinned.put(r->h_data, r->h_data_cap);
     delete r;
-  }
-  for (auto& kv : s->held) {
-    s->free_device(kv.second);
-    delete kv.second;
-  }
+  };
+  for (Request* r : s->done) drop(r);
+  for (auto& kv : s->held) drop(kv.second);
+  for (cudaEvent_t e : s->spare_events) cudaEventDestroy(e);
   if (s->release_stream) {
     cudaStreamSynchronize(s->release_stream);
     cudaStreamDestroy(s->release_stream);
   }
+  if (s->d2h_stream) cudaStreamDestroy(s->d2h_stream);
   delete s;
 }
 

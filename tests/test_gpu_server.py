@@ -111,10 +111,10 @@ def test_arrivals_while_busy_join_later_batches(mix30, resident):
 
 @pytest.mark.parametrize("resident", [False, True], ids=["host", "device"])
 def test_failed_batch_reruns_its_unfinished_requests_alone(mix40, resident):
-    """The first shared batch fails at its third mesh (fault injection on the host: the
-    result sink refuses it, or its allocation fails as if out of memory).  The batch's
-    first two requests are complete already; every other one runs again alone.  All
-    results still equal the oracle."""
+    """The first shared batch fails at its third mesh (fault injection on the host: that
+    mesh's allocation fails as if out of memory).  The batch's first two requests are
+    complete already; every other one runs again alone.  All results still equal the
+    oracle."""
     reqs, want = mix40
     ids, got = serve_all(reqs, engines=1, max_batch=16, memory_budget=8 << 30, resident=resident,
                          fail_batch_at_mesh=3)
