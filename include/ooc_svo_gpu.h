@@ -171,6 +171,10 @@ typedef struct {
   uint64_t batch_budget;      /* occupancy-pyramid bytes per sub-batch (>= 4096), as ooc_set_batch_budget */
   uint32_t graphs;            /* 1: replay each sub-batch's two launch sequences as CUDA graphs; 0: launch directly */
   uint32_t light_per_thread;  /* elements each thread of the per-block and per-node kernels takes (1..16) */
+  uint32_t pdl;               /* 1: each kernel of a launch sequence may start while its predecessor drains
+                                 (programmatic dependent launch; it waits for the predecessor's results
+                                 before touching memory); 0: it starts when the predecessor has finished */
+  uint32_t reserved;          /* 0 */
 } ooc_tuning;
 
 int ooc_get_tuning(const ooc_ctx* ctx, ooc_tuning* out);

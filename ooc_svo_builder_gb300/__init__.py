@@ -81,7 +81,7 @@ class Result(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("small_vol", ctypes.c_uint32), ("lines_per_lane", ctypes.c_uint32), ("large_block", ctypes.c_uint32),
                 ("large_ctas_per_sm", ctypes.c_uint32), ("batch_budget", ctypes.c_uint64), ("graphs", ctypes.c_uint32),
-                ("light_per_thread", ctypes.c_uint32)]
+                ("light_per_thread", ctypes.c_uint32), ("pdl", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

@@ -148,7 +148,7 @@ struct ooc_ctx {
   std::vector<cudaEvent_t> up_events;    // recorded on h2d_stream as groups of meshes arrive
   DevBuf d_tables1, d_tables2;
   std::vector<DevBuf> d_mesh_items;
-  ooc_tuning tuning = {64, 16, 256, 4, 4ull << 30, 0, 8};  // launch choices (ooc_set_tuning / ooc_autotune)
+  ooc_tuning tuning = {64, 16, 256, 4, 4ull << 30, 0, 8, 1, 0};  // launch choices (ooc_set_tuning / ooc_autotune)
   // executable graphs of captured launch sequences, by shape (launch count and kernels)
   std::vector<std::pair<uint64_t, cudaGraphExec_t>> graph_execs;
   DevBuf d_tune_arena;                               // autotuner outputs
@@ -278,13 +278,17 @@ void run_launches(ooc_ctx* c, cudaStream_t st, int which, F&& launches, bool dir
   }
   ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
   cudaGraph_t graph = nullptr;
+  const bool pdl = c->lstate.pdl;
+  c->lstate.pdl = false;  // captured launches keep plain stream order
   try {
     launches();
   } catch (...) {
+    c->lstate.pdl = pdl;
     cudaStreamEndCapture(st, &graph);
     if (graph) cudaGraphDestroy(graph);
     throw;
   }
+  c->lstate.pdl = pdl;
   ck(cudaStreamEndCapture(st, &graph), "cudaStreamEndCapture");
   // shape key: which sequence, node count, and the kernels in capture order
   size_t count = 0;
@@ -1662,6 +1666,7 @@ void begin_build(ooc_ctx* c) {
   c->ev_used = 0;
   c->res_valid = false;
   c->lstate.launches = 0;
+  c->lstate.pdl = c->tuning.pdl != 0;
   if (c->kfilter.empty()) {
     c->lstate.hooks = KernelHooks();
   } else {
@@ -2060,7 +2065,7 @@ bool tuning_ok(const ooc_tuning& t) {
   return t.small_vol >= 1 && t.small_vol <= 64 && t.lines_per_lane >= 1 && t.lines_per_lane <= 64 &&
          (t.large_block == 64 || t.large_block == 128 || t.large_block == 256) && t.large_ctas_per_sm >= 1 &&
          t.large_ctas_per_sm <= 16 && t.batch_budget >= 4096 && t.graphs <= 1 && t.light_per_thread >= 1 &&
-         t.light_per_thread <= 16;
+         t.light_per_thread <= 16 && t.pdl <= 1 && t.reserved == 0;
 }
 
 struct TuneArena {
@@ -2128,7 +2133,7 @@ int ooc_autotune(ooc_ctx* c, const ooc_mesh* sample, uint64_t n, ooc_tuning* bes
   if (rc == OOC_OK) rc = time_one(cur, cur_ms);
   // one coordinate pass: each choice in turn, the others held at their best so far
   const uint32_t lpl[] = {4, 8, 16, 32}, cps[] = {2, 4, 8}, blk[] = {128, 256}, svol[] = {16, 32, 48, 64}, gr[] = {0, 1},
-                 ept[] = {1, 2, 4, 8};
+                 ept[] = {1, 2, 4, 8}, pdl[] = {0, 1};
   const uint64_t bud[] = {1ull << 30, 2ull << 30, 4ull << 30, 8ull << 30};
   auto try_values = [&](auto setter, const auto& values) {
     for (const auto& v : values) {
@@ -2151,6 +2156,7 @@ int ooc_autotune(ooc_ctx* c, const ooc_mesh* sample, uint64_t n, ooc_tuning* bes
   try_values([](ooc_tuning& t, uint64_t v) { t.batch_budget = v; }, bud);
   try_values([](ooc_tuning& t, uint32_t v) { t.light_per_thread = v; }, ept);
   try_values([](ooc_tuning& t, uint32_t v) { t.graphs = v; }, gr);
+  try_values([](ooc_tuning& t, uint32_t v) { t.pdl = v; }, pdl);
   c->tuning = rc == OOC_OK ? cur : start;
   if (best) *best = c->tuning;
   return rc;

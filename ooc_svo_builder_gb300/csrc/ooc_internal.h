@@ -148,6 +148,7 @@ struct KernelHooks {
 struct LaunchState {
   unsigned long long launches = 0;
   KernelHooks hooks;
+  bool pdl = false;  // launch with programmatic stream serialization (ooc_tuning::pdl)
 };
 LaunchState* current_launch_state();
 struct LaunchScope {

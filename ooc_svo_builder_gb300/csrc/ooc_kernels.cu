@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <utility>
 
 #include "ooc_device.cuh"
 #include "ooc_internal.h"
@@ -38,6 +39,33 @@ struct KScope {
     if (ls && ls->hooks.end) ls->hooks.end(ls->hooks.user, name, st);
   }
 };
+// Programmatic dependent launch.  Every kernel here first waits until the
+// grid before it on the stream has finished and its memory is visible, then
+// lets the grid after it launch, so that grid's CTAs take the SMs this one's
+// last CTAs free instead of waiting for the whole grid to drain.  Without the
+// launch attribute (launch_k with ooc_tuning::pdl off) both are no-ops.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" :::);
+}
+
+// Launch `k` on `st`, with programmatic stream serialization when the calling
+// thread's launch state asks for it.
+template <typename... P, typename... A>
+void launch_k(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A&&... args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = (t_launch && t_launch->pdl) ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
+}
+
 constexpr int SCAN_THREADS = 256;
 
 inline unsigned grid_for(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
@@ -83,6 +111,7 @@ constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 template <typename T>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const T* __restrict__ in, uint64_t n,
                                                               T* __restrict__ partials) {
+  pdl_enter();
   const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
   T v = 0;
 #pragma unroll
@@ -98,6 +127,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const T* __restric
 // Also partials[np] = the grand total.
 template <typename T>
 __global__ void __launch_bounds__(1024) k_scan_partials(T* partials, uint64_t np) {
+  pdl_enter();
   T carry = 0;
   for (uint64_t base = 0; base < np; base += blockDim.x) {
     const uint64_t i = base + threadIdx.x;
@@ -114,6 +144,7 @@ __global__ void __launch_bounds__(1024) k_scan_partials(T* partials, uint64_t np
 // (`partials` NULL: a single tile, nothing before it).
 template <typename T>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(T* data, uint64_t n, const T* __restrict__ partials) {
+  pdl_enter();
   // the elements are counts: a zero total means all zero, which is already their scan
   if (partials && partials[gridDim.x] == T(0)) return;
   __shared__ T tile[SCAN_TILE + SCAN_TILE / 32];
@@ -156,20 +187,20 @@ void scan_exclusive(T* data, uint64_t n, T* partials, cudaStream_t st) {
   const unsigned nb = (unsigned)((n + SCAN_TILE - 1) / SCAN_TILE);
   if (nb == 1) {  // one tile: one launch
     KScope k("scan_down", st);
-    k_scan_down<T><<<1, SCAN_THREADS, 0, st>>>(data, n, nullptr);
+    launch_k(k_scan_down<T>, dim3(1), dim3(SCAN_THREADS), 0, st, data, n, nullptr);
     return;
   }
   {
     KScope k("scan_reduce", st);
-    k_scan_reduce<T><<<nb, SCAN_THREADS, 0, st>>>(data, n, partials);
+    launch_k(k_scan_reduce<T>, dim3(nb), dim3(SCAN_THREADS), 0, st, data, n, partials);
   }
   {
     KScope k("scan_partials", st);
-    k_scan_partials<T><<<1, 1024, 0, st>>>(partials, nb);
+    launch_k(k_scan_partials<T>, dim3(1), dim3(1024), 0, st, partials, nb);
   }
   {
     KScope k("scan_down", st);
-    k_scan_down<T><<<nb, SCAN_THREADS, 0, st>>>(data, n, partials);
+    launch_k(k_scan_down<T>, dim3(nb), dim3(SCAN_THREADS), 0, st, data, n, partials);
   }
 }
 
@@ -210,6 +241,7 @@ __device__ __forceinline__ bool axis_run(float lo, float hi, const float* __rest
 __global__ void k_part_count(const float* __restrict__ tris, int stride, uint64_t n_tris,
                              const float* __restrict__ axis_lo, const float* __restrict__ axis_hi, int pa_bits,
                              uint32_t n_parts, uint32_t* __restrict__ hist, int use_smem) {
+  pdl_enter();
   extern __shared__ uint32_t sh[];
   if (use_smem) {
     for (uint32_t i = threadIdx.x; i < n_parts; i += blockDim.x) sh[i] = 0;
@@ -243,6 +275,7 @@ __global__ void k_part_emit(const float* __restrict__ tris, int stride, uint64_t
                             const float* __restrict__ axis_lo, const float* __restrict__ axis_hi, int pa_bits,
                             uint32_t n_parts, uint32_t* __restrict__ cursor, uint32_t* __restrict__ items,
                             int use_smem) {
+  pdl_enter();
   extern __shared__ uint32_t sh[];  // [n_parts] counts, [n_parts] bases
   uint32_t* cnt = sh;
   uint32_t* base = sh + n_parts;
@@ -322,6 +355,7 @@ __global__ void __launch_bounds__(kStreamCta) k_stream_count(const float* __rest
                                                              const float* __restrict__ axis_hi, int pa_bits,
                                                              uint32_t p0, uint32_t gp, uint32_t* __restrict__ mat,
                                                              uint32_t n_cta) {
+  pdl_enter();
   extern __shared__ uint32_t cnt[];
   for (uint32_t q = threadIdx.x; q < gp; q += kStreamCta) cnt[q] = 0;
   if (blockIdx.x == 0 && threadIdx.x == 0) mat[(uint64_t)gp * n_cta] = 0;  // the scan's total entry
@@ -349,6 +383,7 @@ __global__ void __launch_bounds__(kStreamCta) k_stream_emit(const float* __restr
                                                             uint32_t p0, uint32_t gp, const uint32_t* __restrict__ mat,
                                                             uint32_t n_cta, const uint64_t* __restrict__ base,
                                                             float* __restrict__ out) {
+  pdl_enter();
   __shared__ uint64_t runs[kStreamCta];
   const uint64_t t = (uint64_t)blockIdx.x * kStreamCta + threadIdx.x;
   const uint64_t r = t < n ? stream_runs(tris, stride, t, axis_lo, axis_hi, 1 << pa_bits) : 0ull;
@@ -376,6 +411,7 @@ __global__ void __launch_bounds__(kStreamCta) k_stream_emit(const float* __restr
 
 __global__ void k_stream_bases(const uint32_t* __restrict__ part_off, uint32_t p0, uint32_t gp,
                                uint64_t* __restrict__ base) {
+  pdl_enter();
   const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q < gp) base[q] = (uint64_t)(part_off[p0 + q] - part_off[p0]);
 }
@@ -383,6 +419,7 @@ __global__ void k_stream_bases(const uint32_t* __restrict__ part_off, uint32_t p
 // After a chunk: every group partition's next record moves past the chunk's records of it.
 __global__ void k_stream_advance(const uint32_t* __restrict__ mat, uint32_t n_cta, uint32_t gp,
                                  uint64_t* __restrict__ base) {
+  pdl_enter();
   const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q < gp) base[q] += mat[(uint64_t)(q + 1) * n_cta] - mat[(uint64_t)q * n_cta];
 }
@@ -669,6 +706,7 @@ __device__ __forceinline__ void vox_small_occ_item(const VoxJob& j, uint64_t i) 
 }
 
 __global__ void k_vox_small_occ(VoxJob j) {
+  pdl_enter();
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < j.n_items) vox_small_occ_item(j, i);
 }
@@ -754,6 +792,7 @@ __device__ __forceinline__ void vox_large_task(const VoxJob& j, uint64_t i, uint
 // Persistent warps pull 32-column tasks of large items from a global counter.
 template <int PASS>
 __global__ void __launch_bounds__(256, 4) k_vox_large(VoxJob j) {
+  pdl_enter();
   extern __shared__ uint32_t lines_smem[];  // 32 x lines_per_lane per warp
   const int lane = threadIdx.x & 31;
   uint32_t* wl = lines_smem + (threadIdx.x >> 5) * 32u * j.lines_per_lane;
@@ -1346,6 +1385,7 @@ __device__ void root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base
 }
 
 __global__ void k_scatter_records(const uint64_t* __restrict__ src, uint64_t n, int words, uint64_t* __restrict__ dst) {
+  pdl_enter();
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint64_t* s = src + i * (1 + words);
@@ -1355,6 +1395,7 @@ __global__ void k_scatter_records(const uint64_t* __restrict__ src, uint64_t n, 
 
 // Records with their own destination: src[i] = {address, words...}.
 __global__ void k_scatter_to(const uint64_t* __restrict__ src, uint64_t n, int words) {
+  pdl_enter();
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint64_t* s = src + i * (1 + words);
@@ -1402,6 +1443,7 @@ __device__ __forceinline__ uint32_t cta_stripe(const uint64_t* __restrict__ cta_
 template <int PASS, bool SINGLE>
 __global__ void __launch_bounds__(kChunk, 4) kb_vox_small(const VoxJob* __restrict__ jobs,
                                                        const uint64_t* __restrict__ cta_beg, uint32_t n, VoxJob j0) {
+  pdl_enter();
   if constexpr (SINGLE) {
     const uint64_t i = (uint64_t)blockIdx.x * kChunk + threadIdx.x;
     if (i >= j0.n_items) return;
@@ -1426,6 +1468,7 @@ __global__ void __launch_bounds__(kChunk) kb_task_map(const uint64_t* __restrict
                                                       const uint64_t* __restrict__ item_beg,
                                                       const uint64_t* __restrict__ task_off, uint64_t total_items,
                                                       uint64_t* __restrict__ map, uint64_t cap) {
+  pdl_enter();
   uint64_t cta;
   const uint32_t s = cta_stripe(cta_beg, n, cta);
   if (task_off[total_items] > cap) return;
@@ -1440,6 +1483,7 @@ __global__ void __launch_bounds__(256, 4) kb_vox_large(const VoxJob* __restrict_
                                                     uint64_t total_items, unsigned long long* counter,
                                                     uint32_t lines_per_lane, const uint64_t* __restrict__ map,
                                                     uint64_t cap) {
+  pdl_enter();
   extern __shared__ uint32_t lines_smem[];  // 32 x lines_per_lane per warp (every job has this lines_per_lane)
   const int lane = threadIdx.x & 31;
   uint32_t* wl = lines_smem + (threadIdx.x >> 5) * 32u * lines_per_lane;
@@ -1485,6 +1529,7 @@ template <bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_pyramid(const Pyramid* __restrict__ pyrs,
                                                      const uint64_t* __restrict__ cta_beg, uint32_t n, int r, uint32_t ept,
                                                      Pyramid p0) {
+  pdl_enter();
   if constexpr (SINGLE) {
     const int l = p0.depth - r;
     for (uint32_t k = 0; k < ept; k++) {
@@ -1506,6 +1551,7 @@ __global__ void __launch_bounds__(kChunk) kb_pyramid(const Pyramid* __restrict__
 }
 
 __global__ void kb_pyramid_top(const Pyramid* __restrict__ pyrs, int l_hi, uint32_t* __restrict__ scan_end) {
+  pdl_enter();
   if (blockIdx.x == 0 && threadIdx.x == 0) *scan_end = 0u;  // the scan's total entry
   __shared__ Pyramid sp;
   stage(sp, pyrs[blockIdx.x]);
@@ -1525,6 +1571,7 @@ template <bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_clean_leaves(const Pyramid* __restrict__ pyrs,
                                                           const uint64_t* __restrict__ cta_beg, uint32_t n, uint32_t ept,
                                                           Pyramid p0) {
+  pdl_enter();
   if constexpr (SINGLE) {
     for (uint32_t k = 0; k < ept; k++) clean_touch16(p0, ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x);
   } else {
@@ -1542,6 +1589,7 @@ template <bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__ pyrs,
                                                      const uint64_t* __restrict__ cta_beg, uint32_t n,
                                                      uint32_t* __restrict__ keys, uint32_t ept, Pyramid p0) {
+  pdl_enter();
   if constexpr (SINGLE) {
     for (uint32_t k = 0; k < ept; k++)
       compact_elem(p0, ((uint64_t)blockIdx.x * ept + k) * kChunk + threadIdx.x, keys);
@@ -1558,6 +1606,7 @@ __global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__
 __global__ void kb_level_bases(const Pyramid* __restrict__ pyrs, uint32_t n_stripes, uint32_t* __restrict__ out,
                                const uint64_t* __restrict__ tasks, uint64_t* __restrict__ tasks_out,
                                uint32_t* __restrict__ flag) {
+  pdl_enter();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0) {
     *tasks_out = *tasks;
@@ -1591,6 +1640,7 @@ template <int OP, bool SINGLE>
 __global__ void __launch_bounds__(kChunk) kb_nodes(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits,
                                                    const uint64_t* __restrict__ cta_beg, uint32_t n, int arg, uint32_t ept,
                                                    Pyramid p0, EmitJob e0) {
+  pdl_enter();
   if constexpr (SINGLE) {
     if constexpr (OP == OP_TOP_DOWN) {
       for (uint32_t k = 0; k < ept; k += 2) {
@@ -1621,6 +1671,7 @@ __global__ void __launch_bounds__(kChunk) kb_nodes(const Pyramid* __restrict__ p
 
 // One CTA per stripe: bottom-up of levels l_small .. 0.
 __global__ void kb_bottom_up_top(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits) {
+  pdl_enter();
   __shared__ Pyramid sp;
   __shared__ EmitJob se;
   stage(sp, pyrs[blockIdx.x]);
@@ -1635,6 +1686,7 @@ __global__ void kb_bottom_up_top(const Pyramid* __restrict__ pyrs, const EmitJob
 
 // One CTA per stripe: the root starts at the stripe's bases; parents of levels 0 .. min(l_small, depth-2).
 __global__ void kb_top_down_top(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits) {
+  pdl_enter();
   __shared__ Pyramid sp;
   __shared__ EmitJob se;
   stage(sp, pyrs[blockIdx.x]);
@@ -1655,6 +1707,7 @@ __global__ void kb_top_down_top(const Pyramid* __restrict__ pyrs, const EmitJob*
 
 __global__ void kb_root_info(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits, uint32_t n_stripes,
                              uint32_t* __restrict__ out) {
+  pdl_enter();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_stripes) return;
   if (pyrs[s].lv[pyrs[s].depth].n == 0) return;
@@ -1682,8 +1735,8 @@ void launch_part_count(const float* tris, int stride, uint64_t n_tris, const flo
   const int use_smem = n_parts <= 4096;
   const size_t smem = use_smem ? n_parts * sizeof(uint32_t) : 0;
   KScope k("part_count", st);
-  k_part_count<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
-                                                          (uint32_t)n_parts, hist, use_smem);
+  launch_k(k_part_count, dim3(grid_for(n_tris, 256)), dim3(256), smem, st, tris, stride, n_tris, axis_lo, axis_hi,
+           pa_bits, (uint32_t)n_parts, hist, use_smem);
 }
 
 void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
@@ -1692,8 +1745,8 @@ void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const floa
   const int use_smem = n_parts <= 4096;
   const size_t smem = use_smem ? 2 * n_parts * sizeof(uint32_t) : 0;
   KScope k("part_emit", st);
-  k_part_emit<<<grid_for(n_tris, 256), 256, smem, st>>>(tris, stride, n_tris, axis_lo, axis_hi, pa_bits,
-                                                         (uint32_t)n_parts, cursor, items, use_smem);
+  launch_k(k_part_emit, dim3(grid_for(n_tris, 256)), dim3(256), smem, st, tris, stride, n_tris, axis_lo, axis_hi,
+           pa_bits, (uint32_t)n_parts, cursor, items, use_smem);
 }
 
 uint32_t stream_ctas(uint64_t n) { return (uint32_t)((n + kStreamCta - 1) / kStreamCta); }
@@ -1701,7 +1754,7 @@ uint32_t stream_ctas(uint64_t n) { return (uint32_t)((n + kStreamCta - 1) / kStr
 void launch_stream_bases(const uint32_t* part_off, uint32_t p0, uint32_t gp, uint64_t* base, cudaStream_t st) {
   if (gp == 0) return;
   KScope k("stream_bases", st);
-  k_stream_bases<<<grid_for(gp, 256), 256, 0, st>>>(part_off, p0, gp, base);
+  launch_k(k_stream_bases, dim3(grid_for(gp, 256)), dim3(256), 0, st, part_off, p0, gp, base);
 }
 
 void launch_stream_group_chunk(const float* tris, int stride, uint64_t n, const float* axis_lo, const float* axis_hi,
@@ -1711,17 +1764,17 @@ void launch_stream_group_chunk(const float* tris, int stride, uint64_t n, const 
   const uint32_t n_cta = stream_ctas(n);
   {
     KScope k("stream_count", st);
-    k_stream_count<<<n_cta, kStreamCta, gp * sizeof(uint32_t), st>>>(tris, stride, n, axis_lo, axis_hi, pa_bits, p0,
-                                                                     gp, mat, n_cta);
+    launch_k(k_stream_count, dim3(n_cta), dim3(kStreamCta), gp * sizeof(uint32_t), st, tris, stride, n, axis_lo,
+             axis_hi, pa_bits, p0, gp, mat, n_cta);
   }
   scan_exclusive<uint32_t>(mat, (uint64_t)gp * n_cta + 1, mat_partials, st);
   {
     KScope k("stream_emit", st);
-    k_stream_emit<<<n_cta, kStreamCta, 0, st>>>(tris, stride, n, axis_lo, axis_hi, pa_bits, p0, gp, mat, n_cta, base,
-                                                out);
+    launch_k(k_stream_emit, dim3(n_cta), dim3(kStreamCta), 0, st, tris, stride, n, axis_lo, axis_hi, pa_bits, p0, gp,
+             mat, n_cta, base, out);
   }
   KScope k("stream_advance", st);
-  k_stream_advance<<<grid_for(gp, 256), 256, 0, st>>>(mat, n_cta, gp, base);
+  launch_k(k_stream_advance, dim3(grid_for(gp, 256)), dim3(256), 0, st, mat, n_cta, gp, base);
 }
 
 // One-stripe occupancy pass with the job as a kernel parameter (the
@@ -1783,13 +1836,13 @@ cudaError_t scan_u64_exclusive_checked(uint64_t* data, uint64_t n, uint64_t* par
 void launch_scatter_records(const uint64_t* src, uint64_t n, int words, uint64_t* dst, cudaStream_t st) {
   if (n == 0) return;
   KScope k("scatter_records", st);
-  k_scatter_records<<<grid_for(n, 128), 128, 0, st>>>(src, n, words, dst);
+  launch_k(k_scatter_records, dim3(grid_for(n, 128)), dim3(128), 0, st, src, n, words, dst);
 }
 
 void launch_scatter_to(const uint64_t* src, uint64_t n, int words, cudaStream_t st) {
   if (n == 0) return;
   KScope k("scatter_records", st);
-  k_scatter_to<<<grid_for(n, 128), 128, 0, st>>>(src, n, words);
+  launch_k(k_scatter_to, dim3(grid_for(n, 128)), dim3(128), 0, st, src, n, words);
 }
 
 // ---- batched launch wrappers ----
@@ -1801,11 +1854,11 @@ void launch_b_vox_small(const VoxJob* jobs, const uint64_t* cta_beg, uint32_t n,
   std::memset(&j0, 0, sizeof(j0));
   if (single) j0 = *single;
   if (pass == 0) {
-    if (single) kb_vox_small<0, true><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n, j0);
-    else kb_vox_small<0, false><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n, j0);
+    if (single) launch_k(kb_vox_small<0, true>, dim3((unsigned)ctas), dim3(kChunk), 0, st, jobs, cta_beg, n, j0);
+    else launch_k(kb_vox_small<0, false>, dim3((unsigned)ctas), dim3(kChunk), 0, st, jobs, cta_beg, n, j0);
   } else {
-    if (single) kb_vox_small<1, true><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n, j0);
-    else kb_vox_small<1, false><<<(unsigned)ctas, kChunk, 0, st>>>(jobs, cta_beg, n, j0);
+    if (single) launch_k(kb_vox_small<1, true>, dim3((unsigned)ctas), dim3(kChunk), 0, st, jobs, cta_beg, n, j0);
+    else launch_k(kb_vox_small<1, false>, dim3((unsigned)ctas), dim3(kChunk), 0, st, jobs, cta_beg, n, j0);
   }
 }
 
@@ -1813,7 +1866,8 @@ void launch_b_task_map(const uint64_t* cta_beg, uint32_t n, uint64_t ctas, const
                        const uint64_t* task_off, uint64_t total_items, uint64_t* map, uint64_t cap, cudaStream_t st) {
   if (ctas == 0) return;
   KScope k("task_map", st);
-  kb_task_map<<<(unsigned)ctas, kChunk, 0, st>>>(cta_beg, n, item_beg, task_off, total_items, map, cap);
+  launch_k(kb_task_map, dim3((unsigned)ctas), dim3(kChunk), 0, st, cta_beg, n, item_beg, task_off, total_items, map,
+           cap);
 }
 
 void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n_stripes, const uint64_t* task_off,
@@ -1829,11 +1883,11 @@ void launch_b_vox_large(const VoxJob* jobs, const uint64_t* item_beg, uint32_t n
   }
   KScope k(pass == 0 ? "vox_large_occupancy" : "vox_large_winner", st);
   if (pass == 0)
-    kb_vox_large<0><<<grid, block, smem, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter, lines_per_lane,
-                                               map, cap);
+    launch_k(kb_vox_large<0>, dim3(grid), dim3(block), smem, st, jobs, item_beg, n_stripes, task_off, total_items,
+             counter, lines_per_lane, map, cap);
   else
-    kb_vox_large<1><<<grid, block, smem, st>>>(jobs, item_beg, n_stripes, task_off, total_items, counter, lines_per_lane,
-                                               map, cap);
+    launch_k(kb_vox_large<1>, dim3(grid), dim3(block), smem, st, jobs, item_beg, n_stripes, task_off, total_items,
+             counter, lines_per_lane, map, cap);
 }
 
 void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, int r,
@@ -1843,14 +1897,14 @@ void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, 
   Pyramid p0;
   std::memset(&p0, 0, sizeof(p0));
   if (single) p0 = *single;
-  if (single) kb_pyramid<true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, r, ept, p0);
-  else kb_pyramid<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, r, ept, p0);
+  if (single) launch_k(kb_pyramid<true>, dim3((unsigned)ctas), dim3(kChunk), 0, st, pyrs, cta_beg, n, r, ept, p0);
+  else launch_k(kb_pyramid<false>, dim3((unsigned)ctas), dim3(kChunk), 0, st, pyrs, cta_beg, n, r, ept, p0);
 }
 
 void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, uint32_t* scan_end, cudaStream_t st) {
   if (n_stripes == 0) return;
   KScope k("pyramid_top", st);
-  kb_pyramid_top<<<n_stripes, 512, 0, st>>>(pyrs, l_hi, scan_end);
+  launch_k(kb_pyramid_top, dim3(n_stripes), dim3(512), 0, st, pyrs, l_hi, scan_end);
 }
 
 void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept,
@@ -1860,8 +1914,8 @@ void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, 
   Pyramid p0;
   std::memset(&p0, 0, sizeof(p0));
   if (single) p0 = *single;
-  if (single) kb_compact<true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys, ept, p0);
-  else kb_compact<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, keys, ept, p0);
+  if (single) launch_k(kb_compact<true>, dim3((unsigned)ctas), dim3(kChunk), 0, st, pyrs, cta_beg, n, keys, ept, p0);
+  else launch_k(kb_compact<false>, dim3((unsigned)ctas), dim3(kChunk), 0, st, pyrs, cta_beg, n, keys, ept, p0);
 }
 
 void launch_b_clean_leaves(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept,
@@ -1871,15 +1925,16 @@ void launch_b_clean_leaves(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_
   Pyramid p0;
   std::memset(&p0, 0, sizeof(p0));
   if (single) p0 = *single;
-  if (single) kb_clean_leaves<true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, ept, p0);
-  else kb_clean_leaves<false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, cta_beg, n, ept, p0);
+  if (single) launch_k(kb_clean_leaves<true>, dim3((unsigned)ctas), dim3(kChunk), 0, st, pyrs, cta_beg, n, ept, p0);
+  else launch_k(kb_clean_leaves<false>, dim3((unsigned)ctas), dim3(kChunk), 0, st, pyrs, cta_beg, n, ept, p0);
 }
 
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, const uint64_t* tasks,
                           uint64_t* tasks_out, uint32_t* flag, cudaStream_t st) {
   if (n_stripes == 0) return;
   KScope k("level_bases", st);
-  kb_level_bases<<<grid_for(n_stripes, 128), 128, 0, st>>>(pyrs, n_stripes, out, tasks, tasks_out, flag);
+  launch_k(kb_level_bases, dim3(grid_for(n_stripes, 128)), dim3(128), 0, st, pyrs, n_stripes, out, tasks, tasks_out,
+           flag);
 }
 
 namespace {
@@ -1895,9 +1950,9 @@ void launch_nodes(const char* name, const Pyramid* pyrs, const EmitJob* emits, c
   if (sp && se) {
     p0 = *sp;
     e0 = *se;
-    kb_nodes<OP, true><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, arg, ept, p0, e0);
+    launch_k(kb_nodes<OP, true>, dim3((unsigned)ctas), dim3(kChunk), 0, st, pyrs, emits, cta_beg, n, arg, ept, p0, e0);
   } else {
-    kb_nodes<OP, false><<<(unsigned)ctas, kChunk, 0, st>>>(pyrs, emits, cta_beg, n, arg, ept, p0, e0);
+    launch_k(kb_nodes<OP, false>, dim3((unsigned)ctas), dim3(kChunk), 0, st, pyrs, emits, cta_beg, n, arg, ept, p0, e0);
   }
 }
 }  // namespace
@@ -1916,13 +1971,13 @@ void launch_b_bottom_up(const Pyramid* pyrs, const EmitJob* emits, const uint64_
 void launch_b_bottom_up_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, cudaStream_t st) {
   if (n_stripes == 0) return;
   KScope k("bottom_up_top", st);
-  kb_bottom_up_top<<<n_stripes, 256, 0, st>>>(pyrs, emits);
+  launch_k(kb_bottom_up_top, dim3(n_stripes), dim3(256), 0, st, pyrs, emits);
 }
 
 void launch_b_top_down_top(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, cudaStream_t st) {
   if (n_stripes == 0) return;
   KScope k("top_down_top", st);
-  kb_top_down_top<<<n_stripes, 256, 0, st>>>(pyrs, emits);
+  launch_k(kb_top_down_top, dim3(n_stripes), dim3(256), 0, st, pyrs, emits);
 }
 
 void launch_b_top_down(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n, uint64_t ctas,
@@ -1939,7 +1994,7 @@ void launch_b_root_info(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_st
                         cudaStream_t st) {
   if (n_stripes == 0) return;
   KScope k("root_info", st);
-  kb_root_info<<<grid_for(n_stripes, 128), 128, 0, st>>>(pyrs, emits, n_stripes, out);
+  launch_k(kb_root_info, dim3(grid_for(n_stripes, 128)), dim3(128), 0, st, pyrs, emits, n_stripes, out);
 }
 
 }  // namespace ooc

@@ -103,13 +103,52 @@ bool valid(const ooc_mesh& m) {
 
 // HBM a request may hold while it is in flight: its triangles, the occupancy
 // pyramids of its stripes, and per-node arrays plus output records for an upper
-// bound on its nodes.  The leaves are at most the grid voxels inside the
-// triangles' grid boxes (voxelizer.cpp:189-204 tests no voxel outside them),
-// and a tree with L leaves at depth D has at most min(8^l, L) nodes at level l.
-// A node costs at most kNodeBytes: its 24-byte record and 32-byte data record,
-// its key, subtree sizes and starts, first child and winner (7 x 4 bytes) and
-// its -levels cache (24 bytes), with room for the batch's job tables.
+// bound on its nodes.  A tree with L leaves at depth D has at most min(8^l, L)
+// nodes at level l.  The leaves are at most the summed per-triangle bounds on the
+// voxels a triangle can set: the voxels of its grid box (voxelizer.cpp:189-204
+// tests no other), and, for a triangle with a finite plane, the voxels that
+// overlap it (the Schwarz-Seidel test is the triangle-box overlap test): their
+// centres lie within the triangle grown by a cube of side u, so the voxels
+// themselves lie within the triangle grown by a ball of radius sqrt(3) u, whose
+// volume is 2 r A + (pi / 2) r^2 L + (4 / 3) pi r^3 for area A and perimeter L
+// (Steiner's formula for a flat convex body).  A node costs at most kNodeBytes:
+// its 24-byte record and 32-byte data record, its key, subtree sizes and
+// starts, first child and winner (7 x 4 bytes) and its -levels cache (24
+// bytes), with room for the batch's job tables.
 constexpr uint64_t kNodeBytes = 120;
+
+double voxel_bound(const float* v, float unit_div, uint64_t N) {
+  double box = 1.0;
+  for (int a = 0; a < 3; a++) {
+    const float lo = std::min(v[a], std::min(v[3 + a], v[6 + a])) * unit_div;
+    const float hi = std::max(v[a], std::max(v[3 + a], v[6 + a])) * unit_div;
+    // NaN or out-of-range coordinates count as the whole axis
+    const double l = (lo >= 0.0f) ? std::min((double)lo, (double)N - 1) : 0.0;
+    const double h = (hi < (float)N) ? std::max((double)hi, 0.0) : (double)N - 1;
+    box *= (h >= l) ? std::floor(h) - std::floor(l) + 1.0 : (double)N;
+  }
+  // in voxel units
+  double p[3][3];
+  for (int k = 0; k < 3; k++)
+    for (int a = 0; a < 3; a++) p[k][a] = (double)v[3 * k + a] * (double)unit_div;
+  double e[3][3], len = 0.0;
+  for (int k = 0; k < 3; k++) {
+    double l2 = 0.0;
+    for (int a = 0; a < 3; a++) {
+      e[k][a] = p[(k + 1) % 3][a] - p[k][a];
+      l2 += e[k][a] * e[k][a];
+    }
+    len += std::sqrt(l2);
+  }
+  const double cx = e[0][1] * e[1][2] - e[0][2] * e[1][1], cy = e[0][2] * e[1][0] - e[0][0] * e[1][2],
+               cz = e[0][0] * e[1][1] - e[0][1] * e[1][0];
+  const double area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+  // a degenerate triangle has no plane test (its normal is NaN): only its box bounds it
+  if (!(area > 1e-6) || !std::isfinite(area) || !std::isfinite(len)) return box;
+  const double r = std::sqrt(3.0), pi = 3.14159265358979323846;
+  const double grown = 2.0 * r * area + 0.5 * pi * r * r * len + 4.0 / 3.0 * pi * r * r * r;
+  return std::min(box, 1.01 * grown + 1.0);
+}
 
 uint64_t footprint(const ooc_mesh& m) {
   const ooc_build_params& p = m.params;
@@ -126,23 +165,10 @@ uint64_t footprint(const ooc_mesh& m) {
   for (int l = 0; l <= Ds; l++) words += (((1ull << (3 * l)) + 31) / 32 + 7) / 8 * 8;
   const uint64_t stripes = (N * N * N) >> (3 * Ds);
   bytes += words * 4 * stripes;
-  // grid boxes as voxelizer.cpp:189-204 forms them: truncated, clamped to the grid
   const float unit_div = 1.0f / ((p.bbox_max[0] - p.bbox_min[0]) / (float)N);
   const double cells = (double)N * (double)N * (double)N;
   double leaves = 0.0;
-  for (uint64_t t = 0; t < m.n_tris && leaves < cells; t++) {
-    const float* v = m.tris + t * stride;
-    double vol = 1.0;
-    for (int a = 0; a < 3; a++) {
-      const float lo = std::min(v[a], std::min(v[3 + a], v[6 + a])) * unit_div;
-      const float hi = std::max(v[a], std::max(v[3 + a], v[6 + a])) * unit_div;
-      // NaN or out-of-range coordinates count as the whole axis
-      const double l = (lo >= 0.0f) ? std::min((double)lo, (double)N - 1) : 0.0;
-      const double h = (hi < (float)N) ? std::max((double)hi, 0.0) : (double)N - 1;
-      vol *= (h >= l) ? std::floor(h) - std::floor(l) + 1.0 : (double)N;
-    }
-    leaves += vol;
-  }
+  for (uint64_t t = 0; t < m.n_tris && leaves < cells; t++) leaves += voxel_bound(m.tris + t * stride, unit_div, N);
   leaves = std::min(leaves, cells);
   double nodes = 0.0;
   for (int l = 0; l <= D; l++) nodes += std::min(std::ldexp(1.0, 3 * l), leaves);

@@ -101,11 +101,12 @@ def test_every_tuning_gives_the_same_octrees(builder):
         nodes, data, _ = pyoracle.build(t, a["gridsize"], a["memory_limit_mb"], color=a["color"], levels=a["levels"])
         want.append(octree.Octree(a["gridsize"], nodes, data))
     try:
-        for small_vol, lpl, block, cps, budget, graphs, ept in [(1, 1, 64, 1, 4096, 1, 1),
-                                                                (64, 64, 256, 16, 1 << 30, 0, 16),
-                                                                (27, 3, 128, 2, 700_000, 1, 3),
-                                                                (64, 16, 256, 4, 4 << 30, 1, 4)]:
-            builder.set_tuning(ooc.Tuning(small_vol, lpl, block, cps, budget, graphs, ept))
+        for small_vol, lpl, block, cps, budget, graphs, ept, pdl in [(1, 1, 64, 1, 4096, 1, 1, 1),
+                                                                     (64, 64, 256, 16, 1 << 30, 0, 16, 1),
+                                                                     (27, 3, 128, 2, 700_000, 1, 3, 0),
+                                                                     (64, 16, 256, 4, 4 << 30, 1, 4, 0),
+                                                                     (64, 16, 256, 4, 4 << 30, 0, 8, 0)]:
+            builder.set_tuning(ooc.Tuning(small_vol, lpl, block, cps, budget, graphs, ept, pdl, 0))
             for r, w in zip(builder.build_batch_device(meshes, params), want):
                 assert not octree.diff(r.tree, w)
     finally:

@@ -36,8 +36,8 @@ def test_result_struct_layout():
 
 def test_tuning_calls_reject_null():
     lib = ooc.load_library()
-    t = ooc.Tuning(64, 16, 256, 4, 1 << 30, 0, 4)
+    t = ooc.Tuning(64, 16, 256, 4, 1 << 30, 0, 4, 1, 0)
     assert lib.ooc_set_tuning(None, ctypes.byref(t)) == 1
     assert lib.ooc_get_tuning(None, ctypes.byref(t)) == 1
     assert lib.ooc_autotune(None, None, 0, None) == 1
-    assert ctypes.sizeof(ooc.Tuning) == 32
+    assert ctypes.sizeof(ooc.Tuning) == 40
