@@ -919,10 +919,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     }
   }, pieces != nullptr);  // waits on the upload stream are not captured
   wait_level_counts(st, idle);
-  // the host lays out phase B next; the previous sub-batch's landed records keep moving meanwhile
-  auto pump = [&]() {
-    if (idle) idle();
-  };
   uint64_t tasks_seen;
   std::memcpy(&tasks_seen, lvl + (uint64_t)n * 16 + 8, 8);
   c->max_tasks = std::max(c->max_tasks, tasks_seen);
@@ -976,7 +972,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       tb.push(tb.top, ph);
     }
   }
-  pump();
   // ---- per-node arrays and output windows ----
   bool any_levels = false, any_payload = false;
   for (auto& m : meshes) {
@@ -1089,7 +1084,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     while (ls + 1 <= P.depth - 1 && P.lv[ls + 1].n <= 256) ls++;
     e.l_small = ls;
   }
-  pump();
   auto live = [&](uint32_t s) { return !pl[s].empty; };
   const std::vector<uint64_t> cp_pay = cta_prefix(n, kChunk, [&](uint32_t s) -> uint64_t {
     return meshes[sb[s].mesh].pl.binary ? 0 : sb[s].n_items;
@@ -1120,7 +1114,6 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       const int last_top = std::min(ej[s].l_small, pyr[s].depth - 2);
       return (live(s) && l > last_top && l <= pyr[s].depth - 2) ? pyr[s].lv[l + 1].n : 0;  // one thread per child
     });
-  pump();
   Uploader up2;
   const size_t o_vj2 = up2.add(vj.data(), n * sizeof(VoxJob));
   const size_t o_pyr2 = up2.add(pyr.data(), n * sizeof(Pyramid));

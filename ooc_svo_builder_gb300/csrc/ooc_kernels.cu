@@ -476,55 +476,6 @@ __device__ __forceinline__ uint32_t leaf_rank(const VoxJob& j, uint32_t b) {
   return base - j.leafscan_base + in_block_rank(j.leafbits + (uint64_t)blk * 8, b);
 }
 
-// One z column of a small item: sets its voxels' bits and returns the column's
-// pass bits (bit z - z0, columns of at most 64 voxels).  The halves of the YZ
-// and ZX edge functions that depend only on the column are formed once: each
-// is the same rounded product the per-voxel expression would form, and the
-// one addition that joins the halves is commutative, so every test is bit for
-// bit the reference's (voxelizer.cpp:266-287).
-// `mxy` holds the Morton bits of (x, y) and `mz0` those of z0, stripe-local.
-__device__ __forceinline__ uint64_t vox_column(const VoxJob& j, const TriSetup& s, int x, int y, int z0, int z1,
-                                               uint32_t mxy, uint32_t mz0) {
-  const float px = __fmul_rn((float)x, j.u);
-  const float py = __fmul_rn((float)y, j.u);
-  if (!pass_xy(s, px, py)) return 0;
-  const float nxy = plane_xy(s, px, py);
-  float yz_col[3], zx_col[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    yz_col[k] = __fmul_rn(s.yz[k][0], py);  // dot2(yz, (py, pz)) = yz0*py + yz1*pz
-    zx_col[k] = __fmul_rn(s.zx[k][1], px);  // dot2(zx, (pz, px)) = zx0*pz + zx1*px
-  }
-  constexpr uint32_t ZBITS = 0x24924924u;  // Morton bit positions of z (2, 5, ..., 29)
-  uint32_t mz = mz0;
-  uint32_t cur_w = 0xffffffffu, acc = 0;
-  uint64_t col = 0;
-  for (int z = z0; z <= z1; z++, mz = ((mz | ~ZBITS) + 4u) & ZBITS) {
-    const float pz = __fmul_rn((float)z, j.u);
-    const float nDOTp = __fadd_rn(nxy, __fmul_rn(s.n[2], pz));
-    if (__fmul_rn(__fadd_rn(nDOTp, s.d1), __fadd_rn(nDOTp, s.d2)) > 0.0f) continue;
-    bool pass = true;
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-      pass = pass && !(__fadd_rn(__fadd_rn(yz_col[k], __fmul_rn(s.yz[k][1], pz)), s.dyz[k]) < 0.0f);
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-      pass = pass && !(__fadd_rn(__fadd_rn(__fmul_rn(s.zx[k][0], pz), zx_col[k]), s.dzx[k]) < 0.0f);
-    if (!pass) continue;
-    const uint32_t m = mxy | mz;
-    const uint32_t w = m >> 5;
-    if (w != cur_w) {
-      if (acc) set_leaf(j, cur_w, acc);
-      cur_w = w;
-      acc = 0;
-    }
-    acc |= 1u << (m & 31);
-    if (z - z0 < 64) col |= 1ull << (z - z0);
-  }
-  if (acc) set_leaf(j, cur_w, acc);
-  return col;
-}
-
 __device__ __forceinline__ uint64_t item_triangle(const VoxJob& j, uint64_t i) {
   return j.item_tri ? (uint64_t)j.item_tri[j.ibeg + i] : j.ibeg + i;
 }
@@ -663,6 +614,185 @@ __device__ __forceinline__ void vox_line(const VoxJob& j, const TriSetup& s, uin
   if (PASS == 0 && acc) set_leaf(j, cur_w, acc);
 }
 
+// ---------------------------------------------------------------------------
+// Small items: the candidate tests by projection.  Of the seven tests of a
+// candidate voxel (voxelizer.cpp:266-287) the three XY edge tests depend only
+// on (x, y), the YZ tests only on (y, z), the ZX tests only on (z, x); only the
+// plane test depends on all three.  Each is a pure function of its
+// coordinates, so evaluating it once per distinct projection and reusing the
+// result gives the reference's verdict for every candidate, bit for bit; the
+// FP32 expressions are the reference's, operation by operation.  A candidate
+// passes when all seven pass (the reference's order of early exits only saves
+// work).  The pass mask of an item has bit (ix * by + iy) * bz + iz for box
+// coordinates (ix, iy, iz).
+// ---------------------------------------------------------------------------
+
+// Sets a passing voxel's bit: bits of one leaf word are gathered in `acc`
+// while consecutive voxels stay in it.
+__device__ __forceinline__ void leaf_bit(const VoxJob& j, bool pass, uint32_t m, uint32_t& cur_w, uint32_t& acc) {
+  if (!pass) return;
+  const uint32_t w = m >> 5;
+  if (w != cur_w) {
+    if (acc) set_leaf(j, cur_w, acc);
+    cur_w = w;
+    acc = 0;
+  }
+  acc |= 1u << (m & 31);
+}
+
+__device__ __forceinline__ uint64_t bit_if(bool p, uint32_t pos) { return p ? (1ull << (pos & 63u)) : 0ull; }
+
+// Boxes at most two voxels wide in x and y (the common small triangle): z is
+// walked in 2 x 2 x 2 bricks, every test of a brick evaluated without
+// branches; slots outside the box are masked.  The Morton bits of a
+// coordinate + 1 come from the carry trick: setting every bit outside an
+// axis' positions makes +1 carry across them.
+__device__ __forceinline__ uint64_t vox_small_bricks(const VoxJob& j, const TriSetup& s, const int lo[3], uint32_t bx,
+                                                     uint32_t by, uint32_t bz) {
+  const float px0 = __fmul_rn((float)lo[0], j.u), px1 = __fmul_rn((float)(lo[0] + 1), j.u);
+  const float py0 = __fmul_rn((float)lo[1], j.u), py1 = __fmul_rn((float)(lo[1] + 1), j.u);
+  // XY over the four columns (x_i, y_j)
+  bool c00 = true, c01 = by > 1, c10 = bx > 1, c11 = bx > 1 && by > 1;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float a0 = __fmul_rn(s.xy[k][0], px0), a1 = __fmul_rn(s.xy[k][0], px1);
+    const float b0 = __fmul_rn(s.xy[k][1], py0), b1 = __fmul_rn(s.xy[k][1], py1);
+    c00 &= !(__fadd_rn(__fadd_rn(a0, b0), s.dxy[k]) < 0.0f);
+    c01 &= !(__fadd_rn(__fadd_rn(a0, b1), s.dxy[k]) < 0.0f);
+    c10 &= !(__fadd_rn(__fadd_rn(a1, b0), s.dxy[k]) < 0.0f);
+    c11 &= !(__fadd_rn(__fadd_rn(a1, b1), s.dxy[k]) < 0.0f);
+  }
+  // n.x * p.x + n.y * p.y per column, and the halves of the YZ and ZX dot products
+  // that do not depend on z
+  const float n0x0 = __fmul_rn(s.n[0], px0), n0x1 = __fmul_rn(s.n[0], px1);
+  const float n1y0 = __fmul_rn(s.n[1], py0), n1y1 = __fmul_rn(s.n[1], py1);
+  const float q00 = __fadd_rn(n0x0, n1y0), q01 = __fadd_rn(n0x0, n1y1), q10 = __fadd_rn(n0x1, n1y0),
+              q11 = __fadd_rn(n0x1, n1y1);
+  float yz_y0[3], yz_y1[3], zx_x0[3], zx_x1[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    yz_y0[k] = __fmul_rn(s.yz[k][0], py0);
+    yz_y1[k] = __fmul_rn(s.yz[k][0], py1);
+    zx_x0[k] = __fmul_rn(s.zx[k][1], px0);
+    zx_x1[k] = __fmul_rn(s.zx[k][1], px1);
+  }
+  constexpr uint32_t XBITS = 0x09249249u, YBITS = 0x12492492u, ZBITS = 0x24924924u;
+  const uint32_t mx0 = spread3_10((uint32_t)(lo[0] - j.sa[0])), mx1 = ((mx0 | ~XBITS) + 1u) & XBITS;
+  const uint32_t my0 = spread3_10((uint32_t)(lo[1] - j.sa[1])) << 1, my1 = ((my0 | ~YBITS) + 2u) & YBITS;
+  uint32_t mz = spread3_10((uint32_t)(lo[2] - j.sa[2])) << 2;
+  uint32_t cur_w = 0xffffffffu, acc = 0;
+  uint64_t mask = 0;
+  for (uint32_t zc = 0; zc < bz; zc += 2) {
+    const bool z1ok = zc + 1 < bz;
+    const float pz0 = __fmul_rn((float)(lo[2] + (int)zc), j.u), pz1 = __fmul_rn((float)(lo[2] + (int)zc + 1), j.u);
+    bool y0z0 = true, y0z1 = z1ok, y1z0 = true, y1z1 = z1ok;  // YZ over (y_j, z_k)
+    bool z0x0 = true, z0x1 = true, z1x0 = z1ok, z1x1 = z1ok;  // ZX over (z_k, x_i)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      // dot((-e.z, e.y) * fx, (p.y, p.z)) + d and dot((-e.x, e.z) * fy, (p.z, p.x)) + d
+      const float e0 = __fmul_rn(s.yz[k][1], pz0), e1 = __fmul_rn(s.yz[k][1], pz1);
+      y0z0 &= !(__fadd_rn(__fadd_rn(yz_y0[k], e0), s.dyz[k]) < 0.0f);
+      y0z1 &= !(__fadd_rn(__fadd_rn(yz_y0[k], e1), s.dyz[k]) < 0.0f);
+      y1z0 &= !(__fadd_rn(__fadd_rn(yz_y1[k], e0), s.dyz[k]) < 0.0f);
+      y1z1 &= !(__fadd_rn(__fadd_rn(yz_y1[k], e1), s.dyz[k]) < 0.0f);
+      const float f0 = __fmul_rn(s.zx[k][0], pz0), f1 = __fmul_rn(s.zx[k][0], pz1);
+      z0x0 &= !(__fadd_rn(__fadd_rn(f0, zx_x0[k]), s.dzx[k]) < 0.0f);
+      z0x1 &= !(__fadd_rn(__fadd_rn(f0, zx_x1[k]), s.dzx[k]) < 0.0f);
+      z1x0 &= !(__fadd_rn(__fadd_rn(f1, zx_x0[k]), s.dzx[k]) < 0.0f);
+      z1x1 &= !(__fadd_rn(__fadd_rn(f1, zx_x1[k]), s.dzx[k]) < 0.0f);
+    }
+    // the plane test: (n.p + d1) (n.p + d2) > 0 fails
+    const float g0 = __fmul_rn(s.n[2], pz0), g1 = __fmul_rn(s.n[2], pz1);
+    auto plane = [&](float q, float g) {
+      const float nd = __fadd_rn(q, g);
+      return !(__fmul_rn(__fadd_rn(nd, s.d1), __fadd_rn(nd, s.d2)) > 0.0f);
+    };
+    const bool p000 = c00 & y0z0 & z0x0 & plane(q00, g0), p001 = c00 & y0z1 & z1x0 & plane(q00, g1);
+    const bool p010 = c01 & y1z0 & z0x0 & plane(q01, g0), p011 = c01 & y1z1 & z1x0 & plane(q01, g1);
+    const bool p100 = c10 & y0z0 & z0x1 & plane(q10, g0), p101 = c10 & y0z1 & z1x1 & plane(q10, g1);
+    const bool p110 = c11 & y1z0 & z0x1 & plane(q11, g0), p111 = c11 & y1z1 & z1x1 & plane(q11, g1);
+    const uint32_t mz1 = ((mz | ~ZBITS) + 4u) & ZBITS;
+    mask |= bit_if(p000, zc) | bit_if(p001, zc + 1) | bit_if(p010, bz + zc) | bit_if(p011, bz + zc + 1) |
+            bit_if(p100, by * bz + zc) | bit_if(p101, by * bz + zc + 1) | bit_if(p110, (by + 1) * bz + zc) |
+            bit_if(p111, (by + 1) * bz + zc + 1);
+    leaf_bit(j, p000, mx0 | my0 | mz, cur_w, acc);
+    leaf_bit(j, p001, mx0 | my0 | mz1, cur_w, acc);
+    leaf_bit(j, p010, mx0 | my1 | mz, cur_w, acc);
+    leaf_bit(j, p011, mx0 | my1 | mz1, cur_w, acc);
+    leaf_bit(j, p100, mx1 | my0 | mz, cur_w, acc);
+    leaf_bit(j, p101, mx1 | my0 | mz1, cur_w, acc);
+    leaf_bit(j, p110, mx1 | my1 | mz, cur_w, acc);
+    leaf_bit(j, p111, mx1 | my1 | mz1, cur_w, acc);
+    mz = ((mz1 | ~ZBITS) + 4u) & ZBITS;
+  }
+  if (acc) set_leaf(j, cur_w, acc);
+  return mask;
+}
+
+// Other small boxes (at most 64 voxels): the YZ verdicts over (y, z) and the
+// ZX verdicts over (z, x) as bit masks first, then per column the XY test and
+// per candidate the plane test.
+__device__ __forceinline__ uint64_t vox_small_factored(const VoxJob& j, const TriSetup& s, const int lo[3],
+                                                       uint32_t bx, uint32_t by, uint32_t bz) {
+  uint64_t yzm = 0;  // bit iy * bz + iz
+  for (uint32_t iy = 0; iy < by; iy++) {
+    const float py = __fmul_rn((float)(lo[1] + (int)iy), j.u);
+    const float a0 = __fmul_rn(s.yz[0][0], py), a1 = __fmul_rn(s.yz[1][0], py), a2 = __fmul_rn(s.yz[2][0], py);
+    for (uint32_t iz = 0; iz < bz; iz++) {
+      const float pz = __fmul_rn((float)(lo[2] + (int)iz), j.u);
+      const bool ok = !(__fadd_rn(__fadd_rn(a0, __fmul_rn(s.yz[0][1], pz)), s.dyz[0]) < 0.0f) &
+                      !(__fadd_rn(__fadd_rn(a1, __fmul_rn(s.yz[1][1], pz)), s.dyz[1]) < 0.0f) &
+                      !(__fadd_rn(__fadd_rn(a2, __fmul_rn(s.yz[2][1], pz)), s.dyz[2]) < 0.0f);
+      yzm |= bit_if(ok, iy * bz + iz);
+    }
+  }
+  uint64_t zxm = 0;  // bit ix * bz + iz
+  for (uint32_t ix = 0; ix < bx; ix++) {
+    const float px = __fmul_rn((float)(lo[0] + (int)ix), j.u);
+    const float b0 = __fmul_rn(s.zx[0][1], px), b1 = __fmul_rn(s.zx[1][1], px), b2 = __fmul_rn(s.zx[2][1], px);
+    for (uint32_t iz = 0; iz < bz; iz++) {
+      const float pz = __fmul_rn((float)(lo[2] + (int)iz), j.u);
+      const bool ok = !(__fadd_rn(__fadd_rn(__fmul_rn(s.zx[0][0], pz), b0), s.dzx[0]) < 0.0f) &
+                      !(__fadd_rn(__fadd_rn(__fmul_rn(s.zx[1][0], pz), b1), s.dzx[1]) < 0.0f) &
+                      !(__fadd_rn(__fadd_rn(__fmul_rn(s.zx[2][0], pz), b2), s.dzx[2]) < 0.0f);
+      zxm |= bit_if(ok, ix * bz + iz);
+    }
+  }
+  constexpr uint32_t XBITS = 0x09249249u, YBITS = 0x12492492u, ZBITS = 0x24924924u;
+  const uint32_t mz0 = spread3_10((uint32_t)(lo[2] - j.sa[2])) << 2;
+  const uint32_t my0 = spread3_10((uint32_t)(lo[1] - j.sa[1])) << 1;
+  uint32_t mx = spread3_10((uint32_t)(lo[0] - j.sa[0]));
+  const uint64_t zfull = bz >= 64 ? ~0ull : ((1ull << bz) - 1);
+  uint32_t cur_w = 0xffffffffu, acc = 0;
+  uint64_t mask = 0;
+  for (uint32_t ix = 0; ix < bx; ix++, mx = ((mx | ~XBITS) + 1u) & XBITS) {
+    const float px = __fmul_rn((float)(lo[0] + (int)ix), j.u);
+    const float n0px = __fmul_rn(s.n[0], px);
+    const uint64_t zx_col = (zxm >> ((ix * bz) & 63u)) & zfull;
+    uint32_t my = my0;
+    for (uint32_t iy = 0; iy < by; iy++, my = ((my | ~YBITS) + 2u) & YBITS) {
+      const uint64_t zb = zx_col & (yzm >> ((iy * bz) & 63u));
+      if (!zb) continue;
+      const float py = __fmul_rn((float)(lo[1] + (int)iy), j.u);
+      if (!pass_xy(s, px, py)) continue;
+      const float nxy = __fadd_rn(n0px, __fmul_rn(s.n[1], py));
+      const uint32_t mxy = mx | my;
+      const uint32_t cbase = (ix * by + iy) * bz;
+      uint32_t mz = mz0;
+      for (uint32_t iz = 0; iz < bz; iz++, mz = ((mz | ~ZBITS) + 4u) & ZBITS) {
+        if (!((zb >> iz) & 1u)) continue;
+        const float pz = __fmul_rn((float)(lo[2] + (int)iz), j.u);
+        const float nd = __fadd_rn(nxy, __fmul_rn(s.n[2], pz));
+        if (__fmul_rn(__fadd_rn(nd, s.d1), __fadd_rn(nd, s.d2)) > 0.0f) continue;
+        leaf_bit(j, true, mxy | mz, cur_w, acc);
+        mask |= 1ull << (cbase + iz);
+      }
+    }
+  }
+  if (acc) set_leaf(j, cur_w, acc);
+  return mask;
+}
+
 // Pass 0, one thread per item: items with at most small_vol (<= 64) candidates
 // are voxelized here and leave their pass mask; larger ones get a warp-task
 // count (32 x lines_per_lane lines per task).
@@ -672,29 +802,18 @@ __device__ __forceinline__ void vox_small_occ_item(const VoxJob& j, uint64_t i) 
   int lo[3], hi[3];
   uint64_t cost = 0, mask = 0;
   if (item_box(j, tv, lo, hi)) {
-    const uint64_t bx = (uint64_t)(hi[0] - lo[0] + 1), by = (uint64_t)(hi[1] - lo[1] + 1),
-                   bz = (uint64_t)(hi[2] - lo[2] + 1);
-    if (bx * by * bz <= j.small_vol) {
+    const uint32_t bx = (uint32_t)(hi[0] - lo[0] + 1), by = (uint32_t)(hi[1] - lo[1] + 1),
+                   bz = (uint32_t)(hi[2] - lo[2] + 1);
+    // extents are at most a stripe's 1024: the product fits 64 bits
+    if ((uint64_t)bx * by * bz <= j.small_vol) {
       TriSetup s;
       tri_setup(tv, j.u, s);
-      // Morton bits of the box's coordinates, stepped by the carry trick: setting every
-      // bit outside an axis' positions makes +1 carry across them
-      constexpr uint32_t XBITS = 0x09249249u, YBITS = 0x12492492u;
-      const uint32_t mz0 = spread3_10((uint32_t)(lo[2] - j.sa[2])) << 2;
-      const uint32_t my0 = spread3_10((uint32_t)(lo[1] - j.sa[1])) << 1;
-      uint32_t mx = spread3_10((uint32_t)(lo[0] - j.sa[0]));
-      uint32_t shift = 0;
-      for (int x = lo[0]; x <= hi[0]; x++, mx = ((mx | ~XBITS) + 1u) & XBITS) {
-        uint32_t my = my0;
-        for (int y = lo[1]; y <= hi[1]; y++, my = ((my | ~YBITS) + 2u) & YBITS) {
-          mask |= vox_column(j, s, x, y, lo[2], hi[2], mx | my, mz0) << shift;
-          shift += (uint32_t)bz;
-        }
-      }
+      mask = (bx <= 2 && by <= 2) ? vox_small_bricks(j, s, lo, bx, by, bz) : vox_small_factored(j, s, lo, bx, by, bz);
       if (j.item_mask && mask) {
         // stripe-local box origin (10 bits per axis) and extents - 1 (6 bits each)
         j.item_box[i] = (uint64_t)(lo[0] - j.sa[0]) | ((uint64_t)(lo[1] - j.sa[1]) << 10) |
-                        ((uint64_t)(lo[2] - j.sa[2]) << 20) | ((bx - 1) << 30) | ((by - 1) << 36) | ((bz - 1) << 42);
+                        ((uint64_t)(lo[2] - j.sa[2]) << 20) | ((uint64_t)(bx - 1) << 30) | ((uint64_t)(by - 1) << 36) |
+                        ((uint64_t)(bz - 1) << 42);
       }
     } else {
       const uint64_t per_task = 32ull * j.lines_per_lane;

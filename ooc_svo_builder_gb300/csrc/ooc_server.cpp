@@ -127,6 +127,9 @@ double voxel_bound(const float* v, float unit_div, uint64_t N) {
     const double h = (hi < (float)N) ? std::max((double)hi, 0.0) : (double)N - 1;
     box *= (h >= l) ? std::floor(h) - std::floor(l) + 1.0 : (double)N;
   }
+  // both are upper bounds: a small box (every small triangle of a fine mesh) is taken as
+  // it is, sparing the submitting thread the area bound's square roots
+  if (box <= 64.0) return box;
   // in voxel units
   double p[3][3];
   for (int k = 0; k < 3; k++)
