@@ -302,8 +302,10 @@ int ooc_voxelize_occupancy_noalloc(const ooc_build_params* params, const float* 
  * and per-node arrays plus output records for an upper bound on their nodes
  * (a tree whose L leaves are at depth D has at most min(8^l, L) nodes at level
  * l, and L is at most the summed grid boxes of the triangles, clamped to the
- * grid).  A request whose footprint exceeds the whole budget is refused at
- * submission (OOC_ERR_LIMIT).  Requests run in
+ * grid).  Footprints are computed by sizing threads of the server, so a
+ * submission returns at once; a request whose footprint exceeds the whole
+ * budget completes, without running, with status OOC_ERR_LIMIT.  Requests are
+ * admitted in submission order.  Requests run in
  * continuously formed batches: each of `engines` contexts (own streams and
  * scratch) takes, whenever it is free, every queued request that fits (at
  * most max_batch) and builds them in one ooc_build_batch_device call, into
@@ -351,8 +353,7 @@ typedef struct {
 
 int ooc_server_create(const ooc_server_config* cfg, ooc_server** out);
 /* Queue one mesh; its triangles (host memory) must stay valid until its result
- * is polled.  OOC_ERR_INVALID for parameters ooc_build would refuse,
- * OOC_ERR_LIMIT when the request's footprint exceeds memory_budget. */
+ * is polled.  OOC_ERR_INVALID for parameters ooc_build would refuse. */
 int ooc_server_submit(ooc_server* server, const ooc_mesh* mesh, uint64_t* id);
 /* Next completed request (OOC_OK), or OOC_ERR_TIMEOUT after `timeout_ms`. */
 int ooc_server_poll(ooc_server* server, int32_t timeout_ms, ooc_result* out);

@@ -76,6 +76,7 @@ struct Request {
   uint64_t id = 0;
   ooc_mesh mesh;
   uint64_t footprint = 0;
+  bool sized = false;                         // footprint computed (by a sizing thread)
   void* h_nodes = nullptr;                    // host results (pinned pool blocks)
   void* h_data = nullptr;
   size_t h_nodes_cap = 0, h_data_cap = 0;
@@ -116,6 +117,7 @@ bool valid(const ooc_mesh& m) {
 // starts, first child and winner (7 x 4 bytes) and its -levels cache (24
 // bytes), with room for the batch's job tables.
 constexpr uint64_t kNodeBytes = 120;
+constexpr int kSizers = 4;  // threads that compute the footprints of submitted requests
 
 double voxel_bound(const float* v, float unit_div, uint64_t N) {
   double box = 1.0;
@@ -196,7 +198,10 @@ struct ooc_server {
   bool stop_delivery = false;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::deque<Request*> queue;
+  std::deque<Request*> queue;                   // submission order
+  std::deque<Request*> unsized;                 // footprints not yet computed, oldest first
+  std::condition_variable cv_size;
+  std::vector<std::thread> sizers;
   std::deque<Request*> done;
   std::unordered_map<uint64_t, Request*> held;  // polled, not yet released
   uint64_t next_id = 1;
@@ -207,9 +212,40 @@ struct ooc_server {
 
   double now_us() const { return std::chrono::duration<double, std::micro>(Clock::now() - t0).count(); }
 
-  // every queued footprint is within the budget (ooc_server_submit), so a request
-  // always fits once nothing else holds memory
-  bool fits(const Request* r) const { return in_flight + r->footprint <= cfg.memory_budget; }
+  // A request is admitted in submission order, once its footprint is known and
+  // fits.  Every sized request left in the queue is within the budget (larger ones
+  // are refused by the sizing threads), so it fits once nothing else holds memory.
+  bool fits(const Request* r) const { return r->sized && in_flight + r->footprint <= cfg.memory_budget; }
+
+  // Footprints are computed off the submitting thread: one pass over a request's
+  // triangles costs up to milliseconds for large meshes.
+  void sizing_loop() {
+    for (;;) {
+      Request* r = nullptr;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_size.wait(lk, [&] { return stop || !unsized.empty(); });
+        if (stop) return;
+        r = unsized.front();
+        unsized.pop_front();
+      }
+      const uint64_t fp = footprint(r->mesh);
+      bool refused = false;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        if (stop) return;  // the server is shutting down; `r` is dropped with the queue
+        r->footprint = fp;
+        r->sized = true;
+        if (fp > cfg.memory_budget) {
+          auto it = std::find(queue.begin(), queue.end(), r);
+          if (it != queue.end()) queue.erase(it);
+          refused = true;
+        }
+      }
+      if (refused) publish(r, OOC_ERR_LIMIT);
+      cv_work.notify_all();
+    }
+  }
 
   // A request is complete (and can be polled, then released by the caller)
   // as soon as its mesh is; the engine does not touch it afterwards.
@@ -455,6 +491,7 @@ int ooc_server_create(const ooc_server_config* cfg, ooc_server** out) {
     }
   }
   if (cfg->result_location == OOC_RESULT_HOST) s->deliverer = std::thread([s] { s->delivery_loop(); });
+  for (int i = 0; i < kSizers; i++) s->sizers.emplace_back([s] { s->sizing_loop(); });
   for (ooc_ctx* c : s->engines) s->threads.emplace_back([s, c] { s->engine_loop(c); });
   *out = s;
   return OOC_OK;
@@ -466,19 +503,15 @@ int ooc_server_submit(ooc_server* s, const ooc_mesh* mesh, uint64_t* id) {
   Request* r = new (std::nothrow) Request();
   if (!r) return OOC_ERR_OOM;
   r->mesh = *mesh;
-  r->footprint = footprint(*mesh);
-  if (r->footprint > s->cfg.memory_budget) {
-    delete r;
-    return OOC_ERR_LIMIT;
-  }
   r->t_submit = t;
   {
     std::lock_guard<std::mutex> lk(s->mu);
     r->id = s->next_id++;
     s->queue.push_back(r);
+    s->unsized.push_back(r);
   }
   if (id) *id = r->id;
-  s->cv_work.notify_one();
+  s->cv_size.notify_one();
   return OOC_OK;
 }
 
@@ -564,12 +597,16 @@ int ooc_server_release(ooc_server* s, uint64_t id) {
 
 void ooc_server_destroy(ooc_server* s) {
   if (!s) return;
+  std::deque<Request*> dropped;  // never started
   {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop = true;
-    for (Request* r : s->queue) delete r;  // never started
-    s->queue.clear();
+    dropped.swap(s->queue);
+    s->unsized.clear();
   }
+  s->cv_size.notify_all();
+  for (std::thread& t : s->sizers) t.join();  // a sizing thread may still hold one of `dropped`
+  for (Request* r : dropped) delete r;
   s->cv_work.notify_all();
   for (std::thread& t : s->threads) t.join();
   {  // the engines are done: deliver what they queued, then stop
