@@ -246,6 +246,8 @@ def run_ours(args, world, rank, local):
     h_tris = torch.from_numpy(tris).pin_memory()
     stream = torch.cuda.Stream(device=local)
     b = ooc.Builder(local)
+    if args.batch_budget:
+        b.set_batch_budget(args.batch_budget)
 
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     # warm-up (also sizes every device buffer)
@@ -397,6 +399,7 @@ def run_ours(args, world, rank, local):
         "file_to_file": files,
         "kernels_ms": {k: v[0] for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])},
         "clocks": clocks,
+        "tuning": b.tuning().as_dict(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sec, runs = cpu_port_time(tris, w, budget_s=10.0, max_runs=8)
@@ -761,6 +764,8 @@ def main():
     ap.add_argument("--engines", type=int, default=2, help="serve: engines of the served arm")
     ap.add_argument("--burst", type=int, default=4096, help="serve: requests of the capacity burst")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-budget", type=int, default=0,
+                    help="occupancy-pyramid bytes per sub-batch (0: the library's default, 4 GiB)")
     ap.add_argument("--clock-window", type=float, default=1.5,
                     help="seconds of back-to-back builds the clock sampler watches around the timed steps")
     ap.add_argument("--no-files", action="store_true", help="skip the file-to-file measurement")

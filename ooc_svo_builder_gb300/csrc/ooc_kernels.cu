@@ -830,47 +830,24 @@ __global__ void k_vox_small_occ(VoxJob j) {
   if (i < j.n_items) vox_small_occ_item(j, i);
 }
 
-// Pass 1 for small items: rank the voxels their pass mask names.  The box is
-// walked in pass 0's order, with Morton bits stepped by the carry trick, and
-// the words and scan base of a leaf block are reused while consecutive voxels
-// stay in it.
+// Pass 1 for small items: rank the voxels their pass mask names.
 __device__ __forceinline__ void vox_small_win_item(const VoxJob& j, uint64_t i) {
-  const uint64_t mask = j.item_mask[i];
+  uint64_t mask = j.item_mask[i];
   if (!mask) return;
   const uint32_t t = (uint32_t)item_triangle(j, i);
   const uint64_t box = j.item_box[i];
-  const uint32_t bx = (uint32_t)(box >> 30 & 63u) + 1u, by = (uint32_t)(box >> 36 & 63u) + 1u,
-                 bz = (uint32_t)(box >> 42 & 63u) + 1u;
-  constexpr uint32_t XBITS = 0x09249249u, YBITS = 0x12492492u, ZBITS = 0x24924924u;
-  const uint32_t mz0 = spread3_10((uint32_t)(box >> 20) & 1023u) << 2;
-  const uint32_t my0 = spread3_10((uint32_t)(box >> 10) & 1023u) << 1;
-  uint32_t mx = spread3_10((uint32_t)box & 1023u);
-  uint32_t cblk = 0xffffffffu, cbase = 0;
-  uint4 q0 = make_uint4(0u, 0u, 0u, 0u), q1 = q0;
-  uint32_t c = 0;  // candidate index (ix * by + iy) * bz + iz
-  for (uint32_t ix = 0; ix < bx; ix++, mx = ((mx | ~XBITS) + 1u) & XBITS) {
-    uint32_t my = my0;
-    for (uint32_t iy = 0; iy < by; iy++, my = ((my | ~YBITS) + 2u) & YBITS) {
-      if (!(mask >> (c & 63u)) || c >= 64) return;  // no passing candidate left
-      uint32_t mz = mz0;
-      for (uint32_t iz = 0; iz < bz; iz++, c++, mz = ((mz | ~ZBITS) + 4u) & ZBITS) {
-        if (!((mask >> c) & 1u)) continue;
-        const uint32_t m = mx | my | mz, blk = m >> 8;
-        if (blk != cblk) {
-          cblk = blk;
-          cbase = (j.leaflocal ? j.leafscan[blk / kLeafGroup] + j.leaflocal[blk] : j.leafscan[blk]) - j.leafscan_base;
-          const uint4* q = reinterpret_cast<const uint4*>(j.leafbits + (uint64_t)blk * 8);
-          q0 = q[0];
-          q1 = q[1];
-        }
-        const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
-        const uint32_t wi = (m >> 5) & 7u, lowmask = (1u << (m & 31)) - 1u;
-        uint32_t r = cbase;
-#pragma unroll
-        for (uint32_t k = 0; k < 8; k++) r += __popc(k < wi ? w[k] : (k == wi ? (w[k] & lowmask) : 0u));
-        atomicMin(&j.winners[r], t);
-      }
-    }
+  const uint32_t lx = (uint32_t)box & 1023u, ly = (uint32_t)(box >> 10) & 1023u, lz = (uint32_t)(box >> 20) & 1023u;
+  const uint32_t by = (uint32_t)(box >> 36 & 63u) + 1u, bz = (uint32_t)(box >> 42 & 63u) + 1u;
+  // q / d for q < 64, d <= 64 as (q * ceil(2^16 / d)) >> 16: the error of the rounded-up
+  // reciprocal adds less than q / 2^16 < 1/d, which never carries past the next integer
+  const uint32_t rz = (65535u + bz) / bz, ry = (65535u + by) / by;
+  while (mask) {
+    const uint32_t q = (uint32_t)(__ffsll((long long)mask) - 1);
+    mask &= mask - 1;
+    const uint32_t col = (q * rz) >> 16, z = q - col * bz;
+    const uint32_t x = (col * ry) >> 16, y = col - x * by;
+    const uint32_t m = morton_local(lx + x, ly + y, lz + z);
+    atomicMin(&j.winners[leaf_rank(j, m)], t);
   }
 }
 

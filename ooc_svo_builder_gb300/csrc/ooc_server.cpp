@@ -22,6 +22,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
@@ -34,42 +35,39 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 // Pinned host blocks for host results, kept and reused across requests
-// (pinning memory costs far more than copying into it): power-of-two size
-// classes from 64 KiB.
+// (pinning memory costs far more than copying into it).  A request takes the
+// smallest free block that holds it, if that block is at most four times its
+// size; otherwise a new block of the next power of two from 64 KiB is pinned.
 class PinnedPool {
  public:
   ~PinnedPool() {
-    for (auto& kv : free_)
-      for (void* p : kv.second) cudaFreeHost(p);
+    for (auto& kv : free_) cudaFreeHost(kv.second);
   }
   void* get(size_t n, size_t& cap) {
-    cap = klass(n);
     {
       std::lock_guard<std::mutex> lk(mu_);
-      auto it = free_.find(cap);
-      if (it != free_.end() && !it->second.empty()) {
-        void* p = it->second.back();
-        it->second.pop_back();
+      auto it = free_.lower_bound(n);
+      if (it != free_.end() && it->first / 4 <= n) {
+        cap = it->first;
+        void* p = it->second;
+        free_.erase(it);
         return p;
       }
     }
+    cap = 64 << 10;
+    while (cap < n) cap <<= 1;
     void* p = nullptr;
     return cudaMallocHost(&p, cap) == cudaSuccess ? p : nullptr;
   }
   void put(void* p, size_t cap) {
     if (!p) return;
     std::lock_guard<std::mutex> lk(mu_);
-    free_[cap].push_back(p);
+    free_.emplace(cap, p);
   }
 
  private:
-  static size_t klass(size_t n) {
-    size_t c = 64 << 10;
-    while (c < n) c <<= 1;
-    return c;
-  }
   std::mutex mu_;
-  std::unordered_map<size_t, std::vector<void*>> free_;
+  std::multimap<size_t, void*> free_;
 };
 
 struct Request {
@@ -190,7 +188,9 @@ struct ooc_server {
   cudaStream_t release_stream = nullptr;  // device results are freed on it
   cudaStream_t d2h_stream = nullptr;      // host results are copied back on it
   PinnedPool pinned;
-  // host results whose copy back is queued, in order, with the event after it
+  // host results: complete on the device, waiting for the delivery thread to queue their
+  // copy back; and those whose copy back is queued, in order, with the event after it
+  std::deque<Request*> to_copy;
   std::deque<std::pair<Request*, cudaEvent_t>> deliveries;
   std::vector<cudaEvent_t> spare_events;
   std::condition_variable cv_deliver;
@@ -303,16 +303,20 @@ struct ooc_server {
       mark(call, mesh);
       return 0;
     }
-    // host results: the mesh is complete in this batch (never rerun); it is published
-    // once its copy into pinned memory has landed
+    // host results: the mesh is complete in this batch (never rerun); the delivery
+    // thread copies it into pinned memory and publishes it once the copy has landed
     Request* r = call.reqs[mesh];
     r->info = call.infos[mesh];
     (*call.published)[call.index[mesh]] = 1;
-    call.s->deliver(r);
+    {
+      std::lock_guard<std::mutex> lk(call.s->mu);
+      call.s->to_copy.push_back(r);
+    }
+    call.s->cv_deliver.notify_one();
     return 0;
   }
 
-  // Queue a host result's copy back into pinned pool blocks on d2h_stream.
+  // Queue a host result's copy back into pinned pool blocks on d2h_stream (delivery thread).
   void deliver(Request* r) {
     r->h_nodes_bytes = r->d_nodes_bytes;
     r->h_data_bytes = r->d_data_bytes;
@@ -341,26 +345,34 @@ struct ooc_server {
       publish(r, OOC_ERR_OOM);
       return;
     }
-    {
-      std::lock_guard<std::mutex> lk(mu);
-      deliveries.push_back({r, ev});
-    }
-    cv_deliver.notify_one();
+    deliveries.push_back({r, ev});
   }
 
-  // Publishes host results in the order their copies were queued, once each has landed.
+  // The delivery thread: queues the copy back of every host result the engines
+  // hand over (pinning pool blocks as needed, off the engines' threads), and
+  // publishes the results in that order once each copy has landed.
   void delivery_loop() {
     cudaSetDevice(cfg.device);
     for (;;) {
-      std::pair<Request*, cudaEvent_t> d;
+      std::deque<Request*> batch;
       {
         std::unique_lock<std::mutex> lk(mu);
-        cv_deliver.wait(lk, [&] { return stop_delivery || !deliveries.empty(); });
-        if (deliveries.empty()) return;
-        d = deliveries.front();
-        deliveries.pop_front();
+        cv_deliver.wait(lk, [&] { return stop_delivery || !to_copy.empty() || !deliveries.empty(); });
+        if (to_copy.empty() && deliveries.empty()) return;
+        batch.swap(to_copy);
       }
-      const bool ok = cudaEventSynchronize(d.second) == cudaSuccess;
+      for (Request* r : batch) deliver(r);  // `deliveries` is this thread's alone
+      if (deliveries.empty()) continue;
+      const std::pair<Request*, cudaEvent_t> d = deliveries.front();
+      // with more results waiting to be queued, only take the oldest copy if it has landed
+      bool waiting = false;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        waiting = !to_copy.empty();
+      }
+      cudaError_t e = waiting ? cudaEventQuery(d.second) : cudaEventSynchronize(d.second);
+      if (e == cudaErrorNotReady) continue;
+      deliveries.pop_front();
       Request* r = d.first;
       free_device(r);
       r->d_nodes_bytes = r->d_data_bytes = 0;
@@ -368,7 +380,7 @@ struct ooc_server {
         std::lock_guard<std::mutex> lk(mu);
         spare_events.push_back(d.second);
       }
-      publish(r, ok ? OOC_OK : OOC_ERR_DEVICE);
+      publish(r, e == cudaSuccess ? OOC_OK : OOC_ERR_DEVICE);
     }
   }
 
