@@ -196,7 +196,7 @@ def cpu_port_time(tris, w, budget_s: float, max_runs: int, min_runs: int = 1):
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of a workload's dominant
 # kernel, from the ncu captures summarised under profiles/: (workload, kernel) -> (bytes, summary)
 NCU_TRAFFIC = {
-    ("heightfield1024", "vox_small_occupancy"): (179.5e6 + 33.1e6, "profiles/vox_small_heightfield1024.md"),
+    ("heightfield1024", "vox_small_occupancy"): (179.5e6 + 34.5e6, "profiles/vox_small_heightfield1024.md"),
 }
 
 
