@@ -659,6 +659,10 @@ def run_serve(args, world, rank, local):
                 for _ in warm:
                     while srv.poll(1000, copy=False) is None:
                         pass
+                # an unmeasured stream at the same rate first, so the measured one sees the
+                # server in its steady state (engine buffers grown, pinned result blocks pooled)
+                if args.serve_warmup > 0:
+                    serve_stream(srv, pool, r, args.serve_warmup, seed=1005 + int(r), drain_s=args.drain)
                 out[arm].append(serve_stream(srv, pool, r, args.duration, seed=5 + int(r), drain_s=args.drain))
             print("serve %s %.0f req/s: %s" % (arm, r, json.dumps(out[arm][-1])), file=sys.stderr, flush=True)
     # capacity of the resident arms: a burst of requests submitted at once
@@ -682,10 +686,11 @@ def run_serve(args, world, rank, local):
         "metric": "served meshes/s", "value": top["meshes_per_s"], "unit": "meshes/s", "n_gpus": world,
         "steps": top["completed"], "warmup": 1, "ms_per_step": 1e3 / max(top["meshes_per_s"], 1e-9),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "configuration 5: Poisson arrivals at %s req/s, %.0f s each, meshes drawn from a "
-                               "pool of %d configuration-4 meshes with gridsizes 128..2048; 120 GB admission "
-                               "budget; pinned host triangles in, host octree bytes out"
-                               % (args.rates, args.duration, len(pool)),
+        "config": {"workload": "configuration 5: Poisson arrivals at %s req/s, %.0f s each after %.0f s "
+                               "unmeasured at the same rate, meshes drawn from a pool of %d configuration-4 "
+                               "meshes with gridsizes 128..2048; 120 GB admission budget; pinned host "
+                               "triangles in, host octree bytes out"
+                               % (args.rates, args.duration, args.serve_warmup, len(pool)),
                    "name": "serve", "engines": args.engines, "max_batch": 256,
                    "value_arm": "served_resident: octrees resident in HBM, released by the poller"},
         "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
@@ -761,6 +766,8 @@ def main():
     ap.add_argument("--rates", default="200,500,1000,2000", help="serve: offered request rates, req/s")
     ap.add_argument("--duration", type=float, default=5.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--drain", type=float, default=10.0, help="serve: seconds to wait for the queue to drain")
+    ap.add_argument("--serve-warmup", type=float, default=1.0,
+                    help="serve: seconds of unmeasured arrivals at each rate before the measured ones")
     ap.add_argument("--engines", type=int, default=2, help="serve: engines of the served arm")
     ap.add_argument("--burst", type=int, default=4096, help="serve: requests of the capacity burst")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -69,3 +69,22 @@ def test_noalloc_rejects_sizes_beyond_its_limit():
     big = ooc.make_params(2 * ooc.NOALLOC_MAX_GRIDSIZE, 1 << 20, geometry_only=True)
     rc = ooc.voxelize_occupancy_noalloc(big, tris.data_ptr(), 1, out.data_ptr(), out.numel())
     assert rc == 6
+
+
+def test_noalloc_near_its_limits():
+    """Gridsize 1024 (the largest it takes) and 1,040,000 triangles (close to its 1,048,576),
+    half of them large enough for the large-triangle kernel: the sizes that fill its fixed
+    scratch.  The regular build runs in payload mode so that its leaves' Morton codes come
+    straight from the data records."""
+    torch = pytest.importorskip("torch")
+    N = ooc.NOALLOC_MAX_GRIDSIZE
+    tris = tri.soup_tris(1_040_000, N, seed=43, sigma=1.0, n_spheres=50, payload=True)
+    assert tris.shape[0] <= ooc.NOALLOC_MAX_TRIANGLES
+    got = noalloc_occupancy(torch, tris, N, True)
+    with ooc.Builder(0) as b:
+        res = b.build(tris, ooc.make_params(N, 2048, geometry_only=False))
+    m = res.tree.data["morton"][1:].astype(np.int64)
+    want = np.zeros(N ** 3 // 32, dtype=np.uint32)
+    np.bitwise_or.at(want, m >> 5, (np.uint32(1) << (m & 31).astype(np.uint32)))
+    assert int(np.unpackbits(want.view(np.uint8)).sum()) == res.info["n_filled"]
+    assert np.array_equal(got, want), "occupancy differs in %d words" % int((got != want).sum())
