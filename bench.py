@@ -446,8 +446,12 @@ def run_batch(args, world, rank, local):
     for q, i in enumerate(sample_idx):
         sample[q] = arr[i]
     t0 = time.perf_counter()
-    tuning = b.autotune(mesh_array=sample, n_meshes=len(sample_idx)).as_dict()
+    tuned = b.autotune(mesh_array=sample, n_meshes=len(sample_idx))
     tune_s = time.perf_counter() - t0
+    if args.persistent != "auto":  # one phase-A form held, for comparing the two
+        tuned.persistent = int(args.persistent)
+        b.set_tuning(tuned)
+    tuning = tuned.as_dict()
 
     def timed(fn, warm, reps):
         for _ in range(warm):
@@ -643,8 +647,9 @@ def run_serve(args, world, rank, local):
     # resident: octrees stay in HBM (released by the poller); host: copied back to host memory.
     arms = {"served_resident": dict(engines=args.engines, max_batch=256, memory_budget=120 << 30, resident=True),
             "plain_resident": dict(engines=1, max_batch=1, memory_budget=120 << 30, resident=True),
-            "served_host": dict(engines=args.engines, max_batch=256, memory_budget=120 << 30),
-            "plain_host": dict(engines=1, max_batch=1, memory_budget=120 << 30)}
+            "served_host": dict(engines=args.engines, max_batch=256, memory_budget=120 << 30,
+                                host_pool_mb=args.host_pool_mb),
+            "plain_host": dict(engines=1, max_batch=1, memory_budget=120 << 30, host_pool_mb=args.host_pool_mb)}
     # warm-up set: the requests with the largest grids, then a spread of the rest
     order = sorted(range(len(pool)), key=lambda i: -pool[i][3] * pool[i][1])
     warm = order[:16] + order[16::max(1, len(pool) // 64)]
@@ -691,7 +696,7 @@ def run_serve(args, world, rank, local):
                                "meshes with gridsizes 128..2048; 120 GB admission budget; pinned host "
                                "triangles in, host octree bytes out"
                                % (args.rates, args.duration, args.serve_warmup, len(pool)),
-                   "name": "serve", "engines": args.engines, "max_batch": 256,
+                   "name": "serve", "engines": args.engines, "max_batch": 256, "host_pool_mb": args.host_pool_mb,
                    "value_arm": "served_resident: octrees resident in HBM, released by the poller"},
         "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
         "arms": out,
@@ -769,10 +774,15 @@ def main():
     ap.add_argument("--serve-warmup", type=float, default=1.0,
                     help="serve: seconds of unmeasured arrivals at each rate before the measured ones")
     ap.add_argument("--engines", type=int, default=2, help="serve: engines of the served arm")
+    ap.add_argument("--host-pool-mb", type=int, default=8192,
+                    help="serve: pinned host memory each host-result server reserves at creation, MiB")
     ap.add_argument("--burst", type=int, default=4096, help="serve: requests of the capacity burst")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-budget", type=int, default=0,
                     help="occupancy-pyramid bytes per sub-batch (0: the library's default, 4 GiB)")
+    ap.add_argument("--persistent", default="auto", choices=["auto", "0", "1"],
+                    help="configuration 4: the autotuner's phase-A form, or one held (0: a launch per pass, "
+                         "1: the persistent work-queue kernel)")
     ap.add_argument("--clock-window", type=float, default=1.5,
                     help="seconds of back-to-back builds the clock sampler watches around the timed steps")
     ap.add_argument("--no-files", action="store_true", help="skip the file-to-file measurement")

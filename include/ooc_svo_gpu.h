@@ -174,7 +174,10 @@ typedef struct {
   uint32_t pdl;               /* 1: each kernel of a launch sequence may start while its predecessor drains
                                  (programmatic dependent launch; it waits for the predecessor's results
                                  before touching memory); 0: it starts when the predecessor has finished */
-  uint32_t reserved;          /* 0 */
+  uint32_t persistent;        /* 1: the occupancy passes and the pyramid levels of a sub-batch run as one
+                                 persistent launch whose warps take (stripe, chunk), large-triangle task
+                                 and (stripe, level, block range) units from a device work queue; 0: one
+                                 launch per pass and level */
 } ooc_tuning;
 
 int ooc_get_tuning(const ooc_ctx* ctx, ooc_tuning* out);
@@ -333,7 +336,13 @@ typedef struct {
    * batch's requests not yet complete then run again alone, as after any failed
    * batch. */
   uint32_t fail_batch_at_mesh;
-  uint32_t reserved;
+  /* Host results: MiB of pinned host memory to reserve at creation for them
+   * (0: pin blocks on demand).  Pinning takes a lock of the CUDA driver for as
+   * long as it runs, so a block pinned while serving delays every engine; a
+   * reserve that covers the results in flight keeps pinning out of the serving
+   * loop.  A result the reserve cannot hold gets a block pinned on demand.
+   * Ignored for device results; OOC_ERR_OOM when the host cannot pin it. */
+  uint32_t host_pool_mb;
 } ooc_server_config;
 
 typedef struct {
@@ -345,9 +354,10 @@ typedef struct {
   const void* data;       /* data file bytes                                       */
   uint64_t data_bytes;
   ooc_build_info info;
-  double t_submit_us;     /* times in microseconds since the server started        */
-  double t_start_us;
-  double t_done_us;
+  double t_submit_us;     /* times in microseconds since the server started:       */
+  double t_start_us;      /*   its batch started                                   */
+  double t_built_us;      /*   its octree was complete in device memory            */
+  double t_done_us;       /*   it completed (host results: after the copy back)    */
   uint64_t batch_size;    /* requests in the batch this one ran in                 */
 } ooc_result;
 

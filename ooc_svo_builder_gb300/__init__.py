@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import threading
 from dataclasses import dataclass
 
 import numpy as np
@@ -68,20 +69,21 @@ RESULT_HOST, RESULT_DEVICE = 0, 1
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("engines", ctypes.c_int32), ("max_batch", ctypes.c_uint32),
                 ("result_location", ctypes.c_int32), ("memory_budget", ctypes.c_uint64),
-                ("fail_batch_at_mesh", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("fail_batch_at_mesh", ctypes.c_uint32), ("host_pool_mb", ctypes.c_uint32)]
 
 
 class Result(ctypes.Structure):
     _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int32), ("location", ctypes.c_int32),
                 ("nodes", ctypes.c_void_p), ("nodes_bytes", ctypes.c_uint64), ("data", ctypes.c_void_p),
                 ("data_bytes", ctypes.c_uint64), ("info", BuildInfo), ("t_submit_us", ctypes.c_double),
-                ("t_start_us", ctypes.c_double), ("t_done_us", ctypes.c_double), ("batch_size", ctypes.c_uint64)]
+                ("t_start_us", ctypes.c_double), ("t_built_us", ctypes.c_double), ("t_done_us", ctypes.c_double),
+                ("batch_size", ctypes.c_uint64)]
 
 
 class Tuning(ctypes.Structure):
     _fields_ = [("small_vol", ctypes.c_uint32), ("lines_per_lane", ctypes.c_uint32), ("large_block", ctypes.c_uint32),
                 ("large_ctas_per_sm", ctypes.c_uint32), ("batch_budget", ctypes.c_uint64), ("graphs", ctypes.c_uint32),
-                ("light_per_thread", ctypes.c_uint32), ("pdl", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("light_per_thread", ctypes.c_uint32), ("pdl", ctypes.c_uint32), ("persistent", ctypes.c_uint32)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -527,18 +529,22 @@ class Server:
     """The serving loop: submit meshes, poll completed octrees (see ooc_server_* in the C ABI)."""
 
     def __init__(self, device: int = 0, engines: int = 2, max_batch: int = 256, memory_budget: int = 120 << 30,
-                 resident: bool = False, fail_batch_at_mesh: int = 0):
+                 resident: bool = False, fail_batch_at_mesh: int = 0, host_pool_mb: int = 0):
         """`resident`: results stay in device memory (read with poll(copy=True) or ooc_server_read).
-        `fail_batch_at_mesh`: fault injection for tests (ooc_server_config)."""
+        `fail_batch_at_mesh`: fault injection for tests; `host_pool_mb`: pinned host memory reserved
+        for host results at creation (ooc_server_config)."""
         self.lib = load_library()
         cfg = ServerConfig(device, engines, max_batch, RESULT_DEVICE if resident else RESULT_HOST, memory_budget,
-                           fail_batch_at_mesh, 0)
+                           fail_batch_at_mesh, host_pool_mb)
         h = ctypes.c_void_p()
         rc = self.lib.ooc_server_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc != OOC_OK:
             raise OocError(rc, "ooc_server_create failed")
         self.h = h
         self._keep = {}
+        # a request can complete before its submitting call returns: the id is recorded
+        # under this lock, which a poller takes before looking the id up
+        self._lock = threading.Lock()
 
     def submit(self, tris: np.ndarray, params: BuildParams) -> int:
         tris = np.ascontiguousarray(tris, dtype=np.float32)
@@ -550,10 +556,11 @@ class Server:
         m.n_tris = tris.shape[0]
         m.params = params
         rid = ctypes.c_uint64()
-        rc = self.lib.ooc_server_submit(self.h, ctypes.byref(m), ctypes.byref(rid))
-        if rc != OOC_OK:
-            raise OocError(rc, "ooc_server_submit failed")
-        self._keep[rid.value] = (tris, int(params.gridsize))
+        with self._lock:
+            rc = self.lib.ooc_server_submit(self.h, ctypes.byref(m), ctypes.byref(rid))
+            if rc != OOC_OK:
+                raise OocError(rc, "ooc_server_submit failed")
+            self._keep[rid.value] = (tris, int(params.gridsize))
         return rid.value
 
     def submit_ptr(self, tris_ptr: int, n_tris: int, params: BuildParams, gridsize: int) -> int:
@@ -563,10 +570,11 @@ class Server:
         m.n_tris = n_tris
         m.params = params
         rid = ctypes.c_uint64()
-        rc = self.lib.ooc_server_submit(self.h, ctypes.byref(m), ctypes.byref(rid))
-        if rc != OOC_OK:
-            raise OocError(rc, "ooc_server_submit failed")
-        self._keep[rid.value] = (None, gridsize)
+        with self._lock:
+            rc = self.lib.ooc_server_submit(self.h, ctypes.byref(m), ctypes.byref(rid))
+            if rc != OOC_OK:
+                raise OocError(rc, "ooc_server_submit failed")
+            self._keep[rid.value] = (None, gridsize)
         return rid.value
 
     def poll(self, timeout_ms: int = 100, copy: bool = True):
@@ -577,9 +585,11 @@ class Server:
             return None
         if rc != OOC_OK:
             raise OocError(rc, "ooc_server_poll failed")
-        _, gridsize = self._keep.pop(r.id)
+        with self._lock:
+            _, gridsize = self._keep.pop(r.id)
         out = {"id": r.id, "status": r.status, "info": _info_dict(r.info), "t_submit_us": r.t_submit_us,
-               "t_start_us": r.t_start_us, "t_done_us": r.t_done_us, "batch_size": r.batch_size,
+               "t_start_us": r.t_start_us, "t_built_us": r.t_built_us, "t_done_us": r.t_done_us,
+               "batch_size": r.batch_size,
                "bytes": r.nodes_bytes + r.data_bytes, "location": r.location}
         if copy and r.status == OOC_OK:
             nodes = np.empty(r.nodes_bytes, np.uint8)

@@ -135,6 +135,12 @@ struct ooc_ctx {
       d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo, d_itemmask,
       d_firstchild, d_itembox, d_leaf, d_touch, d_local, d_taskmap;
   uint64_t max_tasks = 0;  // most large-item warp tasks a sub-batch has had (sizes the task map)
+  // persistent phase A (ooc_tuning::persistent): its counters, its task map (all ones
+  // between launches: every entry a launch fills is emptied by the warp that reads it)
+  DevBuf d_pctr, d_pmap;
+  bool pmap_empty = false;
+  int persist_per_sm = -1;  // CTAs per SM of the persistent kernel for persist_lpl
+  uint32_t persist_lpl = 0;
   bool leaf_zero = true;  // d_leaf and d_touch hold only zeros (no sub-batch left them dirty)
   PinBuf h_misc, h_recs, h_tables1, h_tables2;
   // double-buffered outputs of pipelined sub-batches
@@ -854,6 +860,37 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     return (upper + 31) / 32 * 32 + (pyr[s].lv[pyr[s].depth].nscan + 31) / 32 * 32;
   });
 
+  // persistent phase A: 32-item chunks and pyramid units per stripe, and the
+  // per-stripe counts of units not yet done that its waits read
+  bool persist = c->tuning.persistent != 0 && !pieces;
+  if (persist && (c->persist_per_sm < 0 || c->persist_lpl != c->tuning.lines_per_lane)) {
+    c->persist_per_sm = persist_ctas_per_sm(c->tuning.lines_per_lane);
+    c->persist_lpl = c->tuning.lines_per_lane;
+  }
+  persist = persist && c->persist_per_sm > 0;
+  constexpr uint32_t kPersistEpt = 32;  // pyramid elements per lane of a unit (1,024 per unit)
+  std::vector<uint64_t> p_chunk, p_unit;
+  std::vector<uint32_t> p_occ, p_pyr;
+  const uint32_t p_levels = (uint32_t)cp_pyr.size();
+  if (persist) {
+    p_chunk = cta_prefix(n, kPersistChunkItems, [&](uint32_t s) { return sb[s].n_items; });
+    p_occ.resize(n);
+    for (uint32_t s = 0; s < n; s++) p_occ[s] = (uint32_t)(p_chunk[s + 1] - p_chunk[s]);
+    p_unit.assign(std::max<uint64_t>((uint64_t)p_levels * (n + 1), 1), 0);  // one entry at least: uploaded as is
+    p_pyr.assign(std::max<uint64_t>((uint64_t)p_levels * n, 1), 0);
+    uint64_t acc = 0;
+    for (uint32_t r = 0; r < p_levels; r++) {
+      for (uint32_t s = 0; s < n; s++) {
+        p_unit[(uint64_t)r * (n + 1) + s] = acc;
+        const int l = pyr[s].depth - (int)r;
+        const uint64_t units = l > kTopPyramidLevel ? (pyr[s].lv[l].nscan + 32 * kPersistEpt - 1) / (32 * kPersistEpt) : 0;
+        p_pyr[(uint64_t)r * n + s] = (uint32_t)units;
+        acc += units;
+      }
+      p_unit[(uint64_t)r * (n + 1) + n] = acc;
+    }
+  }
+
   Uploader up1;
   const size_t o_vj = up1.add(vj.data(), n * sizeof(VoxJob));
   const size_t o_pyr = up1.add(pyr.data(), n * sizeof(Pyramid));
@@ -862,6 +899,13 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   std::vector<size_t> o_cpp(cp_pyr.size());
   for (size_t r = 0; r < cp_pyr.size(); r++) o_cpp[r] = up1.add(cp_pyr[r].beg.data(), (n + 1) * 8);
   const size_t o_cc = up1.add(cp_compact.beg.data(), (n + 1) * 8);
+  size_t o_pc = 0, o_pu = 0, o_po = 0, o_pp = 0;
+  if (persist) {
+    o_pc = up1.add(p_chunk.data(), (n + 1) * 8);
+    o_pu = up1.add(p_unit.data(), p_unit.size() * 8);
+    o_po = up1.add(p_occ.data(), n * 4);
+    o_pp = up1.add(p_pyr.data(), p_pyr.size() * 4);
+  }
   unsigned char* t1 = up1.run(c, c->d_tables1, c->h_tables1, st);
   auto dp1 = [&](size_t off) { return reinterpret_cast<const uint64_t*>(t1 + off); };
   const VoxJob* d_vj = reinterpret_cast<const VoxJob*>(t1 + o_vj);
@@ -879,9 +923,50 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     task_map = ensure<uint64_t>(c->d_taskmap, std::max<uint64_t>(items, c->max_tasks) * 8);
     map_cap = c->d_taskmap.cap / 8;
   }
+  PersistJob pj;
+  std::memset(&pj, 0, sizeof(pj));
+  bool any_payload_stripe = false;
+  for (uint32_t s = 0; s < n; s++) any_payload_stripe = any_payload_stripe || !meshes[sb[s].mesh].pl.binary;
+  if (persist) {
+    // task entries: room for the most tasks seen so far, twice over; a chunk whose tasks
+    // do not fit walks them itself
+    const uint64_t cap = std::max<uint64_t>(std::max<uint64_t>(2 * c->max_tasks, items), 4096);
+    const size_t had = c->d_pmap.cap;
+    unsigned long long* pmap = ensure<unsigned long long>(c->d_pmap, cap * 8);
+    if (c->d_pmap.cap != had || !c->pmap_empty) {
+      ck(cudaMemsetAsync(pmap, 0xff, c->d_pmap.cap, st), "memset task entries");
+      c->pmap_empty = true;
+    }
+    pj.jobs = d_vj;
+    pj.pyrs = d_pyr;
+    pj.item_beg = d_beg;
+    pj.n = n;
+    pj.levels = p_levels;
+    pj.chunk_beg = dp1(o_pc);
+    pj.unit_beg = dp1(o_pu);
+    pj.ept = kPersistEpt;
+    pj.top_level = kTopPyramidLevel;
+    pj.occ_left = reinterpret_cast<uint32_t*>(t1 + o_po);
+    pj.pyr_left = reinterpret_cast<uint32_t*>(t1 + o_pp);
+    pj.ctr = ensure<unsigned long long>(c->d_pctr, kPersistCtrWords * 8);
+    pj.map = pmap;
+    pj.cap = c->d_pmap.cap / 8;
+    pj.scan_end = scan + blocks;
+    pj.lines_per_lane = c->tuning.lines_per_lane;
+    c->pmap_empty = false;  // until this launch is known to have ended without a timeout
+  }
   c->leaf_zero = false;  // until the clean at the end of the sub-batch is queued
   run_launches(c, st, 0, [&] {
-    {
+    if (persist) {
+      PhaseScope ph(c, PH_VOX, st);
+      ck(cudaMemsetAsync(task_off + items, 0, 8, st), "memset task_off");
+      ck(cudaMemsetAsync(pj.ctr, 0, kPersistCtrWords * 8, st), "memset persistent counters");
+      launch_b_persist(pj, c->num_sms, c->persist_per_sm, st);
+      if (any_payload_stripe) {  // the winner pass numbers the tasks by item
+        scan_u64_exclusive(task_off, items + 1, taskpart, st);
+        if (map_cap) launch_b_task_map(dp1(o_cpi), n, cp_items[n], d_beg, task_off, items, task_map, map_cap, st);
+      }
+    } else {
       PhaseScope ph(c, PH_VOX, st);
       ck(cudaMemsetAsync(task_off + items, 0, 8, st), "memset task_off");
       if (pieces) {
@@ -908,17 +993,30 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     }
     {
       PhaseScope ph(c, PH_PYR, st);
-      for (size_t r = 0; r < cp_pyr.size(); r++)
-        launch_b_pyramid(d_pyr, dp1(o_cpp[r]), n, cp_pyr[r].beg[n], cp_pyr[r].ept, (int)r, n == 1 ? &pyr[0] : nullptr,
-                         st);
-      launch_b_pyramid_top(d_pyr, n, kTopPyramidLevel, scan + blocks, st);
+      if (!persist) {
+        for (size_t r = 0; r < cp_pyr.size(); r++)
+          launch_b_pyramid(d_pyr, dp1(o_cpp[r]), n, cp_pyr[r].beg[n], cp_pyr[r].ept, (int)r,
+                           n == 1 ? &pyr[0] : nullptr, st);
+        launch_b_pyramid_top(d_pyr, n, kTopPyramidLevel, scan + blocks, st);
+      }
       scan_u32_exclusive(scan, blocks + 1, scanpart, st);
-      launch_b_level_bases(d_pyr, n, d_root, task_off + items, reinterpret_cast<uint64_t*>(d_root + (uint64_t)n * 16 + 8),
-                           flag, st);
+      // the tasks of the sub-batch (sizes the task maps); the persistent kernel counts them itself
+      const uint64_t* tasks = persist ? reinterpret_cast<const uint64_t*>(pj.ctr + kPersistTasksWord) : task_off + items;
+      launch_b_level_bases(d_pyr, n, d_root, tasks, reinterpret_cast<uint64_t*>(d_root + (uint64_t)n * 16 + 8), flag,
+                           st);
       ck(cudaMemcpyAsync(lvl, d_root, ((uint64_t)n * 16 + 10) * 4, cudaMemcpyDeviceToHost, st), "levels");
+      if (persist)
+        ck(cudaMemcpyAsync(lvl + (uint64_t)n * 16 + 12, pj.ctr + kPersistTimeoutWord, 8, cudaMemcpyDeviceToHost, st),
+           "timeout code");
     }
   }, pieces != nullptr);  // waits on the upload stream are not captured
   wait_level_counts(st, idle);
+  if (persist) {
+    uint64_t code;
+    std::memcpy(&code, lvl + (uint64_t)n * 16 + 12, 8);
+    if (code != 0) fail(OOC_ERR_DEVICE, "persistent voxelization: a wait ran out (code " + std::to_string(code) + ")");
+    c->pmap_empty = true;
+  }
   uint64_t tasks_seen;
   std::memcpy(&tasks_seen, lvl + (uint64_t)n * 16 + 8, 8);
   c->max_tasks = std::max(c->max_tasks, tasks_seen);
@@ -2058,7 +2156,7 @@ bool tuning_ok(const ooc_tuning& t) {
   return t.small_vol >= 1 && t.small_vol <= 64 && t.lines_per_lane >= 1 && t.lines_per_lane <= 64 &&
          (t.large_block == 64 || t.large_block == 128 || t.large_block == 256) && t.large_ctas_per_sm >= 1 &&
          t.large_ctas_per_sm <= 16 && t.batch_budget >= 4096 && t.graphs <= 1 && t.light_per_thread >= 1 &&
-         t.light_per_thread <= 16 && t.pdl <= 1 && t.reserved == 0;
+         t.light_per_thread <= 16 && t.pdl <= 1 && t.persistent <= 1;
 }
 
 struct TuneArena {
@@ -2126,7 +2224,7 @@ int ooc_autotune(ooc_ctx* c, const ooc_mesh* sample, uint64_t n, ooc_tuning* bes
   if (rc == OOC_OK) rc = time_one(cur, cur_ms);
   // one coordinate pass: each choice in turn, the others held at their best so far
   const uint32_t lpl[] = {4, 8, 16, 32}, cps[] = {2, 4, 8}, blk[] = {128, 256}, svol[] = {16, 32, 48, 64}, gr[] = {0, 1},
-                 ept[] = {1, 2, 4, 8}, pdl[] = {0, 1};
+                 ept[] = {1, 2, 4, 8}, pdl[] = {0, 1}, per[] = {0, 1};
   const uint64_t bud[] = {1ull << 30, 2ull << 30, 4ull << 30, 8ull << 30};
   auto try_values = [&](auto setter, const auto& values) {
     for (const auto& v : values) {
@@ -2150,6 +2248,7 @@ int ooc_autotune(ooc_ctx* c, const ooc_mesh* sample, uint64_t n, ooc_tuning* bes
   try_values([](ooc_tuning& t, uint32_t v) { t.light_per_thread = v; }, ept);
   try_values([](ooc_tuning& t, uint32_t v) { t.graphs = v; }, gr);
   try_values([](ooc_tuning& t, uint32_t v) { t.pdl = v; }, pdl);
+  try_values([](ooc_tuning& t, uint32_t v) { t.persistent = v; }, per);
   c->tuning = rc == OOC_OK ? cur : start;
   if (best) *best = c->tuning;
   return rc;

@@ -213,6 +213,33 @@ void launch_b_pyramid(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, 
 // One CTA per stripe: levels min(l_hi, depth) .. 0.
 // Also zeroes *scan_end, the block scan's total entry, before the scan.
 void launch_b_pyramid_top(const Pyramid* pyrs, uint32_t n_stripes, int l_hi, uint32_t* scan_end, cudaStream_t st);
+// The persistent phase-A kernel's inputs (ooc_tuning::persistent).
+struct PersistJob {
+  const VoxJob* jobs;
+  const Pyramid* pyrs;
+  const uint64_t* item_beg;   // n + 1: first item of each stripe in the sub-batch
+  uint32_t n;                 // stripes
+  uint32_t levels;            // R: pyramid levels below the top ones, at most (over the stripes)
+  const uint64_t* chunk_beg;  // n + 1: prefix of 256-item chunks per stripe
+  const uint64_t* unit_beg;   // R x (n + 1): prefix of pyramid units per (level r, stripe), r-major, cumulative
+  uint32_t ept;               // elements per lane of a pyramid unit
+  int top_level;              // levels 0..top_level are the top levels
+  uint32_t* occ_left;         // n: occupancy units of each stripe not yet done (chunks, then its queued tasks)
+  uint32_t* pyr_left;         // R x n: pyramid units of (level r, stripe) not yet done
+  unsigned long long* ctr;    // 64 counters, four used: tickets, chunks done, tasks reserved, timeout code
+                              // (kCtr* in the kernel), each on its own 128-byte line
+  unsigned long long* map;    // cap task entries (item | task << 32), all ones when empty
+  uint64_t cap;
+  uint32_t* scan_end;         // the pyramid scan's total entry
+  uint32_t lines_per_lane;
+};
+// CTAs of the persistent kernel one SM holds (0 on an error).
+int persist_ctas_per_sm(uint32_t lines_per_lane);
+void launch_b_persist(const PersistJob& pj, int num_sms, int ctas_per_sm, cudaStream_t st);
+constexpr uint64_t kPersistChunkItems = 256;  // items of a chunk unit
+constexpr uint32_t kPersistCtrWords = 64;     // counters of the persistent kernel
+constexpr uint32_t kPersistTimeoutWord = 48;  // where it records the code of a wait that ran out
+constexpr uint32_t kPersistTasksWord = 32;    // where it counts the tasks it found (queued or not)
 void launch_b_compact(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_t n, uint64_t ctas, uint32_t ept, uint32_t* keys,
                       const Pyramid* single, cudaStream_t st);
 // Zero the marked leaf blocks of every stripe and the marks: one thread per 16 mark bytes.

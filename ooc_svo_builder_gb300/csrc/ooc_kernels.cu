@@ -796,9 +796,7 @@ __device__ __forceinline__ uint64_t vox_small_factored(const VoxJob& j, const Tr
 // Pass 0, one thread per item: items with at most small_vol (<= 64) candidates
 // are voxelized here and leave their pass mask; larger ones get a warp-task
 // count (32 x lines_per_lane lines per task).
-__device__ __forceinline__ void vox_small_occ_item(const VoxJob& j, uint64_t i) {
-  const uint64_t t = item_triangle(j, i);
-  const TriVerts tv = load_verts(j.tris, t, j.stride);
+__device__ __forceinline__ uint64_t vox_small_occ_item(const VoxJob& j, uint64_t i, const TriVerts& tv) {
   int lo[3], hi[3];
   uint64_t cost = 0, mask = 0;
   if (item_box(j, tv, lo, hi)) {
@@ -822,6 +820,11 @@ __device__ __forceinline__ void vox_small_occ_item(const VoxJob& j, uint64_t i) 
   }
   j.task_off[i] = cost;
   if (j.item_mask) j.item_mask[i] = mask;
+  return cost;
+}
+
+__device__ __forceinline__ uint64_t vox_small_occ_item(const VoxJob& j, uint64_t i) {
+  return vox_small_occ_item(j, i, load_verts(j.tris, item_triangle(j, i), j.stride));
 }
 
 __global__ void k_vox_small_occ(VoxJob j) {
@@ -948,20 +951,32 @@ __device__ __forceinline__ uint32_t* level_words(const Pyramid& p, int l) {
 
 // Whether the leaf blocks under block b of level depth-1 (leaf blocks 8b..8b+7,
 // one word of that block each) are all unmarked, so the block is zero.
+// CG: the loads go to L2 (ld.global.cg), for data that other SMs wrote in the
+// same launch (the persistent phase-A kernel); otherwise plain loads.
+template <bool CG>
+__device__ __forceinline__ uint4 ld4(const uint4* p) {
+  if constexpr (CG) return __ldcg(p);
+  else return *p;
+}
+
+template <bool CG = false>
 __device__ __forceinline__ bool parent_block_empty(const Pyramid& p, uint64_t b) {
-  return reinterpret_cast<const uint64_t*>(p.touch)[b] == 0ull;
+  const unsigned long long* t = reinterpret_cast<const unsigned long long*>(p.touch) + b;
+  if constexpr (CG) return __ldcg(t) == 0ull;
+  else return *t == 0ull;
 }
 
 // Block b of level l (not a marked leaf level): its popcount and parent word.
+template <bool CG = false>
 __device__ __forceinline__ void pyramid_block(const Pyramid& p, int l, uint64_t b) {
   const Level& L = p.lv[l];
-  if (p.touch && l == p.depth - 1 && parent_block_empty(p, b)) {
+  if (p.touch && l == p.depth - 1 && parent_block_empty<CG>(p, b)) {
     p.scan[L.off_b + b] = 0u;
     if (l > 0) level_words(p, l - 1)[b] = 0u;
     return;
   }
   const uint4* q = reinterpret_cast<const uint4*>(level_words(p, l) + 8 * b);
-  const uint4 q0 = q[0], q1 = q[1];
+  const uint4 q0 = ld4<CG>(q), q1 = ld4<CG>(q + 1);
   const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
   uint32_t c = 0, pw = 0;
 #pragma unroll
@@ -988,10 +1003,11 @@ __device__ __forceinline__ uint64_t node_index(const Pyramid& p, int l, uint64_t
 
 // A marked leaf level, group q of kLeafGroup blocks: the parent words, the
 // group's node count (its scan entry) and each marked block's offset in it.
+template <bool CG = false>
 __device__ __forceinline__ void leaf_group(const Pyramid& p, uint64_t q) {
   static_assert(kLeafGroup == 16, "one uint4 of marks per group");
   const Level& L = p.lv[p.depth];
-  const uint4 m4 = reinterpret_cast<const uint4*>(p.touch)[q];
+  const uint4 m4 = ld4<CG>(reinterpret_cast<const uint4*>(p.touch) + q);
   uint4* parent = reinterpret_cast<uint4*>(level_words(p, p.depth - 1) + q * kLeafGroup);
   if (!(m4.x | m4.y | m4.z | m4.w)) {  // the parent words stay zero
     p.scan[L.off_b + q] = 0u;
@@ -1006,7 +1022,7 @@ __device__ __forceinline__ void leaf_group(const Pyramid& p, uint64_t q) {
     if ((mw[k >> 2] >> (8 * (k & 3))) & 0xffu) {
       const uint64_t b = q * kLeafGroup + (uint64_t)k;
       const uint4* w4 = reinterpret_cast<const uint4*>(level_words(p, p.depth) + 8 * b);
-      const uint4 q0 = w4[0], q1 = w4[1];
+      const uint4 q0 = ld4<CG>(w4), q1 = ld4<CG>(w4 + 1);
       const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
       uint32_t c = 0;
 #pragma unroll
@@ -1638,9 +1654,10 @@ __global__ void __launch_bounds__(256, 4) kb_vox_large(const VoxJob* __restrict_
 }
 
 // Element e of level l: a block, or a group of blocks of a marked leaf level.
+template <bool CG = false>
 __device__ __forceinline__ void pyramid_elem(const Pyramid& p, int l, uint64_t e) {
-  if (l == p.depth && p.touch) leaf_group(p, e);
-  else pyramid_block(p, l, e);
+  if (l == p.depth && p.touch) leaf_group<CG>(p, e);
+  else pyramid_block<CG>(p, l, e);
 }
 
 // Level depth - r of every stripe that has CTAs in this launch.
@@ -1821,6 +1838,287 @@ __global__ void kb_top_down_top(const Pyramid* __restrict__ pyrs, const EmitJob*
   for (int l = 0; l <= last; l++) {
     for (uint64_t i = threadIdx.x; i < sp.lv[l].n; i += blockDim.x) top_down_node(sp, se, l, i);
     __syncthreads();
+  }
+}
+
+// ===========================================================================
+// Persistent phase A (ooc_tuning::persistent): the occupancy passes and the
+// pyramid levels of every stripe of a sub-batch in one launch.  Each warp
+// takes tickets from one counter and runs the unit its ticket names.  Tickets
+// come in this order:
+//   [0, C)          32-item chunks of the small pass, stripe by stripe;
+//   [C, C + T)      warp tasks of large items, in the order the chunks queued
+//                   them (T is final once every chunk is done);
+//   [C + T, + U)    pyramid units, level by level from the leaf level up to the
+//                   top levels: 32 x ept elements of one level of one stripe;
+//   [.., + n)       the top levels of each stripe, one warp each.
+// A unit waits only for units with smaller tickets (its stripe's occupancy, or
+// its stripe's level below), which running warps hold already, so every wait
+// ends whether or not the whole grid is resident.  Each wait is still bounded:
+// past kPersistSpins polls it records its code in ctr[3] and every warp stops.
+// ===========================================================================
+// Counters, each on its own 128-byte line so the polls of waiting warps do not
+// queue behind the ticket atomics.
+constexpr int kCtrTicket = 0, kCtrChunksDone = 16, kCtrTasksQueued = kPersistTasksWord,
+              kCtrTimeout = kPersistTimeoutWord;
+static_assert(kPersistChunkItems == 32u * 8u, "a chunk is kPersistChunkRounds x 32 items");
+constexpr uint64_t kPersistWaitNs = 4000000000ull;  // a wait gives up after four seconds
+constexpr uint32_t kPersistChunkRounds = 8;          // a chunk is 8 x 32 items
+
+__device__ __forceinline__ uint64_t ld_acquire(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Polling with a growing pause (64 ns to 4 us) and a bound in time.
+struct Backoff {
+  uint64_t t0 = 0;
+  uint32_t ns = 64;
+  // false once the bound has passed (recording `code`) or another warp has recorded one
+  __device__ __forceinline__ bool pause(unsigned long long* ctr, uint32_t code) {
+    if (ld_acquire(ctr + kCtrTimeout) != 0ull) return false;
+    const uint64_t now = global_ns();
+    if (t0 == 0) t0 = now;
+    if (now - t0 > kPersistWaitNs) {
+      atomicCAS(ctr + kCtrTimeout, 0ull, (unsigned long long)code);
+      return false;
+    }
+    __nanosleep(ns);
+    if (ns < 4096) ns <<= 1;
+    return true;
+  }
+};
+
+// Lane 0: wait until *p is zero; false on a timeout (here or in another warp).
+__device__ __forceinline__ bool persist_wait_zero(const uint32_t* p, unsigned long long* ctr, uint32_t code) {
+  Backoff b;
+  while (ld_acquire(p) != 0u)
+    if (!b.pause(ctr, code)) return false;
+  return true;
+}
+
+// Every lane's writes of the unit reach the GPU scope before lane 0 counts it done.
+__device__ __forceinline__ void persist_done(uint32_t* left, int lane) {
+  __threadfence();
+  __syncwarp();
+  if (lane == 0) atomicSub(left, 1u);
+}
+
+__device__ __forceinline__ uint32_t find_stripe(const uint64_t* __restrict__ beg, uint32_t n, uint64_t x) {
+  uint32_t lo = 0, hi = n;  // beg[lo] <= x < beg[hi]
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (beg[mid] <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <typename T>
+__device__ __forceinline__ void stage_warp(T& dst, const T& src, int lane) {
+  static_assert(sizeof(T) % 4 == 0, "staged structs are word-sized");
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(&src);
+  uint32_t* d = reinterpret_cast<uint32_t*>(&dst);
+  for (uint32_t q = (uint32_t)lane; q < sizeof(T) / 4; q += 32u) d[q] = s[q];
+  __syncwarp();
+}
+
+// 32 items of stripe s from item i0: the small pass, then their large items are
+// queued as warp tasks (or, when the task map is full, walked by this warp).
+__device__ __forceinline__ void persist_items(const PersistJob& pj, uint32_t s, uint64_t i0, int lane, const VoxJob& j,
+                                              uint32_t* __restrict__ wl) {
+  const uint64_t i = i0 + (uint64_t)lane;
+  uint32_t cost = 0;
+  if (i < j.n_items) cost = (uint32_t)vox_small_occ_item(j, i);
+  // warp-aggregated reservation of the items' tasks in the map
+  uint32_t excl = cost;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(FULL, excl, o);
+    if (lane >= o) excl += y;
+  }
+  const uint32_t total = __shfl_sync(FULL, excl, 31);
+  excl -= cost;
+  if (total == 0) return;
+  // One atomicAdd per 32 items (a compare-and-swap loop on this one counter
+  // stalled the whole grid).  Tasks reserved at or past `cap` have no entry:
+  // this warp walks them, and the warps that draw their tickets skip them.
+  unsigned long long base = 0;
+  if (lane == 0) {
+    base = atomicAdd(pj.ctr + kCtrTasksQueued, (unsigned long long)total);
+    const uint64_t queued = base >= pj.cap ? 0 : (base + total <= pj.cap ? total : pj.cap - base);
+    if (queued) {
+      // counted before any entry is written, so no task can finish before it
+      atomicAdd(pj.occ_left + s, (uint32_t)queued);
+      __threadfence();
+    }
+  }
+  base = __shfl_sync(FULL, base, 0);
+  __syncwarp();
+  const uint64_t ig = pj.item_beg[s] + i;  // the item's index in the sub-batch
+  uint32_t todo = __ballot_sync(FULL, cost != 0);
+  while (todo) {
+    const int src = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const uint32_t c = __shfl_sync(FULL, cost, src);
+    const uint64_t item = __shfl_sync(FULL, ig, src);
+    const uint64_t b = base + __shfl_sync(FULL, excl, src);
+    for (uint32_t k = (uint32_t)lane; k < c && b + k < pj.cap; k += 32u) {
+      volatile unsigned long long* e = reinterpret_cast<volatile unsigned long long*>(pj.map + b + k);
+      *e = item | ((uint64_t)k << 32);
+    }
+    const uint32_t walked_from = b >= pj.cap ? 0u : (pj.cap - b < c ? (uint32_t)(pj.cap - b) : c);
+    for (uint32_t k = walked_from; k < c; k++)
+      vox_large_task<0>(j, item - pj.item_beg[s], k, lane, wl);
+  }
+}
+
+__global__ void __launch_bounds__(256, 4) kb_persist(PersistJob pj) {
+  pdl_enter();
+  extern __shared__ uint32_t lines_smem[];  // 32 x lines_per_lane per warp
+  __shared__ VoxJob s_job[8];
+  __shared__ Pyramid s_pyr[8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t* wl = lines_smem + (uint32_t)w * 32u * pj.lines_per_lane;
+  const uint64_t C = pj.chunk_beg[pj.n];
+  const uint64_t U = pj.levels ? pj.unit_beg[(uint64_t)pj.levels * (pj.n + 1) - 1] : 0;
+  uint32_t job_s = ~0u, pyr_s = ~0u;  // the stripe staged in s_job[w] / s_pyr[w]
+  for (;;) {
+    unsigned long long t = 0;
+    if (lane == 0)
+      t = ld_acquire(pj.ctr + kCtrTimeout) != 0ull ? ~0ull : atomicAdd(pj.ctr + kCtrTicket, 1ull);
+    t = __shfl_sync(FULL, t, 0);
+    if (t == ~0ull) return;
+    if (t < C) {  // a chunk of kPersistChunkRounds x 32 items
+      const uint32_t s = find_stripe(pj.chunk_beg, pj.n, t);
+      if (s != job_s) {
+        stage_warp(s_job[w], pj.jobs[s], lane);
+        job_s = s;
+      }
+      const uint64_t c0 = (t - pj.chunk_beg[s]) * (32u * kPersistChunkRounds);
+      for (uint32_t q = 0; q < kPersistChunkRounds; q++) {
+        const uint64_t i0 = c0 + 32u * q;
+        if (i0 >= s_job[w].n_items) break;
+        persist_items(pj, s, i0, lane, s_job[w], wl);
+      }
+      // this chunk's bits, marks and queued tasks are visible before it counts as done
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) {
+        atomicSub(pj.occ_left + s, 1u);
+        atomicAdd(pj.ctr + kCtrChunksDone, 1ull);
+      }
+      continue;
+    }
+    // a queued task, or (once every chunk is done and no task is left) a pyramid unit
+    const uint64_t u = t - C;
+    // kind 1: task, 2: after the tasks, 3: stop, 4: a task its chunk walks
+    unsigned long long kind = 0, tail = 0, entry = 0;
+    if (lane == 0) {
+      Backoff b;
+      for (;;) {
+        if (u < ld_acquire(pj.ctr + kCtrTasksQueued)) {
+          kind = 1;
+          break;
+        }
+        if (ld_acquire(pj.ctr + kCtrChunksDone) == C) {
+          tail = ld_acquire(pj.ctr + kCtrTasksQueued);
+          kind = u < tail ? 1 : 2;
+          break;
+        }
+        if (!b.pause(pj.ctr, 1u)) {
+          kind = 3;
+          break;
+        }
+      }
+      if (kind == 1 && u >= pj.cap) kind = 4;  // a task past the map: its chunk walks it
+      if (kind == 1) {  // the chunk that reserved entry u writes it right after
+        Backoff b2;
+        while ((entry = ld_acquire(pj.map + u)) == ~0ull)
+          if (!b2.pause(pj.ctr, 2u)) {
+            kind = 3;
+            break;
+          }
+        if (kind == 1) *reinterpret_cast<volatile unsigned long long*>(pj.map + u) = ~0ull;  // empty for the next launch
+      }
+    }
+    kind = __shfl_sync(FULL, kind, 0);
+    if (kind == 3) return;
+    if (kind == 4) continue;
+    if (kind == 1) {
+      entry = __shfl_sync(FULL, entry, 0);
+      const uint64_t item = (uint32_t)entry;
+      const uint32_t s = find_stripe(pj.item_beg, pj.n, item);
+      if (s != job_s) {
+        stage_warp(s_job[w], pj.jobs[s], lane);
+        job_s = s;
+      }
+      vox_large_task<0>(s_job[w], item - pj.item_beg[s], entry >> 32, lane, wl);
+      persist_done(pj.occ_left + s, lane);
+      continue;
+    }
+    const uint64_t v = u - __shfl_sync(FULL, tail, 0);
+    if (v < U) {  // pyramid unit: level r of stripe s
+      uint32_t r = 0;
+      while (v >= pj.unit_beg[(uint64_t)r * (pj.n + 1) + pj.n]) r++;
+      const uint64_t* ub = pj.unit_beg + (uint64_t)r * (pj.n + 1);
+      const uint32_t s = find_stripe(ub, pj.n, v);
+      bool ok = true;
+      if (lane == 0)
+        ok = persist_wait_zero(r == 0 ? pj.occ_left + s : pj.pyr_left + (uint64_t)(r - 1) * pj.n + s, pj.ctr, 3u);
+      if (!__shfl_sync(FULL, ok, 0)) return;
+      __syncwarp();  // the lanes' loads below follow lane 0's acquire
+      if (s != pyr_s) {
+        stage_warp(s_pyr[w], pj.pyrs[s], lane);
+        pyr_s = s;
+      }
+      const Pyramid& P = s_pyr[w];
+      const int l = P.depth - (int)r;
+      const uint64_t e0 = (v - ub[s]) * pj.ept * 32u;
+      for (uint32_t k = 0; k < pj.ept; k++) {
+        const uint64_t e = e0 + (uint64_t)k * 32u + (uint64_t)lane;
+        if (e < P.lv[l].nscan) pyramid_elem<true>(P, l, e);
+      }
+      persist_done(pj.pyr_left + (uint64_t)r * pj.n + s, lane);
+      continue;
+    }
+    if (v - U >= pj.n) return;  // past the last unit
+    // the top levels of stripe s, after its last pyramid unit
+    const uint32_t s = (uint32_t)(v - U);
+    if (s != pyr_s) {
+      stage_warp(s_pyr[w], pj.pyrs[s], lane);
+      pyr_s = s;
+    }
+    const Pyramid& P = s_pyr[w];
+    const int below = P.depth - pj.top_level;  // pyramid levels of the stripe under the top ones
+    bool ok = true;
+    if (lane == 0)
+      ok = persist_wait_zero(below <= 0 ? pj.occ_left + s : pj.pyr_left + (uint64_t)(below - 1) * pj.n + s, pj.ctr,
+                             4u);
+    if (!__shfl_sync(FULL, ok, 0)) return;
+    __syncwarp();
+    if (s == 0 && lane == 0) *pj.scan_end = 0u;  // the scan's total entry
+    for (int l = pj.top_level < P.depth ? pj.top_level : P.depth; l >= 0; l--) {
+      for (uint64_t b = (uint64_t)lane; b < P.lv[l].nblocks; b += 32u) pyramid_block<true>(P, l, b);
+      if (l > 0)
+        for (uint64_t x = P.lv[l].nblocks + (uint64_t)lane; x < P.lv[l - 1].nwords; x += 32u)
+          level_words(P, l - 1)[x] = 0u;
+      __threadfence_block();
+      __syncwarp();
+    }
   }
 }
 
@@ -2107,6 +2405,22 @@ void launch_b_top_down(const Pyramid* pyrs, const EmitJob* emits, const uint64_t
 void launch_b_top_down_leaves(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
                               uint64_t ctas, uint32_t ept, const Pyramid* sp, const EmitJob* se, cudaStream_t st) {
   launch_nodes<OP_LEAVES>("top_down_leaves", pyrs, emits, cta_beg, n, ctas, ept, 0, sp, se, st);
+}
+
+int persist_ctas_per_sm(uint32_t lines_per_lane) {
+  int per_sm = 0;
+  const size_t smem = (size_t)256 * lines_per_lane * 4;
+  if (smem > (48u << 10) &&
+      cudaFuncSetAttribute(kb_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_persist, 256, smem) != cudaSuccess) return 0;
+  return per_sm;
+}
+
+void launch_b_persist(const PersistJob& pj, int num_sms, int ctas_per_sm, cudaStream_t st) {
+  KScope k("persistent_phase_a", st);
+  const size_t smem = (size_t)256 * pj.lines_per_lane * 4;
+  launch_k(kb_persist, dim3((unsigned)(num_sms * ctas_per_sm)), dim3(256), smem, st, pj);
 }
 
 void launch_b_root_info(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, uint32_t* out,

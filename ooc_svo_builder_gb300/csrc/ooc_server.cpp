@@ -34,18 +34,45 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
-// Pinned host blocks for host results, kept and reused across requests
-// (pinning memory costs far more than copying into it).  A request takes the
-// smallest free block that holds it, if that block is at most four times its
-// size; otherwise a new block of the next power of two from 64 KiB is pinned.
+// Pinned host memory for host results.  With ooc_server_config::host_pool_mb
+// the server pins that much once, at creation, and carves each result's blocks
+// out of it (best fit, freed extents merged with their neighbours): pinning
+// memory costs far more than copying into it, and it holds a lock of the CUDA
+// driver that other threads' calls wait for.  A block the arena cannot hold, or
+// every block without an arena, comes from a pool of separately pinned blocks
+// kept for reuse: the smallest free block that holds the request, if it is at
+// most four times its size, else a new block of the next power of two from
+// 64 KiB.
 class PinnedPool {
  public:
   ~PinnedPool() {
     for (auto& kv : free_) cudaFreeHost(kv.second);
+    if (arena_) cudaFreeHost(arena_);
+  }
+  // Pins the arena; false when the host cannot pin that much.
+  bool reserve(size_t bytes) {
+    if (bytes == 0) return true;
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) return false;
+    arena_ = static_cast<char*>(p);
+    arena_bytes_ = bytes;
+    add_extent(0, bytes);
+    return true;
   }
   void* get(size_t n, size_t& cap) {
     {
       std::lock_guard<std::mutex> lk(mu_);
+      if (arena_) {
+        const size_t want = (n + kGrain - 1) / kGrain * kGrain;
+        auto it = by_size_.lower_bound(want);
+        if (it != by_size_.end()) {
+          const size_t off = it->second, len = it->first;
+          remove_extent(off, len);
+          if (len > want) add_extent(off + want, len - want);
+          cap = want;
+          return arena_ + off;
+        }
+      }
       auto it = free_.lower_bound(n);
       if (it != free_.end() && it->first / 4 <= n) {
         cap = it->first;
@@ -62,12 +89,50 @@ class PinnedPool {
   void put(void* p, size_t cap) {
     if (!p) return;
     std::lock_guard<std::mutex> lk(mu_);
+    char* c = static_cast<char*>(p);
+    if (arena_ && c >= arena_ && c < arena_ + arena_bytes_) {
+      size_t off = (size_t)(c - arena_), len = cap;
+      auto next = by_off_.lower_bound(off);
+      if (next != by_off_.end() && next->first == off + len) {  // merge with the extent after
+        len += next->second;
+        remove_extent(next->first, next->second);
+      }
+      auto prev = by_off_.lower_bound(off);
+      if (prev != by_off_.begin()) {
+        --prev;
+        if (prev->first + prev->second == off) {  // and the one before
+          off = prev->first;
+          len += prev->second;
+          remove_extent(prev->first, prev->second);
+        }
+      }
+      add_extent(off, len);
+      return;
+    }
     free_.emplace(cap, p);
   }
 
  private:
+  static constexpr size_t kGrain = 64 << 10;
+  void add_extent(size_t off, size_t len) {
+    by_off_[off] = len;
+    by_size_.emplace(len, off);
+  }
+  void remove_extent(size_t off, size_t len) {
+    by_off_.erase(off);
+    auto range = by_size_.equal_range(len);
+    for (auto it = range.first; it != range.second; ++it)
+      if (it->second == off) {
+        by_size_.erase(it);
+        break;
+      }
+  }
   std::mutex mu_;
-  std::multimap<size_t, void*> free_;
+  std::multimap<size_t, void*> free_;  // separately pinned blocks, by capacity
+  char* arena_ = nullptr;
+  size_t arena_bytes_ = 0;
+  std::map<size_t, size_t> by_off_;         // free arena extents: offset -> length
+  std::multimap<size_t, size_t> by_size_;   // the same extents: length -> offset
 };
 
 struct Request {
@@ -84,7 +149,7 @@ struct Request {
   uint64_t d_nodes_bytes = 0, d_data_bytes = 0;
   ooc_build_info info;
   int32_t status = OOC_OK;
-  double t_submit = 0, t_start = 0, t_done = 0;
+  double t_submit = 0, t_start = 0, t_built = 0, t_done = 0;
   uint64_t batch_size = 0;
 };
 
@@ -277,6 +342,7 @@ struct ooc_server {
 
   static void mark(Call& call, uint64_t mesh) {
     Request* r = call.reqs[mesh];
+    r->t_built = call.s->now_us();
     r->info = call.infos[mesh];
     (*call.published)[call.index[mesh]] = 1;
     call.s->publish(r, OOC_OK);
@@ -306,6 +372,7 @@ struct ooc_server {
     // host results: the mesh is complete in this batch (never rerun); the delivery
     // thread copies it into pinned memory and publishes it once the copy has landed
     Request* r = call.reqs[mesh];
+    r->t_built = call.s->now_us();
     r->info = call.infos[mesh];
     (*call.published)[call.index[mesh]] = 1;
     {
@@ -502,6 +569,13 @@ int ooc_server_create(const ooc_server_config* cfg, ooc_server** out) {
       return OOC_ERR_DEVICE;
     }
   }
+  if (cfg->result_location == OOC_RESULT_HOST && !s->pinned.reserve((size_t)cfg->host_pool_mb << 20)) {
+    cudaStreamDestroy(s->release_stream);
+    cudaStreamDestroy(s->d2h_stream);
+    for (ooc_ctx* e : s->engines) ooc_ctx_destroy(e);
+    delete s;
+    return OOC_ERR_OOM;
+  }
   if (cfg->result_location == OOC_RESULT_HOST) s->deliverer = std::thread([s] { s->delivery_loop(); });
   for (int i = 0; i < kSizers; i++) s->sizers.emplace_back([s] { s->sizing_loop(); });
   for (ooc_ctx* c : s->engines) s->threads.emplace_back([s, c] { s->engine_loop(c); });
@@ -557,6 +631,7 @@ int ooc_server_poll(ooc_server* s, int32_t timeout_ms, ooc_result* out) {
   out->info = r->info;
   out->t_submit_us = r->t_submit;
   out->t_start_us = r->t_start;
+  out->t_built_us = r->t_built;
   out->t_done_us = r->t_done;
   out->batch_size = r->batch_size;
   return OOC_OK;

@@ -101,16 +101,37 @@ def test_every_tuning_gives_the_same_octrees(builder):
         nodes, data, _ = pyoracle.build(t, a["gridsize"], a["memory_limit_mb"], color=a["color"], levels=a["levels"])
         want.append(octree.Octree(a["gridsize"], nodes, data))
     try:
-        for small_vol, lpl, block, cps, budget, graphs, ept, pdl in [(1, 1, 64, 1, 4096, 1, 1, 1),
-                                                                     (64, 64, 256, 16, 1 << 30, 0, 16, 1),
-                                                                     (27, 3, 128, 2, 700_000, 1, 3, 0),
-                                                                     (64, 16, 256, 4, 4 << 30, 1, 4, 0),
-                                                                     (64, 16, 256, 4, 4 << 30, 0, 8, 0)]:
-            builder.set_tuning(ooc.Tuning(small_vol, lpl, block, cps, budget, graphs, ept, pdl, 0))
+        for small_vol, lpl, block, cps, budget, graphs, ept, pdl, persistent in [
+                (1, 1, 64, 1, 4096, 1, 1, 1, 0), (64, 64, 256, 16, 1 << 30, 0, 16, 1, 0),
+                (27, 3, 128, 2, 700_000, 1, 3, 0, 0), (64, 16, 256, 4, 4 << 30, 1, 4, 0, 0),
+                (64, 16, 256, 4, 4 << 30, 0, 8, 0, 0),
+                # the persistent phase A: tiny sub-batches, captured; wide task lists; defaults
+                (1, 1, 64, 1, 4096, 1, 1, 1, 1), (64, 64, 256, 16, 1 << 30, 0, 16, 1, 1),
+                (27, 3, 128, 2, 700_000, 1, 3, 0, 1), (64, 16, 256, 4, 4 << 30, 0, 8, 1, 1)]:
+            builder.set_tuning(ooc.Tuning(small_vol, lpl, block, cps, budget, graphs, ept, pdl, persistent))
             for r, w in zip(builder.build_batch_device(meshes, params), want):
                 assert not octree.diff(r.tree, w)
     finally:
         builder.set_tuning(old)
+
+
+def test_persistent_phase_walks_the_tasks_that_do_not_fit_its_queue():
+    # Three flat triangles across a 512^2 face: 262,144 lines each, 8,192 warp tasks at
+    # one line per lane, 24,576 in all, more than the 4,096 entries a fresh context's task
+    # queue holds, so their chunk walks them itself.  Their boxes are two voxels deep, so
+    # the oracle tests few candidates.
+    rng = np.random.default_rng(12)
+    tris = []
+    for k in range(3):
+        z = 0.1 + 0.3 * k + rng.uniform(0, 0.001, size=3)
+        tris.append([0.0005, 0.0005, z[0], 0.9995, 0.0007, z[1], 0.0006, 0.9993, z[2]])
+    tris = np.asarray(tris, dtype=np.float32)
+    want = octree.Octree(512, *pyoracle.build(tris, 512, 2048, color="model")[:2])
+    with ooc.Builder(0) as fresh:  # no tasks seen yet: the smallest queue
+        fresh.set_tuning(ooc.Tuning(64, 1, 256, 4, 4 << 30, 0, 8, 1, 1))
+        for _ in range(2):  # the second build has the larger queue the first one sized
+            got = fresh.build_batch_device([tris], [make_params(512, 2048, geometry_only=True)])[0]
+            assert not octree.diff(got.tree, want)
 
 
 def test_autotune_keeps_a_valid_tuning(builder):

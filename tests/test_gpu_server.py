@@ -93,10 +93,21 @@ def test_results_in_the_mix_equal_oracle(builder, mix40, resident):
         assert r["location"] == (1 if resident else 0)
         d = octree.diff(r["tree"], w)
         assert not d, "request %d: %s" % (k, "\n".join(d))
-        assert r["t_submit_us"] <= r["t_start_us"] <= r["t_done_us"]
+        assert r["t_submit_us"] <= r["t_start_us"] <= r["t_built_us"] <= r["t_done_us"]
     # and the same mesh built alone through ooc_build
     for k in range(0, len(reqs), 7):
         assert not octree.diff(builder.build(*reqs[k]).tree, want[k])
+
+
+def test_host_results_from_a_pinned_reserve_equal_oracle(mix40):
+    """Host results carved out of a 2 MiB pinned reserve: small results share it (freed
+    blocks merge with their neighbours for the next ones), larger ones get blocks pinned
+    on demand.  Every result still equals the oracle."""
+    reqs, want = mix40
+    ids, got = serve_all(reqs, engines=2, max_batch=16, memory_budget=8 << 30, host_pool_mb=2)
+    for k, (rid, w) in enumerate(zip(ids, want)):
+        assert got[rid]["status"] == 0, k
+        assert not octree.diff(got[rid]["tree"], w), k
 
 
 @pytest.mark.parametrize("resident", [False, True], ids=["host", "device"])

@@ -28,9 +28,9 @@ def test_server_calls_reject_null():
 
 
 def test_result_struct_layout():
-    # ooc_result: id, status, reserved, nodes, nodes_bytes, data, data_bytes, info (6 x u64), 3 doubles, batch_size
-    assert ctypes.sizeof(ooc.Result) == 8 + 4 + 4 + 8 * 4 + 48 + 24 + 8
-    # ooc_server_config: device, engines, max_batch, result_location, memory_budget, fail_batch_at_mesh, reserved
+    # ooc_result: id, status, location, nodes, nodes_bytes, data, data_bytes, info (6 x u64), 4 doubles, batch_size
+    assert ctypes.sizeof(ooc.Result) == 8 + 4 + 4 + 8 * 4 + 48 + 32 + 8
+    # ooc_server_config: device, engines, max_batch, result_location, memory_budget, fail_batch_at_mesh, host_pool_mb
     assert ctypes.sizeof(ooc.ServerConfig) == 32
 
 
