@@ -625,6 +625,55 @@ def serve_burst(srv, pool, n: int, seed: int) -> dict:
             "failed": int(sum(r["status"] != 0 for r in done))}
 
 
+def serve_bounds(pool, local: int, n: int) -> dict:
+    """What limits capacity, on `n` requests drawn like the burst's: one batch call over all of
+    them (no serving loop), the kernel time alone (events around every kernel of that call), and
+    one call per request.  Results stay in one HBM arena."""
+    import torch
+    import ooc_svo_builder_gb300 as ooc
+
+    rng = np.random.default_rng(77)
+    picks = rng.integers(0, len(pool), size=n)
+    arr = (ooc.Mesh * n)()
+    for q, k in enumerate(picks):
+        ptr, nt, params, _ = pool[k]
+        arr[q].tris = ptr
+        arr[q].n_tris = nt
+        arr[q].params = params
+    infos = (ooc.BuildInfo * n)()
+    out = {"requests": n}
+    with ooc.Builder(local) as b:
+        sink = ooc.BATCH_SINK(lambda user, mesh, kind, p, nb: 0)
+        b.build_batch_ptrs(arr, n, sink, infos)  # sizes the arena
+        out_bytes = sum(int(infos[i].n_nodes) * 24 + int(infos[i].n_data) * 32 for i in range(n))
+        arena_buf = torch.empty(out_bytes + 512 * n + (64 << 20), dtype=torch.uint8, device="cuda")
+        arena = ooc.DeviceArena(arena_buf.data_ptr(), arena_buf.numel(), 0)
+
+        def batch():
+            arena.used = 0
+            b.build_batch_device_ptrs(arr, n, arena, infos)
+        batch()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        batch()
+        out["one_batch_meshes_per_s"] = n / (time.perf_counter() - t0)
+        b.set_kernel_timing("*")
+        batch()
+        kernel_ms = sum(v[0] for v in b.kernel_times().values())
+        b.set_kernel_timing(None)
+        out["kernel_ms_per_request"] = kernel_ms / n
+        out["kernel_bound_meshes_per_s"] = n / (kernel_ms / 1e3)
+        one = (ooc.Mesh * 1)()
+        t0 = time.perf_counter()
+        for q in range(n):
+            one[0] = arr[q]
+            arena.used = 0
+            b.build_batch_device_ptrs(one, 1, arena, infos)
+        out["one_call_per_request_meshes_per_s"] = n / (time.perf_counter() - t0)
+        del arena_buf
+    return out
+
+
 def run_serve(args, world, rank, local):
     """Configuration 5: Poisson request streams through the serving loop (continuous batching,
     footprint admission) and, on the same streams, through the plain path (one request at a time)."""
@@ -681,6 +730,8 @@ def run_serve(args, world, rank, local):
                     pass
             capacity[arm] = serve_burst(srv, pool, args.burst, seed=77)
         print("serve burst %s: %s" % (arm, json.dumps(capacity[arm])), file=sys.stderr, flush=True)
+    bounds = serve_bounds(pool, local, args.bound_meshes)
+    print("serve bounds: %s" % json.dumps(bounds), file=sys.stderr, flush=True)
     top = out["served_resident"][-1]
     top_host = out["served_host"][-1]
 
@@ -704,6 +755,7 @@ def run_serve(args, world, rank, local):
         "capacity": dict(capacity, speedup_vs_plain=capacity["served_resident"]["meshes_per_s"] /
                          max(capacity["plain_resident"]["meshes_per_s"], 1e-9)),
         "speedup_vs_plain_host": ratio("served_host", "plain_host"),
+        "bounds": bounds,
         "e2e": {"value": top_host["meshes_per_s"], "unit": "meshes/s", "p50_ms": top_host["p50_ms"],
                 "p99_ms": top_host["p99_ms"], "note": "results copied back to host memory",
                 "h2d_bytes_per_step": int(np.mean([t.nbytes for t, _, _ in meshes])),
@@ -771,12 +823,14 @@ def main():
     ap.add_argument("--rates", default="200,500,1000,2000", help="serve: offered request rates, req/s")
     ap.add_argument("--duration", type=float, default=5.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--drain", type=float, default=10.0, help="serve: seconds to wait for the queue to drain")
-    ap.add_argument("--serve-warmup", type=float, default=1.0,
+    ap.add_argument("--serve-warmup", type=float, default=3.0,
                     help="serve: seconds of unmeasured arrivals at each rate before the measured ones")
     ap.add_argument("--engines", type=int, default=2, help="serve: engines of the served arm")
     ap.add_argument("--host-pool-mb", type=int, default=8192,
                     help="serve: pinned host memory each host-result server reserves at creation, MiB")
     ap.add_argument("--burst", type=int, default=4096, help="serve: requests of the capacity burst")
+    ap.add_argument("--bound-meshes", type=int, default=512,
+                    help="serve: requests of the capacity bounds (one batch call; kernels alone; one call each)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-budget", type=int, default=0,
                     help="occupancy-pyramid bytes per sub-batch (0: the library's default, 4 GiB)")

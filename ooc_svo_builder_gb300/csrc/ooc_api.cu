@@ -842,6 +842,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     j.leafbits = leaf + P.lv[P.depth].off_w;
     j.leaftouch = P.touch;
     j.task_off = task_off + item_beg[s];
+    j.task_flag = task_off + items;
     j.task_counter = counter;
     j.item_mask = m.pl.binary ? nullptr : item_mask + item_beg[s];
     j.item_box = m.pl.binary ? nullptr : item_box + item_beg[s];
@@ -963,7 +964,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       ck(cudaMemsetAsync(pj.ctr, 0, kPersistCtrWords * 8, st), "memset persistent counters");
       launch_b_persist(pj, c->num_sms, c->persist_per_sm, st);
       if (any_payload_stripe) {  // the winner pass numbers the tasks by item
-        scan_u64_exclusive(task_off, items + 1, taskpart, st);
+        scan_u64_exclusive(task_off, items + 1, taskpart, st, true);
         if (map_cap) launch_b_task_map(dp1(o_cpi), n, cp_items[n], d_beg, task_off, items, task_map, map_cap, st);
       }
     } else {
@@ -986,7 +987,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       } else {
         launch_b_vox_small(d_vj, dp1(o_cpi), n, cp_items[n], 0, n == 1 ? &vj[0] : nullptr, st);
       }
-      scan_u64_exclusive(task_off, items + 1, taskpart, st);
+      scan_u64_exclusive(task_off, items + 1, taskpart, st, true);
       if (map_cap) launch_b_task_map(dp1(o_cpi), n, cp_items[n], d_beg, task_off, items, task_map, map_cap, st);
       launch_b_vox_large(d_vj, d_beg, n, task_off, items, counter, 0, st, c->num_sms, (int)c->tuning.large_block,
                          (int)c->tuning.large_ctas_per_sm, c->tuning.lines_per_lane, task_map, map_cap);
@@ -1656,7 +1657,10 @@ void build_meshes(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, co
       Level tmp[kMaxLevels];
       uint64_t w = 0, b = 0;
       pyramid_levels(m.pl.Ds, tmp, w, w, b, false);
-      if (!sb.empty() && budget_words + w > budget) flush();
+      // host output: the first sub-batch takes an eighth of the budget, so that the copy
+      // back (the longer part of a large build) starts after a short first compute
+      const uint64_t cap = (os.mode == OUT_HOST && k == 0) ? budget / 8 : budget;
+      if (!sb.empty() && budget_words + w > cap) flush();
       sb.push_back(StripeRef{mi, s, part, ibeg, cnt});
       budget_words += w;
     }

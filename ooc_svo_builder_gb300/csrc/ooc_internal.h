@@ -77,6 +77,7 @@ struct VoxJob {
   uint32_t leafscan_base;
   uint32_t* winners;        // per leaf: min triangle index
   uint64_t* task_off;       // per item: exclusive prefix of warp tasks (n_items + 1)
+  uint64_t* task_flag;      // set to 1 by an item with tasks (the sub-batch's task_off[items]); may be NULL
   unsigned long long* task_counter;
   uint64_t* item_mask;      // per small item: which of its candidates passed (pass 0 -> pass 1); may be NULL
   uint64_t* item_box;       // per small item with a non-zero mask: its packed stripe-local box
@@ -160,7 +161,9 @@ struct LaunchScope {
 };
 
 void scan_u32_exclusive(uint32_t* data, uint64_t n, uint32_t* partials, cudaStream_t st);
-void scan_u64_exclusive(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st);
+// flag_last: data[n-1] is not an input but a flag; zero means every element is zero,
+// and the scan is left out.
+void scan_u64_exclusive(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st, bool flag_last = false);
 uint64_t scan_partials_needed(uint64_t n);
 
 void launch_part_count(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,

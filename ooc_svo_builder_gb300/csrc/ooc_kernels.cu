@@ -108,10 +108,13 @@ __device__ __forceinline__ T block_exclusive(T v, T& total) {
 constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
+// `skip` (may be NULL): when it points at a zero, every element is zero and the
+// scan is left out (all zeros are their own exclusive scan).
 template <typename T>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const T* __restrict__ in, uint64_t n,
-                                                              T* __restrict__ partials) {
+                                                              T* __restrict__ partials, const T* skip) {
   pdl_enter();
+  if (skip && *skip == T(0)) return;
   const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
   T v = 0;
 #pragma unroll
@@ -126,8 +129,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const T* __restric
 
 // Also partials[np] = the grand total.
 template <typename T>
-__global__ void __launch_bounds__(1024) k_scan_partials(T* partials, uint64_t np) {
+__global__ void __launch_bounds__(1024) k_scan_partials(T* partials, uint64_t np, const T* skip) {
   pdl_enter();
+  if (skip && *skip == T(0)) return;
   T carry = 0;
   for (uint64_t base = 0; base < np; base += blockDim.x) {
     const uint64_t i = base + threadIdx.x;
@@ -143,8 +147,12 @@ __global__ void __launch_bounds__(1024) k_scan_partials(T* partials, uint64_t np
 // Each thread scans SCAN_ITEMS consecutive elements staged through shared memory
 // (`partials` NULL: a single tile, nothing before it).
 template <typename T>
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(T* data, uint64_t n, const T* __restrict__ partials) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(T* data, uint64_t n, const T* __restrict__ partials,
+                                                            const T* skip) {
   pdl_enter();
+  // `skip` is read before any CTA writes: a scan that runs has a non-zero flag and a
+  // non-zero total, so a late CTA reading the written total skips nothing either
+  if (skip && *skip == T(0)) return;
   // the elements are counts: a zero total means all zero, which is already their scan
   if (partials && partials[gridDim.x] == T(0)) return;
   __shared__ T tile[SCAN_TILE + SCAN_TILE / 32];
@@ -182,25 +190,25 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(T* data, uint64_t n,
 }
 
 template <typename T>
-void scan_exclusive(T* data, uint64_t n, T* partials, cudaStream_t st) {
+void scan_exclusive(T* data, uint64_t n, T* partials, cudaStream_t st, const T* skip = nullptr) {
   if (n == 0) return;
   const unsigned nb = (unsigned)((n + SCAN_TILE - 1) / SCAN_TILE);
   if (nb == 1) {  // one tile: one launch
     KScope k("scan_down", st);
-    launch_k(k_scan_down<T>, dim3(1), dim3(SCAN_THREADS), 0, st, data, n, nullptr);
+    launch_k(k_scan_down<T>, dim3(1), dim3(SCAN_THREADS), 0, st, data, n, nullptr, skip);
     return;
   }
   {
     KScope k("scan_reduce", st);
-    launch_k(k_scan_reduce<T>, dim3(nb), dim3(SCAN_THREADS), 0, st, data, n, partials);
+    launch_k(k_scan_reduce<T>, dim3(nb), dim3(SCAN_THREADS), 0, st, data, n, partials, skip);
   }
   {
     KScope k("scan_partials", st);
-    launch_k(k_scan_partials<T>, dim3(1), dim3(1024), 0, st, partials, nb);
+    launch_k(k_scan_partials<T>, dim3(1), dim3(1024), 0, st, partials, nb, skip);
   }
   {
     KScope k("scan_down", st);
-    launch_k(k_scan_down<T>, dim3(nb), dim3(SCAN_THREADS), 0, st, data, n, partials);
+    launch_k(k_scan_down<T>, dim3(nb), dim3(SCAN_THREADS), 0, st, data, n, partials, skip);
   }
 }
 
@@ -819,6 +827,7 @@ __device__ __forceinline__ uint64_t vox_small_occ_item(const VoxJob& j, uint64_t
     }
   }
   j.task_off[i] = cost;
+  if (cost && j.task_flag) *j.task_flag = 1ull;  // the sub-batch has tasks: its scan runs
   if (j.item_mask) j.item_mask[i] = mask;
   return cost;
 }
@@ -2141,9 +2150,10 @@ uint64_t scan_partials_needed(uint64_t n) { return (n + SCAN_TILE - 1) / SCAN_TI
 void scan_u32_exclusive(uint32_t* data, uint64_t n, uint32_t* partials, cudaStream_t st) {
   scan_exclusive<uint32_t>(data, n, partials, st);
 }
-void scan_u64_exclusive(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st) {
-  scan_exclusive<unsigned long long>(reinterpret_cast<unsigned long long*>(data), n,
-                                     reinterpret_cast<unsigned long long*>(partials), st);
+void scan_u64_exclusive(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st, bool flag_last) {
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(data);
+  scan_exclusive<unsigned long long>(d, n, reinterpret_cast<unsigned long long*>(partials), st,
+                                     flag_last ? d + n - 1 : nullptr);
 }
 
 void launch_part_count(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
@@ -2221,17 +2231,17 @@ cudaError_t launch_vox_large_occupancy(const VoxJob& j, cudaStream_t st, int num
 cudaError_t scan_u64_exclusive_checked(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   const unsigned nb = (unsigned)((n + SCAN_TILE - 1) / SCAN_TILE);
-  const uint64_t* none = nullptr;
+  const uint64_t* none = nullptr;  // no partials (one tile) / no skip flag
   if (nb == 1) {
     KScope k("scan_down", st);
-    void* args[] = {&data, &n, &none};
+    void* args[] = {&data, &n, &none, &none};
     return cudaLaunchKernel(reinterpret_cast<const void*>(&k_scan_down<uint64_t>), dim3(1), dim3(SCAN_THREADS), args,
                             0, st);
   }
   cudaError_t e;
   {
     KScope k("scan_reduce", st);
-    void* args[] = {&data, &n, &partials};
+    void* args[] = {&data, &n, &partials, &none};
     e = cudaLaunchKernel(reinterpret_cast<const void*>(&k_scan_reduce<uint64_t>), dim3(nb), dim3(SCAN_THREADS), args,
                          0, st);
   }
@@ -2239,13 +2249,13 @@ cudaError_t scan_u64_exclusive_checked(uint64_t* data, uint64_t n, uint64_t* par
   {
     KScope k("scan_partials", st);
     uint64_t np = nb;
-    void* args[] = {&partials, &np};
+    void* args[] = {&partials, &np, &none};
     e = cudaLaunchKernel(reinterpret_cast<const void*>(&k_scan_partials<uint64_t>), dim3(1), dim3(1024), args, 0, st);
   }
   if (e != cudaSuccess) return e;
   KScope k("scan_down", st);
   const uint64_t* cp = partials;
-  void* args[] = {&data, &n, &cp};
+  void* args[] = {&data, &n, &cp, &none};
   return cudaLaunchKernel(reinterpret_cast<const void*>(&k_scan_down<uint64_t>), dim3(nb), dim3(SCAN_THREADS), args, 0,
                           st);
 }

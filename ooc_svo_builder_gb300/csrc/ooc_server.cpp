@@ -180,6 +180,7 @@ bool valid(const ooc_mesh& m) {
 // starts, first child and winner (7 x 4 bytes) and its -levels cache (24
 // bytes), with room for the batch's job tables.
 constexpr uint64_t kNodeBytes = 120;
+constexpr uint64_t kDeliverPiece = 16ull << 20;  // bytes per copy of a host result's copy back
 constexpr int kSizers = 4;  // threads that compute the footprints of submitted requests
 
 double voxel_bound(const float* v, float unit_div, uint64_t N) {
@@ -399,10 +400,16 @@ struct ooc_server {
       }
     }
     if (ok && !ev) ok = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
-    if (ok && r->h_nodes_bytes)
-      ok = cudaMemcpyAsync(r->h_nodes, r->d_nodes, r->h_nodes_bytes, cudaMemcpyDeviceToHost, d2h_stream) == cudaSuccess;
-    if (ok && r->h_data_bytes)
-      ok = cudaMemcpyAsync(r->h_data, r->d_data, r->h_data_bytes, cudaMemcpyDeviceToHost, d2h_stream) == cudaSuccess;
+    // in pieces, so that the engines' own small reads back (their level counts) do not
+    // wait behind a whole result of hundreds of megabytes on the copy engine
+    auto copy = [&](void* dst, const void* src, uint64_t bytes) {
+      for (uint64_t off = 0; ok && off < bytes; off += kDeliverPiece)
+        ok = cudaMemcpyAsync(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off,
+                             std::min<uint64_t>(kDeliverPiece, bytes - off), cudaMemcpyDeviceToHost,
+                             d2h_stream) == cudaSuccess;
+    };
+    if (ok && r->h_nodes_bytes) copy(r->h_nodes, r->d_nodes, r->h_nodes_bytes);
+    if (ok && r->h_data_bytes) copy(r->h_data, r->d_data, r->h_data_bytes);
     if (ok) ok = cudaEventRecord(ev, d2h_stream) == cudaSuccess;
     if (!ok) {
       if (ev) cudaEventDestroy(ev);
