@@ -594,6 +594,8 @@ def serve_stream(srv, pool, rate: float, duration: float, seed: int, drain_s: fl
     stop.set()
     th.join()
     lat = np.array([(r["t_done_us"] - r["t_submit_us"]) / 1e3 for r in results])
+    built = np.array([(r["t_built_us"] - r["t_submit_us"]) / 1e3 for r in results])  # queue + build
+    deliver = np.array([(r["t_done_us"] - r["t_built_us"]) / 1e3 for r in results])  # host copy back
     done = np.array([r["t_done_us"] for r in results])
     sub = np.array([r["t_submit_us"] for r in results])
     span = (done.max() - sub.min()) / 1e6 if len(results) else float("nan")
@@ -602,6 +604,8 @@ def serve_stream(srv, pool, rate: float, duration: float, seed: int, drain_s: fl
             "meshes_per_s": len(results) / span if len(results) else 0.0,
             "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+            "p99_built_ms": float(np.percentile(built, 99)) if len(lat) else None,
+            "p99_deliver_ms": float(np.percentile(deliver, 99)) if len(lat) else None,
             "mean_batch": float(np.mean([r["batch_size"] for r in results])) if results else None,
             "output_gb": float(sum(r["bytes"] for r in results) / 1e9)}
 

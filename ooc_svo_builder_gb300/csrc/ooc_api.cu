@@ -109,6 +109,7 @@ constexpr uint64_t kRingChunk = 32ull << 20;
 
 struct D2HRing {
   PinBuf buf;
+  cudaStream_t st = nullptr;  // the stream its copies go on (one per sub-batch slot)
   cudaEvent_t ev[kRingK] = {};
   const char* src = nullptr;
   uint64_t len = 0, n_chunks = 0;
@@ -142,7 +143,7 @@ struct ooc_ctx {
   int persist_per_sm = -1;  // CTAs per SM of the persistent kernel for persist_lpl
   uint32_t persist_lpl = 0;
   bool leaf_zero = true;  // d_leaf and d_touch hold only zeros (no sub-batch left them dirty)
-  PinBuf h_misc, h_recs, h_tables1, h_tables2;
+  PinBuf h_misc, h_recs, h_tables1, h_tables2, h_words;
   // double-buffered outputs of pipelined sub-batches
   DevBuf d_out_nodes[2], d_out_data[2];
   PinBuf h_root[2];
@@ -150,6 +151,7 @@ struct ooc_ctx {
   cudaEvent_t ev_compute[2] = {nullptr, nullptr};
   cudaEvent_t ev_data[2] = {nullptr, nullptr};  // host output: a sub-batch's data file is final
   cudaStream_t copy_stream = nullptr;
+  cudaStream_t ring_stream[2] = {nullptr, nullptr};  // host output: the copy back of each sub-batch slot
   cudaStream_t h2d_stream = nullptr;     // batch uploads, overlapping the sub-batches that do not need them yet
   std::vector<cudaEvent_t> up_events;    // recorded on h2d_stream as groups of meshes arrive
   DevBuf d_tables1, d_tables2;
@@ -219,17 +221,18 @@ void ring_issue(ooc_ctx* c, D2HRing& r) {
   const uint64_t off = j * kRingChunk;
   const uint64_t n = std::min(kRingChunk, r.len - off);
   char* dst = static_cast<char*>(r.buf.p) + (j % kRingK) * kRingChunk;
-  ck(cudaMemcpyAsync(dst, r.src + off, n, cudaMemcpyDeviceToHost, c->copy_stream), "D2H");
-  ck(cudaEventRecord(r.ev[j % kRingK], c->copy_stream), "event");
+  ck(cudaMemcpyAsync(dst, r.src + off, n, cudaMemcpyDeviceToHost, r.st), "D2H");
+  ck(cudaEventRecord(r.ev[j % kRingK], r.st), "event");
   if (c->timing && r.issued == r.n_chunks) {
     const size_t e = c->ev_used;
-    ck(cudaEventRecord(next_event(c), c->copy_stream), "cudaEventRecord");
+    ck(cudaEventRecord(next_event(c), r.st), "cudaEventRecord");
     c->marks.push_back({(size_t)PH_COPY, r.t_begin, e});
   }
 }
 
-// Queue the first chunks of `len` device bytes (the copy stream already waits for their producer).
-void ring_start(ooc_ctx* c, D2HRing& r, const void* src, uint64_t len) {
+// Queue the first chunks of `len` device bytes on `st` (which already waits for their producer).
+void ring_start(ooc_ctx* c, D2HRing& r, const void* src, uint64_t len, cudaStream_t st) {
+  r.st = st;
   r.src = static_cast<const char*>(src);
   r.len = len;
   r.n_chunks = (len + kRingChunk - 1) / kRingChunk;
@@ -240,7 +243,7 @@ void ring_start(ooc_ctx* c, D2HRing& r, const void* src, uint64_t len) {
     if (!r.ev[k]) ck(cudaEventCreateWithFlags(&r.ev[k], cudaEventDisableTiming), "cudaEventCreate");
   if (c->timing) {
     r.t_begin = c->ev_used;
-    ck(cudaEventRecord(next_event(c), c->copy_stream), "cudaEventRecord");
+    ck(cudaEventRecord(next_event(c), st), "cudaEventRecord");
   }
   while (r.issued < r.n_chunks && r.issued < (uint64_t)kRingK) ring_issue(c, r);
 }
@@ -743,6 +746,17 @@ struct Pending {
   uint64_t cur = 0;      // next byte of the current range
 };
 
+// Queues the read back of n device words into the context's pinned buffer (by a
+// kernel's stores, so it does not wait behind copies on the copy engine); the
+// returned host pointer holds them once `st` has reached this point.
+const uint32_t* read_back_words(ooc_ctx* c, const uint32_t* src, uint64_t n, cudaStream_t st) {
+  uint32_t* h = ensure_pinned<uint32_t>(c->h_words, std::max<uint64_t>(n, 1) * 4);
+  uint32_t* d = nullptr;
+  ck(cudaHostGetDevicePointer(reinterpret_cast<void**>(&d), h, 0), "mapped read back");
+  launch_copy_words(src, n, d, st);
+  return h;
+}
+
 // Waits for the level counts on `st`.  Meanwhile `idle` (if set) hands the previous
 // sub-batch's landed copy-back chunks to the sink, so the copy stream keeps moving;
 // it returns false once there is nothing left for it to do.
@@ -914,6 +928,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const uint64_t* d_beg = reinterpret_cast<const uint64_t*>(t1 + o_beg);
 
   uint32_t* lvl = ensure_pinned<uint32_t>(c->h_misc, ((uint64_t)n * 16 + 64) * 4);  // level bases, then root info
+  uint32_t* lvl_dev = nullptr;  // the same pinned memory as the kernels address it
+  ck(cudaHostGetDevicePointer(reinterpret_cast<void**>(&lvl_dev), lvl, 0), "mapped level counts");
   // Warp task -> item map, sized by the items and the most tasks a sub-batch has had.
   // Built once the context has seen a sub-batch with many tasks: with few, the large
   // items' search of the task offsets costs less than the map's launch.
@@ -1003,12 +1019,12 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       scan_u32_exclusive(scan, blocks + 1, scanpart, st);
       // the tasks of the sub-batch (sizes the task maps); the persistent kernel counts them itself
       const uint64_t* tasks = persist ? reinterpret_cast<const uint64_t*>(pj.ctr + kPersistTasksWord) : task_off + items;
-      launch_b_level_bases(d_pyr, n, d_root, tasks, reinterpret_cast<uint64_t*>(d_root + (uint64_t)n * 16 + 8), flag,
-                           st);
-      ck(cudaMemcpyAsync(lvl, d_root, ((uint64_t)n * 16 + 10) * 4, cudaMemcpyDeviceToHost, st), "levels");
-      if (persist)
-        ck(cudaMemcpyAsync(lvl + (uint64_t)n * 16 + 12, pj.ctr + kPersistTimeoutWord, 8, cudaMemcpyDeviceToHost, st),
-           "timeout code");
+      // The level counts go straight into pinned host memory, written by the kernel: a
+      // copy on the copy engine would queue behind the previous sub-batch's copy back,
+      // which the host keeps refilling while it waits, and hold up the whole pipeline.
+      launch_b_level_bases(d_pyr, n, lvl_dev, tasks, reinterpret_cast<uint64_t*>(lvl_dev + (uint64_t)n * 16 + 8),
+                           flag, persist ? reinterpret_cast<const uint64_t*>(pj.ctr + kPersistTimeoutWord) : nullptr,
+                           reinterpret_cast<uint64_t*>(lvl_dev + (uint64_t)n * 16 + 12), st);
     }
   }, pieces != nullptr);  // waits on the upload stream are not captured
   wait_level_counts(st, idle);
@@ -1233,6 +1249,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   const EmitJob* se1 = n == 1 ? &ej[0] : nullptr;
 
   uint32_t* hr = ensure_pinned<uint32_t>(c->h_root[slot], ((uint64_t)n * 16 + 1) * 4);
+  uint32_t* hr_dev = nullptr;
+  ck(cudaHostGetDevicePointer(reinterpret_cast<void**>(&hr_dev), hr, 0), "mapped root info");
   if (any_payload) run_launches(c, st, 1, [&] {
     {
       PhaseScope ph(c, PH_VOX, st);
@@ -1257,8 +1275,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       for (size_t l = 0; l < cp_td.size(); l++)
         launch_b_top_down(d_pyr2, d_ej, dp2(o_td[l]), n, cp_td[l].beg[n], cp_td[l].ept, (int)l, sp1, se1, st);
       launch_b_top_down_leaves(d_pyr2, d_ej, dp2(o_cl), n, cp_leaves.beg[n], cp_leaves.ept, sp1, se1, st);
-      launch_b_root_info(d_pyr2, d_ej, n, d_root, st);
-      ck(cudaMemcpyAsync(hr, d_root, ((uint64_t)n * 16 + 1) * 4, cudaMemcpyDeviceToHost, st), "root info");
+      // into pinned host memory by the kernel, like the level counts: not behind the copy back
+      launch_b_root_info(d_pyr2, d_ej, n, hr_dev, flag, st);
       // the last reader of the leaf levels is done: zero them for the next sub-batch
       launch_b_clean_leaves(d_pyr2, dp2(o_cln), n, cp_clean.beg[n], cp_clean.ept, sp1, st);
     }
@@ -1266,14 +1284,17 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   c->leaf_zero = true;
   ck(cudaEventRecord(c->ev_compute[slot], st), "event");
   if (os.mode == OUT_HOST) {
-    // the records travel to the host on the copy stream while the next sub-batch computes
+    // The records travel to the host while the next sub-batch computes, on the slot's own
+    // copy stream: the previous sub-batch's remaining chunks, refilled on the other slot's
+    // stream, do not queue behind this one's wait for its compute.
+    cudaStream_t cs = c->ring_stream[slot];
     if (early_data) {
-      ck(cudaStreamWaitEvent(c->copy_stream, c->ev_data[slot], 0), "wait");
-      ring_start(c, c->ring[slot][OOC_STREAM_DATA], c->d_out_data[slot].p, out_data * 32);
+      ck(cudaStreamWaitEvent(cs, c->ev_data[slot], 0), "wait");
+      ring_start(c, c->ring[slot][OOC_STREAM_DATA], c->d_out_data[slot].p, out_data * 32, cs);
     }
-    ck(cudaStreamWaitEvent(c->copy_stream, c->ev_compute[slot], 0), "wait");
-    ring_start(c, c->ring[slot][OOC_STREAM_NODES], c->d_out_nodes[slot].p, out_nodes * 24);
-    if (!early_data) ring_start(c, c->ring[slot][OOC_STREAM_DATA], c->d_out_data[slot].p, out_data * 32);
+    ck(cudaStreamWaitEvent(cs, c->ev_compute[slot], 0), "wait");
+    ring_start(c, c->ring[slot][OOC_STREAM_NODES], c->d_out_nodes[slot].p, out_nodes * 24, cs);
+    if (!early_data) ring_start(c, c->ring[slot][OOC_STREAM_DATA], c->d_out_data[slot].p, out_data * 32, cs);
   }
   out_pending.active = true;
   out_pending.slot = slot;
@@ -1387,8 +1408,7 @@ void bin_mesh(ooc_ctx* c, cudaStream_t st, MeshWork& m, DevBuf& items_buf) {
   uint32_t* hist = ensure<uint32_t>(c->d_hist, pl.P * 4);
   ck(cudaMemsetAsync(hist, 0, pl.P * 4, st), "memset hist");
   launch_part_count(m.d_tris, stride, m.n_tris, d_axis, d_axis + 3 * PA, pl.kP, pl.P, hist, st);
-  std::vector<uint32_t> h(pl.P);
-  ck(cudaMemcpyAsync(h.data(), hist, pl.P * 4, cudaMemcpyDeviceToHost, st), "hist");
+  const uint32_t* h = read_back_words(c, hist, pl.P, st);
   ck(cudaStreamSynchronize(st), "binning");
   m.part_off.assign(pl.P + 1, 0);
   uint64_t acc = 0;
@@ -1491,8 +1511,7 @@ void stream_count(ooc_ctx* c, cudaStream_t st, MeshWork& m) {
   stream_pass(c, st, *m.src, std::max<uint64_t>(1, kStreamChunkBytes / m.src->rec), [&](const float* d, uint64_t n) {
     launch_part_count(d, stride, n, d_axis, d_axis + 3 * PA, pl.kP, pl.P, hist, st);
   });
-  std::vector<uint32_t> h(pl.P);
-  ck(cudaMemcpyAsync(h.data(), hist, pl.P * 4, cudaMemcpyDeviceToHost, st), "hist");
+  const uint32_t* h = read_back_words(c, hist, pl.P, st);
   ck(cudaStreamSynchronize(st), "counts");
   m.part_off.assign(pl.P + 1, 0);
   uint64_t acc = 0;
@@ -1754,6 +1773,8 @@ void begin_build(ooc_ctx* c) {
   c->part_filled.clear();
   // a build that failed part-way may have left copies queued into the staging buffers
   ck(cudaStreamSynchronize(c->copy_stream), "cudaStreamSynchronize");
+  ck(cudaStreamSynchronize(c->ring_stream[0]), "cudaStreamSynchronize");
+  ck(cudaStreamSynchronize(c->ring_stream[1]), "cudaStreamSynchronize");
   ck(cudaStreamSynchronize(c->h2d_stream), "cudaStreamSynchronize");
   c->err.clear();
   c->marks.clear();
@@ -1879,12 +1900,14 @@ int ooc_ctx_create(int32_t device, ooc_ctx** out) {
       cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->ring_stream[0], cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->ring_stream[1], cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->h2d_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_compute[0], cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_compute[1], cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_data[0], cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_data[1], cudaEventDisableTiming) != cudaSuccess) {
-    delete c;
+    ooc_ctx_destroy(c);  // frees whatever was created
     return OOC_ERR_DEVICE;
   }
   *out = c;
@@ -1896,16 +1919,23 @@ void ooc_ctx_destroy(ooc_ctx* c) {
   cudaSetDevice(c->device);
   if (c->own_stream) cudaStreamSynchronize(c->own_stream);
   if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+  for (cudaStream_t rs : c->ring_stream)
+    if (rs) cudaStreamSynchronize(rs);
   if (c->h2d_stream) cudaStreamSynchronize(c->h2d_stream);
   DevBuf* bufs[] = {&c->d_tris, &c->d_hist, &c->d_axis, &c->d_bits, &c->d_scan, &c->d_scanpart,
                     &c->d_keys, &c->d_size, &c->d_dsize, &c->d_start, &c->d_dstart, &c->d_cache, &c->d_winners,
                     &c->d_taskoff, &c->d_taskpart, &c->d_counter, &c->d_nodes, &c->d_data, &c->d_recs,
-                    &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox, &c->d_leaf, &c->d_touch, &c->d_local, &c->d_taskmap};
+                    &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox, &c->d_leaf, &c->d_touch, &c->d_local,
+                    &c->d_taskmap, &c->d_pctr, &c->d_pmap, &c->d_chunk[0], &c->d_chunk[1], &c->d_group[0],
+                    &c->d_group[1], &c->d_stream_mat, &c->d_stream_part, &c->d_stream_base, &c->d_part_off};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
-  PinBuf* pins[] = {&c->h_misc, &c->h_recs, &c->h_tables1, &c->h_tables2};
+  PinBuf* pins[] = {&c->h_misc, &c->h_recs, &c->h_tables1, &c->h_tables2, &c->h_words, &c->h_stage[0],
+                    &c->h_stage[1]};
   for (PinBuf* b : pins)
     if (b->p) cudaFreeHost(b->p);
+  for (cudaEvent_t e : c->ev_stage)
+    if (e) cudaEventDestroy(e);
   for (int i = 0; i < 2; i++) {
     if (c->d_out_nodes[i].p) cudaFree(c->d_out_nodes[i].p);
     if (c->d_out_data[i].p) cudaFree(c->d_out_data[i].p);
@@ -1919,6 +1949,8 @@ void ooc_ctx_destroy(ooc_ctx* c) {
     if (c->ev_data[i]) cudaEventDestroy(c->ev_data[i]);
   }
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  for (cudaStream_t rs : c->ring_stream)
+    if (rs) cudaStreamDestroy(rs);
   if (c->h2d_stream) cudaStreamDestroy(c->h2d_stream);
   for (auto& kv : c->graph_execs) cudaGraphExecDestroy(kv.second);
   for (cudaEvent_t e : c->up_events) cudaEventDestroy(e);

@@ -166,6 +166,8 @@ void scan_u32_exclusive(uint32_t* data, uint64_t n, uint32_t* partials, cudaStre
 void scan_u64_exclusive(uint64_t* data, uint64_t n, uint64_t* partials, cudaStream_t st, bool flag_last = false);
 uint64_t scan_partials_needed(uint64_t n);
 
+// n words from device memory into `dst`, mapped pinned host memory, by a kernel.
+void launch_copy_words(const uint32_t* src, uint64_t n, uint32_t* dst, cudaStream_t st);
 void launch_part_count(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
                        int pa_bits, uint64_t n_parts, uint32_t* hist, cudaStream_t st);
 void launch_part_emit(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
@@ -251,8 +253,11 @@ void launch_b_clean_leaves(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_
 // out[s * (kMaxLevels + 1) + l] = global node index of level l's first node, l = 0..depth+1.
 // Also *tasks_out = *tasks (the large-item task count travels back with the level counts)
 // and *flag = 0 (the layout check flag the record kernels may set).
+// Level counts of every stripe and the task count (and, when `code` is set, the
+// persistent kernel's timeout code) into `out` (pinned host memory in the library's use).
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, const uint64_t* tasks,
-                          uint64_t* tasks_out, uint32_t* flag, cudaStream_t st);
+                          uint64_t* tasks_out, uint32_t* flag, const uint64_t* code, uint64_t* code_out,
+                          cudaStream_t st);
 void launch_b_leaf_payload(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
                            uint64_t ctas, uint32_t ept, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 // Level depth - r of each stripe.
@@ -266,7 +271,9 @@ void launch_b_top_down(const Pyramid* pyrs, const EmitJob* emits, const uint64_t
 void launch_b_top_down_leaves(const Pyramid* pyrs, const EmitJob* emits, const uint64_t* cta_beg, uint32_t n,
                               uint64_t ctas, uint32_t ept, const Pyramid* sp, const EmitJob* se, cudaStream_t st);
 // out[s * 16 + 0..6] = stripe s's root child mask and cache.
+// Root information of every stripe, and the layout check flag after it, written into
+// `out` (pinned host memory in the library's use).
 void launch_b_root_info(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, uint32_t* out,
-                        cudaStream_t st);
+                        const uint32_t* flag, cudaStream_t st);
 
 }  // namespace ooc

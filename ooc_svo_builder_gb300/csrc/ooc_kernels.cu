@@ -1528,6 +1528,14 @@ __device__ void root_info(const Pyramid& p, const EmitJob& e, uint64_t data_base
   }
 }
 
+// n words into `dst` (mapped pinned host memory): small results the host waits for
+// travel as the kernel's stores, not as copies queued on the copy engine.
+__global__ void k_copy_words(const uint32_t* __restrict__ src, uint64_t n, uint32_t* __restrict__ dst) {
+  pdl_enter();
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
 __global__ void k_scatter_records(const uint64_t* __restrict__ src, uint64_t n, int words, uint64_t* __restrict__ dst) {
   pdl_enter();
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1748,13 +1756,16 @@ __global__ void __launch_bounds__(kChunk) kb_compact(const Pyramid* __restrict__
   }
 }
 
+// Also copies *tasks to *tasks_out and, when `code` is set, *code to *code_out.
 __global__ void kb_level_bases(const Pyramid* __restrict__ pyrs, uint32_t n_stripes, uint32_t* __restrict__ out,
                                const uint64_t* __restrict__ tasks, uint64_t* __restrict__ tasks_out,
-                               uint32_t* __restrict__ flag) {
+                               uint32_t* __restrict__ flag, const uint64_t* __restrict__ code,
+                               uint64_t* __restrict__ code_out) {
   pdl_enter();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0) {
     *tasks_out = *tasks;
+    if (code) *code_out = *code;
     *flag = 0u;  // the layout check flag of the sub-batch's record kernels
   }
   if (s >= n_stripes) return;
@@ -2131,10 +2142,13 @@ __global__ void __launch_bounds__(256, 4) kb_persist(PersistJob pj) {
   }
 }
 
+// Root information of every stripe into `out` (16 words each), and the layout
+// check flag after them (out[16 n]).
 __global__ void kb_root_info(const Pyramid* __restrict__ pyrs, const EmitJob* __restrict__ emits, uint32_t n_stripes,
-                             uint32_t* __restrict__ out) {
+                             uint32_t* __restrict__ out, const uint32_t* __restrict__ flag) {
   pdl_enter();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) out[(uint64_t)n_stripes * 16] = *flag;
   if (s >= n_stripes) return;
   if (pyrs[s].lv[pyrs[s].depth].n == 0) return;
   root_info(pyrs[s], emits[s], emits[s].data_base, out + (uint64_t)s * 16);
@@ -2154,6 +2168,13 @@ void scan_u64_exclusive(uint64_t* data, uint64_t n, uint64_t* partials, cudaStre
   unsigned long long* d = reinterpret_cast<unsigned long long*>(data);
   scan_exclusive<unsigned long long>(d, n, reinterpret_cast<unsigned long long*>(partials), st,
                                      flag_last ? d + n - 1 : nullptr);
+}
+
+void launch_copy_words(const uint32_t* src, uint64_t n, uint32_t* dst, cudaStream_t st) {
+  if (n == 0) return;
+  KScope k("copy_words", st);
+  const uint64_t g = std::min<uint64_t>((n + 255) / 256, 4096);
+  launch_k(k_copy_words, dim3((unsigned)g), dim3(256), 0, st, src, n, dst);
 }
 
 void launch_part_count(const float* tris, int stride, uint64_t n_tris, const float* axis_lo, const float* axis_hi,
@@ -2357,11 +2378,12 @@ void launch_b_clean_leaves(const Pyramid* pyrs, const uint64_t* cta_beg, uint32_
 }
 
 void launch_b_level_bases(const Pyramid* pyrs, uint32_t n_stripes, uint32_t* out, const uint64_t* tasks,
-                          uint64_t* tasks_out, uint32_t* flag, cudaStream_t st) {
+                          uint64_t* tasks_out, uint32_t* flag, const uint64_t* code, uint64_t* code_out,
+                          cudaStream_t st) {
   if (n_stripes == 0) return;
   KScope k("level_bases", st);
   launch_k(kb_level_bases, dim3(grid_for(n_stripes, 128)), dim3(128), 0, st, pyrs, n_stripes, out, tasks, tasks_out,
-           flag);
+           flag, code, code_out);
 }
 
 namespace {
@@ -2434,10 +2456,10 @@ void launch_b_persist(const PersistJob& pj, int num_sms, int ctas_per_sm, cudaSt
 }
 
 void launch_b_root_info(const Pyramid* pyrs, const EmitJob* emits, uint32_t n_stripes, uint32_t* out,
-                        cudaStream_t st) {
+                        const uint32_t* flag, cudaStream_t st) {
   if (n_stripes == 0) return;
   KScope k("root_info", st);
-  launch_k(kb_root_info, dim3(grid_for(n_stripes, 128)), dim3(128), 0, st, pyrs, emits, n_stripes, out);
+  launch_k(kb_root_info, dim3(grid_for(n_stripes, 128)), dim3(128), 0, st, pyrs, emits, n_stripes, out, flag);
 }
 
 }  // namespace ooc
