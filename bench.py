@@ -722,6 +722,10 @@ def run_serve(args, world, rank, local):
                 if args.serve_warmup > 0:
                     serve_stream(srv, pool, r, args.serve_warmup, seed=1005 + int(r), drain_s=args.drain)
                 out[arm].append(serve_stream(srv, pool, r, args.duration, seed=5 + int(r), drain_s=args.drain))
+                st = srv.stats()
+                out[arm][-1]["server"] = {"pinned_on_demand_gb": st["pinned_on_demand_bytes"] / 1e9,
+                                          "pinned_on_demand_allocs": st["pinned_on_demand_allocs"],
+                                          "pinned_reserve_gb": st["pinned_reserve_bytes"] / 1e9}
             print("serve %s %.0f req/s: %s" % (arm, r, json.dumps(out[arm][-1])), file=sys.stderr, flush=True)
     # capacity of the resident arms: a burst of requests submitted at once
     capacity = {}

@@ -367,6 +367,20 @@ int ooc_server_create(const ooc_server_config* cfg, ooc_server** out);
 int ooc_server_submit(ooc_server* server, const ooc_mesh* mesh, uint64_t* id);
 /* Next completed request (OOC_OK), or OOC_ERR_TIMEOUT after `timeout_ms`. */
 int ooc_server_poll(ooc_server* server, int32_t timeout_ms, ooc_result* out);
+/* The serving loop's state, for monitoring. */
+typedef struct {
+  uint64_t queued;                   /* submitted, not yet started                         */
+  uint64_t in_flight_bytes;          /* HBM held: admitted footprints, results not released
+                                        (resident) or not yet copied back (host)           */
+  uint64_t completed_unpolled;       /* complete, not yet polled                           */
+  uint64_t held;                     /* polled, not yet released                           */
+  uint64_t deliveries;               /* host results waiting for their copy back to start  */
+  uint64_t pinned_reserve_bytes;     /* host_pool_mb, pinned at creation                   */
+  uint64_t pinned_reserve_free_bytes;
+  uint64_t pinned_on_demand_bytes;   /* pinned while serving (kept for reuse)              */
+  uint64_t pinned_on_demand_allocs;  /* pins made while serving                            */
+} ooc_server_state;
+int ooc_server_stats(ooc_server* server, ooc_server_state* out);
 /* Copy a polled result's files into host memory (either location). */
 int ooc_server_read(ooc_server* server, uint64_t id, void* nodes_host, void* data_host);
 /* Free a polled result's buffers.  A device-resident result is freed stream-

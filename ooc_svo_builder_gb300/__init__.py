@@ -38,7 +38,7 @@ EXPORTS = ("ooc_ctx_create", "ooc_ctx_destroy", "ooc_last_error", "ooc_estimate_
            "ooc_arena_alloc", "ooc_set_batch_budget", "ooc_batch_budget", "ooc_server_read", "ooc_get_tuning",
            "ooc_set_tuning", "ooc_autotune", "ooc_check_octree_device", "ooc_build_from_device",
            "ooc_partition_counts", "ooc_file_times", "ooc_set_stream_budget", "ooc_stream_budget",
-           "ooc_stream_passes")
+           "ooc_stream_passes", "ooc_server_stats")
 CHECK_BITS = {1: "child group order", 2: "reference count", 4: "depth", 8: "data index", 16: "payload Morton code"}
 
 
@@ -78,6 +78,12 @@ class Result(ctypes.Structure):
                 ("data_bytes", ctypes.c_uint64), ("info", BuildInfo), ("t_submit_us", ctypes.c_double),
                 ("t_start_us", ctypes.c_double), ("t_built_us", ctypes.c_double), ("t_done_us", ctypes.c_double),
                 ("batch_size", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_uint64) for k in (
+        "queued", "in_flight_bytes", "completed_unpolled", "held", "deliveries", "pinned_reserve_bytes",
+        "pinned_reserve_free_bytes", "pinned_on_demand_bytes", "pinned_on_demand_allocs")]
 
 
 class Tuning(ctypes.Structure):
@@ -207,6 +213,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ooc_server_poll.restype = ctypes.c_int
     lib.ooc_server_read.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
     lib.ooc_server_read.restype = ctypes.c_int
+    lib.ooc_server_stats.argtypes = [ctypes.c_void_p, P(ServerStats)]
+    lib.ooc_server_stats.restype = ctypes.c_int
     lib.ooc_server_release.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
     lib.ooc_server_release.restype = ctypes.c_int
     lib.ooc_server_destroy.argtypes = [ctypes.c_void_p]
@@ -600,6 +608,14 @@ class Server:
             out["tree"] = _octree.from_bytes(gridsize, nodes.tobytes(), data.tobytes())
         self.lib.ooc_server_release(self.h, r.id)
         return out
+
+    def stats(self) -> dict:
+        """The serving loop's state (ooc_server_stats)."""
+        st = ServerStats()
+        rc = self.lib.ooc_server_stats(self.h, ctypes.byref(st))
+        if rc != OOC_OK:
+            raise OocError(rc, "ooc_server_stats failed")
+        return {k: int(getattr(st, k)) for k, _ in st._fields_}
 
     def close(self):
         if self.h:

@@ -84,7 +84,20 @@ class PinnedPool {
     cap = 64 << 10;
     while (cap < n) cap <<= 1;
     void* p = nullptr;
-    return cudaMallocHost(&p, cap) == cudaSuccess ? p : nullptr;
+    if (cudaMallocHost(&p, cap) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(mu_);
+    on_demand_bytes_ += cap;
+    on_demand_allocs_++;
+    return p;
+  }
+  // reserve bytes, of them free, pinned outside the reserve, and the pins that took
+  void stats(uint64_t& reserve, uint64_t& reserve_free, uint64_t& on_demand, uint64_t& allocs) {
+    std::lock_guard<std::mutex> lk(mu_);
+    reserve = arena_bytes_;
+    reserve_free = 0;
+    for (const auto& kv : by_off_) reserve_free += kv.second;
+    on_demand = on_demand_bytes_;
+    allocs = on_demand_allocs_;
   }
   void put(void* p, size_t cap) {
     if (!p) return;
@@ -128,6 +141,7 @@ class PinnedPool {
       }
   }
   std::mutex mu_;
+  uint64_t on_demand_bytes_ = 0, on_demand_allocs_ = 0;
   std::multimap<size_t, void*> free_;  // separately pinned blocks, by capacity
   char* arena_ = nullptr;
   size_t arena_bytes_ = 0;
@@ -371,13 +385,16 @@ struct ooc_server {
       return 0;
     }
     // host results: the mesh is complete in this batch (never rerun); the delivery
-    // thread copies it into pinned memory and publishes it once the copy has landed
+    // thread copies it into pinned memory and publishes it once the copy has landed.
+    // Its device memory counts against the budget until then, so deliveries that fall
+    // behind hold back admission instead of filling HBM.
     Request* r = call.reqs[mesh];
     r->t_built = call.s->now_us();
     r->info = call.infos[mesh];
     (*call.published)[call.index[mesh]] = 1;
     {
       std::lock_guard<std::mutex> lk(call.s->mu);
+      call.s->in_flight += r->d_nodes_bytes + r->d_data_bytes;
       call.s->to_copy.push_back(r);
     }
     call.s->cv_deliver.notify_one();
@@ -414,8 +431,7 @@ struct ooc_server {
     if (!ok) {
       if (ev) cudaEventDestroy(ev);
       cudaStreamSynchronize(d2h_stream);  // nothing of this request stays queued
-      free_device(r);
-      r->d_nodes_bytes = r->d_data_bytes = 0;
+      release_delivered(r);
       publish(r, OOC_ERR_OOM);
       return;
     }
@@ -448,14 +464,25 @@ struct ooc_server {
       if (e == cudaErrorNotReady) continue;
       deliveries.pop_front();
       Request* r = d.first;
-      free_device(r);
-      r->d_nodes_bytes = r->d_data_bytes = 0;
+      release_delivered(r);
       {
         std::lock_guard<std::mutex> lk(mu);
         spare_events.push_back(d.second);
       }
       publish(r, e == cudaSuccess ? OOC_OK : OOC_ERR_DEVICE);
     }
+  }
+
+  // A host result's device memory, once its copy back is done or failed: freed and
+  // taken off the budget.
+  void release_delivered(Request* r) {
+    free_device(r);
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      in_flight -= r->d_nodes_bytes + r->d_data_bytes;
+    }
+    r->d_nodes_bytes = r->d_data_bytes = 0;
+    cv_work.notify_all();
   }
 
   void free_device(Request* r) {
@@ -641,6 +668,22 @@ int ooc_server_poll(ooc_server* s, int32_t timeout_ms, ooc_result* out) {
   out->t_built_us = r->t_built;
   out->t_done_us = r->t_done;
   out->batch_size = r->batch_size;
+  return OOC_OK;
+}
+
+int ooc_server_stats(ooc_server* s, ooc_server_state* out) {
+  if (!s || !out) return OOC_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    out->queued = s->queue.size();
+    out->in_flight_bytes = s->in_flight;
+    out->completed_unpolled = s->done.size();
+    out->held = s->held.size();
+    out->deliveries = s->to_copy.size();
+  }
+  s->pinned.stats(out->pinned_reserve_bytes, out->pinned_reserve_free_bytes, out->pinned_on_demand_bytes,
+                  out->pinned_on_demand_allocs);
   return OOC_OK;
 }
 

@@ -24,9 +24,10 @@ def oracle_tree(t, p):
     return octree.Octree(int(p.gridsize), nodes, data)
 
 
-def serve_all(reqs, feed_delay=0.0, **server_kw):
+def serve_all(reqs, feed_delay=0.0, stats=None, **server_kw):
     """Submit every request (from a second thread when feed_delay > 0) and poll until all
-    are back: (ids, {id: polled result})."""
+    are back: (ids, {id: polled result}); `stats` (a dict) receives the server's state
+    after the last poll."""
     with ooc.Server(0, **server_kw) as srv:
         ids = [None] * len(reqs)
 
@@ -47,6 +48,8 @@ def serve_all(reqs, feed_delay=0.0, **server_kw):
             if r is not None:
                 got[r["id"]] = r
         th.join()
+        if stats is not None:
+            stats.update(srv.stats())
     return ids, got
 
 
@@ -104,10 +107,16 @@ def test_host_results_from_a_pinned_reserve_equal_oracle(mix40):
     blocks merge with their neighbours for the next ones), larger ones get blocks pinned
     on demand.  Every result still equals the oracle."""
     reqs, want = mix40
-    ids, got = serve_all(reqs, engines=2, max_batch=16, memory_budget=8 << 30, host_pool_mb=2)
+    stats = {}
+    ids, got = serve_all(reqs, engines=2, max_batch=16, memory_budget=8 << 30, host_pool_mb=2, stats=stats)
     for k, (rid, w) in enumerate(zip(ids, want)):
         assert got[rid]["status"] == 0, k
         assert not octree.diff(got[rid]["tree"], w), k
+    # everything polled and released: the reserve is whole again, nothing is left in flight
+    assert stats["pinned_reserve_bytes"] == 2 << 20
+    assert stats["pinned_reserve_free_bytes"] == 2 << 20
+    assert stats["in_flight_bytes"] == 0 and stats["queued"] == 0 and stats["held"] == 0
+    assert stats["pinned_on_demand_allocs"] >= 1  # the larger results
 
 
 @pytest.mark.parametrize("resident", [False, True], ids=["host", "device"])

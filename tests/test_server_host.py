@@ -24,6 +24,8 @@ def test_server_calls_reject_null():
     assert lib.ooc_server_poll(None, 0, ctypes.byref(r)) == 1
     assert lib.ooc_server_release(None, 1) == 1
     assert lib.ooc_server_read(None, 1, None, None) == 1
+    st = ooc.ServerStats()
+    assert lib.ooc_server_stats(None, ctypes.byref(st)) == 1
     lib.ooc_server_destroy(None)
 
 
