@@ -678,13 +678,14 @@ def serve_bounds(pool, local: int, n: int) -> dict:
     return out
 
 
-def run_serve(args, world, rank, local):
-    """Configuration 5: Poisson request streams through the serving loop (continuous batching,
-    footprint admission) and, on the same streams, through the plain path (one request at a time)."""
+SERVE_ARMS = ("served_resident", "plain_resident", "served_host", "plain_host")
+
+
+def serve_pool(args):
+    """The request pool of configuration 5: (meshes, pinned host buffer, [(ptr, n_tris, params, N)])."""
     import torch
     import ooc_svo_builder_gb300 as ooc
 
-    torch.cuda.set_device(local)
     meshes = tri.batch_meshes(args.n_meshes, seed=5, gridsizes=(128, 256, 512, 1024, 2048))
     offs = [0]
     for t, _, _ in meshes:
@@ -695,7 +696,19 @@ def run_serve(args, world, rank, local):
     for i, (t, N, payload) in enumerate(meshes):
         host[offs[i]:offs[i] + t.nbytes] = t.reshape(-1).view(np.uint8)
         pool.append((pinned.data_ptr() + offs[i], t.shape[0], ooc.make_params(N, 2048, geometry_only=not payload), N))
-    rates = [float(r) for r in args.rates.split(",")]
+    return meshes, pinned, pool
+
+
+def serve_part(args, local, part):
+    """One part of configuration 5, in a process of its own: an arm at every rate, a capacity
+    burst of a resident arm ("burst:<arm>"), or the capacity bounds ("bounds")."""
+    import torch
+    import ooc_svo_builder_gb300 as ooc
+
+    torch.cuda.set_device(local)
+    meshes, pinned, pool = serve_pool(args)
+    if part == "bounds":
+        return serve_bounds(pool, local, args.bound_meshes)
     # served: continuous batching over engines; plain: one request at a time through the same library.
     # resident: octrees stay in HBM (released by the poller); host: copied back to host memory.
     arms = {"served_resident": dict(engines=args.engines, max_batch=256, memory_budget=120 << 30, resident=True),
@@ -706,42 +719,65 @@ def run_serve(args, world, rank, local):
     # warm-up set: the requests with the largest grids, then a spread of the rest
     order = sorted(range(len(pool)), key=lambda i: -pool[i][3] * pool[i][1])
     warm = order[:16] + order[16::max(1, len(pool) // 64)]
-    out = {}
-    for arm, cfg in arms.items():
-        out[arm] = []
-        for r in rates:
-            # a fresh server per rate: a backlog left by an overloaded rate does not carry over
-            with ooc.Server(local, **cfg) as srv:
-                for i in warm:
-                    srv.submit_ptr(*pool[i])
-                for _ in warm:
-                    while srv.poll(1000, copy=False) is None:
-                        pass
-                # an unmeasured stream at the same rate first, so the measured one sees the
-                # server in its steady state (engine buffers grown, pinned result blocks pooled)
-                if args.serve_warmup > 0:
-                    serve_stream(srv, pool, r, args.serve_warmup, seed=1005 + int(r), drain_s=args.drain)
-                out[arm].append(serve_stream(srv, pool, r, args.duration, seed=5 + int(r), drain_s=args.drain))
-                st = srv.stats()
-                out[arm][-1]["server"] = {"pinned_on_demand_gb": st["pinned_on_demand_bytes"] / 1e9,
-                                          "pinned_on_demand_allocs": st["pinned_on_demand_allocs"],
-                                          "pinned_reserve_gb": st["pinned_reserve_bytes"] / 1e9}
-            print("serve %s %.0f req/s: %s" % (arm, r, json.dumps(out[arm][-1])), file=sys.stderr, flush=True)
-    # capacity of the resident arms: a burst of requests submitted at once
-    capacity = {}
-    for arm in ("served_resident", "plain_resident"):
-        with ooc.Server(local, **arms[arm]) as srv:
-            for i in warm:
-                srv.submit_ptr(*pool[i])
-            for _ in warm:
-                while srv.poll(1000, copy=False) is None:
-                    pass
-            capacity[arm] = serve_burst(srv, pool, args.burst, seed=77)
-        print("serve burst %s: %s" % (arm, json.dumps(capacity[arm])), file=sys.stderr, flush=True)
-    bounds = serve_bounds(pool, local, args.bound_meshes)
+
+    def warmed(cfg):
+        srv = ooc.Server(local, **cfg)
+        for i in warm:
+            srv.submit_ptr(*pool[i])
+        for _ in warm:
+            while srv.poll(1000, copy=False) is None:
+                pass
+        return srv
+
+    if part.startswith("burst:"):
+        arm = part.split(":", 1)[1]
+        with warmed(arms[arm]) as srv:
+            out = serve_burst(srv, pool, args.burst, seed=77)
+        print("serve burst %s: %s" % (arm, json.dumps(out)), file=sys.stderr, flush=True)
+        return out
+    out = []
+    for r in (float(x) for x in args.rates.split(",")):
+        # a fresh server per rate: a backlog left by an overloaded rate does not carry over
+        with warmed(arms[part]) as srv:
+            # an unmeasured stream at the same rate first, so the measured one sees the
+            # server in its steady state (engine buffers grown, pinned result blocks pooled)
+            if args.serve_warmup > 0:
+                serve_stream(srv, pool, r, args.serve_warmup, seed=1005 + int(r), drain_s=args.drain)
+            out.append(serve_stream(srv, pool, r, args.duration, seed=5 + int(r), drain_s=args.drain))
+            st = srv.stats()
+            out[-1]["server"] = {"pinned_on_demand_gb": st["pinned_on_demand_bytes"] / 1e9,
+                                 "pinned_on_demand_allocs": st["pinned_on_demand_allocs"],
+                                 "pinned_reserve_gb": st["pinned_reserve_bytes"] / 1e9}
+        print("serve %s %.0f req/s: %s" % (part, r, json.dumps(out[-1])), file=sys.stderr, flush=True)
+    return out
+
+
+def run_serve(args, world, rank, local):
+    """Configuration 5: Poisson request streams through the serving loop (continuous batching,
+    footprint admission) and, on the same streams, through the plain path (one request at a time).
+    Each arm, each capacity burst and the bounds run in a child process of their own, so no
+    arm inherits the process state (device memory pool, pinned memory) an earlier one left."""
+    import subprocess
+
+    fwd = ["--workload", "serve", "--rates", args.rates, "--duration", str(args.duration), "--drain",
+           str(args.drain), "--serve-warmup", str(args.serve_warmup), "--engines", str(args.engines), "--burst",
+           str(args.burst), "--bound-meshes", str(args.bound_meshes), "--host-pool-mb", str(args.host_pool_mb),
+           "--n-meshes", str(args.n_meshes)]
+
+    def child(part):
+        p = subprocess.run([sys.executable, os.path.abspath(__file__), *fwd, "--serve-part", part],
+                           stdout=subprocess.PIPE, text=True, env=dict(os.environ, LOCAL_RANK=str(local)))
+        if p.returncode != 0:
+            raise RuntimeError("serve part %s failed (exit %d)" % (part, p.returncode))
+        return json.loads(p.stdout.strip().splitlines()[-1])
+
+    out = {arm: child(arm) for arm in SERVE_ARMS}
+    capacity = {arm: child("burst:" + arm) for arm in ("served_resident", "plain_resident")}
+    bounds = child("bounds")
     print("serve bounds: %s" % json.dumps(bounds), file=sys.stderr, flush=True)
     top = out["served_resident"][-1]
     top_host = out["served_host"][-1]
+    meshes = tri.batch_meshes(args.n_meshes, seed=5, gridsizes=(128, 256, 512, 1024, 2048))
 
     def ratio(a, b):
         return [x["meshes_per_s"] / max(y["meshes_per_s"], 1e-9) for x, y in zip(out[a], out[b])]
@@ -753,8 +789,8 @@ def run_serve(args, world, rank, local):
         "config": {"workload": "configuration 5: Poisson arrivals at %s req/s, %.0f s each after %.0f s "
                                "unmeasured at the same rate, meshes drawn from a pool of %d configuration-4 "
                                "meshes with gridsizes 128..2048; 120 GB admission budget; pinned host "
-                               "triangles in, host octree bytes out"
-                               % (args.rates, args.duration, args.serve_warmup, len(pool)),
+                               "triangles in, host octree bytes out; each arm in a process of its own"
+                               % (args.rates, args.duration, args.serve_warmup, len(meshes)),
                    "name": "serve", "engines": args.engines, "max_batch": 256, "host_pool_mb": args.host_pool_mb,
                    "value_arm": "served_resident: octrees resident in HBM, released by the poller"},
         "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
@@ -837,6 +873,7 @@ def main():
     ap.add_argument("--host-pool-mb", type=int, default=8192,
                     help="serve: pinned host memory each host-result server reserves at creation, MiB")
     ap.add_argument("--burst", type=int, default=4096, help="serve: requests of the capacity burst")
+    ap.add_argument("--serve-part", default=None, help=argparse.SUPPRESS)  # set by run_serve for its children
     ap.add_argument("--bound-meshes", type=int, default=512,
                     help="serve: requests of the capacity bounds (one batch call; kernels alone; one call each)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -862,6 +899,9 @@ def main():
         line = run_batch(args, world, rank, local)
     elif args.workload == "serve":
         args.n_meshes = args.n_meshes or 512
+        if args.serve_part:  # a child of run_serve: print its part alone
+            print(json.dumps(serve_part(args, local, args.serve_part)))
+            return
         line = run_serve(args, world, rank, local)
     else:
         line = run_ours(args, world, rank, local)

@@ -340,8 +340,11 @@ typedef struct {
    * (0: pin blocks on demand).  Pinning takes a lock of the CUDA driver for as
    * long as it runs, so a block pinned while serving delays every engine; a
    * reserve that covers the results in flight keeps pinning out of the serving
-   * loop.  A result the reserve cannot hold gets a block pinned on demand.
-   * Ignored for device results; OOC_ERR_OOM when the host cannot pin it. */
+   * loop.  A result the reserve cannot hold gets a block pinned on demand; such
+   * blocks total at most the reserve's size (8 GiB at least).  At that bound a
+   * delivery waits for the caller to release results, and after 10 s its
+   * request completes with OOC_ERR_OOM.  Ignored for device results;
+   * OOC_ERR_OOM from ooc_server_create when the host cannot pin the reserve. */
   uint32_t host_pool_mb;
 } ooc_server_config;
 

@@ -43,52 +43,72 @@ using Clock = std::chrono::steady_clock;
 // kept for reuse: the smallest free block that holds the request, if it is at
 // most four times its size, else a new block of the next power of two from
 // 64 KiB.
+//
+// A reserve outlives its server: it goes back to a process-wide list and the
+// next server that asks for that many bytes takes it, pinned already.
+std::mutex g_reserves_mu;
+std::multimap<size_t, void*> g_reserves;  // pinned reserves of destroyed servers, by size
+
 class PinnedPool {
  public:
   ~PinnedPool() {
     for (auto& kv : free_) cudaFreeHost(kv.second);
-    if (arena_) cudaFreeHost(arena_);
+    if (arena_) {
+      std::lock_guard<std::mutex> lk(g_reserves_mu);
+      g_reserves.emplace(arena_bytes_, arena_);
+    }
   }
-  // Pins the arena; false when the host cannot pin that much.
+  // Pins the arena (or takes a kept one of that size); false when the host cannot pin that much.
   bool reserve(size_t bytes) {
     if (bytes == 0) return true;
     void* p = nullptr;
-    if (cudaMallocHost(&p, bytes) != cudaSuccess) return false;
+    {
+      std::lock_guard<std::mutex> lk(g_reserves_mu);
+      auto it = g_reserves.find(bytes);
+      if (it != g_reserves.end()) {
+        p = it->second;
+        g_reserves.erase(it);
+      }
+    }
+    if (!p && cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) return false;
     arena_ = static_cast<char*>(p);
     arena_bytes_ = bytes;
     add_extent(0, bytes);
     return true;
   }
+  // A block of at least n bytes: from the reserve, from the kept blocks, or newly pinned.
+  // Blocks pinned while serving are bounded (the reserve's size, 8 GiB at least): at the
+  // bound, the call waits for released results to free a block, and gives up (nullptr)
+  // after kPinWait or once the server is closing.
   void* get(size_t n, size_t& cap) {
-    {
-      std::lock_guard<std::mutex> lk(mu_);
-      if (arena_) {
-        const size_t want = (n + kGrain - 1) / kGrain * kGrain;
-        auto it = by_size_.lower_bound(want);
-        if (it != by_size_.end()) {
-          const size_t off = it->second, len = it->first;
-          remove_extent(off, len);
-          if (len > want) add_extent(off + want, len - want);
-          cap = want;
-          return arena_ + off;
+    const auto deadline = Clock::now() + kPinWait;
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+      if (void* p = take(n, cap)) return p;
+      size_t c = 64 << 10;
+      while (c < n) c <<= 1;
+      if (on_demand_bytes_ + c <= on_demand_limit()) {
+        on_demand_bytes_ += c;
+        on_demand_allocs_++;
+        lk.unlock();
+        void* p = nullptr;
+        if (cudaMallocHost(&p, c) == cudaSuccess) {
+          cap = c;
+          return p;
         }
+        lk.lock();
+        on_demand_bytes_ -= c;
+        on_demand_allocs_--;
+        return nullptr;
       }
-      auto it = free_.lower_bound(n);
-      if (it != free_.end() && it->first / 4 <= n) {
-        cap = it->first;
-        void* p = it->second;
-        free_.erase(it);
-        return p;
-      }
+      if (closing_ || cv_.wait_until(lk, deadline) == std::cv_status::timeout) return take(n, cap);
     }
-    cap = 64 << 10;
-    while (cap < n) cap <<= 1;
-    void* p = nullptr;
-    if (cudaMallocHost(&p, cap) != cudaSuccess) return nullptr;
+  }
+  // Wakes a get() waiting at the bound, for good (the server is being destroyed).
+  void close() {
     std::lock_guard<std::mutex> lk(mu_);
-    on_demand_bytes_ += cap;
-    on_demand_allocs_++;
-    return p;
+    closing_ = true;
+    cv_.notify_all();
   }
   // reserve bytes, of them free, pinned outside the reserve, and the pins that took
   void stats(uint64_t& reserve, uint64_t& reserve_free, uint64_t& on_demand, uint64_t& allocs) {
@@ -102,6 +122,7 @@ class PinnedPool {
   void put(void* p, size_t cap) {
     if (!p) return;
     std::lock_guard<std::mutex> lk(mu_);
+    cv_.notify_all();  // a get() waiting at the bound may fit now
     char* c = static_cast<char*>(p);
     if (arena_ && c >= arena_ && c < arena_ + arena_bytes_) {
       size_t off = (size_t)(c - arena_), len = cap;
@@ -127,6 +148,30 @@ class PinnedPool {
 
  private:
   static constexpr size_t kGrain = 64 << 10;
+  static constexpr std::chrono::seconds kPinWait{10};
+  size_t on_demand_limit() const { return std::max<size_t>(arena_bytes_, 8ull << 30); }
+  // From the reserve (best fit) or a kept block at most four times the size; mu_ held.
+  void* take(size_t n, size_t& cap) {
+    if (arena_) {
+      const size_t want = (n + kGrain - 1) / kGrain * kGrain;
+      auto it = by_size_.lower_bound(want);
+      if (it != by_size_.end()) {
+        const size_t off = it->second, len = it->first;
+        remove_extent(off, len);
+        if (len > want) add_extent(off + want, len - want);
+        cap = want;
+        return arena_ + off;
+      }
+    }
+    auto it = free_.lower_bound(n);
+    if (it != free_.end() && it->first / 4 <= n) {
+      cap = it->first;
+      void* p = it->second;
+      free_.erase(it);
+      return p;
+    }
+    return nullptr;
+  }
   void add_extent(size_t off, size_t len) {
     by_off_[off] = len;
     by_size_.emplace(len, off);
@@ -141,6 +186,8 @@ class PinnedPool {
       }
   }
   std::mutex mu_;
+  std::condition_variable cv_;
+  bool closing_ = false;
   uint64_t on_demand_bytes_ = 0, on_demand_allocs_ = 0;
   std::multimap<size_t, void*> free_;  // separately pinned blocks, by capacity
   char* arena_ = nullptr;
@@ -750,6 +797,7 @@ void ooc_server_destroy(ooc_server* s) {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop_delivery = true;
   }
+  s->pinned.close();  // a delivery waiting for pinned memory gives up rather than wait for releases
   s->cv_deliver.notify_all();
   if (s->deliverer.joinable()) s->deliverer.join();
   for (ooc_ctx* c : s->engines) ooc_ctx_destroy(c);
