@@ -78,33 +78,33 @@ class PinnedPool {
   }
   // A block of at least n bytes: from the reserve, from the kept blocks, or newly pinned.
   // Blocks pinned while serving are bounded (the reserve's size, 8 GiB at least): at the
-  // bound, the call waits for released results to free a block, and gives up (nullptr)
-  // after kPinWait or once the server is closing.
-  void* get(size_t n, size_t& cap) {
-    const auto deadline = Clock::now() + kPinWait;
+  // bound (or once the server is closing) this returns nullptr, and the caller retries
+  // after results have been released (wait_put).
+  void* try_get(size_t n, size_t& cap) {
     std::unique_lock<std::mutex> lk(mu_);
-    for (;;) {
-      if (void* p = take(n, cap)) return p;
-      size_t c = 64 << 10;
-      while (c < n) c <<= 1;
-      if (on_demand_bytes_ + c <= on_demand_limit()) {
-        on_demand_bytes_ += c;
-        on_demand_allocs_++;
-        lk.unlock();
-        void* p = nullptr;
-        if (cudaMallocHost(&p, c) == cudaSuccess) {
-          cap = c;
-          return p;
-        }
-        lk.lock();
-        on_demand_bytes_ -= c;
-        on_demand_allocs_--;
-        return nullptr;
-      }
-      if (closing_ || cv_.wait_until(lk, deadline) == std::cv_status::timeout) return take(n, cap);
+    if (void* p = take(n, cap)) return p;
+    size_t c = 64 << 10;
+    while (c < n) c <<= 1;
+    if (closing_ || on_demand_bytes_ + c > on_demand_limit()) return nullptr;
+    on_demand_bytes_ += c;
+    on_demand_allocs_++;
+    lk.unlock();
+    void* p = nullptr;
+    if (cudaMallocHost(&p, c) == cudaSuccess) {
+      cap = c;
+      return p;
     }
+    lk.lock();
+    on_demand_bytes_ -= c;
+    on_demand_allocs_--;
+    return nullptr;
   }
-  // Wakes a get() waiting at the bound, for good (the server is being destroyed).
+  // Waits until a block is returned (or the pool closes), at most `t`.
+  void wait_put(std::chrono::microseconds t) {
+    std::unique_lock<std::mutex> lk(mu_);
+    if (!closing_) cv_.wait_for(lk, t);
+  }
+  // Refuses new pins and wakes wait_put, for good (the server is being destroyed).
   void close() {
     std::lock_guard<std::mutex> lk(mu_);
     closing_ = true;
@@ -122,7 +122,7 @@ class PinnedPool {
   void put(void* p, size_t cap) {
     if (!p) return;
     std::lock_guard<std::mutex> lk(mu_);
-    cv_.notify_all();  // a get() waiting at the bound may fit now
+    cv_.notify_all();  // a delivery waiting at the bound may fit now
     char* c = static_cast<char*>(p);
     if (arena_ && c >= arena_ && c < arena_ + arena_bytes_) {
       size_t off = (size_t)(c - arena_), len = cap;
@@ -148,7 +148,6 @@ class PinnedPool {
 
  private:
   static constexpr size_t kGrain = 64 << 10;
-  static constexpr std::chrono::seconds kPinWait{10};
   size_t on_demand_limit() const { return std::max<size_t>(arena_bytes_, 8ull << 30); }
   // From the reserve (best fit) or a kept block at most four times the size; mu_ held.
   void* take(size_t n, size_t& cap) {
@@ -242,6 +241,7 @@ bool valid(const ooc_mesh& m) {
 // bytes), with room for the batch's job tables.
 constexpr uint64_t kNodeBytes = 120;
 constexpr uint64_t kDeliverPiece = 16ull << 20;  // bytes per copy of a host result's copy back
+constexpr std::chrono::seconds kPinWait{10};     // a host result waits this long for pinned memory
 constexpr int kSizers = 4;  // threads that compute the footprints of submitted requests
 
 double voxel_bound(const float* v, float unit_div, uint64_t N) {
@@ -448,13 +448,18 @@ struct ooc_server {
     return 0;
   }
 
-  // Queue a host result's copy back into pinned pool blocks on d2h_stream (delivery thread).
-  void deliver(Request* r) {
+  // Queue a host result's copy back into pinned pool blocks on d2h_stream (delivery thread):
+  // kQueued, kNoMemory (pinned memory at its bound: retry once results are released; a
+  // block already taken stays with the request), or kFailed (published with an error).
+  enum { kQueued = 0, kNoMemory = 1, kFailed = 2 };
+  int deliver(Request* r) {
     r->h_nodes_bytes = r->d_nodes_bytes;
     r->h_data_bytes = r->d_data_bytes;
+    if (r->h_nodes_bytes && !r->h_nodes && !(r->h_nodes = pinned.try_get(r->h_nodes_bytes, r->h_nodes_cap)))
+      return kNoMemory;
+    if (r->h_data_bytes && !r->h_data && !(r->h_data = pinned.try_get(r->h_data_bytes, r->h_data_cap)))
+      return kNoMemory;
     bool ok = true;
-    if (r->h_nodes_bytes) ok = (r->h_nodes = pinned.get(r->h_nodes_bytes, r->h_nodes_cap)) != nullptr;
-    if (ok && r->h_data_bytes) ok = (r->h_data = pinned.get(r->h_data_bytes, r->h_data_cap)) != nullptr;
     cudaEvent_t ev = nullptr;
     {
       std::lock_guard<std::mutex> lk(mu);
@@ -463,7 +468,7 @@ struct ooc_server {
         spare_events.pop_back();
       }
     }
-    if (ok && !ev) ok = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+    if (!ev) ok = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
     // in pieces, so that the engines' own small reads back (their level counts) do not
     // wait behind a whole result of hundreds of megabytes on the copy engine
     auto copy = [&](void* dst, const void* src, uint64_t bytes) {
@@ -480,43 +485,76 @@ struct ooc_server {
       cudaStreamSynchronize(d2h_stream);  // nothing of this request stays queued
       release_delivered(r);
       publish(r, OOC_ERR_OOM);
-      return;
+      return kFailed;
     }
     deliveries.push_back({r, ev});
+    return kQueued;
   }
 
-  // The delivery thread: queues the copy back of every host result the engines
-  // hand over (pinning pool blocks as needed, off the engines' threads), and
-  // publishes the results in that order once each copy has landed.
+  // The delivery thread: queues the copy back of every host result the engines hand
+  // over, in order (pinning pool blocks as needed, off the engines' threads), and
+  // publishes the results in that order once each copy has landed.  When pinned memory
+  // is at its bound, the waiting results stay queued while landed copies are published
+  // (so the caller can release them); with nothing in flight either, the oldest waiting
+  // result fails with OOC_ERR_OOM after kPinWait, or at once when the server is closing.
   void delivery_loop() {
     cudaSetDevice(cfg.device);
+    std::deque<Request*> waiting;  // this thread's: handed over, copy not yet queued
+    Clock::time_point starved_since{};
     for (;;) {
-      std::deque<Request*> batch;
+      bool closing = false;
       {
         std::unique_lock<std::mutex> lk(mu);
-        cv_deliver.wait(lk, [&] { return stop_delivery || !to_copy.empty() || !deliveries.empty(); });
-        if (to_copy.empty() && deliveries.empty()) return;
-        batch.swap(to_copy);
+        cv_deliver.wait(lk, [&] { return stop_delivery || !to_copy.empty() || !deliveries.empty() || !waiting.empty(); });
+        waiting.insert(waiting.end(), to_copy.begin(), to_copy.end());
+        to_copy.clear();
+        closing = stop_delivery;
+        if (waiting.empty() && deliveries.empty()) return;
       }
-      for (Request* r : batch) deliver(r);  // `deliveries` is this thread's alone
-      if (deliveries.empty()) continue;
-      const std::pair<Request*, cudaEvent_t> d = deliveries.front();
-      // with more results waiting to be queued, only take the oldest copy if it has landed
-      bool waiting = false;
-      {
-        std::lock_guard<std::mutex> lk(mu);
-        waiting = !to_copy.empty();
+      bool starved = false;
+      while (!waiting.empty()) {
+        if (deliver(waiting.front()) == kNoMemory) {
+          starved = true;
+          break;
+        }
+        waiting.pop_front();
       }
-      cudaError_t e = waiting ? cudaEventQuery(d.second) : cudaEventSynchronize(d.second);
-      if (e == cudaErrorNotReady) continue;
-      deliveries.pop_front();
-      Request* r = d.first;
-      release_delivered(r);
-      {
-        std::lock_guard<std::mutex> lk(mu);
-        spare_events.push_back(d.second);
+      if (!starved) starved_since = Clock::time_point{};
+      else if (starved_since == Clock::time_point{}) starved_since = Clock::now();
+      if (!deliveries.empty()) {
+        const std::pair<Request*, cudaEvent_t> d = deliveries.front();
+        // with results waiting (to be queued, or for memory), only take the oldest copy if it has landed
+        bool more = starved;
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          more = more || !to_copy.empty();
+        }
+        const cudaError_t e = more ? cudaEventQuery(d.second) : cudaEventSynchronize(d.second);
+        if (e == cudaErrorNotReady) {
+          if (starved) pinned.wait_put(std::chrono::microseconds(200));
+          continue;
+        }
+        deliveries.pop_front();
+        Request* r = d.first;
+        release_delivered(r);
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          spare_events.push_back(d.second);
+        }
+        publish(r, e == cudaSuccess ? OOC_OK : OOC_ERR_DEVICE);
+        continue;
       }
-      publish(r, e == cudaSuccess ? OOC_OK : OOC_ERR_DEVICE);
+      if (starved) {  // nothing in flight: only the caller's releases free pinned memory
+        if (closing || Clock::now() - starved_since > kPinWait) {
+          Request* r = waiting.front();
+          waiting.pop_front();
+          release_delivered(r);
+          publish(r, OOC_ERR_OOM);
+          starved_since = Clock::time_point{};
+        } else {
+          pinned.wait_put(std::chrono::milliseconds(10));
+        }
+      }
     }
   }
 
