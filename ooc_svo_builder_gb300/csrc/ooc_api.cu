@@ -134,7 +134,7 @@ struct ooc_ctx {
   ooc::LaunchState lstate;  // this context's launch count and timing hooks, installed per API call
   DevBuf d_tris, d_hist, d_axis, d_bits, d_scan, d_scanpart, d_keys, d_size, d_dsize, d_start, d_dstart,
       d_cache, d_winners, d_taskoff, d_taskpart, d_counter, d_nodes, d_data, d_recs, d_rootinfo, d_itemmask,
-      d_firstchild, d_itembox, d_leaf, d_touch, d_local, d_taskmap;
+      d_firstchild, d_itembox, d_leaf, d_touch, d_local, d_taskmap, d_woff;
   uint64_t max_tasks = 0;  // most large-item warp tasks a sub-batch has had (sizes the task map)
   // persistent phase A (ooc_tuning::persistent): its counters, its task map (all ones
   // between launches: every entry a launch fills is emptied by the warp that reads it)
@@ -782,8 +782,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   // ---- geometry of every stripe ----
   std::vector<Pyramid> pyr(n);
   std::vector<VoxJob> vj(n);
-  std::vector<uint64_t> item_beg(n + 1, 0), touch_beg(n, 0), local_beg(n, 0);
-  uint64_t words = 0, leaf_words = 0, blocks = 0, tbytes = 0, nlocal = 0, items = 0;
+  std::vector<uint64_t> item_beg(n + 1, 0), touch_beg(n, 0), local_beg(n, 0), woff_beg(n, 0);
+  uint64_t words = 0, leaf_words = 0, blocks = 0, tbytes = 0, nlocal = 0, items = 0, nwoff = 0;
   int max_depth = 0;
   for (uint32_t s = 0; s < n; s++) {
     const StripeRef& r = sb[s];
@@ -795,6 +795,8 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     tbytes += touch_bytes(pyr[s].lv[m.pl.Ds]);
     local_beg[s] = nlocal;
     if (m.pl.Ds >= kMarkDepth) nlocal += pyr[s].lv[m.pl.Ds].nblocks;
+    woff_beg[s] = nwoff;  // the winner pass's bit ranks: payload stripes only
+    if (!m.pl.binary) nwoff += pyr[s].lv[m.pl.Ds].nblocks;
     max_depth = std::max(max_depth, m.pl.Ds);
     item_beg[s] = items;
     items += r.n_items;
@@ -806,6 +808,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
   uint32_t* leaf = ensure<uint32_t>(c->d_leaf, leaf_words * 4);
   uint8_t* touch = ensure<uint8_t>(c->d_touch, tbytes);
   uint16_t* local = ensure<uint16_t>(c->d_local, nlocal * 2);
+  uint64_t* woff = nwoff ? ensure<uint64_t>(c->d_woff, nwoff * 8) : nullptr;
   if (!c->leaf_zero) {
     ck(cudaMemsetAsync(leaf, 0, c->d_leaf.cap, st), "memset leaf levels");
     ck(cudaMemsetAsync(touch, 0, c->d_touch.cap, st), "memset leaf marks");
@@ -832,6 +835,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
     P.zl = P.depth >= kMarkDepth ? P.depth - 1 : P.depth;
     P.local = P.depth >= kMarkDepth ? local + local_beg[s] : nullptr;
     P.scan = scan;
+    P.woff = m.pl.binary ? nullptr : woff + woff_beg[s];
     VoxJob& j = vj[s];
     std::memset(&j, 0, sizeof(j));
     uint32_t pa[3], sa[3];
@@ -1193,6 +1197,7 @@ void run_sub_batch(ooc_ctx* c, cudaStream_t st, std::vector<MeshWork>& meshes, c
       vj[s].leafscan = scan + P.lv[P.depth].off_b;
       vj[s].leaflocal = P.local;
       vj[s].leafscan_base = (uint32_t)P.lv[P.depth].koff;
+      vj[s].leafwoff = P.woff;
     }
     if (q.empty) continue;
     int ls = 0;
@@ -1926,7 +1931,7 @@ void ooc_ctx_destroy(ooc_ctx* c) {
                     &c->d_keys, &c->d_size, &c->d_dsize, &c->d_start, &c->d_dstart, &c->d_cache, &c->d_winners,
                     &c->d_taskoff, &c->d_taskpart, &c->d_counter, &c->d_nodes, &c->d_data, &c->d_recs,
                     &c->d_rootinfo, &c->d_itemmask, &c->d_firstchild, &c->d_itembox, &c->d_leaf, &c->d_touch, &c->d_local,
-                    &c->d_taskmap, &c->d_pctr, &c->d_pmap, &c->d_chunk[0], &c->d_chunk[1], &c->d_group[0],
+                    &c->d_taskmap, &c->d_woff, &c->d_pctr, &c->d_pmap, &c->d_chunk[0], &c->d_chunk[1], &c->d_group[0],
                     &c->d_group[1], &c->d_stream_mat, &c->d_stream_part, &c->d_stream_base, &c->d_part_off};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);

@@ -50,6 +50,8 @@ struct Pyramid {
   uint8_t* touch;   // byte b non-zero: leaf block b may have a set bit (NULL: every block is read)
   uint16_t* local;  // marked leaf level: nodes of block b's group before block b (written for marked blocks)
   uint32_t* scan;   // exclusive prefix popcount per 256-bit block, all levels (+1 total)
+  uint64_t* woff;   // leaf level, payload stripes: per block, byte k = set bits in its words 0..k-1
+                    // (written for every block of an unmarked level, for marked blocks otherwise); or NULL
 };
 
 constexpr uint64_t kLeafGroup = 16;  // leaf blocks per scan entry of a marked leaf level
@@ -75,6 +77,7 @@ struct VoxJob {
   const uint32_t* leafscan; // scan entries of level Ds (exclusive, minus its base)
   const uint16_t* leaflocal;// marked leaf level: Pyramid::local (leafscan then has one entry per group)
   uint32_t leafscan_base;
+  const uint64_t* leafwoff; // Pyramid::woff of the leaf level (the rank of a bit without a popcount per word)
   uint32_t* winners;        // per leaf: min triangle index
   uint64_t* task_off;       // per item: exclusive prefix of warp tasks (n_items + 1)
   uint64_t* task_flag;      // set to 1 by an item with tasks (the sub-batch's task_off[items]); may be NULL

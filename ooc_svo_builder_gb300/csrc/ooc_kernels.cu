@@ -481,6 +481,11 @@ __device__ __forceinline__ void set_leaf(const VoxJob& j, uint32_t w, uint32_t a
 __device__ __forceinline__ uint32_t leaf_rank(const VoxJob& j, uint32_t b) {
   const uint32_t blk = b >> 8;
   const uint32_t base = j.leaflocal ? j.leafscan[blk / kLeafGroup] + j.leaflocal[blk] : j.leafscan[blk];
+  if (j.leafwoff) {  // the set bits before the bit's word, from the pyramid pass, and one popcount
+    const uint32_t wi = (b >> 5) & 7u;
+    const uint32_t before = (uint32_t)(j.leafwoff[blk] >> (8 * wi)) & 0xffu;
+    return base - j.leafscan_base + before + __popc(j.leafbits[b >> 5] & ((1u << (b & 31)) - 1u));
+  }
   return base - j.leafscan_base + in_block_rank(j.leafbits + (uint64_t)blk * 8, b);
 }
 
@@ -988,13 +993,16 @@ __device__ __forceinline__ void pyramid_block(const Pyramid& p, int l, uint64_t 
   const uint4 q0 = ld4<CG>(q), q1 = ld4<CG>(q + 1);
   const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
   uint32_t c = 0, pw = 0;
+  uint64_t wo = 0;  // byte k: set bits in words 0..k-1 (at most 224)
 #pragma unroll
   for (int k = 0; k < 8; k++) {
+    wo |= (uint64_t)c << (8 * k);
     c += __popc(w[k]);
     pw |= nonzero_bytes(w[k]) << (4 * k);
   }
   p.scan[L.off_b + b] = c;
   if (l > 0) level_words(p, l - 1)[b] = pw;
+  if (l == p.depth && p.woff) p.woff[b] = wo;
 }
 
 // Global node index of the first node of block blk of level l: the
@@ -1007,6 +1015,11 @@ __device__ __forceinline__ uint64_t block_base(const Pyramid& p, int l, uint64_t
 // Global node index of bit `b` of level l.
 __device__ __forceinline__ uint64_t node_index(const Pyramid& p, int l, uint64_t b) {
   const uint64_t blk = b >> 8;
+  if (l == p.depth && p.woff) {  // the leaf level of a payload stripe: word offsets from the pyramid pass
+    const uint32_t wi = (uint32_t)(b >> 5) & 7u;
+    return block_base(p, l, blk) + ((p.woff[blk] >> (8 * wi)) & 0xffu) +
+           __popc(level_words(p, l)[b >> 5] & ((1u << (b & 31)) - 1u));
+  }
   return block_base(p, l, blk) + in_block_rank(level_words(p, l) + blk * 8, b);
 }
 
@@ -1034,11 +1047,14 @@ __device__ __forceinline__ void leaf_group(const Pyramid& p, uint64_t q) {
       const uint4 q0 = ld4<CG>(w4), q1 = ld4<CG>(w4 + 1);
       const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
       uint32_t c = 0;
+      uint64_t wo = 0;
 #pragma unroll
       for (int i = 0; i < 8; i++) {
+        wo |= (uint64_t)c << (8 * i);
         c += __popc(w[i]);
         pw[k] |= nonzero_bytes(w[i]) << (4 * i);
       }
+      if (p.woff) p.woff[b] = wo;
       p.local[b] = (uint16_t)total;
       total += c;
     }
