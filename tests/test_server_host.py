@@ -34,6 +34,8 @@ def test_result_struct_layout():
     assert ctypes.sizeof(ooc.Result) == 8 + 4 + 4 + 8 * 4 + 48 + 32 + 8
     # ooc_server_config: device, engines, max_batch, result_location, memory_budget, fail_batch_at_mesh, host_pool_mb
     assert ctypes.sizeof(ooc.ServerConfig) == 32
+    # ooc_server_state: nine u64 counters
+    assert ctypes.sizeof(ooc.ServerStats) == 9 * 8
 
 
 def test_tuning_calls_reject_null():
