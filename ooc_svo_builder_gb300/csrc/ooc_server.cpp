@@ -70,7 +70,10 @@ class PinnedPool {
         g_reserves.erase(it);
       }
     }
-    if (!p && cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) return false;
+    if (!p) {
+      if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) return false;
+      first_touch(p, bytes);
+    }
     arena_ = static_cast<char*>(p);
     arena_bytes_ = bytes;
     add_extent(0, bytes);
@@ -103,6 +106,25 @@ class PinnedPool {
   void wait_put(std::chrono::microseconds t) {
     std::unique_lock<std::mutex> lk(mu_);
     if (!closing_) cv_.wait_for(lk, t);
+  }
+  // Copies from the device over all of a freshly pinned block, once.  The first copy
+  // into a page of newly pinned memory is the slow one: 56 GB/s against 193 GB/s into
+  // the same block afterwards, measured on a box that had been serving.  Done here, it
+  // stays out of the deliveries.
+  static void first_touch(void* p, size_t bytes) {
+    constexpr size_t kPiece = 64ull << 20;
+    void* d = nullptr;
+    cudaStream_t st = nullptr;
+    if (cudaMalloc(&d, kPiece) != cudaSuccess) return;  // only a warm-up: skipped without memory
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess) {
+      for (size_t off = 0; off < bytes; off += kPiece)
+        if (cudaMemcpyAsync(static_cast<char*>(p) + off, d, std::min(kPiece, bytes - off), cudaMemcpyDeviceToHost,
+                            st) != cudaSuccess)
+          break;
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
+    cudaFree(d);
   }
   // Refuses new pins and wakes wait_put, for good (the server is being destroyed).
   void close() {
