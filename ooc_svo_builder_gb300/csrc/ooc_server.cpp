@@ -28,11 +28,13 @@
 #include <unordered_map>
 #include <vector>
 
+#include "ooc_extents.h"
 #include "ooc_svo_gpu.h"
 
 namespace {
 
 using Clock = std::chrono::steady_clock;
+using ooc::Extents;
 
 // Pinned host memory for host results.  With ooc_server_config::host_pool_mb
 // the server pins that much once, at creation, and carves each result's blocks
@@ -76,7 +78,7 @@ class PinnedPool {
     }
     arena_ = static_cast<char*>(p);
     arena_bytes_ = bytes;
-    add_extent(0, bytes);
+    extents_.reset(bytes, kGrain);
     return true;
   }
   // A block of at least n bytes: from the reserve, from the kept blocks, or newly pinned.
@@ -136,8 +138,7 @@ class PinnedPool {
   void stats(uint64_t& reserve, uint64_t& reserve_free, uint64_t& on_demand, uint64_t& allocs) {
     std::lock_guard<std::mutex> lk(mu_);
     reserve = arena_bytes_;
-    reserve_free = 0;
-    for (const auto& kv : by_off_) reserve_free += kv.second;
+    reserve_free = extents_.free_bytes();
     on_demand = on_demand_bytes_;
     allocs = on_demand_allocs_;
   }
@@ -147,22 +148,7 @@ class PinnedPool {
     cv_.notify_all();  // a delivery waiting at the bound may fit now
     char* c = static_cast<char*>(p);
     if (arena_ && c >= arena_ && c < arena_ + arena_bytes_) {
-      size_t off = (size_t)(c - arena_), len = cap;
-      auto next = by_off_.lower_bound(off);
-      if (next != by_off_.end() && next->first == off + len) {  // merge with the extent after
-        len += next->second;
-        remove_extent(next->first, next->second);
-      }
-      auto prev = by_off_.lower_bound(off);
-      if (prev != by_off_.begin()) {
-        --prev;
-        if (prev->first + prev->second == off) {  // and the one before
-          off = prev->first;
-          len += prev->second;
-          remove_extent(prev->first, prev->second);
-        }
-      }
-      add_extent(off, len);
+      extents_.put((size_t)(c - arena_), cap);
       return;
     }
     free_.emplace(cap, p);
@@ -173,17 +159,8 @@ class PinnedPool {
   size_t on_demand_limit() const { return std::max<size_t>(arena_bytes_, 8ull << 30); }
   // From the reserve (best fit) or a kept block at most four times the size; mu_ held.
   void* take(size_t n, size_t& cap) {
-    if (arena_) {
-      const size_t want = (n + kGrain - 1) / kGrain * kGrain;
-      auto it = by_size_.lower_bound(want);
-      if (it != by_size_.end()) {
-        const size_t off = it->second, len = it->first;
-        remove_extent(off, len);
-        if (len > want) add_extent(off + want, len - want);
-        cap = want;
-        return arena_ + off;
-      }
-    }
+    size_t off = 0;
+    if (arena_ && extents_.take(n, off, cap)) return arena_ + off;
     auto it = free_.lower_bound(n);
     if (it != free_.end() && it->first / 4 <= n) {
       cap = it->first;
@@ -193,19 +170,6 @@ class PinnedPool {
     }
     return nullptr;
   }
-  void add_extent(size_t off, size_t len) {
-    by_off_[off] = len;
-    by_size_.emplace(len, off);
-  }
-  void remove_extent(size_t off, size_t len) {
-    by_off_.erase(off);
-    auto range = by_size_.equal_range(len);
-    for (auto it = range.first; it != range.second; ++it)
-      if (it->second == off) {
-        by_size_.erase(it);
-        break;
-      }
-  }
   std::mutex mu_;
   std::condition_variable cv_;
   bool closing_ = false;
@@ -213,8 +177,7 @@ class PinnedPool {
   std::multimap<size_t, void*> free_;  // separately pinned blocks, by capacity
   char* arena_ = nullptr;
   size_t arena_bytes_ = 0;
-  std::map<size_t, size_t> by_off_;         // free arena extents: offset -> length
-  std::multimap<size_t, size_t> by_size_;   // the same extents: length -> offset
+  Extents extents_;  // the reserve's free blocks
 };
 
 struct Request {
